@@ -1,0 +1,52 @@
+/*
+ * xtb_gb300.h -- engine extensions of libxtb_gb300.so beyond the reference C API.
+ *
+ * These entry points have no counterpart in the reference's include/xtb.h; they
+ * expose information the GPU engine has and that tests, benchmarks and
+ * serving layers need.  Same conventions as xtb.h: errors go to the
+ * environment, NULL environment is a no-op, output arrays are caller-owned.
+ */
+#pragma once
+#include "xtb.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Number of CUDA devices visible to the engine (0 if none). */
+extern int xtbgb_deviceCount(void);
+
+/* SCC iterations of the last single point and whether it converged (1/0). */
+extern void xtbgb_getIterations(xtb_TEnvironment env, xtb_TResults res, int* iterations, int* converged);
+
+/* Energy decomposition of the last single point, Hartree (gap in eV):
+ * parts[0] electronic (incl. three-body dispersion), [1] repulsion, [2] isotropic ES,
+ * [3] anisotropic ES, [4] anisotropic XC, [5] dispersion, [6] three-body dispersion,
+ * [7] HOMO-LUMO gap (eV). */
+extern void xtbgb_getEnergyParts(xtb_TEnvironment env, xtb_TResults res, double* parts);
+
+/* Shell charges[nshell] and cumulative atomic multipoles dipm[natoms][3],
+ * qp[natoms][6] (packed xx, xy, yy, xz, yz, zz) of the last single point. */
+extern void xtbgb_getShellCharges(xtb_TEnvironment env, xtb_TResults res, double* qsh);
+extern void xtbgb_getMultipoles(xtb_TEnvironment env, xtb_TResults res, double* dipm, double* qp);
+
+/* Device time (ms) of the last single point per engine phase, measured with CUDA
+ * events on the engine's stream.  ms[0..11] = setup, integrals, cholesky, hbuild,
+ * stdform, sytrd, trieig, backtransform, density, popmix, gradient, total. */
+extern void xtbgb_getPhaseTimes(xtb_TEnvironment env, xtb_TResults res, double* ms);
+
+/* Host<->device traffic of the last single point: bytes[0] host->device, bytes[1] device->host,
+ * bytes[2] number of device kernels the single point launched. */
+extern void xtbgb_getTransferBytes(xtb_TEnvironment env, xtb_TResults res, long long* bytes);
+
+/* Whether the engine keeps orbital data (MO coefficients, density, overlap) on the host after a
+ * single point; needed by xtb_getOrbitalCoefficients.  Default 1 (as the reference). */
+extern void xtbgb_setKeepOrbitals(xtb_TEnvironment env, xtb_TCalculator calc, int keep);
+
+/* Measured FP64 FMA throughput of device 0 in TFLOP/s (roofline denominator for FP64 kernels);
+ * returns 0 when no device is present. */
+extern double xtbgb_fp64PeakTflops(void);
+
+#ifdef __cplusplus
+}
+#endif

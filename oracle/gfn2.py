@@ -790,7 +790,9 @@ def fermismear(eig, nel, etemp):
     thr = 1e-9
     occ = np.zeros(norbs)
     if nel + 1 > norbs:
+        # no LUMO: the integer occupations from occu stay (src/scc_core.f90:1001-1004)
         ef = eig[nel - 1]
+        occ[:nel] = 1.0
     elif nel == 0:
         ef = eig[0]
     else:
@@ -1007,7 +1009,22 @@ def singlepoint(Z, xyz, charge=0.0, uhf=0, etemp=300.0, accuracy=1.0, maxiter=25
     grad += gd4
     grad += coulomb_grad(basis, xyz, qsh)
 
+    # dipole moment (calc_dipole, src/dipole.f90:94-128) and Wiberg-Mayer bond orders
+    # (get_wiberg, src/scc_core.f90:1208-1245) from the last density
+    dip = np.sum(xyz * zval[:, None], axis=0) - np.einsum("kij,ij->k", D, Pm)
+    PS = Pm @ S
+    wbo = np.zeros((n, n))
+    ao0 = basis.sh_ao[np.searchsorted(basis.sh_atom, np.arange(n))]
+    ao1 = np.append(ao0[1:], nao)
+    for i in range(n):
+        for j in range(i):
+            if np.sum((xyz[i] - xyz[j]) ** 2) < 100.0:
+                blk = PS[ao0[i]:ao1[i], ao0[j]:ao1[j]] * PS[ao0[j]:ao1[j], ao0[i]:ao1[i]].T
+                wbo[i, j] = wbo[j, i] = np.sum(blk)
+
     r = Result()
+    r.dipole = dip
+    r.wbo = wbo
     r.energy = eel + erep + embd
     r.e_elec = eel + embd
     r.e_rep = erep

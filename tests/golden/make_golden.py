@@ -1,0 +1,89 @@
+"""Generate tests/golden/gfn2_reference.json from the reference's own GFN2 tests.
+
+Reads (as text) test/unit/test_gfn2.f90 and test/api/c_api_example.c of the
+reference tree and extracts, for each known-answer case, the geometry and the
+values the reference asserts, with the tolerance it asserts them at:
+
+* ``scc``   test_gfn2.f90:48-170   water, zero-charge guess, energy parts, charges, multipoles
+* ``api``   test_gfn2.f90:172-235  propyne C3H4, EEQ guess, energy, gap, gradient
+* ``pcem``  test_gfn2.f90:383-457  (H2O)4 cluster without point charges, energy, gap, gradient
+* ``capi``  c_api_example.c:38-112 propyne through the C ABI: energy, q[5], dipole, wbo
+
+Usage: python tests/golden/make_golden.py [reference_root]
+"""
+import json
+import os
+import re
+import sys
+
+REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "gfn2_reference.json")
+NUM = r"[-+]?(?:\d+\.\d*|\.\d+|\d+)(?:[eEdD][-+]?\d+)?"
+
+
+def fnum(t):
+    return float(t.replace("_wp", "").replace("d", "e").replace("D", "e"))
+
+
+def sub(src, name):
+    a = src.index(f"subroutine {name}(")
+    b = src.index(f"end subroutine {name}", a)
+    return src[a:b]
+
+
+def array(block, decl):
+    m = re.search(decl + r"[^=]*=\s*(?:reshape\(\s*)?\[?&?(.*?)\]", block, re.S)
+    body = re.sub(r"!.*", "", m.group(1)).replace("&", " ")
+    return [fnum(t) for t in re.findall(NUM + r"(?:_wp)?", body)]
+
+
+def checks(block):
+    out = []
+    for m in re.finditer(r"call check_\(error,\s*((?:[^,(\n]|\([^)\n]*\))+),\s*(" + NUM + r")_wp(?:,\s*thr=([^)]+))?\)", block):
+        out.append({"expr": m.group(1).strip(), "value": fnum(m.group(2)), "thr": m.group(3)})
+    return out
+
+
+def main():
+    src = open(os.path.join(REF, "test/unit/test_gfn2.f90")).read()
+    cases = {}
+    for key, name in (("scc", "test_gfn2_scc"), ("api", "test_gfn2_api"), ("pcem", "test_gfn2_pcem_api")):
+        blk = sub(src, name)
+        if key == "pcem":
+            blk = blk[:blk.index("! reset")]
+        at = [int(v) for v in array(blk, r"integer, parameter :: at\(nat\)")]
+        xyz = array(blk, r"real\(wp\),parameter :: xyz\(3,nat\)")
+        thr = {}
+        for m in re.finditer(r"real\(wp\),parameter :: (thr2?)\s*=\s*(" + NUM + r")_wp", blk):
+            thr[m.group(1)] = fnum(m.group(2))
+        cs = checks(blk)
+        for c in cs:
+            t = c["thr"]
+            if t is None:
+                c["thr"] = 1e-15
+            elif t in thr:
+                c["thr"] = thr[t]
+            elif "*" in t:
+                base, fac = t.split("*")
+                c["thr"] = thr[base.strip()] * float(fac)
+            else:
+                c["thr"] = fnum(t)
+        maxiter = int(re.search(r"maxiter\s*=\s*(\d+)", blk).group(1))
+        cases[key] = {"numbers": at, "positions": xyz, "checks": cs, "maxiter": maxiter,
+                      "guess": "zero" if key == "scc" else "eeq"}
+    capi = open(os.path.join(REF, "test/api/c_api_example.c")).read()
+    first = capi[capi.index("testFirst"):capi.index("testSecond")]
+    m = re.search(r"double const coord\[[^\]]*\]\s*=\s*\{(.*?)\};", first, re.S)
+    coord = [fnum(t) for t in re.findall(NUM, m.group(1))]
+    m = re.search(r"int const attyp\[7\]\s*=\s*\{(.*?)\};", first, re.S)
+    at = [int(t) for t in re.findall(r"\d+", m.group(1))]
+    cks = []
+    for m in re.finditer(r"check\((\w+(?:\[\d+\])?),\s*(" + NUM + r"),\s*(" + NUM + r")", first):
+        cks.append({"expr": m.group(1), "value": fnum(m.group(2)), "thr": fnum(m.group(3))})
+    cases["capi"] = {"numbers": at, "positions": coord, "checks": cks[:4], "maxiter": 30, "guess": "eeq"}
+    json.dump(cases, open(OUT, "w"), indent=1)
+    print("wrote", OUT)
+
+
+if __name__ == "__main__":
+    main()

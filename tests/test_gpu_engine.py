@@ -1,0 +1,145 @@
+"""GPU parity of the plain FP64 engine through the C ABI (needs a GB300).
+
+Tolerances (stated once, used everywhere): |dE| <= 1e-6 Eh, charges <= 1e-5 e,
+gradient components <= 1e-5 Eh/bohr, SCC iterations within +-1 of the oracle.
+"""
+import os
+import subprocess
+import types
+
+import numpy as np
+import pytest
+
+from helpers import TOL_E, TOL_G, TOL_ITER, TOL_Q, case_geometry, evaluate, golden
+from oracle import gfn2
+from xtb_gb300 import interface as X
+from xtb_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLD = os.path.join(ROOT, "tests", "golden")
+
+
+def gpu(Z, xyz, **kw):
+    return X.Calculator(Z, xyz, **kw).singlepoint()
+
+
+def as_eval(r):
+    return types.SimpleNamespace(energy=r.energy, gnorm=r.gnorm, hl_gap=r.hl_gap, gradient=r.gradient,
+                                 q=r.charges, dipole=r.dipole, wbo=r.bond_orders)
+
+
+def assert_parity(r, o, iters=True):
+    assert abs(r.energy - o.energy) <= TOL_E, (r.energy, o.energy)
+    assert np.max(np.abs(r.charges - o.q)) <= TOL_Q
+    assert np.max(np.abs(r.gradient - o.gradient)) <= TOL_G
+    if iters:
+        assert abs(r.iterations - o.iterations) <= TOL_ITER, (r.iterations, o.iterations)
+
+
+@pytest.mark.parametrize("key", ["api", "pcem", "capi"])
+def test_reference_known_answers(key):
+    """Values asserted by the reference's own tests, reproduced through the C ABI."""
+    case = golden()[key]
+    Z, xyz = case_geometry(case)
+    r = gpu(Z, xyz, maxiter=case["maxiter"])
+    assert r.converged
+    e = as_eval(r)
+    for c in case["checks"]:
+        kind = "g" if "gradient" in c["expr"] else ("q" if c["expr"].startswith("q") else "e")
+        tol = min({"e": TOL_E, "g": TOL_G, "q": TOL_Q}[kind] if kind != "e" or "gap" not in c["expr"] else 1e-4,
+                  max(c["thr"], 2e-10))
+        got = evaluate(c["expr"], e)
+        assert abs(got - c["value"]) <= tol, (c["expr"], got, c["value"], tol)
+
+
+MOLECULES = {
+    "water": ([8, 1, 1], [[0.0, 0.0, -0.7357858611], [1.4418315287, 0.0, 0.3678929305], [-1.4418315287, 0.0, 0.3678929305]], 0, 0),
+    "hydroxide": ([8, 1], [[0.0, 0.0, 0.0], [0.0, 0.0, 1.83]], -1, 0),
+    "ammonium": ([7, 1, 1, 1, 1], [[0, 0, 0], [1.12, 1.12, 1.12], [-1.12, -1.12, 1.12], [-1.12, 1.12, -1.12], [1.12, -1.12, -1.12]], 1, 0),
+    "methyl_radical": ([6, 1, 1, 1], [[0, 0, 0], [2.04, 0, 0], [-1.02, 1.767, 0], [-1.02, -1.767, 0.05]], 0, 1),
+    "hydrogen_sulfide": ([16, 1, 1], [[0, 0, 0], [2.52, 0, 0.1], [-0.2, 2.5, 0]], 0, 0),
+    "silane": ([14, 1, 1, 1, 1], [[0, 0, 0], [1.61, 1.61, 1.61], [-1.61, -1.61, 1.61], [-1.61, 1.61, -1.61], [1.61, -1.61, -1.6]], 0, 0),
+    "hydrogen_chloride": ([17, 1], [[0, 0, 0], [0, 0, 2.41]], 0, 0),
+    "dihydrogen": ([1, 1], [[0, 0, 0], [0, 0, 1.4]], 0, 0),
+}
+
+
+@pytest.mark.parametrize("name", sorted(MOLECULES))
+def test_small_molecules_match_oracle(name):
+    Z, xyz, charge, uhf = MOLECULES[name]
+    xyz = np.array(xyz, dtype=float)
+    r = gpu(Z, xyz, charge=charge, uhf=uhf)
+    o = gfn2.singlepoint(Z, xyz, charge=charge, uhf=uhf)
+    assert_parity(r, o)
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 7])
+def test_alkanes_match_oracle(n):
+    Z, xyz = W.alkane(n, 0.02, seed=10 + n)
+    assert_parity(gpu(Z, xyz), gfn2.singlepoint(Z, xyz))
+
+
+@pytest.mark.parametrize("m", [2, 5, 12])
+def test_water_clusters_match_oracle(m):
+    Z, xyz = W.water_cluster(m, seed=20 + m)
+    assert_parity(gpu(Z, xyz), gfn2.singlepoint(Z, xyz))
+
+
+@pytest.mark.parametrize("name", ["c10h22_seed1", "h2o_30_seed1", "c50h102_seed3", "h2o_300_seed1"])
+def test_workload_fixtures(name):
+    path = os.path.join(GOLD, f"{name}.npz")
+    if not os.path.exists(path):
+        pytest.skip(f"fixture {name} not generated")
+    f = np.load(path)
+    r = gpu(f["numbers"], f["positions"])
+    o = types.SimpleNamespace(energy=float(f["energy"]), q=f["charges"], gradient=f["gradient"],
+                              iterations=int(f["iterations"]))
+    assert_parity(r, o)
+
+
+def test_full_size_invariants():
+    """(H2O)300 (N = 900, nao = 1800): charge conservation, zero net force, and the
+    gradient against a central finite difference of the energy along a random direction."""
+    Z, xyz = W.water_cluster(300, seed=1)
+    calc = X.Calculator(Z, xyz)
+    r = calc.singlepoint()
+    assert abs(np.sum(r.charges)) < 1e-8
+    assert np.max(np.abs(np.sum(r.gradient, axis=0))) < 1e-7
+    d = np.random.default_rng(5).normal(size=xyz.shape)
+    d /= np.linalg.norm(d)
+    h = 1e-3
+    calc.update(xyz + h * d)
+    ep = calc.singlepoint().energy
+    calc.update(xyz - h * d)
+    em = calc.singlepoint().energy
+    fd = (ep - em) / (2 * h)
+    assert abs(fd - np.sum(r.gradient * d)) < 1e-6 * max(1.0, abs(fd))
+
+
+def test_warm_start_and_determinism():
+    Z, xyz = W.alkane(6, 0.02, seed=3)
+    calc = X.Calculator(Z, xyz)
+    r1 = calc.singlepoint()
+    r2 = calc.singlepoint(fresh=False)               # restarts from the converged charges
+    assert abs(r1.energy - r2.energy) < 1e-8
+    assert r2.iterations <= r1.iterations
+    r3 = calc.singlepoint()
+    assert r3.energy == r1.energy                     # bit-identical repeat
+    assert np.max(np.abs(r3.gradient - r1.gradient)) < 1e-12
+
+
+def test_unconverged_scc_reports_error():
+    Z, xyz = W.water_cluster(4, seed=2)
+    with pytest.raises(X.XTBException, match="did not converge"):
+        gpu(Z, xyz, maxiter=2)
+
+
+def test_c_program_drop_in(tmp_path):
+    exe = tmp_path / "test_c_api"
+    cmd = ["gcc", "-O1", "-I", os.path.join(ROOT, "include"), os.path.join(ROOT, "tests", "c", "test_c_api.c"),
+           "-o", str(exe), "-L", os.path.join(ROOT, "xtb_gb300"), "-lxtb_gb300", "-lm",
+           "-Wl,-rpath," + os.path.join(ROOT, "xtb_gb300")]
+    subprocess.run(cmd, check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0, out.stdout + out.stderr

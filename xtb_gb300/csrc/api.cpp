@@ -1,0 +1,509 @@
+// C ABI of the GB300 GFN2-xTB engine: drop-in for the reference xtb C API.
+//
+// Handle life cycle, error log and argument checks restate the reference's
+// bind(C) layer (src/api/environment.f90:47-245, src/api/molecule.f90:47-137,
+// src/api/calculator.f90:58-699, src/api/interface.f90:40-156,
+// src/api/results.f90:54-504).  Unlike the reference, no state is global: every
+// handle owns its data, so different threads may drive different handles
+// concurrently; the device work of one call is serialised on the calling
+// thread's CUDA stream.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/xtb_gb300.h"
+#include "engine.h"
+#include "host_model.h"
+#include "linalg.h"
+
+struct LogEntry {
+    bool error;
+    std::string text;
+};
+
+struct _xtb_TEnvironment {
+    std::vector<LogEntry> log;
+    int verbosity = XTB_VERBOSITY_FULL;
+    FILE* out = stdout;
+    bool own_out = false;
+    void error(const std::string& msg, const char* source) { log.push_back({true, std::string(source) + ": " + msg}); }
+    void warning(const std::string& msg, const char* source) { log.push_back({false, std::string(source) + ": " + msg}); }
+    bool failed() const {
+        for (auto& e : log)
+            if (e.error) return true;
+        return false;
+    }
+};
+
+struct _xtb_TMolecule {
+    int nat = 0;
+    std::vector<int> Z;
+    std::vector<double> xyz;
+    double charge = 0.0;
+    int uhf = 0;
+};
+
+struct _xtb_TCalculator {
+    bool loaded = false;
+    bool keep_orbitals = true;
+    xg::SPSettings set;
+    int nat = 0;
+    std::vector<int> Z;   // element list the parametrisation was loaded for
+};
+
+struct _xtb_TResults {
+    bool has = false;
+    xg::Wavefunction wfn;
+    xg::SPResult sp;
+    int nat = 0;
+};
+
+namespace {
+
+constexpr int kMaxElem = 86;   // GFN2-xTB parametrisation (src/xtb/gfn2.f90:70)
+
+bool check_env(xtb_TEnvironment env) { return env != nullptr; }
+
+}  // namespace
+
+extern "C" {
+
+int xtb_getAPIVersion(void) { return XTB_API_VERSION; }
+
+// ------------------------------------------------------------------ environment
+xtb_TEnvironment xtb_newEnvironment(void) { return new _xtb_TEnvironment(); }
+
+void xtb_delEnvironment(xtb_TEnvironment* env) {
+    if (env && *env) {
+        if ((*env)->own_out && (*env)->out) fclose((*env)->out);
+        delete *env;
+        *env = nullptr;
+    }
+}
+
+int xtb_checkEnvironment(xtb_TEnvironment env) {
+    if (!check_env(env)) return 0;
+    return env->failed() ? 1 : 0;
+}
+
+void xtb_showEnvironment(xtb_TEnvironment env, const char* message) {
+    if (!check_env(env) || env->log.empty()) return;
+    FILE* f = env->out ? env->out : stdout;
+    fprintf(f, "########################################################################\n");
+    fprintf(f, "[%s] %s\n", env->failed() ? "ERROR" : "WARNING", message ? message : "");
+    for (size_t i = env->log.size(); i-- > 0;) fprintf(f, "-%zu- %s\n", i + 1, env->log[i].text.c_str());
+    fprintf(f, "########################################################################\n");
+    fflush(f);
+    env->log.clear();
+}
+
+void xtb_getError(xtb_TEnvironment env, char* buffer, const int* buffersize) {
+    if (!check_env(env) || !buffer) return;
+    if (!env->failed()) return;
+    std::string msg;
+    for (size_t i = env->log.size(); i-- > 0;) {
+        if (!msg.empty()) msg += "\n";
+        msg += "-" + std::to_string(i + 1) + "- " + env->log[i].text;
+    }
+    env->log.clear();
+    const size_t cap = buffersize ? (size_t)std::max(*buffersize, 0) : msg.size() + 1;
+    if (cap == 0) return;
+    const size_t n = std::min(msg.size(), cap - 1);
+    memcpy(buffer, msg.data(), n);
+    buffer[n] = '\0';
+}
+
+void xtb_setOutput(xtb_TEnvironment env, const char* filename) {
+    xtb_releaseOutput(env);
+    if (!check_env(env) || !filename) return;
+    const std::string f(filename);
+    if (f == "-" || f == "STDOUT") env->out = stdout;
+    else if (f == "STDERR") env->out = stderr;
+    else {
+        FILE* fp = fopen(filename, "w");
+        if (!fp) {
+            env->error("cannot open output file " + f, "xtb_api_setOutput");
+            return;
+        }
+        env->out = fp;
+        env->own_out = true;
+    }
+}
+
+void xtb_releaseOutput(xtb_TEnvironment env) {
+    if (!check_env(env)) return;
+    if (env->own_out && env->out) fclose(env->out);
+    env->own_out = false;
+    env->out = stdout;
+}
+
+void xtb_setVerbosity(xtb_TEnvironment env, int verbosity) {
+    if (!check_env(env)) return;
+    if (verbosity < 0 || verbosity > 2) env->warning("Verbosity specified is out of range", "xtb_api_setVerbosity");
+    env->verbosity = verbosity;
+}
+
+// ------------------------------------------------------------------ molecule
+xtb_TMolecule xtb_newMolecule(xtb_TEnvironment env, const int* natoms, const int* numbers, const double* positions,
+                              const double* charge, const int* uhf, const double* lattice, const bool* periodic) {
+    const char* src = "xtb_api_newMolecule";
+    if (!check_env(env)) return nullptr;
+    if (!natoms || *natoms <= 0) {
+        env->error("Number of atoms must be positive", src);
+        return nullptr;
+    }
+    const int n = *natoms;
+    if (!numbers || !positions) {
+        env->error("Could not generate molecular structure", src);
+        return nullptr;
+    }
+    for (int i = 0; i < n; ++i)
+        if (numbers[i] <= 0 || numbers[i] > 118) {
+            env->error("Invalid atomic number present", src);
+            return nullptr;
+        }
+    if (periodic && (periodic[0] || periodic[1] || periodic[2])) {
+        env->error("Periodic boundary conditions are not supported by this engine", src);
+        return nullptr;
+    }
+    (void)lattice;
+    for (int i = 0; i < 3 * n; ++i)
+        if (!std::isfinite(positions[i])) {
+            env->error("Could not generate molecular structure", src);
+            return nullptr;
+        }
+    auto* mol = new _xtb_TMolecule();
+    mol->nat = n;
+    mol->Z.assign(numbers, numbers + n);
+    mol->xyz.assign(positions, positions + 3 * n);
+    mol->charge = charge ? *charge : 0.0;
+    mol->uhf = uhf ? *uhf : 0;
+    return mol;
+}
+
+void xtb_delMolecule(xtb_TMolecule* mol) {
+    if (mol && *mol) {
+        delete *mol;
+        *mol = nullptr;
+    }
+}
+
+void xtb_updateMolecule(xtb_TEnvironment env, xtb_TMolecule mol, const double* positions, const double* lattice) {
+    const char* src = "xtb_api_updateMolecule";
+    if (!check_env(env)) return;
+    if (!mol) {
+        env->error("Molecular structure data is not allocated", src);
+        return;
+    }
+    if (!positions) {
+        env->error("Position array is not allocated", src);
+        return;
+    }
+    (void)lattice;
+    mol->xyz.assign(positions, positions + 3 * mol->nat);
+}
+
+// ------------------------------------------------------------------ calculator
+xtb_TCalculator xtb_newCalculator(void) { return new _xtb_TCalculator(); }
+
+void xtb_delCalculator(xtb_TCalculator* calc) {
+    if (calc && *calc) {
+        delete *calc;
+        *calc = nullptr;
+    }
+}
+
+void xtb_loadGFN2xTB(xtb_TEnvironment env, xtb_TMolecule mol, xtb_TCalculator calc, char* filename) {
+    const char* src = "xtb_api_loadGFN2xTB";
+    if (!check_env(env)) return;
+    if (!mol) {
+        env->error("Molecular structure data is not allocated", src);
+        return;
+    }
+    if (!calc) {
+        env->error("Singlepoint calculator is not allocated", src);
+        return;
+    }
+    (void)filename;   // the GFN2-xTB parameter set is built in
+    for (int z : mol->Z)
+        if (z > kMaxElem) {
+            env->error("Element not parametrised for GFN2-xTB", src);
+            return;
+        }
+    calc->loaded = true;
+    calc->nat = mol->nat;
+    calc->Z = mol->Z;
+}
+
+static void unsupported(xtb_TEnvironment env, const char* what, const char* src) {
+    if (check_env(env)) env->error(std::string(what) + " is not supported by the GB300 GFN2-xTB engine", src);
+}
+
+void xtb_loadGFN0xTB(xtb_TEnvironment env, xtb_TMolecule, xtb_TCalculator, char*) {
+    unsupported(env, "GFN0-xTB", "xtb_api_loadGFN0xTB");
+}
+void xtb_loadGFN1xTB(xtb_TEnvironment env, xtb_TMolecule, xtb_TCalculator, char*) {
+    unsupported(env, "GFN1-xTB", "xtb_api_loadGFN1xTB");
+}
+void xtb_loadGFNFF(xtb_TEnvironment env, xtb_TMolecule, xtb_TCalculator, char*) {
+    unsupported(env, "GFN-FF", "xtb_api_loadGFNFF");
+}
+void xtb_setSolvent(xtb_TEnvironment env, xtb_TCalculator, char*, int*, double*, int*, char*) {
+    unsupported(env, "Implicit solvation", "xtb_api_setSolvent");
+}
+void xtb_releaseSolvent(xtb_TEnvironment, xtb_TCalculator) {}
+void xtb_setExternalCharges(xtb_TEnvironment env, xtb_TCalculator, int*, int*, double*, double*) {
+    unsupported(env, "External point charges", "xtb_api_setExternalCharges");
+}
+void xtb_releaseExternalCharges(xtb_TEnvironment, xtb_TCalculator) {}
+
+void xtb_setAccuracy(xtb_TEnvironment env, xtb_TCalculator calc, double accuracy) {
+    const char* src = "xtb_api_setAccuracy";
+    if (!check_env(env)) return;
+    if (!calc) {
+        env->error("Singlepoint calculator is not allocated", src);
+        return;
+    }
+    if (!calc->loaded) {
+        env->error("Setting accuracy not possible, no calculator loaded", src);
+        return;
+    }
+    if (accuracy < 1.0e-4) {
+        env->warning("We cannot provide this level of accuracy, resetted accuracy to 0.0001", src);
+        accuracy = 1.0e-4;
+    } else if (accuracy > 1.0e3) {
+        env->warning("We cannot provide this level of accuracy, resetted accuracy to 1000", src);
+        accuracy = 1.0e3;
+    }
+    calc->set.accuracy = accuracy;
+}
+
+void xtb_setMaxIter(xtb_TEnvironment env, xtb_TCalculator calc, int iterations) {
+    const char* src = "xtb_api_setMaxIter";
+    if (!check_env(env)) return;
+    if (!calc) {
+        env->error("Singlepoint calculator is not allocated", src);
+        return;
+    }
+    if (!calc->loaded) {
+        env->error("Setting iterations not possible, no calculator loaded", src);
+        return;
+    }
+    calc->set.maxiter = std::max(iterations, 1);
+}
+
+void xtb_setElectronicTemp(xtb_TEnvironment env, xtb_TCalculator calc, double temperature) {
+    const char* src = "xtb_api_setElectronicTemp";
+    if (!check_env(env)) return;
+    if (!calc) {
+        env->error("Singlepoint calculator is not allocated", src);
+        return;
+    }
+    if (!calc->loaded) {
+        env->error("Setting electronic temperature not possible, no calculator loaded", src);
+        return;
+    }
+    calc->set.etemp = std::max(temperature, 1.0e-6);
+}
+
+// ------------------------------------------------------------------ single point
+void xtb_singlepoint(xtb_TEnvironment env, xtb_TMolecule mol, xtb_TCalculator calc, xtb_TResults res) {
+    const char* src = "xtb_api_singlepoint";
+    if (!check_env(env)) return;
+    if (!mol) {
+        env->error("Molecular structure data is not allocated", src);
+        return;
+    }
+    if (!calc) {
+        env->error("Singlepoint calculator is not allocated", src);
+        return;
+    }
+    if (!calc->loaded) {
+        env->error("No calculator loaded for single point", src);
+        return;
+    }
+    if (!res) {
+        env->error("Calculation results are not allocated", src);
+        return;
+    }
+    xg::HostMol hm;
+    const std::string err = xg::build_host_mol(mol->nat, mol->Z.data(), mol->xyz.data(), mol->charge, mol->uhf, hm);
+    if (!err.empty()) {
+        env->error(err, "xtb_calculator_singlepoint");
+        env->error("Electronic structure method terminated", "xtb_calculator_singlepoint");
+        return;
+    }
+    // warm start only when the sizes of the kept wavefunction match (src/api/interface.f90:83-92)
+    if (res->wfn.valid() && (res->wfn.nat != hm.nat || res->wfn.nao != hm.nao || res->wfn.nsh != hm.nsh))
+        res->wfn = xg::Wavefunction();
+    bool failed = false;
+    try {
+        xg::run_singlepoint(hm, calc->set, res->wfn, res->sp, calc->keep_orbitals, failed);
+    } catch (const std::exception& e) {
+        env->error(e.what(), "scf");
+        env->error("Electronic structure method terminated", "xtb_calculator_singlepoint");
+        res->has = false;
+        return;
+    }
+    res->has = true;
+    res->nat = hm.nat;
+    if (failed) env->error("Self consistent charge iterator did not converge", "scf");
+    if (env->verbosity >= XTB_VERBOSITY_MINIMAL && env->out) {
+        fprintf(env->out, "          | TOTAL ENERGY %28.12f Eh   |\n", res->sp.energy);
+        fprintf(env->out, "          | GRADIENT NORM %27.12f Eh/a0|\n", res->sp.gnorm);
+        fprintf(env->out, "          | HOMO-LUMO GAP %27.12f eV   |\n", res->sp.hl_gap);
+        fflush(env->out);
+    }
+}
+
+// ------------------------------------------------------------------ results
+xtb_TResults xtb_newResults(void) { return new _xtb_TResults(); }
+
+void xtb_delResults(xtb_TResults* res) {
+    if (res && *res) {
+        delete *res;
+        *res = nullptr;
+    }
+}
+
+xtb_TResults xtb_copyResults(xtb_TResults res) {
+    if (!res) return nullptr;
+    return new _xtb_TResults(*res);
+}
+
+static bool res_ready(xtb_TEnvironment env, xtb_TResults res, const char* src, const char* what) {
+    if (!check_env(env)) return false;
+    if (!res) {
+        env->error("Results object is not allocated", src);
+        return false;
+    }
+    if (!res->has) {
+        env->error(std::string(what) + " is not available in results", src);
+        return false;
+    }
+    return true;
+}
+
+void xtb_getEnergy(xtb_TEnvironment env, xtb_TResults res, double* energy) {
+    if (!res_ready(env, res, "xtb_api_getEnergy", "Energy") || !energy) return;
+    *energy = res->sp.energy;
+}
+
+void xtb_getGradient(xtb_TEnvironment env, xtb_TResults res, double* grad) {
+    if (!res_ready(env, res, "xtb_api_getGradient", "Gradient") || !grad) return;
+    std::copy(res->sp.gradient.begin(), res->sp.gradient.end(), grad);
+}
+
+void xtb_getCharges(xtb_TEnvironment env, xtb_TResults res, double* charges) {
+    if (!res_ready(env, res, "xtb_api_getCharges", "Partial charges") || !charges) return;
+    std::copy(res->wfn.q.begin(), res->wfn.q.end(), charges);
+}
+
+void xtb_getDipole(xtb_TEnvironment env, xtb_TResults res, double* dipole) {
+    if (!res_ready(env, res, "xtb_api_getDipole", "Dipole moment") || !dipole) return;
+    std::copy(res->sp.dipole.begin(), res->sp.dipole.end(), dipole);
+}
+
+// Wiberg-Mayer bond orders (get_wiberg, src/scc_core.f90:1208-1245), evaluated on the device
+void xtb_getBondOrders(xtb_TEnvironment env, xtb_TResults res, double* wbo) {
+    if (!res_ready(env, res, "xtb_api_getBondOrders", "Bond orders") || !wbo) return;
+    if (res->sp.wbo.empty()) {
+        env->error("Bond orders are not available in results", "xtb_api_getBondOrders");
+        return;
+    }
+    std::copy(res->sp.wbo.begin(), res->sp.wbo.end(), wbo);
+}
+
+void xtb_getNao(xtb_TEnvironment env, xtb_TResults res, int* nao) {
+    if (!res_ready(env, res, "xtb_api_getNao", "Orbitals") || !nao) return;
+    *nao = res->wfn.nao;
+}
+
+void xtb_getOrbitalEigenvalues(xtb_TEnvironment env, xtb_TResults res, double* emo) {
+    if (!res_ready(env, res, "xtb_api_getOrbitalEigenvalues", "Orbital eigenvalues") || !emo) return;
+    std::copy(res->wfn.emo.begin(), res->wfn.emo.end(), emo);
+}
+
+void xtb_getOrbitalOccupations(xtb_TEnvironment env, xtb_TResults res, double* focc) {
+    if (!res_ready(env, res, "xtb_api_getOrbitalOccupations", "Orbital occupations") || !focc) return;
+    std::copy(res->wfn.focc.begin(), res->wfn.focc.end(), focc);
+}
+
+void xtb_getOrbitalCoefficients(xtb_TEnvironment env, xtb_TResults res, double* c) {
+    if (!res_ready(env, res, "xtb_api_getOrbitalCoefficients", "Orbital coefficients") || !c) return;
+    if (res->wfn.C.empty()) {
+        env->error("Orbital coefficients are not available in results", "xtb_api_getOrbitalCoefficients");
+        return;
+    }
+    // the reference returns the Fortran array C(nao, nao) (AO index fastest), i.e. MO-major in C order
+    const int n = res->wfn.nao;
+    for (int mo = 0; mo < n; ++mo)
+        for (int mu = 0; mu < n; ++mu) c[(size_t)mo * n + mu] = res->wfn.C[(size_t)mu * n + mo];
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------ engine extensions (xtb_gb300.h)
+extern "C" {
+
+int xtbgb_deviceCount(void) { return xg::device_count(); }
+
+double xtbgb_fp64PeakTflops(void) {
+    if (xg::device_count() == 0) return 0.0;
+    try {
+        return xg::fp64_peak_tflops();
+    } catch (const std::exception&) {
+        return 0.0;
+    }
+}
+
+void xtbgb_getIterations(xtb_TEnvironment env, xtb_TResults res, int* iterations, int* converged) {
+    if (!res_ready(env, res, "xtbgb_getIterations", "SCC information")) return;
+    if (iterations) *iterations = res->sp.iterations;
+    if (converged) *converged = res->sp.converged ? 1 : 0;
+}
+
+void xtbgb_getEnergyParts(xtb_TEnvironment env, xtb_TResults res, double* parts) {
+    if (!res_ready(env, res, "xtbgb_getEnergyParts", "Energy parts") || !parts) return;
+    const auto& s = res->sp;
+    const double v[8] = {s.e_elec, s.e_rep, s.e_es, s.e_aes, s.e_axc, s.e_disp, s.e_atm, s.hl_gap};
+    std::copy(v, v + 8, parts);
+}
+
+void xtbgb_getPhaseTimes(xtb_TEnvironment env, xtb_TResults res, double* ms) {
+    if (!res_ready(env, res, "xtbgb_getPhaseTimes", "Timings") || !ms) return;
+    for (int k = 0; k < xg::PH_COUNT; ++k) ms[k] = k < (int)res->sp.phase_ms.size() ? res->sp.phase_ms[k] : 0.0;
+}
+
+void xtbgb_getTransferBytes(xtb_TEnvironment env, xtb_TResults res, long long* bytes) {
+    if (!res_ready(env, res, "xtbgb_getTransferBytes", "Transfer statistics") || !bytes) return;
+    bytes[0] = res->sp.h2d_bytes;
+    bytes[1] = res->sp.d2h_bytes;
+    bytes[2] = res->sp.launches;
+}
+
+void xtbgb_setKeepOrbitals(xtb_TEnvironment env, xtb_TCalculator calc, int keep) {
+    if (!check_env(env)) return;
+    if (!calc) {
+        env->error("Singlepoint calculator is not allocated", "xtbgb_setKeepOrbitals");
+        return;
+    }
+    calc->keep_orbitals = keep != 0;
+}
+
+void xtbgb_getShellCharges(xtb_TEnvironment env, xtb_TResults res, double* qsh) {
+    if (!res_ready(env, res, "xtbgb_getShellCharges", "Shell charges") || !qsh) return;
+    std::copy(res->wfn.qsh.begin(), res->wfn.qsh.end(), qsh);
+}
+
+void xtbgb_getMultipoles(xtb_TEnvironment env, xtb_TResults res, double* dipm, double* qp) {
+    if (!res_ready(env, res, "xtbgb_getMultipoles", "Multipoles")) return;
+    if (dipm) std::copy(res->wfn.dipm.begin(), res->wfn.dipm.end(), dipm);
+    if (qp) std::copy(res->wfn.qp.begin(), res->wfn.qp.end(), qp);
+}
+
+}  // extern "C"

@@ -1,0 +1,609 @@
+// Plain per-molecule FP64 GFN2-xTB single point: host orchestration of the device kernels.
+//
+// Follows scf (src/scf_module.F90:74-920) and scc (src/scc_core.f90:255-640):
+// set-up (CN, EEQ guess, integrals, Coulomb/AES/D4 kernels) -> SCC iterations
+// (potentials, H, generalised eigenproblem, Fermi smearing, density, Mulliken,
+// energies, Broyden) -> analytic gradient.  All O(N^2) and O(N^3) work runs on
+// the device; per iteration the host reads back four scalars for the
+// convergence test.
+#include <cmath>
+#include <cstring>
+#include <stdexcept>
+
+#include "engine.h"
+#include "gfn2_kernels.h"
+#include "linalg.h"
+
+namespace xg {
+
+long long& launch_counter() {
+    thread_local long long n = 0;
+    return n;
+}
+
+const char* const kPhaseNames[PH_COUNT] = {"setup", "integrals", "cholesky", "hbuild", "stdform", "sytrd",
+                                           "trieig", "backtransform", "density", "popmix", "gradient", "total"};
+
+int device_count() {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+namespace {
+
+// --------------------------------------------------------------- small kernels
+__global__ void k_self_energy(int nsh, const int* __restrict__ sh_atom, const double* __restrict__ se0,
+                              const double* __restrict__ kcn, const double* __restrict__ cn, double* __restrict__ se) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < nsh) se[s] = se0[s] - kcn[s] * cn[sh_atom[s]];
+}
+
+__global__ void k_ini_qsh(int nsh, const int* __restrict__ sh_atom, const double* __restrict__ zsh,
+                          const double* __restrict__ zval, const double* __restrict__ q, double* __restrict__ qsh) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < nsh) qsh[s] = zsh[s] / zval[sh_atom[s]] * q[sh_atom[s]];
+}
+
+__global__ void k_scale_energy_weights(int n, const double* __restrict__ focc, const double* __restrict__ emo,
+                                       double* __restrict__ fe) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) fe[i] = focc[i] * emo[i] * EVTOAU;
+}
+
+// SCC energy from the current populations (electro + aniso_electro + edisp_scc + entropy;
+// src/scc_core.f90:686-722, src/aespot.F90:566-664, src/disp/dftd4.F90:821-864)
+// out: [0] eel, [1] es, [2] eaes, [3] epol, [4] ed, [5] entropy term
+__global__ void k_scc_energy(int nsh, int nat, const double* __restrict__ qsh, const double* __restrict__ Jq,
+                             const double* __restrict__ gam3, const double* __restrict__ eh0,
+                             const double* __restrict__ eaes, const double* __restrict__ ed4,
+                             const double* __restrict__ fermi_scal, double* __restrict__ out) {
+    __shared__ double red[32];
+    double es = 0.0, h = 0.0, ea = 0.0, ep = 0.0, ed = 0.0;
+    for (int s = threadIdx.x; s < nsh; s += blockDim.x)
+        es += 0.5 * qsh[s] * Jq[s] + gam3[s] * qsh[s] * qsh[s] * qsh[s] / 3.0;
+    for (int a = threadIdx.x; a < nat; a += blockDim.x) {
+        h += eh0[a];
+        ea += eaes[a];
+        ep += eaes[nat + a];
+        ed += ed4[a];
+    }
+    es = block_sum(es, red);
+    h = block_sum(h, red);
+    ea = block_sum(ea, red);
+    ep = block_sum(ep, red);
+    ed = block_sum(ed, red);
+    if (threadIdx.x == 0) {
+        const double ts = fermi_scal[0];
+        out[0] = es + h * EVTOAU + ea + ep + ed + ts;
+        out[1] = es;
+        out[2] = ea;
+        out[3] = ep;
+        out[4] = ed;
+        out[5] = ts;
+    }
+}
+
+// dipole moment (calc_dipole, src/dipole.f90:94-128) from the population row sums
+__global__ void k_dipole(int nat, int nao, const double* __restrict__ xyz, const double* __restrict__ zval,
+                         const double* __restrict__ rows, double* __restrict__ out) {
+    __shared__ double red[32];
+    for (int k = 0; k < 3; ++k) {
+        double s = 0.0;
+        for (int a = threadIdx.x; a < nat; a += blockDim.x) s += xyz[3 * a + k] * zval[a];
+        for (int mu = threadIdx.x; mu < nao; mu += blockDim.x) s -= rows[(size_t)mu * 12 + 1 + k];
+        s = block_sum(s, red);
+        if (threadIdx.x == 0) out[k] = s;
+    }
+}
+
+// Wiberg-Mayer bond orders from PS (get_wiberg, src/scc_core.f90:1208-1245); one warp per atom pair
+__global__ void k_wiberg(int nat, int nao, const double* __restrict__ xyz, const int* __restrict__ ao0,
+                         const int* __restrict__ nao_at, const double* __restrict__ PS, double* __restrict__ wbo) {
+    const long w = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (w >= (long)nat * nat) return;
+    const int i = (int)(w / nat), j = (int)(w % nat);
+    double s = 0.0;
+    if (i != j) {
+        const double r2 = (xyz[3 * i] - xyz[3 * j]) * (xyz[3 * i] - xyz[3 * j]) +
+                          (xyz[3 * i + 1] - xyz[3 * j + 1]) * (xyz[3 * i + 1] - xyz[3 * j + 1]) +
+                          (xyz[3 * i + 2] - xyz[3 * j + 2]) * (xyz[3 * i + 2] - xyz[3 * j + 2]);
+        if (r2 < 100.0) {
+            const int ni = nao_at[i], nj = nao_at[j];
+            for (int t = lane; t < ni * nj; t += 32) {
+                const int k = ao0[i] + t / nj, mm = ao0[j] + t % nj;
+                s += PS[(size_t)k * nao + mm] * PS[(size_t)mm * nao + k];
+            }
+        }
+    }
+    s = warp_sum(s);
+    if (lane == 0) wbo[w] = s;
+}
+
+// --------------------------------------------------------------- device workspace
+struct Arena {
+    char* base = nullptr;
+    size_t cap = 0, used = 0;
+    bool counting = false;
+    void reset(size_t need) {
+        counting = false;
+        need += 4096;
+        if (need > cap) {
+            if (base) cudaFree(base);
+            base = nullptr;
+            cap = 0;
+            XG_CUDA(cudaMalloc(&base, need));
+            cap = need;
+        }
+        used = 0;
+    }
+    template <typename T>
+    T* take(size_t count) {
+        const size_t bytes = ((count * sizeof(T) + 255) / 256) * 256;
+        if (counting) {
+            used += bytes;
+            return nullptr;
+        }
+        if (used + bytes > cap) throw CudaError("workspace overflow");
+        T* p = reinterpret_cast<T*>(base + used);
+        used += bytes;
+        return p;
+    }
+};
+
+struct Sizer {
+    size_t bytes = 0;
+    template <typename T>
+    void add(size_t count) { bytes += ((count * sizeof(T) + 255) / 256) * 256; }
+};
+
+thread_local Arena g_arena;
+thread_local cudaStream_t g_stream = nullptr;
+
+// CUDA-event phase timer on the engine stream; elapsed times are read after the final sync.
+struct PhaseTimer {
+    std::vector<cudaEvent_t> pool;
+    std::vector<std::pair<int, std::pair<int, int>>> spans;   // phase, (start event, stop event)
+    size_t next = 0;
+    cudaStream_t st = nullptr;
+    int open_phase = -1, open_ev = -1;
+    cudaEvent_t get() {
+        if (next == pool.size()) {
+            cudaEvent_t e;
+            XG_CUDA(cudaEventCreate(&e));
+            pool.push_back(e);
+        }
+        return pool[next++];
+    }
+    void begin(cudaStream_t s) { st = s; next = 0; spans.clear(); open_phase = -1; }
+    void start(int ph) {
+        const int idx = (int)next;
+        XG_CUDA(cudaEventRecord(get(), st));
+        open_phase = ph;
+        open_ev = idx;
+    }
+    void stop() {
+        const int idx = (int)next;
+        XG_CUDA(cudaEventRecord(get(), st));
+        spans.push_back({open_phase, {open_ev, idx}});
+    }
+    void mark(int ph) {   // stop the open phase and start the next one
+        if (open_phase >= 0) stop();
+        start(ph);
+    }
+    std::vector<double> collect() {
+        std::vector<double> ms(PH_COUNT, 0.0);
+        for (auto& sp : spans) {
+            float t = 0.0f;
+            XG_CUDA(cudaEventElapsedTime(&t, pool[sp.second.first], pool[sp.second.second]));
+            ms[sp.first] += t;
+        }
+        return ms;
+    }
+};
+thread_local PhaseTimer g_timer;
+
+thread_local long long g_h2d = 0;
+
+template <typename T>
+T* upload(Arena& ar, cudaStream_t st, const std::vector<T>& v) {
+    T* d = ar.take<T>(std::max<size_t>(v.size(), 1));
+    if (!ar.counting && !v.empty()) {
+        XG_CUDA(cudaMemcpyAsync(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st));
+        g_h2d += (long long)(v.size() * sizeof(T));
+    }
+    return d;
+}
+
+}  // namespace
+
+void run_singlepoint(const HostMol& hm, const SPSettings& set, Wavefunction& wfn, SPResult& res, bool keep_orbitals,
+                     bool& scc_failed) {
+    if (device_count() == 0) throw CudaError("no CUDA device available for the GFN2 engine");
+    if (!g_stream) XG_CUDA(cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking));
+    cudaStream_t st = g_stream;
+    const int nat = hm.nat, nsh = hm.nsh, nao = hm.nao, ne = hm.nelem;
+    const size_t nn = (size_t)nao * nao;
+    const size_t aa = (size_t)nat * nat;
+    const int maxit = std::max(1, set.maxiter);
+    const int nbr = nsh + 9 * nat;
+
+    // ---- thresholds (src/scf_module.F90:266-277)
+    const double acc = set.accuracy;
+    Thresholds th;
+    th.intcut = std::max(20.0, 25.0 - 10.0 * std::log10(acc));
+    th.neglect = 10.0e-9 * acc;
+    const double scfconv = 1.0e-6 * acc;
+    const double qconv = 1.0e-4 * acc;
+
+    g_h2d = 0;
+    long long d2h = 0;
+    const long long launches0 = launch_counter();
+    PhaseTimer& tm = g_timer;
+    tm.begin(st);
+    const int total_ev = (int)tm.next;
+    XG_CUDA(cudaEventRecord(tm.get(), st));
+    tm.start(PH_SETUP);
+    // ---- workspace: exact two-pass layout (count, allocate, carve)
+    Arena& ar = g_arena;
+    DevMol m;
+    const double* d_zval = nullptr;
+    double *S, *D, *Q, *H0, *X, *H, *A, *T1, *C, *Pm, *Wm, *V, *Y, *Zt, *iscr, *J, *gab3, *gab5, *c6, *dc6, *c6z,
+        *dc6z, *eeqA, *eeqX, *cn_gfn, *cn_tmp, *se, *q, *qsh, *dipm, *qp, *shift, *Jq, *vs, *vd, *vq, *radcn, *gw, *dgw,
+        *zeta, *dzeta, *Wz, *zv, *zr, *zdcn, *zrdcn, *vat, *ed4, *eh0, *eaes, *erep, *e2, *e3, *grad, *dhdcn, *tmp2,
+        *rows, *emo, *focc, *fe, *tri_d, *tri_e, *tri_e2, *tri_tau, *tri_p, *bounds, *fscal, *escal, *rms, *dip, *qin,
+        *qout, *dq;
+    unsigned char* piv;
+    int* info;
+    BroydenState bs;
+    auto layout = [&]() {
+    // ---- upload molecule
+    m.nat = nat; m.nsh = nsh; m.nao = nao; m.nelem = ne;
+    m.Z = upload(ar, st, hm.Z);
+    m.eid = upload(ar, st, hm.eid);
+    m.xyz = upload(ar, st, hm.xyz);
+    m.at_sh0 = upload(ar, st, hm.at_sh0);
+    m.at_nsh = upload(ar, st, hm.at_nsh);
+    m.at_ao0 = upload(ar, st, hm.at_ao0);
+    m.at_nao = upload(ar, st, hm.at_nao);
+    m.rcov = upload(ar, st, hm.rcov);
+    m.en = upload(ar, st, hm.en);
+    m.rcov4 = upload(ar, st, hm.rcov4);
+    m.en4 = upload(ar, st, hm.en4);
+    m.eeq_en = upload(ar, st, hm.eeq_en);
+    m.eeq_gam = upload(ar, st, hm.eeq_gam);
+    m.eeq_kappa = upload(ar, st, hm.eeq_kappa);
+    m.eeq_alpha = upload(ar, st, hm.eeq_alpha);
+    m.mrad = upload(ar, st, hm.mrad);
+    m.valcn = upload(ar, st, hm.valcn);
+    m.dkern = upload(ar, st, hm.dkern);
+    m.qkern = upload(ar, st, hm.qkern);
+    m.rep_alpha = upload(ar, st, hm.rep_alpha);
+    m.rep_zeff = upload(ar, st, hm.rep_zeff);
+    m.r4r2 = upload(ar, st, hm.r4r2);
+    m.arad = upload(ar, st, hm.arad);
+    m.d4_nref = upload(ar, st, hm.d4_nref);
+    m.d4_zeff = upload(ar, st, hm.d4_zeff);
+    m.d4_gam = upload(ar, st, hm.d4_gam);
+    m.d4_refq = upload(ar, st, hm.d4_refq);
+    m.d4_refcn = upload(ar, st, hm.d4_refcn);
+    m.d4_ncount = upload(ar, st, hm.d4_ncount);
+    m.d4_c6 = upload(ar, st, hm.d4_c6);
+    m.sh_atom = upload(ar, st, hm.sh_atom);
+    m.sh_l = upload(ar, st, hm.sh_l);
+    m.sh_ao = upload(ar, st, hm.sh_ao);
+    m.sh_nprim = upload(ar, st, hm.sh_nprim);
+    m.sh_alpha = upload(ar, st, hm.sh_alpha);
+    m.sh_coef = upload(ar, st, hm.sh_coef);
+    m.sh_zeta = upload(ar, st, hm.sh_zeta);
+    m.sh_se0 = upload(ar, st, hm.sh_se0);
+    m.sh_kcn = upload(ar, st, hm.sh_kcn);
+    m.sh_poly = upload(ar, st, hm.sh_poly);
+    m.sh_eta = upload(ar, st, hm.sh_eta);
+    m.sh_gam3 = upload(ar, st, hm.sh_gam3);
+    m.sh_zsh = upload(ar, st, hm.sh_zsh);
+    m.ao_sh = upload(ar, st, hm.ao_sh);
+    m.ao_at = upload(ar, st, hm.ao_at);
+    d_zval = upload(ar, st, hm.zval);
+
+    // ---- device buffers
+    S = ar.take<double>(nn);
+    D = ar.take<double>(3 * nn);
+    Q = ar.take<double>(6 * nn);
+    H0 = ar.take<double>(nn);
+    X = ar.take<double>(nn);
+    H = ar.take<double>(nn);
+    A = ar.take<double>(nn);
+    T1 = ar.take<double>(nn);
+    C = ar.take<double>(nn);
+    Pm = ar.take<double>(nn);
+    Wm = ar.take<double>(nn);
+    V = ar.take<double>(nn);
+    Y = ar.take<double>(nn);
+    Zt = ar.take<double>(nn);
+    iscr = ar.take<double>(4 * nn);
+    piv = ar.take<unsigned char>(nn);
+    J = ar.take<double>((size_t)nsh * nsh);
+    gab3 = ar.take<double>(aa);
+    gab5 = ar.take<double>(aa);
+    c6 = ar.take<double>(aa);
+    dc6 = ar.take<double>(aa);
+    c6z = ar.take<double>(aa);
+    dc6z = ar.take<double>(aa);
+    eeqA = ar.take<double>(std::max(aa, (size_t)1));
+    eeqX = ar.take<double>(2 * (size_t)nat);
+    cn_gfn = ar.take<double>(nat);
+    cn_tmp = ar.take<double>(nat);
+    se = ar.take<double>(nsh);
+    q = ar.take<double>(nat);
+    qsh = ar.take<double>(nsh);
+    dipm = ar.take<double>(3 * (size_t)nat);
+    qp = ar.take<double>(6 * (size_t)nat);
+    shift = ar.take<double>(nsh);
+    Jq = ar.take<double>(nsh);
+    vs = ar.take<double>(nat);
+    vd = ar.take<double>(3 * (size_t)nat);
+    vq = ar.take<double>(6 * (size_t)nat);
+    radcn = ar.take<double>(nat);
+    gw = ar.take<double>((size_t)nat * MAXREF);
+    dgw = ar.take<double>((size_t)nat * MAXREF);
+    zeta = ar.take<double>((size_t)nat * MAXREF);
+    dzeta = ar.take<double>((size_t)nat * MAXREF);
+    Wz = ar.take<double>((size_t)nat * MAXREF);
+    zv = ar.take<double>((size_t)nat * MAXREF);
+    zr = ar.take<double>((size_t)nat * MAXREF);
+    zdcn = ar.take<double>((size_t)nat * MAXREF);
+    zrdcn = ar.take<double>((size_t)nat * MAXREF);
+    vat = ar.take<double>(nat);
+    ed4 = ar.take<double>(nat);
+    eh0 = ar.take<double>(nat);
+    eaes = ar.take<double>(2 * (size_t)nat);
+    erep = ar.take<double>(nat);
+    e2 = ar.take<double>(nat);
+    e3 = ar.take<double>(((size_t)nat * (nat + 1)) / 2 + 1);
+    grad = ar.take<double>(3 * (size_t)nat);
+    dhdcn = ar.take<double>(nat);
+    tmp2 = ar.take<double>(nat);
+    rows = ar.take<double>((size_t)nao * 12);
+    emo = ar.take<double>(nao);
+    focc = ar.take<double>(nao);
+    fe = ar.take<double>(nao);
+    tri_d = ar.take<double>(nao);
+    tri_e = ar.take<double>(nao);
+    tri_e2 = ar.take<double>(nao);
+    tri_tau = ar.take<double>(nao);
+    tri_p = ar.take<double>(nao);
+    bounds = ar.take<double>(8);
+    fscal = ar.take<double>(8 + (size_t)nao);
+    escal = ar.take<double>(16);
+    rms = ar.take<double>(4);
+    dip = ar.take<double>(4);
+    qin = ar.take<double>(nbr);
+    qout = ar.take<double>(nbr);
+    dq = ar.take<double>(nbr);
+    info = ar.take<int>(4);
+    bs.nbr = nbr;
+    bs.maxit = maxit;
+    bs.df = ar.take<double>((size_t)maxit * nbr);
+    bs.u = ar.take<double>((size_t)maxit * nbr);
+    bs.a = ar.take<double>((size_t)maxit * maxit);
+    bs.omega = ar.take<double>(maxit);
+    bs.qlast = ar.take<double>(nbr);
+    bs.dqlast = ar.take<double>(nbr);
+    bs.scratch = ar.take<double>(2 * (size_t)maxit * maxit + 2 * (size_t)maxit + 64);
+
+    };
+    ar.counting = true;
+    ar.used = 0;
+    layout();
+    const size_t need = ar.used;
+    ar.reset(need);
+    layout();
+
+    XG_CUDA(cudaMemsetAsync(grad, 0, 3 * (size_t)nat * sizeof(double), st));
+    XG_CUDA(cudaMemsetAsync(dhdcn, 0, nat * sizeof(double), st));
+
+    // ---- coordination number, self energies
+    cn(st, m, 0, cn_gfn);
+    k_self_energy<<<ceil_div(nsh, 128), 128, 0, st>>>(nsh, m.sh_atom, m.sh_se0, m.sh_kcn, cn_gfn, se);
+    XG_LAUNCH_CHECK();
+
+    // ---- initial charges: warm start or EEQ guess (newWavefunction, src/xtb/calculator.f90:432-496)
+    const bool warm = wfn.valid() && wfn.nat == nat && wfn.nao == nao && wfn.nsh == nsh;
+    if (warm) {
+        XG_CUDA(cudaMemcpyAsync(qsh, wfn.qsh.data(), nsh * sizeof(double), cudaMemcpyHostToDevice, st));
+        XG_CUDA(cudaMemcpyAsync(dipm, wfn.dipm.data(), 3 * nat * sizeof(double), cudaMemcpyHostToDevice, st));
+        XG_CUDA(cudaMemcpyAsync(qp, wfn.qp.data(), 6 * nat * sizeof(double), cudaMemcpyHostToDevice, st));
+    } else {
+        cn(st, m, 2, cn_tmp);
+        eeq_setup(st, m, cn_tmp, eeqA, eeqX);
+        potrf_upper(st, nat, eeqA, nat, info);
+        eeq_finish(st, nat, eeqA, eeqX, hm.charge, q, nullptr);
+        int hinfo = 0;
+        XG_CUDA(cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, st));
+        XG_CUDA(cudaStreamSynchronize(st));
+        if (hinfo != 0) {
+            // EEQ guess failed: uniform charges (the reference's rescue path)
+            std::vector<double> qq(nat, hm.charge / nat);
+            XG_CUDA(cudaMemcpyAsync(q, qq.data(), nat * sizeof(double), cudaMemcpyHostToDevice, st));
+        }
+        k_ini_qsh<<<ceil_div(nsh, 128), 128, 0, st>>>(nsh, m.sh_atom, m.sh_zsh, d_zval, q, qsh);
+        XG_LAUNCH_CHECK();
+        XG_CUDA(cudaMemsetAsync(dipm, 0, 3 * (size_t)nat * sizeof(double), st));
+        XG_CUDA(cudaMemsetAsync(qp, 0, 6 * (size_t)nat * sizeof(double), st));
+    }
+    broyden_pack(st, m, qsh, dipm, qp, qin);
+    broyden_unpack(st, m, qin, qsh, dipm, qp, q);   // q = sum of qsh (qsh2qat)
+
+    // ---- classical terms and integrals
+    repulsion(st, m, erep, grad);
+    tm.mark(PH_INTEGRALS);
+    build_sdqh0(st, m, se, th, S, D, Q, H0);
+    aes_setup(st, m, cn_gfn, radcn, gab3, gab5);
+    coulomb_matrix(st, m, J);
+    cn(st, m, 3, cn_tmp);
+    d4_weights(st, m, cn_tmp, gw, nullptr);
+    // S = U^T U, X = U^-1
+    tm.mark(PH_CHOLESKY);
+    XG_CUDA(cudaMemcpyAsync(T1, S, nn * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    potrf_upper(st, nao, T1, nao, info);
+    trinv_upper(st, nao, T1, nao, X, nao);
+    {
+        int hinfo = 0;
+        XG_CUDA(cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, st));
+        XG_CUDA(cudaStreamSynchronize(st));
+        if (hinfo != 0) throw std::runtime_error("overlap matrix is not positive definite (Cholesky failed)");
+    }
+
+    // ---- SCC iterations
+    double eel = 0.0, eold = 0.0;
+    bool lastdiag = false, converged = false;
+    int iter = 0;
+    double hsc[8] = {0};
+    for (int it = 1; it <= maxit; ++it) {
+        iter = it;
+        tm.mark(PH_HBUILD);
+        d4_scc(st, m, gw, q, zeta, dzeta, Wz, vat, ed4);
+        shell_shift(st, m, J, qsh, vat, shift, Jq);
+        aes_potential(st, m, q, dipm, qp, gab3, gab5, true, vs, vd, vq);
+        build_h(st, m, th, H0, S, D, Q, shift, vs, vd, vq, H);
+        // standard form A = X^T H X, eigenpairs, back-transformation
+        tm.mark(PH_STDFORM);
+        dgemm(st, false, false, nao, nao, nao, 1.0, H, nao, X, nao, 0.0, T1, nao);
+        dgemm(st, true, false, nao, nao, nao, 1.0, X, nao, T1, nao, 0.0, A, nao);
+        tm.mark(PH_SYTRD);
+        sytrd(st, nao, A, nao, V, tri_tau, tri_d, tri_e, tri_p);
+        tm.mark(PH_TRIEIG);
+        tridiag_eig(st, nao, tri_d, tri_e, tri_e2, bounds, emo, Y, iscr, piv);
+        tm.mark(PH_BACKTR);
+        ormtr(st, nao, V, tri_tau, Y, Zt);
+        dgemm(st, false, true, nao, nao, nao, 1.0, X, nao, Zt, nao, 0.0, C, nao);
+        tm.mark(PH_DENSITY);
+        fermi(st, nao, emo, hm.nel_a, hm.nel_b, set.etemp, focc, fscal);
+        scale_cols(st, nao, C, focc, T1);
+        dgemm(st, false, true, nao, nao, nao, 1.0, T1, nao, C, nao, 0.0, Pm, nao);
+        tm.mark(PH_POPMIX);
+        populations(st, m, Pm, S, D, Q, H0, rows, qsh, q, dipm, qp, eh0);
+        shell_shift(st, m, J, qsh, nullptr, T1, Jq);    // Jq for the electrostatic energy
+        aes_energy(st, m, q, dipm, qp, gab3, gab5, eaes);
+        d4_scc(st, m, gw, q, zeta, dzeta, Wz, vat, ed4);
+        k_scc_energy<<<1, 512, 0, st>>>(nsh, nat, qsh, Jq, m.sh_gam3, eh0, eaes, ed4, fscal, escal);
+        XG_LAUNCH_CHECK();
+        broyden_pack(st, m, qsh, dipm, qp, qout);
+        broyden_step(st, bs, it, 0.4, qin, qout, dq, rms, nat);
+        broyden_unpack(st, m, qin, qsh, dipm, qp, q);
+        XG_CUDA(cudaMemcpyAsync(hsc, escal, 6 * sizeof(double), cudaMemcpyDeviceToHost, st));
+        double hrms[2];
+        XG_CUDA(cudaMemcpyAsync(hrms, rms, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+        XG_CUDA(cudaStreamSynchronize(st));
+        d2h += 8 * sizeof(double);
+        eold = eel;
+        eel = hsc[0];
+        const bool econv = std::fabs(eel - eold) < scfconv;
+        const bool qconvd = hrms[0] < qconv;
+        if (!std::isfinite(eel)) throw std::runtime_error("SCC energy is not finite");
+        if (econv && qconvd) {
+            converged = true;
+            if (lastdiag) break;
+            lastdiag = true;
+        }
+    }
+    scc_failed = !converged;
+
+    // ---- gradient (src/scf_module.F90:665-798)
+    tm.mark(PH_GRADIENT);
+    k_scale_energy_weights<<<ceil_div(nao, 128), 128, 0, st>>>(nao, focc, emo, fe);
+    XG_LAUNCH_CHECK();
+    scale_cols(st, nao, C, fe, T1);
+    dgemm(st, false, true, nao, nao, nao, 1.0, T1, nao, C, nao, 0.0, Wm, nao);
+    aes_potential(st, m, q, dipm, qp, gab3, gab5, false, vs, vd, vq);
+    grad_sdqh0(st, m, th, se, Pm, Wm, shift, vs, vd, vq, grad, dhdcn);
+    dhdcn_diag(st, m, Pm, dhdcn);
+    aes_grad(st, m, q, dipm, qp, radcn, gab3, gab5, grad, tmp2);
+    aes_dradcn(st, m, cn_gfn, tmp2, dhdcn);
+    cn_chain(st, m, 0, dhdcn, grad);
+    // D4 two-body and ATM at the final charges, covalent CN
+    cn(st, m, 1, cn_tmp);
+    XG_CUDA(cudaMemsetAsync(tmp2, 0, nat * sizeof(double), st));
+    d4_grad(st, m, cn_tmp, q, gw, dgw, zv, zr, zdcn, zrdcn, c6, dc6, c6z, dc6z, e2, e3, tmp2, grad);
+    cn_chain(st, m, 1, tmp2, grad);
+    coulomb_grad(st, m, qsh, grad);
+    k_dipole<<<1, 256, 0, st>>>(nat, nao, m.xyz, d_zval, rows, dip);
+    XG_LAUNCH_CHECK();
+    const bool closed = hm.nel_a == hm.nel_b;
+    if (closed) {
+        dgemm(st, false, false, nao, nao, nao, 1.0, Pm, nao, S, nao, 0.0, T1, nao);
+        k_wiberg<<<ceil_div((long)aa * 32, 256), 256, 0, st>>>(nat, nao, m.xyz, m.at_ao0, m.at_nao, T1, c6);
+        XG_LAUNCH_CHECK();
+    }
+    reduce_sum(st, erep, nat, escal + 8);
+    reduce_sum(st, e3, (int)(((size_t)nat * (nat + 1)) / 2), escal + 9);
+
+    tm.stop();
+    const int total_end = (int)tm.next;
+    XG_CUDA(cudaEventRecord(tm.get(), st));
+    // ---- results
+    double hs2[2];
+    res.gradient.assign(3 * (size_t)nat, 0.0);
+    res.dipole.assign(3, 0.0);
+    if (closed) {
+        res.wbo.assign(aa, 0.0);
+        XG_CUDA(cudaMemcpyAsync(res.wbo.data(), c6, aa * sizeof(double), cudaMemcpyDeviceToHost, st));
+    } else {
+        res.wbo.clear();
+    }
+    wfn.nat = nat; wfn.nao = nao; wfn.nsh = nsh;
+    wfn.q.resize(nat); wfn.qsh.resize(nsh); wfn.dipm.resize(3 * nat); wfn.qp.resize(6 * nat);
+    wfn.emo.resize(nao); wfn.focc.resize(nao);
+    XG_CUDA(cudaMemcpyAsync(hs2, escal + 8, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    XG_CUDA(cudaMemcpyAsync(res.gradient.data(), grad, 3 * nat * sizeof(double), cudaMemcpyDeviceToHost, st));
+    XG_CUDA(cudaMemcpyAsync(res.dipole.data(), dip, 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    XG_CUDA(cudaMemcpyAsync(wfn.q.data(), q, nat * sizeof(double), cudaMemcpyDeviceToHost, st));
+    XG_CUDA(cudaMemcpyAsync(wfn.qsh.data(), qsh, nsh * sizeof(double), cudaMemcpyDeviceToHost, st));
+    XG_CUDA(cudaMemcpyAsync(wfn.dipm.data(), dipm, 3 * nat * sizeof(double), cudaMemcpyDeviceToHost, st));
+    XG_CUDA(cudaMemcpyAsync(wfn.qp.data(), qp, 6 * nat * sizeof(double), cudaMemcpyDeviceToHost, st));
+    XG_CUDA(cudaMemcpyAsync(wfn.emo.data(), emo, nao * sizeof(double), cudaMemcpyDeviceToHost, st));
+    XG_CUDA(cudaMemcpyAsync(wfn.focc.data(), focc, nao * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (keep_orbitals) {
+        wfn.C.resize(nn); wfn.P.resize(nn); wfn.S.resize(nn);
+        XG_CUDA(cudaMemcpyAsync(wfn.C.data(), C, nn * sizeof(double), cudaMemcpyDeviceToHost, st));
+        XG_CUDA(cudaMemcpyAsync(wfn.P.data(), Pm, nn * sizeof(double), cudaMemcpyDeviceToHost, st));
+        XG_CUDA(cudaMemcpyAsync(wfn.S.data(), S, nn * sizeof(double), cudaMemcpyDeviceToHost, st));
+    } else {
+        wfn.C.clear(); wfn.P.clear(); wfn.S.clear();
+    }
+    XG_CUDA(cudaStreamSynchronize(st));
+    d2h += (long long)sizeof(double) * (2 + 3 * nat + 3 + nat + nsh + 9 * nat + 2 * nao + (closed ? aa : 0) +
+                                        (keep_orbitals ? 3 * nn : 0));
+    res.h2d_bytes = g_h2d;
+    res.launches = launch_counter() - launches0;
+    res.d2h_bytes = d2h;
+    for (auto& e : wfn.emo) e *= EVTOAU;   // orbital energies are reported in Hartree
+    res.phase_ms = tm.collect();
+    {
+        float t = 0.0f;
+        XG_CUDA(cudaEventElapsedTime(&t, tm.pool[total_ev], tm.pool[total_end]));
+        res.phase_ms[PH_TOTAL] = t;
+    }
+    res.e_rep = hs2[0];
+    res.e_atm = hs2[1];
+    res.energy = eel + hs2[0] + hs2[1];
+    res.e_elec = eel + hs2[1];
+    res.e_es = hsc[1];
+    res.e_aes = hsc[2];
+    res.e_axc = hsc[3];
+    res.e_disp = hsc[4] + hs2[1];
+    res.iterations = iter;
+    res.converged = converged;
+    const int ih = hm.nel_a;
+    res.hl_gap = (ih >= 1 && ih < nao) ? (wfn.emo[ih] - wfn.emo[ih - 1]) * AUTOEV : 0.0;
+    double g2 = 0.0;
+    for (double g : res.gradient) g2 += g * g;
+    res.gnorm = std::sqrt(g2);
+}
+
+}  // namespace xg

@@ -1,0 +1,72 @@
+// Plain per-molecule FP64 GFN2-xTB single point on one GPU (host orchestration).
+#pragma once
+#include <string>
+#include <vector>
+
+#include "host_model.h"
+
+namespace xg {
+
+struct SPSettings {
+    double accuracy = 1.0;     // xtb_setAccuracy
+    double etemp = 300.0;      // xtb_setElectronicTemp (K)
+    int maxiter = 250;         // xtb_setMaxIter
+};
+
+// Wavefunction kept between calls on the same results object (res%chk of the reference).
+struct Wavefunction {
+    int nat = 0, nao = 0, nsh = 0;
+    std::vector<double> q, qsh, dipm, qp;       // converged (mixed) charges and moments
+    std::vector<double> emo, focc;              // orbital energies (Eh) and occupations
+    std::vector<double> C;                      // MO coefficients [nao][nao] (row AO, column MO)
+    std::vector<double> P;                      // density matrix
+    std::vector<double> S;                      // overlap
+    bool valid() const { return nat > 0; }
+};
+
+struct SPResult {
+    double energy = 0.0;
+    std::vector<double> gradient;               // [nat][3]
+    std::vector<double> dipole;                 // [3]
+    std::vector<double> wbo;                    // [nat][nat] Wiberg bond orders (closed shell)
+    double hl_gap = 0.0;                        // eV
+    int iterations = 0;
+    bool converged = false;
+    // energy parts (Eh)
+    double e_elec = 0, e_rep = 0, e_es = 0, e_aes = 0, e_axc = 0, e_disp = 0, e_atm = 0;
+    double gnorm = 0.0;
+    // device time per phase (ms), measured with CUDA events on the engine stream
+    std::vector<double> phase_ms;
+    // bytes copied host->device and device->host by this single point
+    long long h2d_bytes = 0, d2h_bytes = 0;
+    long long launches = 0;   // device kernels launched by this single point
+};
+
+// phases timed inside run_singlepoint
+enum Phase {
+    PH_SETUP = 0,      // uploads, CN, EEQ guess, repulsion
+    PH_INTEGRALS,      // S, D, Q, H0 and the Coulomb / AES / D4 kernels
+    PH_CHOLESKY,       // S = U^T U, X = U^-1
+    PH_HBUILD,         // potentials and H
+    PH_STDFORM,        // A = X^T H X (two FP64 GEMMs)
+    PH_SYTRD,          // Householder tridiagonalisation
+    PH_TRIEIG,         // bisection + inverse iteration (+ cluster re-orthogonalisation)
+    PH_BACKTR,         // Q Y and C = X Z
+    PH_DENSITY,        // Fermi smearing and P = C f C^T
+    PH_POPMIX,         // populations, energies, Broyden
+    PH_GRADIENT,       // analytic gradient
+    PH_TOTAL,          // whole single point on the device stream
+    PH_COUNT
+};
+extern const char* const kPhaseNames[PH_COUNT];
+
+// Run the single point.  `wfn` is the warm-start wavefunction (used when sizes
+// match) and receives the converged one.  Throws std::runtime_error on failure;
+// `scc_failed` reports an unconverged SCC (results still filled).
+void run_singlepoint(const HostMol& hm, const SPSettings& set, Wavefunction& wfn, SPResult& res, bool keep_orbitals,
+                     bool& scc_failed);
+
+// Number of CUDA devices visible (0 when none); never throws.
+int device_count();
+
+}  // namespace xg

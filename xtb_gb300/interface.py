@@ -1,0 +1,200 @@
+"""Python host interface over the C ABI of libxtb_gb300.so.
+
+Mirrors the reference C API (include/xtb.h) one call per method, so a caller
+drives exactly the same sequence as a C program: environment -> molecule ->
+calculator (GFN2-xTB) -> single point -> results getters.  Errors pushed onto
+the environment are raised as ``XTBException`` after each call.
+
+The library is loaded from this package directory; there is no fallback: if the
+compiled engine is missing, importing the loader raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIBPATH = os.path.join(_HERE, "libxtb_gb300.so")
+
+_lib = None
+PHASES = ("setup", "integrals", "cholesky", "hbuild", "stdform", "sytrd", "trieig", "backtransform", "density",
+          "popmix", "gradient", "total")
+
+
+class XTBException(RuntimeError):
+    pass
+
+
+def load_library(path=LIBPATH):
+    """Load the engine library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise XTBException(f"{path} not found: build it with `python -m xtb_gb300.build`")
+    lib = C.CDLL(path)
+    vp, dp, ip = C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int)
+    sig = {
+        "xtb_getAPIVersion": (C.c_int, []),
+        "xtb_newEnvironment": (vp, []),
+        "xtb_delEnvironment": (None, [C.POINTER(vp)]),
+        "xtb_checkEnvironment": (C.c_int, [vp]),
+        "xtb_showEnvironment": (None, [vp, C.c_char_p]),
+        "xtb_getError": (None, [vp, C.c_char_p, ip]),
+        "xtb_setOutput": (None, [vp, C.c_char_p]),
+        "xtb_releaseOutput": (None, [vp]),
+        "xtb_setVerbosity": (None, [vp, C.c_int]),
+        "xtb_newMolecule": (vp, [vp, ip, ip, dp, dp, ip, dp, C.POINTER(C.c_bool)]),
+        "xtb_delMolecule": (None, [C.POINTER(vp)]),
+        "xtb_updateMolecule": (None, [vp, vp, dp, dp]),
+        "xtb_newCalculator": (vp, []),
+        "xtb_delCalculator": (None, [C.POINTER(vp)]),
+        "xtb_loadGFN2xTB": (None, [vp, vp, vp, C.c_char_p]),
+        "xtb_setAccuracy": (None, [vp, vp, C.c_double]),
+        "xtb_setMaxIter": (None, [vp, vp, C.c_int]),
+        "xtb_setElectronicTemp": (None, [vp, vp, C.c_double]),
+        "xtb_singlepoint": (None, [vp, vp, vp, vp]),
+        "xtb_newResults": (vp, []),
+        "xtb_delResults": (None, [C.POINTER(vp)]),
+        "xtb_copyResults": (vp, [vp]),
+        "xtb_getEnergy": (None, [vp, vp, dp]),
+        "xtb_getGradient": (None, [vp, vp, dp]),
+        "xtb_getCharges": (None, [vp, vp, dp]),
+        "xtb_getDipole": (None, [vp, vp, dp]),
+        "xtb_getBondOrders": (None, [vp, vp, dp]),
+        "xtb_getNao": (None, [vp, vp, ip]),
+        "xtb_getOrbitalEigenvalues": (None, [vp, vp, dp]),
+        "xtb_getOrbitalOccupations": (None, [vp, vp, dp]),
+        "xtb_getOrbitalCoefficients": (None, [vp, vp, dp]),
+        "xtbgb_deviceCount": (C.c_int, []),
+        "xtbgb_getIterations": (None, [vp, vp, ip, ip]),
+        "xtbgb_getEnergyParts": (None, [vp, vp, dp]),
+        "xtbgb_getShellCharges": (None, [vp, vp, dp]),
+        "xtbgb_getMultipoles": (None, [vp, vp, dp, dp]),
+        "xtbgb_getPhaseTimes": (None, [vp, vp, dp]),
+        "xtbgb_getTransferBytes": (None, [vp, vp, C.POINTER(C.c_longlong)]),
+        "xtbgb_setKeepOrbitals": (None, [vp, vp, C.c_int]),
+        "xtbgb_fp64PeakTflops": (C.c_double, []),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _dptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class Environment:
+    def __init__(self, verbosity=0):
+        self.lib = load_library()
+        self.h = C.c_void_p(self.lib.xtb_newEnvironment())
+        self.lib.xtb_setVerbosity(self.h, verbosity)
+
+    def check(self):
+        if self.lib.xtb_checkEnvironment(self.h):
+            buf = C.create_string_buffer(4096)
+            n = C.c_int(4096)
+            self.lib.xtb_getError(self.h, buf, C.byref(n))
+            raise XTBException(buf.value.decode())
+
+    def __del__(self):
+        if getattr(self, "h", None) is not None and self.lib is not None:
+            self.lib.xtb_delEnvironment(C.byref(self.h))
+
+
+class Calculator:
+    """GFN2-xTB single point through the C ABI (numbers, positions in Bohr)."""
+
+    def __init__(self, numbers, positions, charge=0.0, uhf=0, accuracy=1.0, etemp=300.0, maxiter=250,
+                 verbosity=0, keep_orbitals=True):
+        self.lib = load_library()
+        self.env = Environment(verbosity)
+        self.numbers = np.ascontiguousarray(numbers, dtype=np.int32)
+        self.positions = np.ascontiguousarray(positions, dtype=np.float64).reshape(-1, 3)
+        n = C.c_int(len(self.numbers))
+        ch = C.c_double(charge)
+        u = C.c_int(uhf)
+        self.mol = C.c_void_p(self.lib.xtb_newMolecule(
+            self.env.h, C.byref(n), self.numbers.ctypes.data_as(C.POINTER(C.c_int)), _dptr(self.positions),
+            C.byref(ch), C.byref(u), None, None))
+        self.env.check()
+        self.calc = C.c_void_p(self.lib.xtb_newCalculator())
+        self.lib.xtb_loadGFN2xTB(self.env.h, self.mol, self.calc, None)
+        self.env.check()
+        self.lib.xtb_setAccuracy(self.env.h, self.calc, accuracy)
+        self.lib.xtb_setElectronicTemp(self.env.h, self.calc, etemp)
+        self.lib.xtb_setMaxIter(self.env.h, self.calc, maxiter)
+        self.lib.xtbgb_setKeepOrbitals(self.env.h, self.calc, int(bool(keep_orbitals)))
+        self.env.check()
+        self.res = C.c_void_p(self.lib.xtb_newResults())
+
+    def update(self, positions):
+        self.positions = np.ascontiguousarray(positions, dtype=np.float64).reshape(-1, 3)
+        self.lib.xtb_updateMolecule(self.env.h, self.mol, _dptr(self.positions), None)
+        self.env.check()
+
+    def shell_charges(self, nshell):
+        out = np.zeros(nshell)
+        self.lib.xtbgb_getShellCharges(self.env.h, self.res, _dptr(out))
+        self.env.check()
+        return out
+
+    def singlepoint(self, fresh=True):
+        """Run xtb_singlepoint; ``fresh`` drops the warm-start wavefunction first."""
+        if fresh:
+            self.lib.xtb_delResults(C.byref(self.res))
+            self.res = C.c_void_p(self.lib.xtb_newResults())
+        self.lib.xtb_singlepoint(self.env.h, self.mol, self.calc, self.res)
+        self.env.check()
+        return Results(self)
+
+    def __del__(self):
+        lib = getattr(self, "lib", None)
+        if lib is None:
+            return
+        for name, fn in (("res", lib.xtb_delResults), ("calc", lib.xtb_delCalculator), ("mol", lib.xtb_delMolecule)):
+            h = getattr(self, name, None)
+            if h is not None:
+                fn(C.byref(h))
+
+
+class Results:
+    def __init__(self, calc):
+        lib, env, res = calc.lib, calc.env, calc.res
+        n = len(calc.numbers)
+        e = C.c_double()
+        lib.xtb_getEnergy(env.h, res, C.byref(e))
+        self.energy = e.value
+        self.gradient = np.zeros((n, 3))
+        lib.xtb_getGradient(env.h, res, _dptr(self.gradient))
+        self.charges = np.zeros(n)
+        lib.xtb_getCharges(env.h, res, _dptr(self.charges))
+        self.dipole = np.zeros(3)
+        lib.xtb_getDipole(env.h, res, _dptr(self.dipole))
+        nao = C.c_int()
+        lib.xtb_getNao(env.h, res, C.byref(nao))
+        self.nao = nao.value
+        self.emo = np.zeros(self.nao)
+        lib.xtb_getOrbitalEigenvalues(env.h, res, _dptr(self.emo))
+        self.focc = np.zeros(self.nao)
+        lib.xtb_getOrbitalOccupations(env.h, res, _dptr(self.focc))
+        self.bond_orders = np.zeros((n, n))
+        lib.xtb_getBondOrders(env.h, res, _dptr(self.bond_orders))
+        it, conv = C.c_int(), C.c_int()
+        lib.xtbgb_getIterations(env.h, res, C.byref(it), C.byref(conv))
+        self.iterations, self.converged = it.value, bool(conv.value)
+        parts = np.zeros(8)
+        lib.xtbgb_getEnergyParts(env.h, res, _dptr(parts))
+        (self.e_elec, self.e_rep, self.e_es, self.e_aes, self.e_axc, self.e_disp, self.e_atm,
+         self.hl_gap) = parts
+        self.gnorm = float(np.sqrt(np.sum(self.gradient ** 2)))
+        self.phase_ms = np.zeros(len(PHASES))
+        lib.xtbgb_getPhaseTimes(env.h, res, _dptr(self.phase_ms))
+        tb = (C.c_longlong * 3)()
+        lib.xtbgb_getTransferBytes(env.h, res, tb)
+        self.h2d_bytes, self.d2h_bytes, self.launches = int(tb[0]), int(tb[1]), int(tb[2])
+        env.check()
