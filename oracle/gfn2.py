@@ -1012,15 +1012,20 @@ def singlepoint(Z, xyz, charge=0.0, uhf=0, etemp=300.0, accuracy=1.0, maxiter=25
     # dipole moment (calc_dipole, src/dipole.f90:94-128) and Wiberg-Mayer bond orders
     # (get_wiberg, src/scc_core.f90:1208-1245) from the last density
     dip = np.sum(xyz * zval[:, None], axis=0) - np.einsum("kij,ij->k", D, Pm)
-    PS = Pm @ S
+    if ihomoa == ihomob:
+        PSs, fac = [Pm @ S], 1.0
+    else:   # get_unrestricted_wiberg, src/scc_core.f90:1248-1295
+        PSs, fac = [((C * fa[None, :]) @ C.T) @ S, ((C * fb[None, :]) @ C.T) @ S], 2.0
     wbo = np.zeros((n, n))
     ao0 = basis.sh_ao[np.searchsorted(basis.sh_atom, np.arange(n))]
     ao1 = np.append(ao0[1:], nao)
     for i in range(n):
         for j in range(i):
             if np.sum((xyz[i] - xyz[j]) ** 2) < 100.0:
-                blk = PS[ao0[i]:ao1[i], ao0[j]:ao1[j]] * PS[ao0[j]:ao1[j], ao0[i]:ao1[i]].T
-                wbo[i, j] = wbo[j, i] = np.sum(blk)
+                tot = 0.0
+                for PS in PSs:
+                    tot += np.sum(PS[ao0[i]:ao1[i], ao0[j]:ao1[j]] * PS[ao0[j]:ao1[j], ao0[i]:ao1[i]].T)
+                wbo[i, j] = wbo[j, i] = fac * tot
 
     r = Result()
     r.dipole = dip

@@ -101,8 +101,10 @@ __global__ void k_dipole(int nat, int nao, const double* __restrict__ xyz, const
 }
 
 // Wiberg-Mayer bond orders from PS (get_wiberg, src/scc_core.f90:1208-1245); one warp per atom pair
+// closed shell: PS = P S, factor 1; open shell (get_unrestricted_wiberg, :1248-1295): PS = Pa S, PS2 = Pb S, factor 2
 __global__ void k_wiberg(int nat, int nao, const double* __restrict__ xyz, const int* __restrict__ ao0,
-                         const int* __restrict__ nao_at, const double* __restrict__ PS, double* __restrict__ wbo) {
+                         const int* __restrict__ nao_at, const double* __restrict__ PS, const double* __restrict__ PS2,
+                         double factor, double* __restrict__ wbo) {
     const long w = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (w >= (long)nat * nat) return;
@@ -117,11 +119,12 @@ __global__ void k_wiberg(int nat, int nao, const double* __restrict__ xyz, const
             for (int t = lane; t < ni * nj; t += 32) {
                 const int k = ao0[i] + t / nj, mm = ao0[j] + t % nj;
                 s += PS[(size_t)k * nao + mm] * PS[(size_t)mm * nao + k];
+                if (PS2) s += PS2[(size_t)k * nao + mm] * PS2[(size_t)mm * nao + k];
             }
         }
     }
     s = warp_sum(s);
-    if (lane == 0) wbo[w] = s;
+    if (lane == 0) wbo[w] = factor * s;
 }
 
 // --------------------------------------------------------------- device workspace
@@ -255,7 +258,7 @@ void run_singlepoint(const HostMol& hm, const SPSettings& set, Wavefunction& wfn
     double *S, *D, *Q, *H0, *X, *H, *A, *T1, *C, *Pm, *Wm, *V, *Y, *Zt, *iscr, *J, *gab3, *gab5, *c6, *dc6, *c6z,
         *dc6z, *eeqA, *eeqX, *cn_gfn, *cn_tmp, *se, *q, *qsh, *dipm, *qp, *shift, *Jq, *vs, *vd, *vq, *radcn, *gw, *dgw,
         *zeta, *dzeta, *Wz, *zv, *zr, *zdcn, *zrdcn, *vat, *ed4, *eh0, *eaes, *erep, *e2, *e3, *grad, *dhdcn, *tmp2,
-        *rows, *emo, *focc, *fe, *tri_d, *tri_e, *tri_e2, *tri_tau, *tri_p, *bounds, *fscal, *escal, *rms, *dip, *qin,
+        *rows, *emo, *focc, *focca, *foccb, *fe, *tri_d, *tri_e, *tri_e2, *tri_tau, *tri_p, *bounds, *fscal, *escal, *rms, *dip, *qin,
         *qout, *dq;
     unsigned char* piv;
     int* info;
@@ -371,6 +374,8 @@ void run_singlepoint(const HostMol& hm, const SPSettings& set, Wavefunction& wfn
     rows = ar.take<double>((size_t)nao * 12);
     emo = ar.take<double>(nao);
     focc = ar.take<double>(nao);
+    focca = ar.take<double>(nao);
+    foccb = ar.take<double>(nao);
     fe = ar.take<double>(nao);
     tri_d = ar.take<double>(nao);
     tri_e = ar.take<double>(nao);
@@ -483,7 +488,7 @@ void run_singlepoint(const HostMol& hm, const SPSettings& set, Wavefunction& wfn
         ormtr(st, nao, V, tri_tau, Y, Zt);
         dgemm(st, false, true, nao, nao, nao, 1.0, X, nao, Zt, nao, 0.0, C, nao);
         tm.mark(PH_DENSITY);
-        fermi(st, nao, emo, hm.nel_a, hm.nel_b, set.etemp, focc, fscal);
+        fermi(st, nao, emo, hm.nel_a, hm.nel_b, set.etemp, focc, focca, foccb, fscal);
         scale_cols(st, nao, C, focc, T1);
         dgemm(st, false, true, nao, nao, nao, 1.0, T1, nao, C, nao, 0.0, Pm, nao);
         tm.mark(PH_POPMIX);
@@ -537,7 +542,18 @@ void run_singlepoint(const HostMol& hm, const SPSettings& set, Wavefunction& wfn
     const bool closed = hm.nel_a == hm.nel_b;
     if (closed) {
         dgemm(st, false, false, nao, nao, nao, 1.0, Pm, nao, S, nao, 0.0, T1, nao);
-        k_wiberg<<<ceil_div((long)aa * 32, 256), 256, 0, st>>>(nat, nao, m.xyz, m.at_ao0, m.at_nao, T1, c6);
+        k_wiberg<<<ceil_div((long)aa * 32, 256), 256, 0, st>>>(nat, nao, m.xyz, m.at_ao0, m.at_nao, T1, nullptr,
+                                                                1.0, c6);
+        XG_LAUNCH_CHECK();
+    } else {
+        // spin densities Pa, Pb from the smeared alpha / beta occupations, then (Pa S), (Pb S)
+        scale_cols(st, nao, C, focca, T1);
+        dgemm(st, false, true, nao, nao, nao, 1.0, T1, nao, C, nao, 0.0, A, nao);
+        dgemm(st, false, false, nao, nao, nao, 1.0, A, nao, S, nao, 0.0, H, nao);
+        scale_cols(st, nao, C, foccb, T1);
+        dgemm(st, false, true, nao, nao, nao, 1.0, T1, nao, C, nao, 0.0, A, nao);
+        dgemm(st, false, false, nao, nao, nao, 1.0, A, nao, S, nao, 0.0, Y, nao);
+        k_wiberg<<<ceil_div((long)aa * 32, 256), 256, 0, st>>>(nat, nao, m.xyz, m.at_ao0, m.at_nao, H, Y, 2.0, c6);
         XG_LAUNCH_CHECK();
     }
     reduce_sum(st, erep, nat, escal + 8);
@@ -550,12 +566,8 @@ void run_singlepoint(const HostMol& hm, const SPSettings& set, Wavefunction& wfn
     double hs2[2];
     res.gradient.assign(3 * (size_t)nat, 0.0);
     res.dipole.assign(3, 0.0);
-    if (closed) {
-        res.wbo.assign(aa, 0.0);
-        XG_CUDA(cudaMemcpyAsync(res.wbo.data(), c6, aa * sizeof(double), cudaMemcpyDeviceToHost, st));
-    } else {
-        res.wbo.clear();
-    }
+    res.wbo.assign(aa, 0.0);
+    XG_CUDA(cudaMemcpyAsync(res.wbo.data(), c6, aa * sizeof(double), cudaMemcpyDeviceToHost, st));
     wfn.nat = nat; wfn.nao = nao; wfn.nsh = nsh;
     wfn.q.resize(nat); wfn.qsh.resize(nsh); wfn.dipm.resize(3 * nat); wfn.qp.resize(6 * nat);
     wfn.emo.resize(nao); wfn.focc.resize(nao);
@@ -577,7 +589,7 @@ void run_singlepoint(const HostMol& hm, const SPSettings& set, Wavefunction& wfn
         wfn.C.clear(); wfn.P.clear(); wfn.S.clear();
     }
     XG_CUDA(cudaStreamSynchronize(st));
-    d2h += (long long)sizeof(double) * (2 + 3 * nat + 3 + nat + nsh + 9 * nat + 2 * nao + (closed ? aa : 0) +
+    d2h += (long long)sizeof(double) * (2 + 3 * nat + 3 + nat + nsh + 9 * nat + 2 * nao + aa +
                                         (keep_orbitals ? 3 * nn : 0));
     res.h2d_bytes = g_h2d;
     res.launches = launch_counter() - launches0;

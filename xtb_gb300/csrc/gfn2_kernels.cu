@@ -597,20 +597,21 @@ __device__ void fermi_channel(int n, const double* emo, int nel, double etemp, d
 }
 
 __global__ void k_fermi(int n, const double* __restrict__ emo, int nel_a, int nel_b, double etemp,
-                        double* __restrict__ focc, double* __restrict__ occb, double* __restrict__ scal) {
+                        double* __restrict__ focc, double* __restrict__ fa, double* __restrict__ fb,
+                        double* __restrict__ scal) {
     __shared__ double red[32];
     double sa, efa, sb, efb;
-    fermi_channel(n, emo, nel_a, etemp, focc, red, sa, efa);
+    fermi_channel(n, emo, nel_a, etemp, fa, red, sa, efa);
     if (nel_b == nel_a) {
         __syncthreads();
-        for (int i = threadIdx.x; i < n; i += blockDim.x) focc[i] *= 2.0;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) fb[i] = fa[i];
         sb = sa;
         efb = efa;
     } else {
-        fermi_channel(n, emo, nel_b, etemp, occb, red, sb, efb);
-        __syncthreads();
-        for (int i = threadIdx.x; i < n; i += blockDim.x) focc[i] += occb[i];
+        fermi_channel(n, emo, nel_b, etemp, fb, red, sb, efb);
     }
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) focc[i] = fa[i] + fb[i];
     if (threadIdx.x == 0) {
         scal[0] = sa + sb;
         scal[1] = efa;
@@ -618,9 +619,9 @@ __global__ void k_fermi(int n, const double* __restrict__ emo, int nel_a, int ne
     }
 }
 
-void fermi(cudaStream_t st, int n, const double* emo, int nel_a, int nel_b, double etemp, double* focc, double* scal) {
-    // scal must provide n extra doubles after the 3 scalars for the beta channel
-    k_fermi<<<1, 1024, 0, st>>>(n, emo, nel_a, nel_b, etemp, focc, scal + 8, scal);
+void fermi(cudaStream_t st, int n, const double* emo, int nel_a, int nel_b, double etemp, double* focc, double* fa,
+           double* fb, double* scal) {
+    k_fermi<<<1, 1024, 0, st>>>(n, emo, nel_a, nel_b, etemp, focc, fa, fb, scal);
     XG_LAUNCH_CHECK();
 }
 

@@ -199,22 +199,25 @@ void potrf_upper(cudaStream_t st, int n, double* A, int lda, int* d_info) {
     XG_LAUNCH_CHECK();
 }
 
-// X = U^-1 (upper triangular), one thread per column.
+// X = U^-1 (upper triangular), one warp per column j: x_i = -(sum_{k=i+1..j} U_ik x_k) / U_ii.
 __global__ void k_trinv_upper(int n, const double* __restrict__ U, int ldu, double* __restrict__ X, int ldx) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (j >= n) return;
-    for (int i = n - 1; i > j; --i) X[(size_t)i * ldx + j] = 0.0;
-    X[(size_t)j * ldx + j] = 1.0 / U[(size_t)j * ldu + j];
+    for (int i = j + 1 + lane; i < n; i += 32) X[(size_t)i * ldx + j] = 0.0;
+    if (lane == 0) X[(size_t)j * ldx + j] = 1.0 / U[(size_t)j * ldu + j];
+    __syncwarp();
     for (int i = j - 1; i >= 0; --i) {
-        double s = 0.0;
         const double* urow = U + (size_t)i * ldu;
-        for (int k = i + 1; k <= j; ++k) s = fma(urow[k], X[(size_t)k * ldx + j], s);
-        X[(size_t)i * ldx + j] = -s / urow[i];
+        double s = 0.0;
+        for (int k = i + 1 + lane; k <= j; k += 32) s = fma(urow[k], X[(size_t)k * ldx + j], s);
+        s = warp_sum(s);
+        if (lane == 0) X[(size_t)i * ldx + j] = -s / urow[i];
+        __syncwarp();
     }
 }
 
 void trinv_upper(cudaStream_t st, int n, const double* U, int ldu, double* X, int ldx) {
-    k_trinv_upper<<<ceil_div(n, 64), 64, 0, st>>>(n, U, ldu, X, ldx);
+    k_trinv_upper<<<ceil_div((long)n * 32, 256), 256, 0, st>>>(n, U, ldu, X, ldx);
     XG_LAUNCH_CHECK();
 }
 
@@ -387,20 +390,30 @@ __global__ void k_tri_prep(int n, const double* __restrict__ d, const double* __
     }
 }
 
+// Eigenvalue j of T by multisection: each round the 32 lanes of a warp evaluate Sturm
+// counts at 31 interior points of the bracket and the bracket shrinks 32-fold.
 __global__ void k_bisect(int n, const double* __restrict__ d, const double* __restrict__ e2,
                          const double* __restrict__ bounds, double* __restrict__ w) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (j >= n) return;
     double lo = bounds[0], hi = bounds[1];
     const double pivmin = bounds[2];
-    for (int it = 0; it < 128; ++it) {
-        const double mid = 0.5 * (lo + hi);
-        if (mid <= lo || mid >= hi) break;
+    for (int round = 0; round < 24; ++round) {
         const double tol = 2.220446049250313e-16 * fmax(fabs(lo), fabs(hi));
         if (hi - lo <= tol) break;
-        if (sturm_count(n, d, e2, mid, pivmin) > j) hi = mid; else lo = mid;
+        const double h = (hi - lo) / 32.0;
+        const double x = lo + h * (lane + 1);          // lane 31 evaluates hi (unused)
+        const int c = (lane < 31) ? sturm_count(n, d, e2, x, pivmin) : n + 1;
+        // the first point whose count exceeds j bounds the eigenvalue from above
+        const unsigned above = __ballot_sync(0xffffffffu, c > j);
+        const int k = __ffs(above) - 1;                // 0..31
+        const double nlo = (k == 0) ? lo : lo + h * k;
+        const double nhi = (k == 31) ? hi : lo + h * (k + 1);
+        if (nlo == lo && nhi == hi) break;             // no representable progress
+        lo = nlo;
+        hi = nhi;
     }
-    w[j] = 0.5 * (lo + hi);
+    if (lane == 0) w[j] = 0.5 * (lo + hi);
 }
 
 // ------------------------------------------------------------------ inverse iteration
@@ -433,19 +446,21 @@ __global__ void k_inviter(int n, const double* __restrict__ d, const double* __r
         if (fabs(w0) >= fabs(sub)) {
             double u0 = w0;
             if (fabs(u0) < pert) u0 = copysign(pert, u0 == 0.0 ? 1.0 : u0);
-            const double m = sub / u0;
-            U1[at(i)] = u0; U2[at(i)] = w1; U3[at(i)] = 0.0; ML[at(i)] = m; piv[at(i)] = 0;
+            const double r0 = 1.0 / u0;
+            const double m = sub * r0;
+            U1[at(i)] = r0; U2[at(i)] = w1; U3[at(i)] = 0.0; ML[at(i)] = m; piv[at(i)] = 0;
             w0 = nd - m * w1;
             w1 = ns;
         } else {
-            const double m = w0 / sub;
-            U1[at(i)] = sub; U2[at(i)] = nd; U3[at(i)] = ns; ML[at(i)] = m; piv[at(i)] = 1;
+            const double r0 = 1.0 / sub;
+            const double m = w0 * r0;
+            U1[at(i)] = r0; U2[at(i)] = nd; U3[at(i)] = ns; ML[at(i)] = m; piv[at(i)] = 1;
             w0 = w1 - m * nd;
             w1 = -m * ns;
         }
     }
     if (fabs(w0) < pert) w0 = copysign(pert, w0 == 0.0 ? 1.0 : w0);
-    U1[at(n - 1)] = w0;
+    U1[at(n - 1)] = 1.0 / w0;   // U1 holds reciprocal pivots
     // start vector: deterministic pseudo-random
     uint32_t s = 0x9e3779b9u ^ (uint32_t)(j * 2654435761u);
     for (int i = 0; i < n; ++i) {
@@ -460,11 +475,11 @@ __global__ void k_inviter(int n, const double* __restrict__ d, const double* __r
             Y[at(i + 1)] = bn - ML[at(i)] * bi;
         }
         // back substitution
-        double x2 = 0.0, x1 = Y[at(n - 1)] / U1[at(n - 1)];
+        double x2 = 0.0, x1 = Y[at(n - 1)] * U1[at(n - 1)];
         Y[at(n - 1)] = x1;
         double mx = fabs(x1);
         for (int i = n - 2; i >= 0; --i) {
-            const double x = (Y[at(i)] - U2[at(i)] * x1 - U3[at(i)] * x2) / U1[at(i)];
+            const double x = (Y[at(i)] - U2[at(i)] * x1 - U3[at(i)] * x2) * U1[at(i)];
             Y[at(i)] = x;
             x2 = x1;
             x1 = x;
@@ -493,10 +508,10 @@ __device__ void tri_solve_col(int n, int j, const double* __restrict__ U1, const
         if (piv[at(i)]) { const double t = bi; bi = bn; bn = t; Y[at(i)] = bi; }
         Y[at(i + 1)] = bn - ML[at(i)] * bi;
     }
-    double x2 = 0.0, x1 = Y[at(n - 1)] / U1[at(n - 1)];
+    double x2 = 0.0, x1 = Y[at(n - 1)] * U1[at(n - 1)];
     Y[at(n - 1)] = x1;
     for (int i = n - 2; i >= 0; --i) {
-        const double x = (Y[at(i)] - U2[at(i)] * x1 - U3[at(i)] * x2) / U1[at(i)];
+        const double x = (Y[at(i)] - U2[at(i)] * x1 - U3[at(i)] * x2) * U1[at(i)];
         Y[at(i)] = x;
         x2 = x1;
         x1 = x;
@@ -550,7 +565,7 @@ void tridiag_eig(cudaStream_t st, int n, const double* d, const double* e, doubl
                  double* Y, double* scratch, unsigned char* pivbuf) {
     k_tri_prep<<<1, 256, 0, st>>>(n, d, e, e2, bounds);
     XG_LAUNCH_CHECK();
-    k_bisect<<<ceil_div(n, 64), 64, 0, st>>>(n, d, e2, bounds, w);
+    k_bisect<<<ceil_div((long)n * 32, 256), 256, 0, st>>>(n, d, e2, bounds, w);
     XG_LAUNCH_CHECK();
     const size_t nn = (size_t)n * n;
     k_inviter<<<ceil_div(n, 64), 64, 0, st>>>(n, d, e, w, bounds, Y, scratch, scratch + nn, scratch + 2 * nn,
