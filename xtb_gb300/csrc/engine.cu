@@ -390,7 +390,7 @@ void run_singlepoint(const HostMol& hm, const SPSettings& set, Wavefunction& wfn
     qin = ar.take<double>(nbr);
     qout = ar.take<double>(nbr);
     dq = ar.take<double>(nbr);
-    info = ar.take<int>(4);
+    info = ar.take<int>(8);
     bs.nbr = nbr;
     bs.maxit = maxit;
     bs.df = ar.take<double>((size_t)maxit * nbr);
@@ -476,21 +476,25 @@ void run_singlepoint(const HostMol& hm, const SPSettings& set, Wavefunction& wfn
         shell_shift(st, m, J, qsh, vat, shift, Jq);
         aes_potential(st, m, q, dipm, qp, gab3, gab5, true, vs, vd, vq);
         build_h(st, m, th, H0, S, D, Q, shift, vs, vd, vq, H);
-        // standard form A = X^T H X, eigenpairs, back-transformation
+        // standard form A = X^T H X (X = U^-1 upper triangular, A symmetric)
         tm.mark(PH_STDFORM);
-        dgemm(st, false, false, nao, nao, nao, 1.0, H, nao, X, nao, 0.0, T1, nao);
-        dgemm(st, true, false, nao, nao, nao, 1.0, X, nao, T1, nao, 0.0, A, nao);
+        dgemm(st, false, false, nao, nao, nao, 1.0, H, nao, X, nao, 0.0, T1, nao, GF_B_UPPER);
+        dgemm(st, true, false, nao, nao, nao, 1.0, X, nao, T1, nao, 0.0, A, nao, GF_A_LOWER | GF_SYM);
+        mirror_lower(st, nao, A, nao);
         tm.mark(PH_SYTRD);
         sytrd(st, nao, A, nao, V, tri_tau, tri_d, tri_e, tri_p);
+        // eigenvalues, occupations, then eigenvectors of the occupied orbitals only
         tm.mark(PH_TRIEIG);
-        tridiag_eig(st, nao, tri_d, tri_e, tri_e2, bounds, emo, Y, iscr, piv);
+        tridiag_eigvals(st, nao, tri_d, tri_e, tri_e2, bounds, emo);
+        fermi(st, nao, emo, hm.nel_a, hm.nel_b, set.etemp, focc, focca, foccb, fscal, info + 1);
+        tridiag_eigvecs(st, nao, tri_d, tri_e, bounds, emo, Y, iscr, piv, info + 1);
         tm.mark(PH_BACKTR);
-        ormtr(st, nao, V, tri_tau, Y, Zt);
-        dgemm(st, false, true, nao, nao, nao, 1.0, X, nao, Zt, nao, 0.0, C, nao);
+        ormtr(st, nao, V, tri_tau, Y, Zt, info + 1);
+        dgemm(st, false, true, nao, nao, nao, 1.0, X, nao, Zt, nao, 0.0, C, nao, GF_A_UPPER, nullptr, info + 1);
         tm.mark(PH_DENSITY);
-        fermi(st, nao, emo, hm.nel_a, hm.nel_b, set.etemp, focc, focca, foccb, fscal);
         scale_cols(st, nao, C, focc, T1);
-        dgemm(st, false, true, nao, nao, nao, 1.0, T1, nao, C, nao, 0.0, Pm, nao);
+        dgemm(st, false, true, nao, nao, nao, 1.0, T1, nao, C, nao, 0.0, Pm, nao, GF_SYM, info + 1);
+        mirror_lower(st, nao, Pm, nao);
         tm.mark(PH_POPMIX);
         populations(st, m, Pm, S, D, Q, H0, rows, qsh, q, dipm, qp, eh0);
         shell_shift(st, m, J, qsh, nullptr, T1, Jq);    // Jq for the electrostatic energy
@@ -519,12 +523,19 @@ void run_singlepoint(const HostMol& hm, const SPSettings& set, Wavefunction& wfn
     }
     scc_failed = !converged;
 
+    if (keep_orbitals) {
+        // all MO coefficients of the last iteration (only occupied ones were needed inside the SCC)
+        tridiag_eigvecs(st, nao, tri_d, tri_e, bounds, emo, Y, iscr, piv, nullptr);
+        ormtr(st, nao, V, tri_tau, Y, Zt, nullptr);
+        dgemm(st, false, true, nao, nao, nao, 1.0, X, nao, Zt, nao, 0.0, C, nao, GF_A_UPPER);
+    }
     // ---- gradient (src/scf_module.F90:665-798)
     tm.mark(PH_GRADIENT);
     k_scale_energy_weights<<<ceil_div(nao, 128), 128, 0, st>>>(nao, focc, emo, fe);
     XG_LAUNCH_CHECK();
     scale_cols(st, nao, C, fe, T1);
-    dgemm(st, false, true, nao, nao, nao, 1.0, T1, nao, C, nao, 0.0, Wm, nao);
+    dgemm(st, false, true, nao, nao, nao, 1.0, T1, nao, C, nao, 0.0, Wm, nao, GF_SYM, info + 1);
+    mirror_lower(st, nao, Wm, nao);
     aes_potential(st, m, q, dipm, qp, gab3, gab5, false, vs, vd, vq);
     grad_sdqh0(st, m, th, se, Pm, Wm, shift, vs, vd, vq, grad, dhdcn);
     dhdcn_diag(st, m, Pm, dhdcn);

@@ -598,8 +598,9 @@ __device__ void fermi_channel(int n, const double* emo, int nel, double etemp, d
 
 __global__ void k_fermi(int n, const double* __restrict__ emo, int nel_a, int nel_b, double etemp,
                         double* __restrict__ focc, double* __restrict__ fa, double* __restrict__ fb,
-                        double* __restrict__ scal) {
+                        double* __restrict__ scal, int* __restrict__ kocc) {
     __shared__ double red[32];
+    __shared__ int kmax;
     double sa, efa, sb, efb;
     fermi_channel(n, emo, nel_a, etemp, fa, red, sa, efa);
     if (nel_b == nel_a) {
@@ -610,9 +611,16 @@ __global__ void k_fermi(int n, const double* __restrict__ emo, int nel_a, int ne
     } else {
         fermi_channel(n, emo, nel_b, etemp, fb, red, sb, efb);
     }
+    if (threadIdx.x == 0) kmax = max(nel_a, nel_b);
     __syncthreads();
-    for (int i = threadIdx.x; i < n; i += blockDim.x) focc[i] = fa[i] + fb[i];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const double f = fa[i] + fb[i];
+        focc[i] = f;
+        if (f > 0.0) atomicMax(&kmax, i + 1);
+    }
+    __syncthreads();
     if (threadIdx.x == 0) {
+        kocc[0] = min(kmax, n);
         scal[0] = sa + sb;
         scal[1] = efa;
         scal[2] = efb;
@@ -620,15 +628,16 @@ __global__ void k_fermi(int n, const double* __restrict__ emo, int nel_a, int ne
 }
 
 void fermi(cudaStream_t st, int n, const double* emo, int nel_a, int nel_b, double etemp, double* focc, double* fa,
-           double* fb, double* scal) {
-    k_fermi<<<1, 1024, 0, st>>>(n, emo, nel_a, nel_b, etemp, focc, fa, fb, scal);
+           double* fb, double* scal, int* kocc) {
+    k_fermi<<<1, 1024, 0, st>>>(n, emo, nel_a, nel_b, etemp, focc, fa, fb, scal, kocc);
     XG_LAUNCH_CHECK();
 }
 
 __global__ void k_scale_cols(int n, const double* __restrict__ C, const double* __restrict__ f, double* __restrict__ Cf) {
     const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (size_t)n * n) return;
-    Cf[t] = C[t] * f[t % n];
+    const double fj = f[t % n];
+    Cf[t] = (fj == 0.0) ? 0.0 : C[t] * fj;     // exact zeros for unoccupied columns
 }
 
 void scale_cols(cudaStream_t st, int n, const double* C, const double* f, double* Cf) {

@@ -23,14 +23,29 @@ constexpr int GBM = 64, GBN = 64, GBK = 16;
 
 // C[M,N] = alpha * op(A) * op(B) + beta * C.
 // op(A)[i,k] = TA ? A[k*lda+i] : A[i*lda+k];  op(B)[k,j] = TB ? B[j*ldb+k] : B[k*ldb+j].
+// Structure flags skip work that is known to be zero or redundant:
+//   GF_B_UPPER  op(B)[k,j] = 0 for k > j      (k < j0 + 64 per tile)
+//   GF_A_LOWER  op(A)[i,k] = 0 for k > i      (k < i0 + 64 per tile)
+//   GF_A_UPPER  op(A)[i,k] = 0 for k < i      (k >= i0 per tile)
+//   GF_SYM      C symmetric: only tiles touching the lower triangle are computed (mirror afterwards)
+// dK / dN (optional, device): K and N limited to *dK / *dN at run time.
 template <bool TA, bool TB>
 __global__ void __launch_bounds__(256) k_dgemm(int M, int N, int K, double alpha, const double* __restrict__ A,
                                                int lda, const double* __restrict__ B, int ldb, double beta,
-                                               double* __restrict__ C, int ldc) {
+                                               double* __restrict__ C, int ldc, int flags, const int* __restrict__ dK,
+                                               const int* __restrict__ dN) {
     __shared__ double As[2][GBK][GBM + 1];
     __shared__ double Bs[2][GBK][GBN + 1];
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
     const int i0 = blockIdx.y * GBM, j0 = blockIdx.x * GBN;
+    if (dN) N = min(N, *dN);
+    if (j0 >= N) return;
+    if ((flags & GF_SYM) && j0 >= i0 + GBM) return;
+    if (dK) K = min(K, *dK);
+    int kbeg = 0, kend = K;
+    if (flags & GF_B_UPPER) kend = min(kend, j0 + GBN);
+    if (flags & GF_A_LOWER) kend = min(kend, i0 + GBM);
+    if (flags & GF_A_UPPER) kbeg = (i0 / GBK) * GBK;
     double acc[4][4];
 #pragma unroll
     for (int r = 0; r < 4; ++r)
@@ -45,7 +60,7 @@ __global__ void __launch_bounds__(256) k_dgemm(int M, int N, int K, double alpha
             if (TA) { ii = t % GBM; kk = t / GBM; } else { kk = t % GBK; ii = t / GBK; }
             const int gi = i0 + ii, gk = k0 + kk;
             double v = 0.0;
-            if (gi < M && gk < K) v = TA ? A[(size_t)gk * lda + gi] : A[(size_t)gi * lda + gk];
+            if (gi < M && gk < kend) v = TA ? A[(size_t)gk * lda + gi] : A[(size_t)gi * lda + gk];
             As[buf][kk][ii] = v;
         }
 #pragma unroll
@@ -55,16 +70,16 @@ __global__ void __launch_bounds__(256) k_dgemm(int M, int N, int K, double alpha
             if (TB) { kk = t % GBK; jj = t / GBK; } else { jj = t % GBN; kk = t / GBN; }
             const int gj = j0 + jj, gk = k0 + kk;
             double v = 0.0;
-            if (gj < N && gk < K) v = TB ? B[(size_t)gj * ldb + gk] : B[(size_t)gk * ldb + gj];
+            if (gj < N && gk < kend) v = TB ? B[(size_t)gj * ldb + gk] : B[(size_t)gk * ldb + gj];
             Bs[buf][kk][jj] = v;
         }
     };
 
     int buf = 0;
-    load(0, 0);
+    if (kbeg < kend) load(0, kbeg);
     __syncthreads();
-    for (int k0 = 0; k0 < K; k0 += GBK) {
-        if (k0 + GBK < K) load(buf ^ 1, k0 + GBK);
+    for (int k0 = kbeg; k0 < kend; k0 += GBK) {
+        if (k0 + GBK < kend) load(buf ^ 1, k0 + GBK);
 #pragma unroll
         for (int kk = 0; kk < GBK; ++kk) {
             double a[4], b[4];
@@ -96,13 +111,26 @@ __global__ void __launch_bounds__(256) k_dgemm(int M, int N, int K, double alpha
 }
 
 void dgemm(cudaStream_t st, bool ta, bool tb, int M, int N, int K, double alpha, const double* A, int lda,
-           const double* B, int ldb, double beta, double* C, int ldc) {
+           const double* B, int ldb, double beta, double* C, int ldc, int flags, const int* dK, const int* dN) {
     if (M <= 0 || N <= 0) return;
     dim3 grid(ceil_div(N, GBN), ceil_div(M, GBM));
-    if (!ta && !tb) k_dgemm<false, false><<<grid, 256, 0, st>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
-    else if (ta && !tb) k_dgemm<true, false><<<grid, 256, 0, st>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
-    else if (!ta && tb) k_dgemm<false, true><<<grid, 256, 0, st>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
-    else k_dgemm<true, true><<<grid, 256, 0, st>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
+    if (!ta && !tb) k_dgemm<false, false><<<grid, 256, 0, st>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, flags, dK, dN);
+    else if (ta && !tb) k_dgemm<true, false><<<grid, 256, 0, st>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, flags, dK, dN);
+    else if (!ta && tb) k_dgemm<false, true><<<grid, 256, 0, st>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, flags, dK, dN);
+    else k_dgemm<true, true><<<grid, 256, 0, st>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, flags, dK, dN);
+    XG_LAUNCH_CHECK();
+}
+
+// copy the lower triangle onto the upper one (after a GF_SYM product)
+__global__ void k_mirror_lower(int n, double* __restrict__ C, int ldc) {
+    const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long)n * n) return;
+    const int i = (int)(t / n), j = (int)(t % n);
+    if (j > i) C[(size_t)i * ldc + j] = C[(size_t)j * ldc + i];
+}
+
+void mirror_lower(cudaStream_t st, int n, double* C, int ldc) {
+    k_mirror_lower<<<ceil_div((long)n * n, 256), 256, 0, st>>>(n, C, ldc);
     XG_LAUNCH_CHECK();
 }
 
@@ -225,22 +253,29 @@ void trinv_upper(cudaStream_t st, int n, const double* U, int ldu, double* X, in
 // A (symmetric, full storage) -> T = Q^T A Q with Q = H(0) H(1) ... H(n-3),
 // H(k) = I - tau_k v_k v_k^T, v_k[0..k] = 0, v_k[k+1] = 1 (LAPACK dsytd2, lower).
 // v_k is stored in row k of V; d (diag), e (sub-diagonal) of T.  A is destroyed.
+//
+// One pass over the trailing rows per column: the rank-2 update of step k-1 is
+// applied lazily while the symmetric product p = tau A22 v of step k is formed,
+// so A22 is read and written once per column.  Row k+1 (the next pivot row) is
+// updated eagerly at the end of step k.  Two grid-wide barriers per column.
 __global__ void __launch_bounds__(256) k_sytrd(int n, double* __restrict__ A, int lda, double* __restrict__ V,
                                                double* __restrict__ tau, double* __restrict__ d, double* __restrict__ e,
                                                double* __restrict__ p) {
     cg::grid_group grid = cg::this_grid();
     extern __shared__ double sm[];
-    double* v = sm;           // [n]
-    double* w = sm + n;       // [n]
-    double* red = sm + 2 * n; // [32]
+    double* v = sm;            // [n] current reflector, offset k+1
+    double* w = sm + n;        // [n]
+    double* vp = sm + 2 * n;   // [n] pending update (previous step), offset k
+    double* wp = sm + 3 * n;   // [n]
+    double* red = sm + 4 * n;  // [32]
     const int lane = threadIdx.x & 31;
     const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    double tprev = 0.0;        // tau of the pending update (0: nothing pending)
 
     for (int k = 0; k < n - 2; ++k) {
-        const int m = n - k - 1;                 // length of the reflected vector
-        const double* xk = A + (size_t)k * lda + k + 1;   // row k == column k (symmetric)
-        // every block: v = x, norm of x[1:]
+        const int m = n - k - 1;
+        const double* xk = A + (size_t)k * lda + k + 1;   // row k, already fully updated
         double ss = 0.0;
         for (int i = threadIdx.x; i < m; i += blockDim.x) {
             const double xv = xk[i];
@@ -270,19 +305,26 @@ __global__ void __launch_bounds__(256) k_sytrd(int n, double* __restrict__ A, in
                 e[k] = beta;
             }
         }
-        if (tk != 0.0) {
-            // p = tau * A22 v  (warp per row of A22)
-            for (int r = gwarp; r < m; r += nwarps) {
-                const double* arow = A + (size_t)(k + 1 + r) * lda + k + 1;
-                double s = 0.0;
-                for (int c = lane; c < m; c += 32) s = fma(arow[c], v[c], s);
-                s = warp_sum(s);
-                if (lane == 0) p[r] = tk * s;
+        // rows k+1 .. n-1: apply the pending update of step k-1 (cols >= k+1) and form
+        // p = tau A22 v (row k itself was updated eagerly at the end of step k-1)
+        for (int r = gwarp; r < m; r += nwarps) {
+            double* arow = A + (size_t)(k + 1 + r) * lda + k + 1;
+            const bool pend = tprev != 0.0;
+            const double vr = pend ? vp[r + 1] : 0.0, wr = pend ? wp[r + 1] : 0.0;
+            double sdot = 0.0;
+            for (int c = lane; c < m; c += 32) {
+                double a = arow[c];
+                if (pend) {
+                    a -= vr * wp[c + 1] + wr * vp[c + 1];
+                    arow[c] = a;
+                }
+                sdot = fma(a, v[c], sdot);
             }
+            sdot = warp_sum(sdot);
+            if (lane == 0) p[r] = tk * sdot;
         }
         grid.sync();
         if (tk != 0.0) {
-            // w = p - (tau/2)(p.v) v
             double pv = 0.0;
             for (int i = threadIdx.x; i < m; i += blockDim.x) {
                 const double pi = p[i];
@@ -292,30 +334,46 @@ __global__ void __launch_bounds__(256) k_sytrd(int n, double* __restrict__ A, in
             pv = block_sum(pv, red);
             const double kk = -0.5 * tk * pv;
             for (int i = threadIdx.x; i < m; i += blockDim.x) w[i] += kk * v[i];
-            __syncthreads();
-            // A22 -= v w^T + w v^T
-            for (int r = gwarp; r < m; r += nwarps) {
-                double* arow = A + (size_t)(k + 1 + r) * lda + k + 1;
-                const double vr = v[r], wr = w[r];
-                for (int c = lane; c < m; c += 32) arow[c] -= vr * w[c] + wr * v[c];
-            }
+        } else {
+            for (int i = threadIdx.x; i < m; i += blockDim.x) w[i] = 0.0;
         }
+        __syncthreads();
+        // the pending update becomes (v, w) of this step (offset k+1)
+        for (int i = threadIdx.x; i < m; i += blockDim.x) { vp[i] = v[i]; wp[i] = w[i]; }
+        tprev = tk;
+        __syncthreads();
+        // eager update of the next pivot row k+1 (cols >= k+1)
+        if (tk != 0.0 && gwarp == 0) {
+            double* arow = A + (size_t)(k + 1) * lda + k + 1;
+            const double vr = vp[0], wr = wp[0];
+            for (int c = lane; c < m; c += 32) arow[c] -= vr * wp[c] + wr * vp[c];
+        }
+        // the shift of the pending vectors to offset k+2 happens through the index r+1 above
         grid.sync();
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         if (n >= 2) {
+            // the last row still carries the pending update of step n-3 (cols n-2, n-1)
+            double a21 = A[(size_t)(n - 1) * lda + n - 2];
+            double a22 = A[(size_t)(n - 1) * lda + n - 1];
+            if (n >= 3 && tprev != 0.0) {
+                a21 -= vp[1] * wp[0] + wp[1] * vp[0];
+                a22 -= vp[1] * wp[1] + wp[1] * vp[1];
+            }
             d[n - 2] = A[(size_t)(n - 2) * lda + n - 2];
-            e[n - 2] = A[(size_t)(n - 1) * lda + n - 2];
+            e[n - 2] = a21;
             tau[n - 2] = 0.0;
+            d[n - 1] = a22;
+        } else {
+            d[n - 1] = A[(size_t)(n - 1) * lda + n - 1];
         }
-        d[n - 1] = A[(size_t)(n - 1) * lda + n - 1];
-        if (n >= 1) tau[n - 1] = 0.0;
+        tau[n - 1] = 0.0;
     }
 }
 
 void sytrd(cudaStream_t st, int n, double* A, int lda, double* V, double* tau, double* d, double* e, double* p) {
     static int nsm = 0, maxblk = 0;
-    const size_t smem = (size_t)(2 * n + 32) * sizeof(double);
+    const size_t smem = (size_t)(4 * n + 32) * sizeof(double);
     if (n <= 2) {
         // trivial: copy diagonal / off-diagonal
         k_sytrd<<<1, 256, smem, st>>>(n, A, lda, V, tau, d, e, p);
@@ -422,9 +480,9 @@ __global__ void k_bisect(int n, const double* __restrict__ d, const double* __re
 __global__ void k_inviter(int n, const double* __restrict__ d, const double* __restrict__ e,
                           const double* __restrict__ w, const double* __restrict__ bounds, double* __restrict__ Y,
                           double* __restrict__ U1, double* __restrict__ U2, double* __restrict__ U3,
-                          double* __restrict__ ML, unsigned char* __restrict__ piv) {
+                          double* __restrict__ ML, unsigned char* __restrict__ piv, const int* __restrict__ ncol) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= n) return;
+    if (j >= n || (ncol && j >= *ncol)) return;
     const double tnorm = fmax(bounds[3], 1e-300);
     const double eps = 2.220446049250313e-16;
     double lam = w[j];
@@ -524,13 +582,14 @@ __device__ void tri_solve_col(int n, int j, const double* __restrict__ U1, const
 __global__ void k_reorth(int n, const double* __restrict__ w, const double* __restrict__ bounds, double ctol,
                          double* __restrict__ Y, const double* __restrict__ U1, const double* __restrict__ U2,
                          const double* __restrict__ U3, const double* __restrict__ ML,
-                         const unsigned char* __restrict__ piv) {
+                         const unsigned char* __restrict__ piv, const int* __restrict__ ncol) {
     const int j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (j >= n) return;
+    const int nc = ncol ? min(n, *ncol) : n;
+    if (j >= nc) return;
     const double tol = ctol * fmax(bounds[3], 1e-300);
     if (j > 0 && w[j] - w[j - 1] < tol) return;          // not the first member
     int end = j + 1;
-    while (end < n && w[end] - w[end - 1] < tol) ++end;
+    while (end < nc && w[end] - w[end - 1] < tol) ++end;
     if (end - j < 2) return;
     for (int k = j + 1; k < end; ++k) {
         for (int rep = 0; rep < 3; ++rep) {
@@ -561,30 +620,34 @@ __global__ void k_reorth(int n, const double* __restrict__ w, const double* __re
     }
 }
 
-void tridiag_eig(cudaStream_t st, int n, const double* d, const double* e, double* e2, double* bounds, double* w,
-                 double* Y, double* scratch, unsigned char* pivbuf) {
+void tridiag_eigvals(cudaStream_t st, int n, const double* d, const double* e, double* e2, double* bounds,
+                     double* w) {
     k_tri_prep<<<1, 256, 0, st>>>(n, d, e, e2, bounds);
     XG_LAUNCH_CHECK();
     k_bisect<<<ceil_div((long)n * 32, 256), 256, 0, st>>>(n, d, e2, bounds, w);
     XG_LAUNCH_CHECK();
+}
+
+void tridiag_eigvecs(cudaStream_t st, int n, const double* d, const double* e, const double* bounds, const double* w,
+                     double* Y, double* scratch, unsigned char* pivbuf, const int* ncol) {
     const size_t nn = (size_t)n * n;
     k_inviter<<<ceil_div(n, 64), 64, 0, st>>>(n, d, e, w, bounds, Y, scratch, scratch + nn, scratch + 2 * nn,
-                                              scratch + 3 * nn, pivbuf);
+                                              scratch + 3 * nn, pivbuf, ncol);
     XG_LAUNCH_CHECK();
     k_reorth<<<ceil_div((long)n * 32, 128), 128, 0, st>>>(n, w, bounds, 1.0e-7, Y, scratch, scratch + nn,
-                                                        scratch + 2 * nn, scratch + 3 * nn, pivbuf);
+                                                        scratch + 2 * nn, scratch + 3 * nn, pivbuf, ncol);
     XG_LAUNCH_CHECK();
 }
 
 // ------------------------------------------------------------------ back-transformation
 // Zt[j][:] = Q * Y[:, j] for every eigenvector j (one warp per eigenvector, vector staged in shared memory).
 __global__ void k_ormtr(int n, const double* __restrict__ V, const double* __restrict__ tau,
-                        const double* __restrict__ Y, double* __restrict__ Zt) {
+                        const double* __restrict__ Y, double* __restrict__ Zt, const int* __restrict__ ncol) {
     extern __shared__ double sm[];
     const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int wpb = blockDim.x >> 5;
     const int j = blockIdx.x * wpb + wib;
-    if (j >= n) return;
+    if (j >= n || (ncol && j >= *ncol)) return;
     double* y = sm + (size_t)wib * n;
     for (int i = lane; i < n; i += 32) y[i] = Y[(size_t)i * n + j];
     __syncwarp();
@@ -601,12 +664,12 @@ __global__ void k_ormtr(int n, const double* __restrict__ V, const double* __res
     for (int i = lane; i < n; i += 32) Zt[(size_t)j * n + i] = y[i];
 }
 
-void ormtr(cudaStream_t st, int n, const double* V, const double* tau, const double* Y, double* Zt) {
+void ormtr(cudaStream_t st, int n, const double* V, const double* tau, const double* Y, double* Zt, const int* ncol) {
     int wpb = 4;
     size_t smem = (size_t)wpb * n * sizeof(double);
     while (wpb > 1 && smem > 200 * 1024) { wpb >>= 1; smem = (size_t)wpb * n * sizeof(double); }
     if (smem > 48 * 1024) XG_CUDA(cudaFuncSetAttribute(k_ormtr, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_ormtr<<<ceil_div(n, wpb), wpb * 32, smem, st>>>(n, V, tau, Y, Zt);
+    k_ormtr<<<ceil_div(n, wpb), wpb * 32, smem, st>>>(n, V, tau, Y, Zt, ncol);
     XG_LAUNCH_CHECK();
 }
 

@@ -6,21 +6,29 @@
 
 namespace xg {
 
-// C = alpha op(A) op(B) + beta C
+// structure flags of dgemm
+constexpr int GF_B_UPPER = 1, GF_A_LOWER = 2, GF_A_UPPER = 4, GF_SYM = 8;
+// C = alpha op(A) op(B) + beta C (see linalg.cu for the flags; dK / dN optional device bounds)
 void dgemm(cudaStream_t st, bool ta, bool tb, int M, int N, int K, double alpha, const double* A, int lda,
-           const double* B, int ldb, double beta, double* C, int ldc);
+           const double* B, int ldb, double beta, double* C, int ldc, int flags = 0, const int* dK = nullptr,
+           const int* dN = nullptr);
+// copy the lower triangle of C onto its upper triangle
+void mirror_lower(cudaStream_t st, int n, double* C, int ldc);
 // A = U^T U, U upper (lower triangle zeroed); d_info[0] = failing column + 1 or 0
 void potrf_upper(cudaStream_t st, int n, double* A, int lda, int* d_info);
 // X = U^-1
 void trinv_upper(cudaStream_t st, int n, const double* U, int ldu, double* X, int ldx);
 // Householder reduction to tridiagonal form (A destroyed); V[n*n], tau[n], d[n], e[n], p[n] scratch
 void sytrd(cudaStream_t st, int n, double* A, int lda, double* V, double* tau, double* d, double* e, double* p);
-// eigenpairs of the tridiagonal (d, e): w[n] ascending, Y[i*n+j] = component i of vector j.
-// scratch: 4*n*n doubles, pivbuf: n*n bytes, e2: n, bounds: 4
-void tridiag_eig(cudaStream_t st, int n, const double* d, const double* e, double* e2, double* bounds, double* w,
-                 double* Y, double* scratch, unsigned char* pivbuf);
-// Zt[j][:] = Q Y[:, j]
-void ormtr(cudaStream_t st, int n, const double* V, const double* tau, const double* Y, double* Zt);
+// eigenvalues of the tridiagonal (d, e): w[n] ascending; e2: n, bounds: 4
+void tridiag_eigvals(cudaStream_t st, int n, const double* d, const double* e, double* e2, double* bounds, double* w);
+// eigenvectors j < *ncol (all if ncol is null): Y[i*n+j] = component i of vector j.
+// scratch: 4*n*n doubles, pivbuf: n*n bytes
+void tridiag_eigvecs(cudaStream_t st, int n, const double* d, const double* e, const double* bounds, const double* w,
+                     double* Y, double* scratch, unsigned char* pivbuf, const int* ncol);
+// Zt[j][:] = Q Y[:, j] for j < *ncol (all if null)
+void ormtr(cudaStream_t st, int n, const double* V, const double* tau, const double* Y, double* Zt,
+           const int* ncol = nullptr);
 // measured FP64 FMA throughput of the current device (TFLOP/s)
 double fp64_peak_tflops();
 
