@@ -311,16 +311,27 @@ __global__ void __launch_bounds__(256) k_sytrd(int n, double* __restrict__ A, in
             double* arow = A + (size_t)(k + 1 + r) * lda + k + 1;
             const bool pend = tprev != 0.0;
             const double vr = pend ? vp[r + 1] : 0.0, wr = pend ? wp[r + 1] : 0.0;
-            double sdot = 0.0;
-            for (int c = lane; c < m; c += 32) {
-                double a = arow[c];
-                if (pend) {
-                    a -= vr * wp[c + 1] + wr * vp[c + 1];
-                    arow[c] = a;
+            double s0 = 0.0, s1 = 0.0;
+            for (int c0 = 0; c0 < m; c0 += 256) {
+                double a[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) {
+                    const int c = c0 + lane + 32 * u;
+                    a[u] = (c < m) ? arow[c] : 0.0;
                 }
-                sdot = fma(a, v[c], sdot);
+#pragma unroll
+                for (int u = 0; u < 8; ++u) {
+                    const int c = c0 + lane + 32 * u;
+                    if (c < m) {
+                        if (pend) {
+                            a[u] -= vr * wp[c + 1] + wr * vp[c + 1];
+                            arow[c] = a[u];
+                        }
+                        if (u & 1) s1 = fma(a[u], v[c], s1); else s0 = fma(a[u], v[c], s0);
+                    }
+                }
             }
-            sdot = warp_sum(sdot);
+            const double sdot = warp_sum(s0 + s1);
             if (lane == 0) p[r] = tk * sdot;
         }
         grid.sync();
@@ -448,30 +459,21 @@ __global__ void k_tri_prep(int n, const double* __restrict__ d, const double* __
     }
 }
 
-// Eigenvalue j of T by multisection: each round the 32 lanes of a warp evaluate Sturm
-// counts at 31 interior points of the bracket and the bracket shrinks 32-fold.
+// Eigenvalue j of T by bisection on Sturm counts, one thread per eigenvalue, to an
+// absolute accuracy of 2 eps ||T|| (the accuracy inverse iteration needs).
 __global__ void k_bisect(int n, const double* __restrict__ d, const double* __restrict__ e2,
                          const double* __restrict__ bounds, double* __restrict__ w) {
-    const int j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
     double lo = bounds[0], hi = bounds[1];
     const double pivmin = bounds[2];
-    for (int round = 0; round < 24; ++round) {
-        const double tol = 2.220446049250313e-16 * fmax(fabs(lo), fabs(hi));
-        if (hi - lo <= tol) break;
-        const double h = (hi - lo) / 32.0;
-        const double x = lo + h * (lane + 1);          // lane 31 evaluates hi (unused)
-        const int c = (lane < 31) ? sturm_count(n, d, e2, x, pivmin) : n + 1;
-        // the first point whose count exceeds j bounds the eigenvalue from above
-        const unsigned above = __ballot_sync(0xffffffffu, c > j);
-        const int k = __ffs(above) - 1;                // 0..31
-        const double nlo = (k == 0) ? lo : lo + h * k;
-        const double nhi = (k == 31) ? hi : lo + h * (k + 1);
-        if (nlo == lo && nhi == hi) break;             // no representable progress
-        lo = nlo;
-        hi = nhi;
+    const double atol = 2.0 * 2.220446049250313e-16 * fmax(bounds[3], 1e-300);
+    for (int it = 0; it < 80; ++it) {
+        const double mid = 0.5 * (lo + hi);
+        if (hi - lo <= atol || mid <= lo || mid >= hi) break;
+        if (sturm_count(n, d, e2, mid, pivmin) > j) hi = mid; else lo = mid;
     }
-    if (lane == 0) w[j] = 0.5 * (lo + hi);
+    w[j] = 0.5 * (lo + hi);
 }
 
 // ------------------------------------------------------------------ inverse iteration
@@ -624,7 +626,7 @@ void tridiag_eigvals(cudaStream_t st, int n, const double* d, const double* e, d
                      double* w) {
     k_tri_prep<<<1, 256, 0, st>>>(n, d, e, e2, bounds);
     XG_LAUNCH_CHECK();
-    k_bisect<<<ceil_div((long)n * 32, 256), 256, 0, st>>>(n, d, e2, bounds, w);
+    k_bisect<<<ceil_div(n, 64), 64, 0, st>>>(n, d, e2, bounds, w);
     XG_LAUNCH_CHECK();
 }
 
