@@ -381,7 +381,7 @@ void run_singlepoint(const HostMol& hm, const SPSettings& set, Wavefunction& wfn
     tri_e = ar.take<double>(nao);
     tri_e2 = ar.take<double>(nao);
     tri_tau = ar.take<double>(nao);
-    tri_p = ar.take<double>(nao);
+    tri_p = ar.take<double>(2 * (size_t)nao);
     bounds = ar.take<double>(8);
     fscal = ar.take<double>(8 + (size_t)nao);
     escal = ar.take<double>(16);

@@ -8,234 +8,95 @@
 #include <cmath>
 
 #include "gfn2_kernels.h"
+#include "gfn2_device.cuh"
 
 namespace xg {
 
-__device__ __forceinline__ double sq(double x) { return x * x; }
-
-// linear index t -> (a, b) with a >= b of a packed lower triangle
-__device__ __forceinline__ void tri_pair(long t, int& a, int& b) {
-    long aa = (long)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
-    while (aa * (aa + 1) / 2 > t) --aa;
-    while ((aa + 1) * (aa + 2) / 2 <= t) ++aa;
-    a = (int)aa;
-    b = (int)(t - aa * (aa + 1) / 2);
-}
-
-// ================================================================== coordination numbers
-// getCoordinationNumberLP (src/disp/coordinationnumber.F90:304-479), ncoord_erf / ncoord_d4
-// (src/disp/ncoord.f90:469-506, 575-615).
-struct CNTerm { double cf, df; };
-
-__device__ __forceinline__ double expc(double k, double r, double r0) { return 1.0 / (1.0 + exp(-k * (r0 / r - 1.0))); }
-__device__ __forceinline__ double dexpc(double k, double r, double r0) {
-    const double e = exp(-k * (r0 / r - 1.0));
-    return (-k * r0 * e) / (r * r * ((e + 1.0) * (e + 1.0)));
-}
-
-__device__ __forceinline__ bool cn_term(const DevMol& m, int mode, int i, int j, double r2, CNTerm& t) {
-    constexpr double k4 = 4.10451, k5 = 19.08857, k6 = 2 * 11.28174 * 11.28174;
-    const double sqrtpi = 1.7724538509055160273;
-    if (mode == 0 || mode == 1) {
-        if (r2 > 1600.0 || r2 < 1e-12) return false;
-    } else {
-        if (r2 > 1600.0) return false;
-    }
-    const double r = sqrt(r2);
-    if (mode == 0) {
-        const double rc = m.rcov[i] + m.rcov[j];
-        t.cf = expc(10.0, r, rc) * expc(20.0, r, rc + 2.0);
-        t.df = dexpc(10.0, r, rc) * expc(20.0, r, rc + 2.0) + expc(10.0, r, rc) * dexpc(20.0, r, rc + 2.0);
-    } else if (mode == 1) {
-        const double rc = m.rcov[i] + m.rcov[j];
-        const double den = k4 * exp(-sq(fabs(m.en[i] - m.en[j]) + k5) / k6);
-        t.cf = den * 0.5 * (1.0 + erf(-7.5 * (r - rc) / rc));
-        t.df = den * (-7.5 / sqrtpi / rc * exp(-56.25 * sq(r - rc) / (rc * rc)));
-    } else if (mode == 2) {
-        const double rc = m.rcov4[j] + m.rcov4[i];
-        t.cf = 0.5 * (1.0 + erf(-7.5 * (r - rc) / rc));
-        t.df = 0.0;
-    } else {
-        const double rc = m.rcov4[j] + m.rcov4[i];
-        const double den = k4 * exp(-sq(fabs(m.en4[i] - m.en4[j]) + k5) / k6);
-        t.cf = den * 0.5 * (1.0 + erf(-7.5 * (r - rc) / rc));
-        t.df = 0.0;
-    }
-    return true;
-}
 
 __global__ void k_cn(DevMol m, int mode, double* __restrict__ cn) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m.nat) return;
-    const double xi = m.xyz[3 * i], yi = m.xyz[3 * i + 1], zi = m.xyz[3 * i + 2];
-    double s = 0.0;
-    for (int j = 0; j < m.nat; ++j) {
-        if (j == i) continue;
-        const double r2 = sq(m.xyz[3 * j] - xi) + sq(m.xyz[3 * j + 1] - yi) + sq(m.xyz[3 * j + 2] - zi);
-        CNTerm t;
-        if (cn_term(m, mode, i, j, r2, t)) s += t.cf;
-    }
-    cn[i] = s;
+    d_cn(m, mode, cn, i);
 }
+
 
 void cn(cudaStream_t st, const DevMol& m, int mode, double* out) {
     k_cn<<<ceil_div(m.nat, 128), 128, 0, st>>>(m, mode, out);
     XG_LAUNCH_CHECK();
 }
 
-// g[a] += sum_b den*dcount(r_ab)*(R_a - R_b)/r_ab * (v_a + v_b)  ==  sum_b dCN_b/dR_a v_b
+
 __global__ void k_cn_chain(DevMol m, int mode, const double* __restrict__ v, double* __restrict__ g) {
     const int a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= m.nat) return;
-    const double xa = m.xyz[3 * a], ya = m.xyz[3 * a + 1], za = m.xyz[3 * a + 2];
-    double gx = 0, gy = 0, gz = 0;
-    for (int b = 0; b < m.nat; ++b) {
-        if (b == a) continue;
-        const double dx = xa - m.xyz[3 * b], dy = ya - m.xyz[3 * b + 1], dz = za - m.xyz[3 * b + 2];
-        const double r2 = dx * dx + dy * dy + dz * dz;
-        CNTerm t;
-        if (!cn_term(m, mode, a, b, r2, t)) continue;
-        const double f = t.df / sqrt(r2) * (v[a] + v[b]);
-        gx += f * dx; gy += f * dy; gz += f * dz;
-    }
-    g[3 * a] += gx; g[3 * a + 1] += gy; g[3 * a + 2] += gz;
+    d_cn_chain(m, mode, v, g, a);
 }
+
 
 void cn_chain(cudaStream_t st, const DevMol& m, int mode, const double* v, double* grad) {
     k_cn_chain<<<ceil_div(m.nat, 128), 128, 0, st>>>(m, mode, v, grad);
     XG_LAUNCH_CHECK();
 }
 
-// ================================================================== EEQ guess
-// get_coulomb_matrix_0d and eeq_chrgeq_core (src/eeq_model.f90:60-80, 678-880), 2019 model.
+
 __global__ void k_eeq_matrix(DevMol m, const double* __restrict__ cn, double* __restrict__ A, double* __restrict__ X) {
     const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
     const int n = m.nat;
     if (t >= (long)n * n) return;
-    const int i = (int)(t / n), j = (int)(t % n);
-    if (i == j) {
-        A[t] = m.eeq_gam[i] + sqrt(2.0 / PI) / m.eeq_alpha[i];
-        const double tmp = m.eeq_kappa[i] / (sqrt(cn[i]) + 1e-14);
-        X[i] = -m.eeq_en[i] + tmp * cn[i];
-        X[n + i] = 1.0;
-    } else {
-        const double r = sqrt(sq(m.xyz[3 * j] - m.xyz[3 * i]) + sq(m.xyz[3 * j + 1] - m.xyz[3 * i + 1]) +
-                              sq(m.xyz[3 * j + 2] - m.xyz[3 * i + 2]));
-        const double gij = 1.0 / sqrt(sq(m.eeq_alpha[i]) + sq(m.eeq_alpha[j]));
-        A[t] = erf(gij * r) / r;
-    }
+    d_eeq_matrix(m, cn, A, X, t);
 }
+
 
 void eeq_setup(cudaStream_t st, const DevMol& m, const double* cnv, double* A, double* X) {
     k_eeq_matrix<<<ceil_div((long)m.nat * m.nat, 256), 256, 0, st>>>(m, cnv, A, X);
     XG_LAUNCH_CHECK();
 }
 
-// Solve U^T U x = b for two right-hand sides in X[0:n], X[n:2n]; then the charge constraint.
+
 __global__ void k_eeq_solve(int n, const double* __restrict__ U, double* __restrict__ X, double charge,
-                            double* __restrict__ q) {
-    __shared__ double red[32];
-    __shared__ double y0, y1;
-    double* b0 = X;
-    double* b1 = X + n;
-    // forward: U^T y = b (row i of U holds column i of U^T)
-    for (int i = 0; i < n; ++i) {
-        if (threadIdx.x == 0) {
-            y0 = b0[i] / U[(size_t)i * n + i];
-            y1 = b1[i] / U[(size_t)i * n + i];
-            b0[i] = y0;
-            b1[i] = y1;
-        }
-        __syncthreads();
-        const double* ur = U + (size_t)i * n;
-        for (int k = i + 1 + threadIdx.x; k < n; k += blockDim.x) {
-            b0[k] -= ur[k] * y0;
-            b1[k] -= ur[k] * y1;
-        }
-        __syncthreads();
-    }
-    // backward: U x = y
-    for (int i = n - 1; i >= 0; --i) {
-        const double* ur = U + (size_t)i * n;
-        double s0 = 0.0, s1 = 0.0;
-        for (int k = i + 1 + threadIdx.x; k < n; k += blockDim.x) {
-            s0 += ur[k] * b0[k];
-            s1 += ur[k] * b1[k];
-        }
-        s0 = block_sum(s0, red);
-        s1 = block_sum(s1, red);
-        if (threadIdx.x == 0) {
-            b0[i] = (b0[i] - s0) / ur[i];
-            b1[i] = (b1[i] - s1) / ur[i];
-        }
-        __syncthreads();
-    }
-    double sx0 = 0.0, sx1 = 0.0;
-    for (int k = threadIdx.x; k < n; k += blockDim.x) { sx0 += b0[k]; sx1 += b1[k]; }
-    sx0 = block_sum(sx0, red);
-    sx1 = block_sum(sx1, red);
-    const double lam = (sx0 - charge) / sx1;
-    for (int k = threadIdx.x; k < n; k += blockDim.x) q[k] = b0[k] - lam * b1[k];
-}
+                            double* __restrict__ q) { d_eeq_solve(n, U, X, charge, q); }
+
 
 void eeq_finish(cudaStream_t st, int nat, const double* Uf, double* X, double charge, double* q, double*) {
     k_eeq_solve<<<1, 1024, 0, st>>>(nat, Uf, X, charge, q);
     XG_LAUNCH_CHECK();
 }
 
-// dE/dCN from the diagonal self energies (src/xtb/hamiltonian.F90:778-786)
+
 __global__ void k_dhdcn_diag(DevMol m, const double* __restrict__ P, double* __restrict__ dhdcn) {
     const int a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= m.nat) return;
-    double s = 0.0;
-    for (int mu = m.at_ao0[a]; mu < m.at_ao0[a] + m.at_nao[a]; ++mu)
-        s += P[(size_t)mu * m.nao + mu] * (-m.sh_kcn[m.ao_sh[mu]]) * EVTOAU;
-    dhdcn[a] += s;
+    d_dhdcn_diag(m, P, dhdcn, a);
 }
+
 
 void dhdcn_diag(cudaStream_t st, const DevMol& m, const double* P, double* dhdcn) {
     k_dhdcn_diag<<<ceil_div(m.nat, 128), 128, 0, st>>>(m, P, dhdcn);
     XG_LAUNCH_CHECK();
 }
 
-// ================================================================== isotropic electrostatics
-// getCoulombMatrixCluster with arithmetic hardness average (src/coulomb/klopmanohno.F90:257-312, 742-755)
+
 __global__ void k_jmat(DevMol m, double* __restrict__ J) {
     const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
     const int ns = m.nsh;
     if (t >= (long)ns * ns) return;
-    const int s = (int)(t / ns), u = (int)(t % ns);
-    const int a = m.sh_atom[s], b = m.sh_atom[u];
-    const double gij = 0.5 * (m.sh_eta[s] + m.sh_eta[u]);
-    if (a == b) {
-        J[t] = (s == u) ? m.sh_eta[s] : gij;
-    } else {
-        const double r = sqrt(sq(m.xyz[3 * a] - m.xyz[3 * b]) + sq(m.xyz[3 * a + 1] - m.xyz[3 * b + 1]) +
-                              sq(m.xyz[3 * a + 2] - m.xyz[3 * b + 2]));
-        J[t] = 1.0 / sqrt(r * r + 1.0 / (gij * gij));
-    }
+    d_jmat(m, J, t);
 }
+
 
 void coulomb_matrix(cudaStream_t st, const DevMol& m, double* J) {
     k_jmat<<<ceil_div((long)m.nsh * m.nsh, 256), 256, 0, st>>>(m, J);
     XG_LAUNCH_CHECK();
 }
 
-// shift_s = (J qsh)_s + Gamma_s qsh_s^2 + v_D4[atom(s)]  (TxTBCoulomb%addShift, src/xtb/coulomb.f90:89-114,
-// src/xtb/thirdorder.f90:100-131); one warp per shell row
+
 __global__ void k_shell_shift(DevMol m, const double* __restrict__ J, const double* __restrict__ qsh,
                               const double* __restrict__ vat, double* __restrict__ shift, double* __restrict__ Jq) {
     const int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (s >= m.nsh) return;
-    const double* row = J + (size_t)s * m.nsh;
-    double acc = 0.0;
-    for (int u = lane; u < m.nsh; u += 32) acc = fma(row[u], qsh[u], acc);
-    acc = warp_sum(acc);
-    if (lane == 0) {
-        Jq[s] = acc;
-        shift[s] = acc + m.sh_gam3[s] * qsh[s] * qsh[s] + (vat ? vat[m.sh_atom[s]] : 0.0);
-    }
+    d_shell_shift(m, J, qsh, vat, shift, Jq, s, lane);
 }
+
 
 void shell_shift(cudaStream_t st, const DevMol& m, const double* J, const double* qsh, const double* vat,
                  double* shift, double* Jq) {
@@ -243,31 +104,21 @@ void shell_shift(cudaStream_t st, const DevMol& m, const double* J, const double
     XG_LAUNCH_CHECK();
 }
 
-// ================================================================== anisotropic electrostatics
-// get_radcn + mmomgabzero (src/aespot.F90:1219-1281, 1309-1329)
+
 __global__ void k_radcn(DevMol m, const double* __restrict__ cn, double* __restrict__ radcn) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m.nat) return;
-    const double rco = m.mrad[i];
-    const double t1 = cn[i] - m.valcn[i] - 1.2;
-    radcn[i] = rco + (5.0 - rco) / (1.0 + exp(-4.0 * t1));
+    d_radcn(m, cn, radcn, i);
 }
+
 
 __global__ void k_gab(DevMol m, const double* __restrict__ radcn, double* __restrict__ gab3, double* __restrict__ gab5) {
     const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
     const int n = m.nat;
     if (t >= (long)n * n) return;
-    const int i = (int)(t / n), j = (int)(t % n);
-    if (i == j) { gab3[t] = 0.0; gab5[t] = 0.0; return; }
-    const double r = sqrt(sq(m.xyz[3 * j] - m.xyz[3 * i]) + sq(m.xyz[3 * j + 1] - m.xyz[3 * i + 1]) +
-                          sq(m.xyz[3 * j + 2] - m.xyz[3 * i + 2]));
-    const double ri = 1.0 / r;
-    const double rco = 0.5 * (radcn[i] + radcn[j]);
-    const double d3 = 1.0 / (1.0 + 6.0 * pow(rco * ri, 3.0));
-    const double d5 = 1.0 / (1.0 + 6.0 * pow(rco * ri, 4.0));
-    gab3[t] = d3 * pow(ri, 3.0);
-    gab5[t] = d5 * pow(ri, 5.0);
+    d_gab(m, radcn, gab3, gab5, t);
 }
+
 
 void aes_setup(cudaStream_t st, const DevMol& m, const double* cnv, double* radcn, double* gab3, double* gab5) {
     k_radcn<<<ceil_div(m.nat, 128), 128, 0, st>>>(m, cnv, radcn);
@@ -276,96 +127,15 @@ void aes_setup(cudaStream_t st, const DevMol& m, const double* cnv, double* radc
     XG_LAUNCH_CHECK();
 }
 
-__device__ __forceinline__ int lin3(int a, int b) {  // packed index of (a,b): xx xy yy xz yz zz
-    const int hi = a > b ? a : b, lo = a > b ? b : a;
-    return hi * (hi + 1) / 2 + lo;
-}
 
-// setvsdq (shifted = true, src/aespot.F90:727-848) / setdvsdq (src/aespot.F90:861-952); one warp per atom
 __global__ void k_aes_pot(DevMol m, const double* __restrict__ q, const double* __restrict__ dipm,
                           const double* __restrict__ qp, const double* __restrict__ gab3, const double* __restrict__ gab5,
                           int shifted, double* __restrict__ vs, double* __restrict__ vd, double* __restrict__ vq) {
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (i >= m.nat) return;
-    const int n = m.nat;
-    const double ra[3] = {m.xyz[3 * i], m.xyz[3 * i + 1], m.xyz[3 * i + 2]};
-    const double r2a = ra[0] * ra[0] + ra[1] * ra[1] + ra[2] * ra[2];
-    double stmp = 0.0, dt[3] = {0, 0, 0}, qt[6] = {0, 0, 0, 0, 0, 0};
-    for (int j = lane; j < n; j += 32) {
-        const double g3 = gab3[(size_t)j * n + i], g5 = gab5[(size_t)j * n + i];
-        if (g3 == 0.0 && g5 == 0.0) continue;
-        const double dra[3] = {ra[0] - m.xyz[3 * j], ra[1] - m.xyz[3 * j + 1], ra[2] - m.xyz[3 * j + 2]};
-        const double qj = q[j];
-        const double* dj = dipm + 3 * j;
-        const double* qpj = qp + 6 * j;
-        double r2ab = 0, t1a = 0, t2a = 0, t3a = 0, qdd = 0;
-        for (int l1 = 0; l1 < 3; ++l1) {
-            r2ab += dra[l1] * dra[l1];
-            t1a += ra[l1] * dra[l1];
-            t2a += dj[l1] * dra[l1];
-            t3a += ra[l1] * dj[l1];
-            for (int l2 = 0; l2 < 3; ++l2) qdd += qpj[lin3(l1, l2)] * dra[l1] * dra[l2];
-        }
-        double dum3a, dum5a;
-        if (shifted) {
-            dum5a = -qdd - 1.5 * qj * t1a * t1a;
-            dum3a = -t1a * qj - t2a;
-            dum5a += t3a * r2ab - 3.0 * t1a * t2a + 0.5 * qj * r2a * r2ab;
-        } else {
-            dum3a = -t2a;
-            dum5a = -qdd;
-        }
-        stmp += dum5a * g5 + dum3a * g3;
-        for (int l1 = 0; l1 < 3; ++l1) {
-            double d5 = 3.0 * dra[l1] * t2a - r2ab * dj[l1];
-            if (shifted) d5 += -qj * r2ab * ra[l1] + 3.0 * qj * dra[l1] * t1a;
-            dt[l1] += dra[l1] * qj * g3 + d5 * g5;
-            qt[l1] += -1.5 * qj * g5 * dra[l1] * dra[l1] + 0.5 * r2ab * qj * g5;
-        }
-        qt[3] += -3.0 * qj * g5 * dra[0] * dra[1];
-        qt[4] += -3.0 * qj * g5 * dra[0] * dra[2];
-        qt[5] += -3.0 * qj * g5 * dra[1] * dra[2];
-    }
-    stmp = warp_sum(stmp);
-    for (int k = 0; k < 3; ++k) dt[k] = warp_sum(dt[k]);
-    for (int k = 0; k < 6; ++k) qt[k] = warp_sum(qt[k]);
-    if (lane != 0) return;
-    const double qs1 = m.dkern[i] * 2.0, qs2 = m.qkern[i] * 6.0;
-    const double* di = dipm + 3 * i;
-    const double* qpi = qp + 6 * i;
-    double t3 = 0.0;
-    for (int l1 = 0; l1 < 3; ++l1) {
-        if (shifted) t3 += ra[l1] * di[l1] * qs1;
-        dt[l1] -= qs1 * di[l1];
-        for (int l2 = 0; l2 < l1; ++l2) {
-            const int ll = lin3(l1, l2), ki = l1 + l2 + 2;
-            qt[ki] -= qpi[ll] * qs2;
-            if (shifted) {
-                t3 -= ra[l1] * ra[l2] * qpi[ll] * qs2;
-                dt[l1] += ra[l2] * qpi[ll] * qs2;
-                dt[l2] += ra[l1] * qpi[ll] * qs2;
-            }
-        }
-        const int ll = lin3(l1, l1);
-        qt[l1] -= qpi[ll] * qs2 * 0.5;
-        if (shifted) {
-            t3 -= ra[l1] * ra[l1] * qpi[ll] * qs2 * 0.5;
-            dt[l1] += ra[l1] * qpi[ll] * qs2;
-        }
-    }
-    if (shifted) stmp += t3;
-    const double tr = (qpi[0] + qpi[2] + qpi[5]) * m.qkern[i];
-    for (int l1 = 0; l1 < 3; ++l1) {
-        qt[l1] += tr;
-        if (shifted) {
-            dt[l1] -= 2.0 * ra[l1] * tr;
-            stmp += tr * ra[l1] * ra[l1];
-        }
-    }
-    vs[i] = stmp;
-    for (int k = 0; k < 3; ++k) vd[3 * i + k] = dt[k];
-    for (int k = 0; k < 6; ++k) vq[6 * i + k] = qt[k];
+    d_aes_pot(m, q, dipm, qp, gab3, gab5, shifted, vs, vd, vq, i, lane);
 }
+
 
 void aes_potential(cudaStream_t st, const DevMol& m, const double* q, const double* dipm, const double* qp,
                    const double* gab3, const double* gab5, bool shifted, double* vs, double* vd, double* vq) {
@@ -373,45 +143,15 @@ void aes_potential(cudaStream_t st, const DevMol& m, const double* q, const doub
     XG_LAUNCH_CHECK();
 }
 
-// aniso_electro_cpu (src/aespot.F90:566-664): e_part[i] = pair terms with j < i, e_part[n+i] = kernel term
+
 __global__ void k_aes_energy(DevMol m, const double* __restrict__ q, const double* __restrict__ dipm,
                              const double* __restrict__ qp, const double* __restrict__ gab3,
                              const double* __restrict__ gab5, double* __restrict__ e_part) {
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (i >= m.nat) return;
-    const int n = m.nat;
-    const double* di = dipm + 3 * i;
-    const double* qi = qp + 6 * i;
-    double e = 0.0;
-    for (int j = lane; j < i; j += 32) {
-        const double rij[3] = {m.xyz[3 * j] - m.xyz[3 * i], m.xyz[3 * j + 1] - m.xyz[3 * i + 1],
-                               m.xyz[3 * j + 2] - m.xyz[3 * i + 2]};
-        const double r2 = rij[0] * rij[0] + rij[1] * rij[1] + rij[2] * rij[2];
-        const double* dj = dipm + 3 * j;
-        const double* qj = qp + 6 * j;
-        double ed = 0, eq = 0, edd = 0;
-        for (int k = 0; k < 3; ++k) {
-            ed += q[j] * di[k] * rij[k] - dj[k] * q[i] * rij[k];
-            for (int l = 0; l < 3; ++l) {
-                const int kl = lin3(l, k);
-                const double tt = rij[l] * rij[k];
-                eq += q[j] * qi[kl] * tt + qj[kl] * q[i] * tt;
-                edd -= dj[k] * di[l] * 3.0 * tt;
-            }
-            edd += dj[k] * di[k] * r2;
-        }
-        e += ed * gab3[(size_t)j * n + i] + (eq + edd) * gab5[(size_t)j * n + i];
-    }
-    e = warp_sum(e);
-    if (lane == 0) {
-        double tt = di[0] * di[0] + di[1] * di[1] + di[2] * di[2];
-        double tt3 = 0.0;
-        for (int k = 0; k < 3; ++k)
-            for (int l = 0; l < 3; ++l) tt3 += qi[lin3(l, k)] * qi[lin3(l, k)];
-        e_part[i] = e;
-        e_part[n + i] = m.dkern[i] * tt + tt3 * m.qkern[i];
-    }
+    d_aes_energy(m, q, dipm, qp, gab3, gab5, e_part, i, lane);
 }
+
 
 void aes_energy(cudaStream_t st, const DevMol& m, const double* q, const double* dipm, const double* qp,
                 const double* gab3, const double* gab5, double* e_part) {
@@ -419,69 +159,16 @@ void aes_energy(cudaStream_t st, const DevMol& m, const double* q, const double*
     XG_LAUNCH_CHECK();
 }
 
-// aniso_grad (src/aespot.F90:1060-1165); tmp2[i] collects the radius-derivative prefactor
+
 __global__ void k_aes_grad(DevMol m, const double* __restrict__ q, const double* __restrict__ dipm,
                            const double* __restrict__ qp, const double* __restrict__ radcn,
                            const double* __restrict__ gab3, const double* __restrict__ gab5, double* __restrict__ grad,
                            double* __restrict__ tmp2) {
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (i >= m.nat) return;
-    const int n = m.nat;
-    const double* di = dipm + 3 * i;
-    const double* Qi = qp + 6 * i;
-    double g[3] = {0, 0, 0}, t2 = 0.0;
-    for (int j = lane; j < n; j += 32) {
-        if (j == i) continue;
-        const double rij[3] = {m.xyz[3 * j] - m.xyz[3 * i], m.xyz[3 * j + 1] - m.xyz[3 * i + 1],
-                               m.xyz[3 * j + 2] - m.xyz[3 * i + 2]};
-        const double r2 = rij[0] * rij[0] + rij[1] * rij[1] + rij[2] * rij[2];
-        const double rabi = 1.0 / sqrt(r2);
-        const double rco = 0.5 * (radcn[i] + radcn[j]);
-        const double damp1 = 1.0 / (1.0 + 6.0 * pow(rco * rabi, 3.0));
-        const double dd1 = -3.0 * rabi * (damp1 * damp1 - damp1);
-        const double dgab3 = (-3.0 * rabi * pow(rabi, 3.0)) * damp1 + dd1 * pow(rabi, 3.0);
-        const double damp2 = 1.0 / (1.0 + 6.0 * pow(rco * rabi, 4.0));
-        const double dd2 = -4.0 * rabi * (damp2 * damp2 - damp2);
-        const double dgab5 = (-5.0 * rabi * pow(rabi, 5.0)) * damp2 + dd2 * pow(rabi, 5.0);
-        const double G3 = gab3[(size_t)j * n + i], G5 = gab5[(size_t)j * n + i];
-        const double* dj = dipm + 3 * j;
-        const double* Qj = qp + 6 * j;
-        double ed = 0, eq = 0, edd = 0;
-        for (int k = 0; k < 3; ++k) {
-            ed += q[j] * di[k] * rij[k] - dj[k] * q[i] * rij[k];
-            g[k] += G3 * (q[i] * dj[k] - q[j] * di[k]);
-            double ddm2 = 0, ddm3a = 0, ddm3b = 0, qqa = 0, qqb = 0;
-            for (int l = 0; l < 3; ++l) {
-                const int kl = lin3(l, k);
-                const double tt = rij[l] * rij[k];
-                eq += q[j] * Qi[kl] * tt + Qj[kl] * q[i] * tt;
-                edd -= dj[k] * di[l] * 3.0 * tt;
-                ddm2 += dj[l] * di[l];
-                ddm3a += di[l] * rij[l];
-                ddm3b += dj[l] * rij[l];
-                qqa += rij[l] * Qj[kl];
-                qqb += rij[l] * Qi[kl];
-            }
-            edd += dj[k] * di[k] * r2;
-            g[k] += -2.0 * G5 * ddm2 * rij[k] + 3.0 * G5 * ddm3a * dj[k] + 3.0 * G5 * ddm3b * di[k] -
-                    2.0 * G5 * qqa * q[i] - 2.0 * G5 * qqb * q[j];
-        }
-        for (int k = 0; k < 3; ++k) {
-            const double dxi = rij[k] * rabi;
-            g[k] -= ed * dgab3 * dxi + (eq + edd) * dgab5 * dxi;
-        }
-        const double rab = 0.5 * (radcn[i] + radcn[j]);
-        t2 += ed * 3.0 * G3 * (damp1 / rab) * pow(rab * rabi, 3.0) + (eq + edd) * 4.0 * G5 * (damp2 / rab) * pow(rab * rabi, 4.0);
-    }
-    for (int k = 0; k < 3; ++k) g[k] = warp_sum(g[k]);
-    t2 = warp_sum(t2);
-    if (lane == 0) {
-        grad[3 * i] += g[0];
-        grad[3 * i + 1] += g[1];
-        grad[3 * i + 2] += g[2];
-        tmp2[i] = 3.0 * t2;
-    }
+    d_aes_grad(m, q, dipm, qp, radcn, gab3, gab5, grad, tmp2, i, lane);
 }
+
 
 void aes_grad(cudaStream_t st, const DevMol& m, const double* q, const double* dipm, const double* qp,
               const double* radcn, const double* gab3, const double* gab5, double* grad, double* tmp2) {
@@ -489,57 +176,30 @@ void aes_grad(cudaStream_t st, const DevMol& m, const double* q, const double* d
     XG_LAUNCH_CHECK();
 }
 
-// dradcn (src/aespot.F90:1292-1307): dhdcn[i] -= tmp2[i] * dR0_i/dCN_i (chain through the gfn CN)
+
 __global__ void k_aes_dradcn(DevMol m, const double* __restrict__ cn, const double* __restrict__ tmp2,
                              double* __restrict__ dhdcn) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m.nat) return;
-    const double rco = m.mrad[i];
-    const double t1 = exp(-4.0 * (cn[i] - m.valcn[i] - 1.2));
-    double t2 = (5.0 - rco) / (1.0 + 2.0 * t1 + t1 * t1);
-    t2 = t2 * 4.0 * t1;
-    dhdcn[i] -= tmp2[i] * t2;
+    d_aes_dradcn(m, cn, tmp2, dhdcn, i);
 }
+
 
 void aes_dradcn(cudaStream_t st, const DevMol& m, const double* cnv, const double* tmp2, double* dhdcn) {
     k_aes_dradcn<<<ceil_div(m.nat, 128), 128, 0, st>>>(m, cnv, tmp2, dhdcn);
     XG_LAUNCH_CHECK();
 }
 
-// ================================================================== Hamiltonian build
-// buildIsoAnisotropicH1 (src/scc_core.f90:154-251) with the setdqlist screening (src/aespot.F90:34-85)
+
 __global__ void k_build_h(DevMol m, double neglect, const double* __restrict__ H0, const double* __restrict__ S,
                           const double* __restrict__ D, const double* __restrict__ Q, const double* __restrict__ shift,
                           const double* __restrict__ vs, const double* __restrict__ vd, const double* __restrict__ vq,
                           double* __restrict__ H) {
-    const size_t nao = m.nao, nn = nao * nao;
     const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nn) return;
-    const int i = (int)(t / nao), j = (int)(t % nao);
-    const int si = m.ao_sh[i], sj = m.ao_sh[j], ai = m.ao_at[i], aj = m.ao_at[j];
-    const double dum = S[t] * AUTOEV * 0.5;
-    double h = H0[t] - dum * (shift[si] + shift[sj]) + dum * (vs[ai] + vs[aj]);
-    const double thr2 = neglect * 1.0e-2;
-    double d[3], tmp1 = 0.0;
-#pragma unroll
-    for (int k = 0; k < 3; ++k) { d[k] = D[k * nn + t]; tmp1 += d[k] * d[k]; }
-    if (tmp1 > thr2) {
-        double e = 0.0;
-#pragma unroll
-        for (int k = 0; k < 3; ++k) e += d[k] * (vd[3 * ai + k] + vd[3 * aj + k]);
-        h += 0.5 * e * AUTOEV;
-    }
-    double qq[6], tmp2 = 0.0;
-#pragma unroll
-    for (int k = 0; k < 6; ++k) { qq[k] = Q[k * nn + t]; tmp2 += (k < 3 ? 1.0 : 2.0) * qq[k] * qq[k]; }
-    if (tmp2 > thr2) {
-        double e = 0.0;
-#pragma unroll
-        for (int k = 0; k < 6; ++k) e += qq[k] * (vq[6 * ai + k] + vq[6 * aj + k]);
-        h += 0.5 * e * AUTOEV;
-    }
-    H[t] = h;
+    if (t >= (size_t)m.nao * m.nao) return;
+    d_build_h(m, neglect, H0, S, D, Q, shift, vs, vd, vq, H, t);
 }
+
 
 void build_h(cudaStream_t st, const DevMol& m, Thresholds th, const double* H0, const double* S, const double* D,
              const double* Q, const double* shift, const double* vs, const double* vd, const double* vq, double* H) {
@@ -548,84 +208,11 @@ void build_h(cudaStream_t st, const DevMol& m, Thresholds th, const double* H0, 
     XG_LAUNCH_CHECK();
 }
 
-// ================================================================== Fermi smearing
-// fermismear (src/scc_core.f90:983-1064) for one spin channel; one block.
-__device__ void fermi_channel(int n, const double* emo, int nel, double etemp, double* occ, double* red,
-                              double& s_out, double& ef_out) {
-    const double bkt = KB_AU * AUTOEV * etemp;
-    const double thr = 1e-9;
-    double ef;
-    if (nel + 1 > n) {
-        // no LUMO: the integer occupations of occu are kept (src/scc_core.f90:1001-1004)
-        ef = emo[nel - 1];
-        for (int i = threadIdx.x; i < n; i += blockDim.x) occ[i] = (i < nel) ? 1.0 : 0.0;
-    } else if (nel == 0) {
-        ef = emo[0];
-        for (int i = threadIdx.x; i < n; i += blockDim.x) occ[i] = 0.0;
-    } else {
-        ef = 0.5 * (emo[nel - 1] + emo[nel]);
-        const double occt = (double)nel;
-        for (int cyc = 0; cyc < 200; ++cyc) {
-            double tot = 0.0, totd = 0.0;
-            for (int i = threadIdx.x; i < n; i += blockDim.x) {
-                const double x = (emo[i] - ef) / bkt;
-                double f = 0.0, df = 0.0;
-                if (x < 50.0) {
-                    const double ex = exp(x);
-                    f = 1.0 / (ex + 1.0);
-                    df = ex / (bkt * (ex + 1.0) * (ex + 1.0));
-                }
-                occ[i] = f;
-                tot += f;
-                totd += df;
-            }
-            tot = block_sum(tot, red);
-            totd = block_sum(totd, red);
-            ef += (occt - tot) / totd;
-            if (fabs(occt - tot) <= thr) break;
-        }
-    }
-    __syncthreads();
-    double s = 0.0;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const double o = occ[i];
-        if (o > thr && 1.0 - o > thr) s += o * log(o) + (1.0 - o) * log(1.0 - o);
-    }
-    s = block_sum(s, red);
-    s_out = s * KB_AU * etemp;
-    ef_out = ef;
-}
 
 __global__ void k_fermi(int n, const double* __restrict__ emo, int nel_a, int nel_b, double etemp,
                         double* __restrict__ focc, double* __restrict__ fa, double* __restrict__ fb,
-                        double* __restrict__ scal, int* __restrict__ kocc) {
-    __shared__ double red[32];
-    __shared__ int kmax;
-    double sa, efa, sb, efb;
-    fermi_channel(n, emo, nel_a, etemp, fa, red, sa, efa);
-    if (nel_b == nel_a) {
-        __syncthreads();
-        for (int i = threadIdx.x; i < n; i += blockDim.x) fb[i] = fa[i];
-        sb = sa;
-        efb = efa;
-    } else {
-        fermi_channel(n, emo, nel_b, etemp, fb, red, sb, efb);
-    }
-    if (threadIdx.x == 0) kmax = max(nel_a, nel_b);
-    __syncthreads();
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const double f = fa[i] + fb[i];
-        focc[i] = f;
-        if (f > 0.0) atomicMax(&kmax, i + 1);
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        kocc[0] = min(kmax, n);
-        scal[0] = sa + sb;
-        scal[1] = efa;
-        scal[2] = efb;
-    }
-}
+                        double* __restrict__ scal, int* __restrict__ kocc) { d_fermi(n, emo, nel_a, nel_b, etemp, focc, fa, fb, scal, kocc); }
+
 
 void fermi(cudaStream_t st, int n, const double* emo, int nel_a, int nel_b, double etemp, double* focc, double* fa,
            double* fb, double* scal, int* kocc) {
@@ -633,85 +220,36 @@ void fermi(cudaStream_t st, int n, const double* emo, int nel_a, int nel_b, doub
     XG_LAUNCH_CHECK();
 }
 
+
 __global__ void k_scale_cols(int n, const double* __restrict__ C, const double* __restrict__ f, double* __restrict__ Cf) {
     const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (size_t)n * n) return;
-    const double fj = f[t % n];
-    Cf[t] = (fj == 0.0) ? 0.0 : C[t] * fj;     // exact zeros for unoccupied columns
+    d_scale_cols(n, C, f, Cf, t);
 }
+
 
 void scale_cols(cudaStream_t st, int n, const double* C, const double* f, double* Cf) {
     k_scale_cols<<<ceil_div((long)n * n, 256), 256, 0, st>>>(n, C, f, Cf);
     XG_LAUNCH_CHECK();
 }
 
-// ================================================================== populations
-// mpopsh + qsh2qat + mmompop_cpu + the H0 energy sum (src/scc_core.f90:1408-1444, src/aespot.F90:288-428,
-// src/scc_core.f90:686-722).  Pass 1: one warp per AO row computes 11 row sums.
+
 __global__ void k_rowsums(DevMol m, const double* __restrict__ P, const double* __restrict__ S,
                           const double* __restrict__ D, const double* __restrict__ Q, const double* __restrict__ H0,
                           double* __restrict__ rows) {
     const int mu = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (mu >= m.nao) return;
-    const size_t nao = m.nao, nn = nao * nao, off = (size_t)mu * nao;
-    double acc[11];
-#pragma unroll
-    for (int k = 0; k < 11; ++k) acc[k] = 0.0;
-    for (int nu = lane; nu < m.nao; nu += 32) {
-        const double p = P[off + nu];
-        acc[0] += p * S[off + nu];
-#pragma unroll
-        for (int k = 0; k < 3; ++k) acc[1 + k] += p * D[k * nn + off + nu];
-#pragma unroll
-        for (int k = 0; k < 6; ++k) acc[4 + k] += p * Q[k * nn + off + nu];
-        acc[10] += p * H0[off + nu];
-    }
-#pragma unroll
-    for (int k = 0; k < 11; ++k) acc[k] = warp_sum(acc[k]);
-    if (lane == 0)
-#pragma unroll
-        for (int k = 0; k < 11; ++k) rows[(size_t)mu * 12 + k] = acc[k];
+    d_rowsums(m, P, S, D, Q, H0, rows, mu, lane);
 }
 
-// Pass 2: one thread per atom.
+
 __global__ void k_atom_pop(DevMol m, const double* __restrict__ rows, double* __restrict__ qsh, double* __restrict__ q,
                            double* __restrict__ dipm, double* __restrict__ qp, double* __restrict__ eh0) {
     const int a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= m.nat) return;
-    const double R[3] = {m.xyz[3 * a], m.xyz[3 * a + 1], m.xyz[3 * a + 2]};
-    double qa = 0.0, e = 0.0;
-    double dp[3] = {0, 0, 0}, qq[6] = {0, 0, 0, 0, 0, 0};
-    for (int s = m.at_sh0[a]; s < m.at_sh0[a] + m.at_nsh[a]; ++s) {
-        double pop = 0.0;
-        const int nfun = 2 * m.sh_l[s] + 1;
-        for (int mu = m.sh_ao[s]; mu < m.sh_ao[s] + nfun; ++mu) {
-            const double* r = rows + (size_t)mu * 12;
-            pop += r[0];
-            e += r[10];
-            for (int k = 0; k < 3; ++k) dp[k] += R[k] * r[0] - r[1 + k];
-            // packed (xx, xy, yy, xz, yz, zz); qpint order xx yy zz xy xz yz
-            const int qidx[3][3] = {{0, 3, 4}, {3, 1, 5}, {4, 5, 2}};
-            for (int k = 0; k < 3; ++k)
-                for (int l = 0; l <= k; ++l) {
-                    const int kl = k * (k + 1) / 2 + l;
-                    double t;
-                    if (k == l) t = 2.0 * r[1 + k] * R[k] - R[k] * R[k] * r[0] - r[4 + qidx[k][k]];
-                    else t = r[1 + k] * R[l] + r[1 + l] * R[k] - R[l] * R[k] * r[0] - r[4 + qidx[k][l]];
-                    qq[kl] += t;
-                }
-        }
-        const double v = m.sh_zsh[s] - pop;
-        qsh[s] = v;
-        qa += v;
-    }
-    q[a] = qa;
-    const double tr = 0.5 * (qq[0] + qq[2] + qq[5]);
-    for (int k = 0; k < 6; ++k) qq[k] *= 1.5;
-    qq[0] -= tr; qq[2] -= tr; qq[5] -= tr;
-    for (int k = 0; k < 3; ++k) dipm[3 * a + k] = dp[k];
-    for (int k = 0; k < 6; ++k) qp[6 * a + k] = qq[k];
-    eh0[a] = e;
+    d_atom_pop(m, rows, qsh, q, dipm, qp, eh0, a);
 }
+
 
 void populations(cudaStream_t st, const DevMol& m, const double* P, const double* S, const double* D, const double* Q,
                  const double* H0, double* rows, double* qsh, double* q, double* dipm, double* qp, double* eh0) {
@@ -721,27 +259,26 @@ void populations(cudaStream_t st, const DevMol& m, const double* P, const double
     XG_LAUNCH_CHECK();
 }
 
-__global__ void k_reduce(const double* __restrict__ x, int n, double* __restrict__ out) {
-    __shared__ double red[32];
-    double s = 0.0;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) s += x[i];
-    s = block_sum(s, red);
-    if (threadIdx.x == 0) *out = s;
-}
+
+__global__ void k_reduce(const double* __restrict__ x, int n, double* __restrict__ out) { d_reduce(x, n, out); }
+
 
 void reduce_sum(cudaStream_t st, const double* x, int n, double* out) {
     k_reduce<<<1, 512, 0, st>>>(x, n, out);
     XG_LAUNCH_CHECK();
 }
 
+
 __global__ void k_add(int n, const double* __restrict__ a, double* __restrict__ b) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) b[i] += a[i];
 }
+
 void add_vec(cudaStream_t st, int n, const double* a, double* b) {
     k_add<<<ceil_div(n, 256), 256, 0, st>>>(n, a, b);
     XG_LAUNCH_CHECK();
 }
+
 
 // ================================================================== Broyden mixing
 // broyden (src/broyden.f90:37-153) with gfn2broyden_save/diff/out packing (src/aespot.F90:1360-1425)
@@ -755,6 +292,7 @@ __global__ void k_broyden_pack(DevMol m, const double* __restrict__ qsh, const d
         for (int k = 0; k < 6; ++k) o[3 + k] = qp[6 * t + k];
     }
 }
+
 __global__ void k_broyden_unpack(DevMol m, const double* __restrict__ v, double* __restrict__ qsh,
                                  double* __restrict__ dipm, double* __restrict__ qp, double* __restrict__ q) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -768,138 +306,24 @@ __global__ void k_broyden_unpack(DevMol m, const double* __restrict__ v, double*
         q[t] = s;
     }
 }
+
 void broyden_pack(cudaStream_t st, const DevMol& m, const double* qsh, const double* dipm, const double* qp, double* vec) {
     k_broyden_pack<<<ceil_div(std::max(m.nsh, m.nat), 256), 256, 0, st>>>(m, qsh, dipm, qp, vec);
     XG_LAUNCH_CHECK();
 }
+
 void broyden_unpack(cudaStream_t st, const DevMol& m, const double* vec, double* qsh, double* dipm, double* qp, double* q) {
     k_broyden_unpack<<<ceil_div(std::max(m.nsh, m.nat), 256), 256, 0, st>>>(m, vec, qsh, dipm, qp, q);
     XG_LAUNCH_CHECK();
 }
 
-// One block: dq = qout - qin, rms, Broyden update of qin in place.
+
 __global__ void k_broyden(int nbr, int it, int maxit, double alpha, double* __restrict__ qin,
                           const double* __restrict__ qout, double* __restrict__ dq, double* __restrict__ df,
                           double* __restrict__ u, double* __restrict__ amat, double* __restrict__ omega,
                           double* __restrict__ qlast, double* __restrict__ dqlast, double* __restrict__ work,
-                          double* __restrict__ rms_out, int nat) {
-    __shared__ double red[32];
-    __shared__ double s_inv;
-    double ss = 0.0;
-    for (int i = threadIdx.x; i < nbr; i += blockDim.x) {
-        const double d = qout[i] - qin[i];
-        dq[i] = d;
-        ss += d * d;
-    }
-    ss = block_sum(ss, red);
-    if (threadIdx.x == 0) { rms_out[0] = sqrt(ss / (double)nat); rms_out[1] = ss; }
-    if (it == 1) {
-        for (int i = threadIdx.x; i < nbr; i += blockDim.x) {
-            dqlast[i] = dq[i];
-            qlast[i] = qin[i];
-            qin[i] += alpha * dq[i];
-        }
-        return;
-    }
-    const int it1 = it - 1, r = it1 - 1;   // new history row r (0-based)
-    const double omega0 = 0.01, minw = 1.0, maxw = 100000.0, wfac = 0.01;
-    double om = sqrt(ss);
-    om = (om > wfac / maxw) ? wfac / om : maxw;
-    if (om < minw) om = minw;
-    double* dfr = df + (size_t)r * nbr;
-    double n2 = 0.0;
-    for (int i = threadIdx.x; i < nbr; i += blockDim.x) {
-        const double d = dq[i] - dqlast[i];
-        dfr[i] = d;
-        n2 += d * d;
-    }
-    n2 = block_sum(n2, red);
-    if (threadIdx.x == 0) { omega[r] = om; s_inv = 1.0 / sqrt(n2); }
-    __syncthreads();
-    const double inv = s_inv;
-    for (int i = threadIdx.x; i < nbr; i += blockDim.x) dfr[i] *= inv;
-    __syncthreads();
-    // a(i, r) for i <= r, c(i) = omega_i df_i . dq
-    double* c = work;                      // [maxit]
-    double* beta = work + maxit;           // [it1 x it1]
-    double* binv = beta + (size_t)maxit * maxit;
-    for (int i = 0; i < it1; ++i) {
-        const double* dfi = df + (size_t)i * nbr;
-        double s1 = 0.0, s2 = 0.0;
-        for (int k = threadIdx.x; k < nbr; k += blockDim.x) {
-            s1 += dfi[k] * dfr[k];
-            s2 += dfi[k] * dq[k];
-        }
-        s1 = block_sum(s1, red);
-        s2 = block_sum(s2, red);
-        if (threadIdx.x == 0) {
-            amat[(size_t)i * maxit + r] = s1;
-            amat[(size_t)r * maxit + i] = s1;
-            c[i] = omega[i] * s2;
-        }
-    }
-    __syncthreads();
-    // beta = omega_i omega_j a_ij + omega0^2 delta_ij ; invert by Gauss-Jordan with partial pivoting
-    for (int t = threadIdx.x; t < it1 * it1; t += blockDim.x) {
-        const int i = t / it1, j = t % it1;
-        beta[t] = omega[i] * omega[j] * amat[(size_t)i * maxit + j] + (i == j ? omega0 * omega0 : 0.0);
-        binv[t] = (i == j) ? 1.0 : 0.0;
-    }
-    __syncthreads();
-    __shared__ int piv;
-    for (int k = 0; k < it1; ++k) {
-        if (threadIdx.x == 0) {
-            int p = k;
-            double best = fabs(beta[k * it1 + k]);
-            for (int i = k + 1; i < it1; ++i)
-                if (fabs(beta[i * it1 + k]) > best) { best = fabs(beta[i * it1 + k]); p = i; }
-            piv = p;
-        }
-        __syncthreads();
-        const int p = piv;
-        if (p != k)
-            for (int j = threadIdx.x; j < it1; j += blockDim.x) {
-                double t1 = beta[k * it1 + j]; beta[k * it1 + j] = beta[p * it1 + j]; beta[p * it1 + j] = t1;
-                double t2 = binv[k * it1 + j]; binv[k * it1 + j] = binv[p * it1 + j]; binv[p * it1 + j] = t2;
-            }
-        __syncthreads();
-        const double pk = beta[k * it1 + k];
-        for (int j = threadIdx.x; j < it1; j += blockDim.x) { beta[k * it1 + j] /= pk; binv[k * it1 + j] /= pk; }
-        __syncthreads();
-        for (int t = threadIdx.x; t < it1 * it1; t += blockDim.x) {
-            const int i = t / it1, j = t % it1;
-            if (i == k) continue;
-            const double f = beta[i * it1 + k];
-            if (j != k) beta[t] -= f * beta[k * it1 + j];
-            binv[t] -= f * binv[k * it1 + j];
-        }
-        __syncthreads();
-        for (int i = threadIdx.x; i < it1; i += blockDim.x)
-            if (i != k) beta[i * it1 + k] = 0.0;
-        __syncthreads();
-    }
-    // gamma_j = sum_i c_i binv_ij ; store omega_j * gamma_j in work tail
-    double* og = binv + (size_t)maxit * maxit;
-    for (int j = threadIdx.x; j < it1; j += blockDim.x) {
-        double s = 0.0;
-        for (int i = 0; i < it1; ++i) s += c[i] * binv[i * it1 + j];
-        og[j] = omega[j] * s;
-    }
-    __syncthreads();
-    double* ur = u + (size_t)r * nbr;
-    for (int k = threadIdx.x; k < nbr; k += blockDim.x) {
-        const double qi = qin[k];
-        ur[k] = alpha * dfr[k] + inv * (qi - qlast[k]);
-        dqlast[k] = dq[k];
-        qlast[k] = qi;
-    }
-    __syncthreads();
-    for (int k = threadIdx.x; k < nbr; k += blockDim.x) {
-        double v = qin[k] + alpha * dq[k];
-        for (int i = 0; i < it1; ++i) v -= og[i] * u[(size_t)i * nbr + k];
-        qin[k] = v;
-    }
-}
+                          double* __restrict__ rms_out, int nat) { d_broyden(nbr, it, maxit, alpha, qin, qout, dq, df, u, amat, omega, qlast, dqlast, work, rms_out, nat); }
+
 
 void broyden_step(cudaStream_t st, BroydenState& bs, int it, double alpha, double* qin, const double* qout, double* dq,
                   double* rms_out, int nat) {
@@ -908,185 +332,62 @@ void broyden_step(cudaStream_t st, BroydenState& bs, int it, double alpha, doubl
     XG_LAUNCH_CHECK();
 }
 
-// ================================================================== repulsion
-// repulsionEnGrad_latp, molecular case (src/xtb/repulsion.F90:41-158)
+
 __global__ void k_repulsion(DevMol m, double* __restrict__ e_atom, double* __restrict__ grad) {
     const int a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= m.nat) return;
-    double e = 0.0, g[3] = {0, 0, 0};
-    for (int b = 0; b < m.nat; ++b) {
-        if (b == a) continue;
-        const double rij[3] = {m.xyz[3 * a] - m.xyz[3 * b], m.xyz[3 * a + 1] - m.xyz[3 * b + 1],
-                               m.xyz[3 * a + 2] - m.xyz[3 * b + 2]};
-        const double r2 = rij[0] * rij[0] + rij[1] * rij[1] + rij[2] * rij[2];
-        if (r2 > 1600.0 || r2 < 1e-8) continue;
-        const double r1 = sqrt(r2);
-        const double alpha = sqrt(m.rep_alpha[a] * m.rep_alpha[b]);
-        const double zeff = m.rep_zeff[a] * m.rep_zeff[b];
-        const double kexp = (m.Z[a] > 2 || m.Z[b] > 2) ? 1.5 : 1.0;
-        const double t16 = pow(r1, kexp);
-        const double t26 = exp(-alpha * t16);
-        const double dE = zeff * t26 / r1;
-        const double f = -(alpha * t16 * kexp + 1.0) * dE / r2;
-        e += 0.5 * dE;
-        for (int k = 0; k < 3; ++k) g[k] += f * rij[k];
-    }
-    e_atom[a] = e;
-    for (int k = 0; k < 3; ++k) grad[3 * a + k] += g[k];
+    d_repulsion(m, e_atom, grad, a);
 }
+
 
 void repulsion(cudaStream_t st, const DevMol& m, double* e_atom, double* grad) {
     k_repulsion<<<ceil_div(m.nat, 128), 128, 0, st>>>(m, e_atom, grad);
     XG_LAUNCH_CHECK();
 }
 
-// ================================================================== Coulomb gradient
-// getCoulombDerivsCluster contracted with qsh (src/coulomb/klopmanohno.F90:471-573); warp per atom
+
 __global__ void k_coulomb_grad(DevMol m, const double* __restrict__ qsh, double* __restrict__ grad) {
     const int a = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (a >= m.nat) return;
-    double g[3] = {0, 0, 0};
-    for (int b = lane; b < m.nat; b += 32) {
-        if (b == a) continue;
-        const double vec[3] = {m.xyz[3 * b] - m.xyz[3 * a], m.xyz[3 * b + 1] - m.xyz[3 * a + 1],
-                               m.xyz[3 * b + 2] - m.xyz[3 * a + 2]};
-        const double r2 = vec[0] * vec[0] + vec[1] * vec[1] + vec[2] * vec[2];
-        double f = 0.0;
-        for (int s = m.at_sh0[a]; s < m.at_sh0[a] + m.at_nsh[a]; ++s)
-            for (int u = m.at_sh0[b]; u < m.at_sh0[b] + m.at_nsh[b]; ++u) {
-                const double gij = 0.5 * (m.sh_eta[s] + m.sh_eta[u]);
-                const double g1 = 1.0 / (r2 + 1.0 / (gij * gij));
-                f += g1 * sqrt(g1) * qsh[s] * qsh[u];
-            }
-        for (int k = 0; k < 3; ++k) g[k] += f * vec[k];
-    }
-    for (int k = 0; k < 3; ++k) g[k] = warp_sum(g[k]);
-    if (lane == 0)
-        for (int k = 0; k < 3; ++k) grad[3 * a + k] += g[k];
+    d_coulomb_grad(m, qsh, grad, a, lane);
 }
+
 
 void coulomb_grad(cudaStream_t st, const DevMol& m, const double* qsh, double* grad) {
     k_coulomb_grad<<<ceil_div((long)m.nat * 32, 128), 128, 0, st>>>(m, qsh, grad);
     XG_LAUNCH_CHECK();
 }
 
-// ================================================================== D4 dispersion
-__device__ __forceinline__ double zeta_fn(double a, double c, double qref, double qmod) {
-    if (qmod < 0.0) return exp(a);
-    return exp(a * (1.0 - exp(c * (1.0 - qref / qmod))));
-}
-__device__ __forceinline__ double dzeta_fn(double a, double c, double qref, double qmod) {
-    if (qmod < 0.0) return 0.0;
-    return -a * c * exp(c * (1.0 - qref / qmod)) * zeta_fn(a, c, qref, qmod) * qref / (qmod * qmod);
-}
 
-// Gaussian CN weights of the reference systems: d4 (src/disp/dftd4.F90:588-657) and
-// weight_references (:948-1065); gw[a*MAXREF + r], dgw = d gw / d CN
 __global__ void k_d4_weights(DevMol m, const double* __restrict__ cnv, double* __restrict__ gw, double* __restrict__ dgw) {
     const int a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= m.nat) return;
-    const int e = m.eid[a];
-    const int nref = m.d4_nref[e];
-    const double wf = 6.0;
-    double expw[MAXREF], expd[MAXREF], norm = 0.0, dnorm = 0.0, rmax = -1e300;
-    for (int r = 0; r < nref; ++r) {
-        const double rcn = m.d4_refcn[e * MAXREF + r];
-        rmax = fmax(rmax, rcn);
-        expw[r] = 0.0;
-        expd[r] = 0.0;
-        for (int c = 1; c <= m.d4_ncount[e * MAXREF + r]; ++c) {
-            const double twf = c * wf;
-            const double val = -twf * sq(cnv[a] - rcn);
-            const double g = (val < -200.0) ? 0.0 : exp(val);
-            expw[r] += g;
-            expd[r] += 2.0 * twf * (rcn - cnv[a]) * g;
-        }
-        norm += expw[r];
-        dnorm += expd[r];
-    }
-    norm = (norm > 1e-80) ? 1.0 / norm : 0.0;
-    for (int r = 0; r < MAXREF; ++r) {
-        double g = 0.0, dg = 0.0;
-        if (r < nref) {
-            g = expw[r] * norm;
-            dg = expd[r] * norm - expw[r] * dnorm * norm * norm;
-            if (norm == 0.0) g = (fabs(rmax - m.d4_refcn[e * MAXREF + r]) < 1e-12) ? 1.0 : 0.0;
-        }
-        gw[a * MAXREF + r] = g;
-        if (dgw) dgw[a * MAXREF + r] = dg;
-    }
+    d_d4_weights(m, cnv, gw, dgw, a);
 }
+
 
 void d4_weights(cudaStream_t st, const DevMol& m, const double* cnv, double* gw, double* dgw) {
     k_d4_weights<<<ceil_div(m.nat, 128), 128, 0, st>>>(m, cnv, gw, dgw);
     XG_LAUNCH_CHECK();
 }
 
-// zeta / dzeta of the SCC dispersion (disppot, src/disp/dftd4.F90:735-818)
+
 __global__ void k_d4_zeta(DevMol m, const double* __restrict__ gw, const double* __restrict__ q,
                           double* __restrict__ zeta, double* __restrict__ dzeta) {
     const int a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= m.nat) return;
-    const int e = m.eid[a];
-    const double iz = m.d4_zeff[e], gi = m.d4_gam[e] * 2.0;
-    for (int r = 0; r < MAXREF; ++r) {
-        double z = 0.0, dz = 0.0;
-        if (r < m.d4_nref[e] && gw[a * MAXREF + r] >= 1e-7) {
-            const double qref = m.d4_refq[e * MAXREF + r] + iz;
-            z = zeta_fn(3.0, gi, qref, q[a] + iz);
-            dz = dzeta_fn(3.0, gi, qref, q[a] + iz);
-        }
-        zeta[a * MAXREF + r] = z;
-        dzeta[a * MAXREF + r] = dz;
-    }
+    d_d4_zeta(m, gw, q, zeta, dzeta, a);
 }
 
-// (W zeta) for atom a, W = build_wdispmat (src/disp/dftd4.F90:660-732) evaluated on the fly; warp per atom
+
 __global__ void k_d4_wz(DevMol m, const double* __restrict__ gw, const double* __restrict__ zeta,
                         const double* __restrict__ dzeta, double* __restrict__ Wz, double* __restrict__ vat,
                         double* __restrict__ e_atom) {
     const int a = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (a >= m.nat) return;
-    const int ea = m.eid[a], na = m.d4_nref[ea];
-    double acc[MAXREF];
-    for (int r = 0; r < MAXREF; ++r) acc[r] = 0.0;
-    for (int b = lane; b < m.nat; b += 32) {
-        if (b == a) continue;
-        const double r2 = sq(m.xyz[3 * a] - m.xyz[3 * b]) + sq(m.xyz[3 * a + 1] - m.xyz[3 * b + 1]) +
-                          sq(m.xyz[3 * a + 2] - m.xyz[3 * b + 2]);
-        if (r2 > 72.0 * 72.0) continue;
-        const double r4r2 = 3.0 * m.r4r2[a] * m.r4r2[b];
-        const double cut = 0.52 * sqrt(r4r2) + 5.0;
-        const double oor6 = 1.0 / (r2 * r2 * r2 + pow(cut, 6.0));
-        const double oor8 = 1.0 / (r2 * r2 * r2 * r2 + pow(cut, 8.0));
-        const int eb = m.eid[b], nb = m.d4_nref[eb];
-        const double* c6 = m.d4_c6 + ((size_t)(ea * m.nelem + eb) * MAXREF) * MAXREF;
-        for (int r = 0; r < na; ++r) {
-            const double gr = gw[a * MAXREF + r];
-            double s = 0.0;
-            for (int u = 0; u < nb; ++u) {
-                const double gg = gr * gw[b * MAXREF + u];
-                if (gg < 1e-7) continue;
-                const double c = c6[r * MAXREF + u];
-                s += gg * (-1.0 * (c * oor6) - 2.7 * (r4r2 * c * oor8)) * zeta[b * MAXREF + u];
-            }
-            acc[r] += s;
-        }
-    }
-    double v = 0.0, e = 0.0;
-    for (int r = 0; r < MAXREF; ++r) {
-        const double t = warp_sum(acc[r]);
-        if (lane == 0 && r < na) {
-            Wz[a * MAXREF + r] = t;
-            v += t * dzeta[a * MAXREF + r];
-            e += 0.5 * t * zeta[a * MAXREF + r];
-        }
-    }
-    if (lane == 0) {
-        vat[a] = v;
-        e_atom[a] = e;
-    }
+    d_d4_wz(m, gw, zeta, dzeta, Wz, vat, e_atom, a, lane);
 }
+
 
 void d4_scc(cudaStream_t st, const DevMol& m, const double* gw, const double* q, double* zeta, double* dzeta,
             double* Wz, double* vat, double* e_atom) {
@@ -1096,77 +397,32 @@ void d4_scc(cudaStream_t st, const DevMol& m, const double* gw, const double* q,
     XG_LAUNCH_CHECK();
 }
 
-// weight_references: zeta-weighted vectors for q and for q = 0 (src/disp/dftd4.F90:948-1065)
+
 __global__ void k_d4_refvec(DevMol m, const double* __restrict__ gw, const double* __restrict__ dgw,
                             const double* __restrict__ q, double* __restrict__ zv, double* __restrict__ zr,
                             double* __restrict__ zdcn, double* __restrict__ zrdcn) {
     const int a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= m.nat) return;
-    const int e = m.eid[a];
-    const double zi = m.d4_zeff[e], gi = 2.0 * m.d4_gam[e];
-    for (int r = 0; r < MAXREF; ++r) {
-        double v0 = 0, v1 = 0, v2 = 0, v3 = 0;
-        if (r < m.d4_nref[e]) {
-            const double qref = m.d4_refq[e * MAXREF + r] + zi;
-            const double zq = zeta_fn(3.0, gi, qref, q[a] + zi);
-            const double z0 = zeta_fn(3.0, gi, qref, zi);
-            const double g = gw[a * MAXREF + r], dg = dgw[a * MAXREF + r];
-            v0 = zq * g; v1 = z0 * g; v2 = zq * dg; v3 = z0 * dg;
-        }
-        zv[a * MAXREF + r] = v0; zr[a * MAXREF + r] = v1; zdcn[a * MAXREF + r] = v2; zrdcn[a * MAXREF + r] = v3;
-    }
+    d_d4_refvec(m, gw, dgw, q, zv, zr, zdcn, zrdcn, a);
 }
 
-// get_atomic_c6 (src/disp/dftd4.F90:1069-1147): c6[a][b], dc6[a][b] = d c6_ab / d CN_a
+
 __global__ void k_d4_c6(DevMol m, const double* __restrict__ zv, const double* __restrict__ zdcn,
                         double* __restrict__ c6o, double* __restrict__ dc6o) {
     const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
     const int n = m.nat;
     if (t >= (long)n * n) return;
-    const int a = (int)(t / n), b = (int)(t % n);
-    const int ea = m.eid[a], eb = m.eid[b];
-    const double* c6 = m.d4_c6 + ((size_t)(ea * m.nelem + eb) * MAXREF) * MAXREF;
-    double c = 0.0, d = 0.0;
-    for (int r = 0; r < m.d4_nref[ea]; ++r)
-        for (int u = 0; u < m.d4_nref[eb]; ++u) {
-            const double ref = c6[r * MAXREF + u];
-            c += zv[a * MAXREF + r] * zv[b * MAXREF + u] * ref;
-            d += zdcn[a * MAXREF + r] * zv[b * MAXREF + u] * ref;
-        }
-    c6o[t] = c;
-    dc6o[t] = d;
+    d_d4_c6(m, zv, zdcn, c6o, dc6o, t);
 }
 
-// two-body dispersion energy / gradient (disp_gradient_latp, src/disp/dftd4.F90:1832-1933); thread per atom
+
 __global__ void k_d4_2body(DevMol m, const double* __restrict__ c6, const double* __restrict__ dc6,
                            double* __restrict__ e_atom, double* __restrict__ dEdcn, double* __restrict__ grad) {
     const int a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= m.nat) return;
-    const int n = m.nat;
-    double e = 0.0, dcn = 0.0, g[3] = {0, 0, 0};
-    for (int b = 0; b < n; ++b) {
-        if (b == a) continue;
-        const double rij[3] = {m.xyz[3 * a] - m.xyz[3 * b], m.xyz[3 * a + 1] - m.xyz[3 * b + 1],
-                               m.xyz[3 * a + 2] - m.xyz[3 * b + 2]};
-        const double r2 = rij[0] * rij[0] + rij[1] * rij[1] + rij[2] * rij[2];
-        if (r2 > 3600.0 || r2 < 1e-10) continue;
-        const double r4r2 = 3.0 * m.r4r2[a] * m.r4r2[b];
-        const double r0 = 0.52 * sqrt(r4r2) + 5.0;
-        const double t6 = 1.0 / (r2 * r2 * r2 + pow(r0, 6.0));
-        const double t8 = 1.0 / (r2 * r2 * r2 * r2 + pow(r0, 8.0));
-        const double d6 = -6.0 * r2 * r2 * t6 * t6;
-        const double d8 = -8.0 * r2 * r2 * r2 * t8 * t8;
-        const double disp = 1.0 * t6 + 2.7 * r4r2 * t8;
-        const double ddisp = 1.0 * d6 + 2.7 * r4r2 * d8;
-        const double cab = c6[(size_t)a * n + b];
-        e += -cab * disp * 0.5;
-        dcn += -dc6[(size_t)a * n + b] * disp;
-        for (int k = 0; k < 3; ++k) g[k] += -cab * ddisp * rij[k];
-    }
-    e_atom[a] = e;
-    dEdcn[a] += dcn;
-    for (int k = 0; k < 3; ++k) grad[3 * a + k] += g[k];
+    d_d4_2body(m, c6, dc6, e_atom, dEdcn, grad, a);
 }
+
 
 // ATM three-body (atm_gradient_latp molecular branch + deriv_atm_triple, src/disp/dftd4.F90:2023-2177, 2354-2433);
 // one thread per pair (i > j), loop over k < j; gradient and dE/dCN of j, k by atomics.
@@ -1245,6 +501,7 @@ __global__ void k_d4_atm(DevMol m, const double* __restrict__ c6, const double* 
     }
     e_pair[t] = esum;
 }
+
 
 void d4_grad(cudaStream_t st, const DevMol& m, const double* cnv, const double* q, double* gw, double* dgw,
              double* zv, double* zr, double* zdcn, double* zrdcn, double* c6, double* dc6, double* c6z, double* dc6z,

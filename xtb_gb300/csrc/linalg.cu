@@ -13,101 +13,19 @@
 #include <cooperative_groups.h>
 
 #include "linalg.h"
+#include "linalg_device.cuh"
 
 namespace cg = cooperative_groups;
 
 namespace xg {
 
-// ------------------------------------------------------------------ GEMM
-constexpr int GBM = 64, GBN = 64, GBK = 16;
-
-// C[M,N] = alpha * op(A) * op(B) + beta * C.
-// op(A)[i,k] = TA ? A[k*lda+i] : A[i*lda+k];  op(B)[k,j] = TB ? B[j*ldb+k] : B[k*ldb+j].
-// Structure flags skip work that is known to be zero or redundant:
-//   GF_B_UPPER  op(B)[k,j] = 0 for k > j      (k < j0 + 64 per tile)
-//   GF_A_LOWER  op(A)[i,k] = 0 for k > i      (k < i0 + 64 per tile)
-//   GF_A_UPPER  op(A)[i,k] = 0 for k < i      (k >= i0 per tile)
-//   GF_SYM      C symmetric: only tiles touching the lower triangle are computed (mirror afterwards)
-// dK / dN (optional, device): K and N limited to *dK / *dN at run time.
 template <bool TA, bool TB>
 __global__ void __launch_bounds__(256) k_dgemm(int M, int N, int K, double alpha, const double* __restrict__ A,
                                                int lda, const double* __restrict__ B, int ldb, double beta,
                                                double* __restrict__ C, int ldc, int flags, const int* __restrict__ dK,
                                                const int* __restrict__ dN) {
-    __shared__ double As[2][GBK][GBM + 1];
-    __shared__ double Bs[2][GBK][GBN + 1];
-    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-    const int i0 = blockIdx.y * GBM, j0 = blockIdx.x * GBN;
-    if (dN) N = min(N, *dN);
-    if (j0 >= N) return;
-    if ((flags & GF_SYM) && j0 >= i0 + GBM) return;
-    if (dK) K = min(K, *dK);
-    int kbeg = 0, kend = K;
-    if (flags & GF_B_UPPER) kend = min(kend, j0 + GBN);
-    if (flags & GF_A_LOWER) kend = min(kend, i0 + GBM);
-    if (flags & GF_A_UPPER) kbeg = (i0 / GBK) * GBK;
-    double acc[4][4];
-#pragma unroll
-    for (int r = 0; r < 4; ++r)
-#pragma unroll
-        for (int c = 0; c < 4; ++c) acc[r][c] = 0.0;
-
-    auto load = [&](int buf, int k0) {
-#pragma unroll
-        for (int s = 0; s < (GBM * GBK) / 256; ++s) {
-            const int t = threadIdx.x + s * 256;
-            int ii, kk;
-            if (TA) { ii = t % GBM; kk = t / GBM; } else { kk = t % GBK; ii = t / GBK; }
-            const int gi = i0 + ii, gk = k0 + kk;
-            double v = 0.0;
-            if (gi < M && gk < kend) v = TA ? A[(size_t)gk * lda + gi] : A[(size_t)gi * lda + gk];
-            As[buf][kk][ii] = v;
-        }
-#pragma unroll
-        for (int s = 0; s < (GBN * GBK) / 256; ++s) {
-            const int t = threadIdx.x + s * 256;
-            int jj, kk;
-            if (TB) { kk = t % GBK; jj = t / GBK; } else { jj = t % GBN; kk = t / GBN; }
-            const int gj = j0 + jj, gk = k0 + kk;
-            double v = 0.0;
-            if (gj < N && gk < kend) v = TB ? B[(size_t)gj * ldb + gk] : B[(size_t)gk * ldb + gj];
-            Bs[buf][kk][jj] = v;
-        }
-    };
-
-    int buf = 0;
-    if (kbeg < kend) load(0, kbeg);
-    __syncthreads();
-    for (int k0 = kbeg; k0 < kend; k0 += GBK) {
-        if (k0 + GBK < kend) load(buf ^ 1, k0 + GBK);
-#pragma unroll
-        for (int kk = 0; kk < GBK; ++kk) {
-            double a[4], b[4];
-#pragma unroll
-            for (int r = 0; r < 4; ++r) a[r] = As[buf][kk][ty + 16 * r];
-#pragma unroll
-            for (int c = 0; c < 4; ++c) b[c] = Bs[buf][kk][tx + 16 * c];
-#pragma unroll
-            for (int r = 0; r < 4; ++r)
-#pragma unroll
-                for (int c = 0; c < 4; ++c) acc[r][c] = fma(a[r], b[c], acc[r][c]);
-        }
-        __syncthreads();
-        buf ^= 1;
-    }
-#pragma unroll
-    for (int r = 0; r < 4; ++r) {
-        const int i = i0 + ty + 16 * r;
-        if (i >= M) continue;
-#pragma unroll
-        for (int c = 0; c < 4; ++c) {
-            const int j = j0 + tx + 16 * c;
-            if (j >= N) continue;
-            double v = alpha * acc[r][c];
-            if (beta != 0.0) v += beta * C[(size_t)i * ldc + j];
-            C[(size_t)i * ldc + j] = v;
-        }
-    }
+    dgemm_tile<TA, TB>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, flags, dK, dN, blockIdx.y * GBM,
+                       blockIdx.x * GBN);
 }
 
 void dgemm(cudaStream_t st, bool ta, bool tb, int M, int N, int K, double alpha, const double* A, int lda,
@@ -256,11 +174,15 @@ void trinv_upper(cudaStream_t st, int n, const double* U, int ldu, double* X, in
 //
 // One pass over the trailing rows per column: the rank-2 update of step k-1 is
 // applied lazily while the symmetric product p = tau A22 v of step k is formed,
-// so A22 is read and written once per column.  Row k+1 (the next pivot row) is
-// updated eagerly at the end of step k.  Two grid-wide barriers per column.
+// so A22 is read and written once per column.  The pivot row of step k misses
+// only the update of step k-1, which every block adds on the fly from the
+// pending vectors it keeps in shared memory.  p alternates between two buffers
+// (p[0..n) and p[n..2n)), so one grid-wide barrier per column suffices: a block
+// still reading p of step k cannot meet a writer of the same buffer before the
+// barrier of step k+1.
 __global__ void __launch_bounds__(256) k_sytrd(int n, double* __restrict__ A, int lda, double* __restrict__ V,
                                                double* __restrict__ tau, double* __restrict__ d, double* __restrict__ e,
-                                               double* __restrict__ p) {
+                                               double* __restrict__ p2) {
     cg::grid_group grid = cg::this_grid();
     extern __shared__ double sm[];
     double* v = sm;            // [n] current reflector, offset k+1
@@ -275,10 +197,14 @@ __global__ void __launch_bounds__(256) k_sytrd(int n, double* __restrict__ A, in
 
     for (int k = 0; k < n - 2; ++k) {
         const int m = n - k - 1;
-        const double* xk = A + (size_t)k * lda + k + 1;   // row k, already fully updated
+        double* p = p2 + (size_t)(k & 1) * n;
+        const double* xk = A + (size_t)k * lda + k + 1;   // row k, pending update of step k-1 missing
+        const bool pend = tprev != 0.0;
+        const double v0 = pend ? vp[0] : 0.0, w0 = pend ? wp[0] : 0.0;
         double ss = 0.0;
         for (int i = threadIdx.x; i < m; i += blockDim.x) {
-            const double xv = xk[i];
+            double xv = xk[i];
+            if (pend) xv -= v0 * wp[i + 1] + w0 * vp[i + 1];
             v[i] = xv;
             if (i > 0) ss += xv * xv;
         }
@@ -301,40 +227,29 @@ __global__ void __launch_bounds__(256) k_sytrd(int n, double* __restrict__ A, in
             for (int i = threadIdx.x; i < n; i += blockDim.x) V[(size_t)k * n + i] = (i <= k) ? 0.0 : v[i - k - 1];
             if (threadIdx.x == 0) {
                 tau[k] = tk;
-                d[k] = A[(size_t)k * lda + k];
+                d[k] = A[(size_t)k * lda + k] - 2.0 * v0 * w0;
                 e[k] = beta;
             }
         }
         // rows k+1 .. n-1: apply the pending update of step k-1 (cols >= k+1) and form
-        // p = tau A22 v (row k itself was updated eagerly at the end of step k-1)
+        // p = tau A22 v
         for (int r = gwarp; r < m; r += nwarps) {
             double* arow = A + (size_t)(k + 1 + r) * lda + k + 1;
-            const bool pend = tprev != 0.0;
             const double vr = pend ? vp[r + 1] : 0.0, wr = pend ? wp[r + 1] : 0.0;
-            double s0 = 0.0, s1 = 0.0;
-            for (int c0 = 0; c0 < m; c0 += 256) {
-                double a[8];
-#pragma unroll
-                for (int u = 0; u < 8; ++u) {
-                    const int c = c0 + lane + 32 * u;
-                    a[u] = (c < m) ? arow[c] : 0.0;
+            double sdot = 0.0;
+            for (int c = lane; c < m; c += 32) {
+                double a = arow[c];
+                if (pend) {
+                    a -= vr * wp[c + 1] + wr * vp[c + 1];
+                    arow[c] = a;
                 }
-#pragma unroll
-                for (int u = 0; u < 8; ++u) {
-                    const int c = c0 + lane + 32 * u;
-                    if (c < m) {
-                        if (pend) {
-                            a[u] -= vr * wp[c + 1] + wr * vp[c + 1];
-                            arow[c] = a[u];
-                        }
-                        if (u & 1) s1 = fma(a[u], v[c], s1); else s0 = fma(a[u], v[c], s0);
-                    }
-                }
+                sdot = fma(a, v[c], sdot);
             }
-            const double sdot = warp_sum(s0 + s1);
+            sdot = warp_sum(sdot);
             if (lane == 0) p[r] = tk * sdot;
         }
         grid.sync();
+        // w = p - (tau/2)(p.v) v; it becomes the pending update (offset k+1)
         if (tk != 0.0) {
             double pv = 0.0;
             for (int i = threadIdx.x; i < m; i += blockDim.x) {
@@ -345,36 +260,33 @@ __global__ void __launch_bounds__(256) k_sytrd(int n, double* __restrict__ A, in
             pv = block_sum(pv, red);
             const double kk = -0.5 * tk * pv;
             for (int i = threadIdx.x; i < m; i += blockDim.x) w[i] += kk * v[i];
-        } else {
-            for (int i = threadIdx.x; i < m; i += blockDim.x) w[i] = 0.0;
         }
         __syncthreads();
-        // the pending update becomes (v, w) of this step (offset k+1)
-        for (int i = threadIdx.x; i < m; i += blockDim.x) { vp[i] = v[i]; wp[i] = w[i]; }
+        if (tk != 0.0)
+            for (int i = threadIdx.x; i < m; i += blockDim.x) { vp[i] = v[i]; wp[i] = w[i]; }
         tprev = tk;
         __syncthreads();
-        // eager update of the next pivot row k+1 (cols >= k+1)
-        if (tk != 0.0 && gwarp == 0) {
-            double* arow = A + (size_t)(k + 1) * lda + k + 1;
-            const double vr = vp[0], wr = wp[0];
-            for (int c = lane; c < m; c += 32) arow[c] -= vr * wp[c] + wr * vp[c];
-        }
-        // the shift of the pending vectors to offset k+2 happens through the index r+1 above
-        grid.sync();
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
-        if (n >= 2) {
-            // the last row still carries the pending update of step n-3 (cols n-2, n-1)
+        if (n >= 3) {
+            // rows n-2 and n-1 still carry the pending update of step n-3 (offset n-2)
+            double a11 = A[(size_t)(n - 2) * lda + n - 2];
             double a21 = A[(size_t)(n - 1) * lda + n - 2];
             double a22 = A[(size_t)(n - 1) * lda + n - 1];
-            if (n >= 3 && tprev != 0.0) {
+            if (tprev != 0.0) {
+                a11 -= 2.0 * vp[0] * wp[0];
                 a21 -= vp[1] * wp[0] + wp[1] * vp[0];
-                a22 -= vp[1] * wp[1] + wp[1] * vp[1];
+                a22 -= 2.0 * vp[1] * wp[1];
             }
-            d[n - 2] = A[(size_t)(n - 2) * lda + n - 2];
+            d[n - 2] = a11;
             e[n - 2] = a21;
             tau[n - 2] = 0.0;
             d[n - 1] = a22;
+        } else if (n == 2) {
+            d[0] = A[0];
+            e[0] = A[(size_t)lda];
+            tau[0] = 0.0;
+            d[1] = A[(size_t)lda + 1];
         } else {
             d[n - 1] = A[(size_t)(n - 1) * lda + n - 1];
         }
@@ -406,15 +318,30 @@ void sytrd(cudaStream_t st, int n, double* A, int lda, double* V, double* tau, d
 }
 
 // ------------------------------------------------------------------ bisection
-__device__ int sturm_count(int n, const double* __restrict__ d, const double* __restrict__ e2, double x, double pivmin) {
-    int cnt = 0;
-    double q = d[0] - x;
-    if (fabs(q) < pivmin) q = -pivmin;
-    if (q < 0.0) ++cnt;
+// Number of eigenvalues of T below x, from the sign changes of the leading principal minors
+// p_i = (d_i - x) p_{i-1} - e_{i-1}^2 p_{i-2}, p_{-1} = 1 (Sturm sequence, three-term form).
+// Only one FMA per row sits on the dependent chain and no division is needed, which matters on
+// a part whose FP64 divide is a long multi-instruction sequence.  A minor that comes out exactly
+// zero is replaced by a tiny value of the sign opposite to its predecessor (the ratio p_i/p_{i-1}
+// becomes a tiny negative number, as the pivmin rule of the ratio form makes it); the pair
+// (p_i, p_{i-1}) is rescaled by an exact power of two whenever its larger exponent leaves
+// [2^-400, 2^400], so neither overflows nor underflows.  Sign and exponent tests use integer
+// operations on the bit pattern.  d and e2 are read from shared memory.
+__device__ __forceinline__ int dexp_bits(double v) { return (__double2hiint(v) >> 20) & 0x7ff; }
+
+__device__ int sturm_count(int n, const double* d, const double* e2, double x) {
+    double pm = 1.0, p = d[0] - x;
+    if (p == 0.0) p = -0x1p-600;
+    int cnt = __double2hiint(p) < 0;
     for (int i = 1; i < n; ++i) {
-        q = d[i] - x - e2[i - 1] / q;
-        if (fabs(q) < pivmin) q = -pivmin;
-        if (q < 0.0) ++cnt;
+        double pn = fma(d[i] - x, p, -e2[i - 1] * pm);
+        if ((__double_as_longlong(pn) << 1) == 0) pn = -0x1p-600 * p;
+        cnt += (__double2hiint(pn) ^ __double2hiint(p)) < 0;
+        const int ex = max(dexp_bits(pn), dexp_bits(p));
+        if (ex > 1023 + 400) { pn *= 0x1p-400; p *= 0x1p-400; }
+        else if (ex < 1023 - 400) { pn *= 0x1p+400; p *= 0x1p+400; }
+        pm = p;
+        p = pn;
     }
     return cnt;
 }
@@ -460,18 +387,27 @@ __global__ void k_tri_prep(int n, const double* __restrict__ d, const double* __
 }
 
 // Eigenvalue j of T by bisection on Sturm counts, one thread per eigenvalue, to an
-// absolute accuracy of 2 eps ||T|| (the accuracy inverse iteration needs).
-__global__ void k_bisect(int n, const double* __restrict__ d, const double* __restrict__ e2,
-                         const double* __restrict__ bounds, double* __restrict__ w) {
+// absolute accuracy of 2 eps ||T|| (the accuracy inverse iteration needs).  One warp per
+// block, so the eigenvalues spread over as many SMs as possible (the FP64 pipe of an SM is
+// the limit); d and e^2 are staged in shared memory (dynamic, 2n doubles).
+__global__ void __launch_bounds__(32) k_bisect(int n, const double* __restrict__ d, const double* __restrict__ e2,
+                                               const double* __restrict__ bounds, double* __restrict__ w) {
+    extern __shared__ double sde[];
+    double* sd = sde;
+    double* se = sde + n;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        sd[i] = d[i];
+        se[i] = (i < n - 1) ? e2[i] : 0.0;
+    }
+    __syncthreads();
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
     double lo = bounds[0], hi = bounds[1];
-    const double pivmin = bounds[2];
     const double atol = 2.0 * 2.220446049250313e-16 * fmax(bounds[3], 1e-300);
     for (int it = 0; it < 80; ++it) {
         const double mid = 0.5 * (lo + hi);
         if (hi - lo <= atol || mid <= lo || mid >= hi) break;
-        if (sturm_count(n, d, e2, mid, pivmin) > j) hi = mid; else lo = mid;
+        if (sturm_count(n, sd, se, mid) > j) hi = mid; else lo = mid;
     }
     w[j] = 0.5 * (lo + hi);
 }
@@ -626,7 +562,10 @@ void tridiag_eigvals(cudaStream_t st, int n, const double* d, const double* e, d
                      double* w) {
     k_tri_prep<<<1, 256, 0, st>>>(n, d, e, e2, bounds);
     XG_LAUNCH_CHECK();
-    k_bisect<<<ceil_div(n, 64), 64, 0, st>>>(n, d, e2, bounds, w);
+    const size_t smem = 2 * (size_t)n * sizeof(double);
+    if (smem > 48 * 1024)
+        XG_CUDA(cudaFuncSetAttribute(k_bisect, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_bisect<<<ceil_div(n, 32), 32, smem, st>>>(n, d, e2, bounds, w);
     XG_LAUNCH_CHECK();
 }
 

@@ -18,7 +18,7 @@ void mirror_lower(cudaStream_t st, int n, double* C, int ldc);
 void potrf_upper(cudaStream_t st, int n, double* A, int lda, int* d_info);
 // X = U^-1
 void trinv_upper(cudaStream_t st, int n, const double* U, int ldu, double* X, int ldx);
-// Householder reduction to tridiagonal form (A destroyed); V[n*n], tau[n], d[n], e[n], p[n] scratch
+// Householder reduction to tridiagonal form (A destroyed); V[n*n], tau[n], d[n], e[n]; p[2n] scratch
 void sytrd(cudaStream_t st, int n, double* A, int lda, double* V, double* tau, double* d, double* e, double* p);
 // eigenvalues of the tridiagonal (d, e): w[n] ascending; e2: n, bounds: 4
 void tridiag_eigvals(cudaStream_t st, int n, const double* d, const double* e, double* e2, double* bounds, double* w);
