@@ -47,6 +47,22 @@ extern void xtbgb_setKeepOrbitals(xtb_TEnvironment env, xtb_TCalculator calc, in
  * returns 0 when no device is present. */
 extern double xtbgb_fp64PeakTflops(void);
 
+/* Repulsion energy and gradient of one molecule, computed from and into DEVICE memory
+ * without allocating anything.  No counterpart in the reference: it exists for callers
+ * that own all device memory themselves (a serving loop that admits work against a fixed
+ * HBM budget, an MD code keeping coordinates resident), for which a library-side
+ * cudaMalloc would break the budget and a cudaFree would stall the whole device.
+ *   numbers[natoms] (int), positions[natoms][3] (Bohr)  -> device inputs
+ *   energy[1] (Hartree), gradient[natoms][3] (Hartree/Bohr) -> device outputs, overwritten
+ *   stream: a cudaStream_t (NULL = legacy default stream); the call only enqueues work.
+ * The scratch is a static device array sized for natoms <= 8192; larger inputs are
+ * rejected.  The first call on each device looks up that array (cudaGetSymbolAddress) and
+ * should come before any stream capture.  Calls that overlap in time share the scratch
+ * and race: serialise them.  Returns 0 on success, else a nonzero code with a message in
+ * errbuf[errlen] (errbuf may be NULL); an element outside 1..86 yields a NaN energy. */
+extern int xtbgb_repulsionNoAlloc(int natoms, const int* numbers, const double* positions, double* energy,
+                                  double* gradient, void* stream, char* errbuf, int errlen);
+
 #ifdef __cplusplus
 }
 #endif
