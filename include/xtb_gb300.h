@@ -47,6 +47,41 @@ extern void xtbgb_setKeepOrbitals(xtb_TEnvironment env, xtb_TCalculator calc, in
  * returns 0 when no device is present. */
 extern double xtbgb_fp64PeakTflops(void);
 
+/* ---- Batched single points (no counterpart in the reference: the reference API runs one
+ * molecule per call).  Many molecules of uneven size are solved together on the device, one
+ * thread block per molecule with its whole SCC state resident; molecules above 512 AOs (or
+ * whose SCC outgrows the batched mixing history) run on the plain per-molecule GPU engine.
+ * GFN2-xTB, gas phase; results are reported per molecule in input order. */
+typedef struct _xtbgb_TBatch* xtbgb_TBatch;
+
+/* natoms[nmol]; numbers[sum natoms] and positions[sum natoms][3] (Bohr) concatenated in
+ * molecule order; charges[nmol] and uhf[nmol] may be NULL (neutral, closed shell). */
+extern xtbgb_TBatch xtbgb_newBatch(xtb_TEnvironment env, int nmol, const int* natoms, const int* numbers,
+                                   const double* positions, const double* charges, const int* uhf);
+extern void xtbgb_delBatch(xtbgb_TBatch* batch);
+/* All single points with one set of settings (accuracy, electronic temperature in K, maximum
+ * SCC iterations, clamped as by xtb_setAccuracy / xtb_setElectronicTemp / xtb_setMaxIter);
+ * gradient != 0 also computes gradients.  Failed or unconverged molecules raise one error on
+ * the environment; their results are still filled. */
+extern void xtbgb_batchSinglepoint(xtb_TEnvironment env, xtbgb_TBatch batch, double accuracy, double etemp,
+                                   int maxiter, int gradient);
+extern void xtbgb_batchGetEnergies(xtb_TEnvironment env, xtbgb_TBatch batch, double* energies);   /* [nmol] */
+extern void xtbgb_batchGetGradients(xtb_TEnvironment env, xtbgb_TBatch batch, double* gradients); /* [N][3] */
+extern void xtbgb_batchGetCharges(xtb_TEnvironment env, xtbgb_TBatch batch, double* charges);     /* [N] */
+extern void xtbgb_batchGetDipoles(xtb_TEnvironment env, xtbgb_TBatch batch, double* dipoles);     /* [nmol][3] */
+/* [nmol][8], the same parts as xtbgb_getEnergyParts */
+extern void xtbgb_batchGetEnergyParts(xtb_TEnvironment env, xtbgb_TBatch batch, double* parts);
+/* per molecule: SCC iterations, converged (1/0), status (0 ok, 1 not converged, 2 overlap not
+ * positive definite, 3 non-finite energy), engine (0 batched, 1 plain); any pointer may be NULL */
+extern void xtbgb_batchGetStatus(xtb_TEnvironment env, xtbgb_TBatch batch, int* iterations, int* converged,
+                                 int* status, int* engine);
+/* times[0] device ms (CUDA events around the batched kernels, plus plain-engine device time),
+ * times[1] wall ms of the call; counts[0] host->device bytes, [1] device->host bytes,
+ * [2] kernel launches, [3] molecules run on the plain engine. */
+extern void xtbgb_batchGetStats(xtb_TEnvironment env, xtbgb_TBatch batch, double* times, long long* counts);
+/* number of AOs of every molecule [nmol] */
+extern void xtbgb_batchNao(xtb_TEnvironment env, xtbgb_TBatch batch, int* nao);
+
 /* Repulsion energy and gradient of one molecule, computed from and into DEVICE memory
  * without allocating anything.  No counterpart in the reference: it exists for callers
  * that own all device memory themselves (a serving loop that admits work against a fixed

@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "../../include/xtb_gb300.h"
+#include "batch.h"
 #include "engine.h"
 #include "host_model.h"
 #include "linalg.h"
@@ -504,6 +505,155 @@ void xtbgb_getMultipoles(xtb_TEnvironment env, xtb_TResults res, double* dipm, d
     if (!res_ready(env, res, "xtbgb_getMultipoles", "Multipoles")) return;
     if (dipm) std::copy(res->wfn.dipm.begin(), res->wfn.dipm.end(), dipm);
     if (qp) std::copy(res->wfn.qp.begin(), res->wfn.qp.end(), qp);
+}
+
+
+// ------------------------------------------------------------------ batched single points
+struct _xtbgb_TBatch {
+    int nmol = 0;
+    std::vector<int> natoms;
+    std::vector<long> atom_off;
+    std::vector<xg::HostMol> mols;
+    xg::BatchResults res;
+    bool has = false;
+};
+
+xtbgb_TBatch xtbgb_newBatch(xtb_TEnvironment env, int nmol, const int* natoms, const int* numbers,
+                            const double* positions, const double* charges, const int* uhf) {
+    static const char* src = "xtbgb_newBatch";
+    if (!check_env(env)) return nullptr;
+    if (nmol < 0 || (nmol > 0 && (!natoms || !numbers || !positions))) {
+        env->error("Invalid batch description", src);
+        return nullptr;
+    }
+    auto* b = new _xtbgb_TBatch();
+    b->nmol = nmol;
+    b->natoms.assign(natoms, natoms + nmol);
+    b->atom_off.assign(nmol + 1, 0);
+    for (int i = 0; i < nmol; ++i) {
+        if (natoms[i] < 1) {
+            env->error("Molecule " + std::to_string(i) + " has no atoms", src);
+            delete b;
+            return nullptr;
+        }
+        b->atom_off[i + 1] = b->atom_off[i] + natoms[i];
+    }
+    b->mols.resize(nmol);
+    for (int i = 0; i < nmol; ++i) {
+        const long o = b->atom_off[i];
+        for (int a = 0; a < natoms[i]; ++a)
+            if (numbers[o + a] < 1 || numbers[o + a] > kMaxElem) {
+                env->error("Molecule " + std::to_string(i) + ": element " + std::to_string(numbers[o + a]) +
+                               " is not parametrised in GFN2-xTB", src);
+                delete b;
+                return nullptr;
+            }
+        const std::string err = xg::build_host_mol(natoms[i], numbers + o, positions + 3 * o,
+                                                   charges ? charges[i] : 0.0, uhf ? uhf[i] : 0, b->mols[i]);
+        if (!err.empty()) {
+            env->error("Molecule " + std::to_string(i) + ": " + err, src);
+            delete b;
+            return nullptr;
+        }
+    }
+    return b;
+}
+
+void xtbgb_delBatch(xtbgb_TBatch* batch) {
+    if (batch && *batch) {
+        delete *batch;
+        *batch = nullptr;
+    }
+}
+
+void xtbgb_batchSinglepoint(xtb_TEnvironment env, xtbgb_TBatch batch, double accuracy, double etemp, int maxiter,
+                            int gradient) {
+    static const char* src = "xtbgb_batchSinglepoint";
+    if (!check_env(env)) return;
+    if (!batch) {
+        env->error("Batch is not allocated", src);
+        return;
+    }
+    xg::BatchSettings set;
+    set.accuracy = std::min(std::max(accuracy, 1.0e-4), 1.0e3);
+    set.etemp = std::max(etemp, 1.0e-6);
+    set.maxiter = std::max(maxiter, 1);
+    std::vector<int> wg(batch->nmol, gradient ? 1 : 0);
+    try {
+        xg::run_batch(batch->mols, set, wg, batch->res);
+    } catch (const std::exception& e) {
+        env->error(e.what(), src);
+        batch->has = false;
+        return;
+    }
+    batch->has = true;
+    int bad = 0;
+    for (int i = 0; i < batch->nmol; ++i) bad += batch->res.status[i] != xg::BST_OK;
+    if (bad) env->error(std::to_string(bad) + " molecule(s) failed or did not converge (see xtbgb_batchGetStatus)", src);
+}
+
+static bool batch_ready(xtb_TEnvironment env, xtbgb_TBatch batch, const char* src) {
+    if (!check_env(env)) return false;
+    if (!batch || !batch->has) {
+        env->error("Batch results are not available", src);
+        return false;
+    }
+    return true;
+}
+
+void xtbgb_batchGetEnergies(xtb_TEnvironment env, xtbgb_TBatch batch, double* energies) {
+    if (!batch_ready(env, batch, "xtbgb_batchGetEnergies") || !energies) return;
+    std::copy(batch->res.energy.begin(), batch->res.energy.end(), energies);
+}
+
+void xtbgb_batchGetGradients(xtb_TEnvironment env, xtbgb_TBatch batch, double* gradients) {
+    if (!batch_ready(env, batch, "xtbgb_batchGetGradients") || !gradients) return;
+    std::copy(batch->res.gradient.begin(), batch->res.gradient.end(), gradients);
+}
+
+void xtbgb_batchGetCharges(xtb_TEnvironment env, xtbgb_TBatch batch, double* charges) {
+    if (!batch_ready(env, batch, "xtbgb_batchGetCharges") || !charges) return;
+    std::copy(batch->res.charges.begin(), batch->res.charges.end(), charges);
+}
+
+void xtbgb_batchGetDipoles(xtb_TEnvironment env, xtbgb_TBatch batch, double* dipoles) {
+    if (!batch_ready(env, batch, "xtbgb_batchGetDipoles") || !dipoles) return;
+    std::copy(batch->res.dipole.begin(), batch->res.dipole.end(), dipoles);
+}
+
+void xtbgb_batchGetEnergyParts(xtb_TEnvironment env, xtbgb_TBatch batch, double* parts) {
+    if (!batch_ready(env, batch, "xtbgb_batchGetEnergyParts") || !parts) return;
+    std::copy(batch->res.parts.begin(), batch->res.parts.end(), parts);
+}
+
+void xtbgb_batchGetStatus(xtb_TEnvironment env, xtbgb_TBatch batch, int* iterations, int* converged, int* status,
+                          int* engine) {
+    if (!batch_ready(env, batch, "xtbgb_batchGetStatus")) return;
+    const auto& r = batch->res;
+    if (iterations) std::copy(r.iterations.begin(), r.iterations.end(), iterations);
+    if (converged) std::copy(r.converged.begin(), r.converged.end(), converged);
+    if (status) std::copy(r.status.begin(), r.status.end(), status);
+    if (engine) std::copy(r.engine.begin(), r.engine.end(), engine);
+}
+
+void xtbgb_batchGetStats(xtb_TEnvironment env, xtbgb_TBatch batch, double* times, long long* counts) {
+    if (!batch_ready(env, batch, "xtbgb_batchGetStats")) return;
+    const auto& r = batch->res;
+    if (times) {
+        times[0] = r.device_ms;
+        times[1] = r.wall_ms;
+    }
+    if (counts) {
+        counts[0] = r.h2d;
+        counts[1] = r.d2h;
+        counts[2] = r.launches;
+        counts[3] = r.plain_count;
+    }
+}
+
+void xtbgb_batchNao(xtb_TEnvironment env, xtbgb_TBatch batch, int* nao) {
+    if (!check_env(env) || !batch || !nao) return;
+    for (int i = 0; i < batch->nmol; ++i) nao[i] = batch->mols[i].nao;
 }
 
 }  // extern "C"

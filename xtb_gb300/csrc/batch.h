@@ -1,0 +1,119 @@
+// Batched GFN2-xTB single points: many molecules of uneven size, one thread block per
+// molecule, every molecule's state resident on the device until it is done.
+//
+// A molecule moves through three stages -- set-up (CN, EEQ guess, integrals,
+// Coulomb/AES/D4 kernels, S = U^T U, X = U^-1), SCC iterations, gradient -- and
+// each launch of the step kernel advances every unfinished molecule by at most a
+// given number of SCC iterations, so a batch can run to completion in one launch
+// or be advanced step by step while a request loop admits new molecules into
+// freed slots.  The arithmetic per molecule is the plain engine's (same device
+// bodies), with the dense linear algebra done by one thread block.
+#pragma once
+#include <string>
+#include <vector>
+
+#include "engine.h"
+#include "gfn2_kernels.h"
+#include "host_model.h"
+
+namespace xg {
+
+// molecules with more AOs than this go to the plain per-molecule engine
+constexpr int BATCH_MAX_NAO = 512;
+// Broyden history rows kept per molecule; an SCC that needs more iterations is
+// handed to the plain engine
+constexpr int BATCH_HIST = 48;
+
+enum BatchStage { BS_SETUP = 0, BS_SCC = 1, BS_GRAD = 2, BS_DONE = 3 };
+enum BatchStatus { BST_OK = 0, BST_NOT_CONVERGED = 1, BST_CHOLESKY = 2, BST_NONFINITE = 3, BST_HISTORY = 4 };
+
+// output slots per molecule
+enum BatchOut {
+    BO_ENERGY = 0, BO_ELEC, BO_REP, BO_ES, BO_AES, BO_AXC, BO_DISP, BO_ATM, BO_GAP, BO_DIPX, BO_DIPY, BO_DIPZ,
+    BO_COUNT = 16
+};
+
+struct BatchMol {
+    DevMol m;
+    // set-up / SCC / gradient work arrays (device)
+    double *S, *D, *Q, *H0, *X, *H, *A, *T1, *C, *P, *W, *V, *Y, *Zt, *iscr;
+    unsigned char* piv;
+    double *J, *gab3, *gab5, *c6, *dc6, *c6z, *dc6z, *eeqA, *eeqX, *cn_gfn, *cn_tmp, *se, *q, *qsh, *dipm, *qp,
+        *shift, *Jq, *vs, *vd, *vq, *radcn, *gw, *dgw, *zeta, *dzeta, *Wz, *zv, *zr, *zdcn, *zrdcn, *vat, *ed4, *eh0,
+        *eaes, *erep, *e2, *e3, *grad, *dhdcn, *tmp2, *rows, *emo, *focc, *focca, *foccb, *fe, *tri_d, *tri_e,
+        *tri_e2, *tri_tau, *tri_p, *bounds, *fscal, *escal, *rms, *qin, *qout, *dq;
+    int* kocc;
+    BroydenState bs;
+    const double* zval;
+    int nel_a, nel_b;
+    double charge;
+    int want_grad;
+    // state, written by the device
+    int stage, iter, lastdiag, converged, status;
+    double eel, eold;
+    double out[BO_COUNT];
+};
+
+struct BatchSettings {
+    double accuracy = 1.0;
+    double etemp = 300.0;
+    int maxiter = 250;
+};
+
+// Integral (S, D, Q, H0) and integral-derivative kernels over a batch: molecules in the set-up
+// (respectively gradient) stage, one grid row per molecule (batch_integrals.cu).
+void batch_integrals(cudaStream_t st, BatchMol* mols, int nmol, int max_nsh, double intcut);
+void batch_integral_gradient(cudaStream_t st, BatchMol* mols, int nmol, int max_nsh, double intcut);
+
+// Device-resident batch: parameters and work arrays of every molecule in one allocation.
+class DeviceBatch {
+public:
+    DeviceBatch() = default;
+    DeviceBatch(const DeviceBatch&) = delete;
+    DeviceBatch& operator=(const DeviceBatch&) = delete;
+    ~DeviceBatch();
+    // Lay out and upload the molecules (HostMol from build_host_mol); nao <= BATCH_MAX_NAO each.
+    void load(const std::vector<const HostMol*>& mols, const std::vector<int>& want_grad, cudaStream_t st);
+    // Advance every unfinished molecule by at most `max_iter` SCC iterations (set-up and
+    // gradient included); returns the number of molecules still unfinished.
+    int step(const BatchSettings& set, int max_iter, cudaStream_t st);
+    // Copy the states back (after step); `mols` receives stage/status/out of every molecule.
+    void fetch_states(std::vector<BatchMol>& mols, cudaStream_t st) const;
+    // Pack every molecule's gradient [nat][3] and charges [nat] at atom offset d_off[i] into
+    // d_grad [sum nat][3] and d_q [sum nat] (device arrays).
+    void gather(const long* d_off, double* d_grad, double* d_q, cudaStream_t st) const;
+    int count() const { return nmol_; }
+    long long h2d_bytes() const { return h2d_; }
+    size_t bytes() const { return bytes_; }
+    static size_t bytes_for(const HostMol& hm);
+
+private:
+    char* base_ = nullptr;
+    size_t bytes_ = 0;
+    int nmol_ = 0;
+    int max_nao_ = 0;
+    int max_nsh_ = 0;
+    BatchMol* d_mols_ = nullptr;
+    std::vector<BatchMol> h_mols_;
+    long long h2d_ = 0;
+};
+
+// Results of run_batch, in input order.
+struct BatchResults {
+    std::vector<double> energy;      // [nmol] Hartree
+    std::vector<double> gradient;    // [sum nat][3] Hartree/Bohr
+    std::vector<double> charges;     // [sum nat] Mulliken (Broyden-mixed, as the plain engine)
+    std::vector<double> dipole;      // [nmol][3]
+    std::vector<double> parts;       // [nmol][8] as xtbgb_getEnergyParts
+    std::vector<int> iterations, converged, status, engine;   // engine: 0 batched, 1 plain
+    double device_ms = 0.0, wall_ms = 0.0;
+    long long h2d = 0, d2h = 0, launches = 0;
+    int plain_count = 0;
+};
+
+// Single points of all molecules (batched engine, plain engine for the ones it cannot take).
+// want_grad[i] (empty: all) selects the gradient.  Throws on device errors.
+std::string run_batch(const std::vector<HostMol>& mols, const BatchSettings& set, const std::vector<int>& want_grad,
+                      BatchResults& out);
+
+}  // namespace xg

@@ -65,7 +65,7 @@ __device__ __forceinline__ bool cn_term(const DevMol& m, int mode, int i, int j,
 }
 
 
-__device__ void d_cn(DevMol m, int mode, double* __restrict__ cn, int i) {
+__device__ inline void d_cn(DevMol m, int mode, double* __restrict__ cn, int i) {
     const double xi = m.xyz[3 * i], yi = m.xyz[3 * i + 1], zi = m.xyz[3 * i + 2];
     double s = 0.0;
     for (int j = 0; j < m.nat; ++j) {
@@ -79,7 +79,7 @@ __device__ void d_cn(DevMol m, int mode, double* __restrict__ cn, int i) {
 
 
 // g[a] += sum_b den*dcount(r_ab)*(R_a - R_b)/r_ab * (v_a + v_b)  ==  sum_b dCN_b/dR_a v_b
-__device__ void d_cn_chain(DevMol m, int mode, const double* __restrict__ v, double* __restrict__ g, int a) {
+__device__ inline void d_cn_chain(DevMol m, int mode, const double* __restrict__ v, double* __restrict__ g, int a) {
     const double xa = m.xyz[3 * a], ya = m.xyz[3 * a + 1], za = m.xyz[3 * a + 2];
     double gx = 0, gy = 0, gz = 0;
     for (int b = 0; b < m.nat; ++b) {
@@ -97,7 +97,7 @@ __device__ void d_cn_chain(DevMol m, int mode, const double* __restrict__ v, dou
 
 // ================================================================== EEQ guess
 // get_coulomb_matrix_0d and eeq_chrgeq_core (src/eeq_model.f90:60-80, 678-880), 2019 model.
-__device__ void d_eeq_matrix(DevMol m, const double* __restrict__ cn, double* __restrict__ A, double* __restrict__ X, long t) {
+__device__ inline void d_eeq_matrix(DevMol m, const double* __restrict__ cn, double* __restrict__ A, double* __restrict__ X, long t) {
     const int n = m.nat;
     const int i = (int)(t / n), j = (int)(t % n);
     if (i == j) {
@@ -115,7 +115,7 @@ __device__ void d_eeq_matrix(DevMol m, const double* __restrict__ cn, double* __
 
 
 // Solve U^T U x = b for two right-hand sides in X[0:n], X[n:2n]; then the charge constraint.
-__device__ void d_eeq_solve(int n, const double* __restrict__ U, double* __restrict__ X, double charge,
+__device__ inline void d_eeq_solve(int n, const double* __restrict__ U, double* __restrict__ X, double charge,
                             double* __restrict__ q) {
     __shared__ double red[32];
     __shared__ double y0, y1;
@@ -163,7 +163,7 @@ __device__ void d_eeq_solve(int n, const double* __restrict__ U, double* __restr
 
 
 // dE/dCN from the diagonal self energies (src/xtb/hamiltonian.F90:778-786)
-__device__ void d_dhdcn_diag(DevMol m, const double* __restrict__ P, double* __restrict__ dhdcn, int a) {
+__device__ inline void d_dhdcn_diag(DevMol m, const double* __restrict__ P, double* __restrict__ dhdcn, int a) {
     double s = 0.0;
     for (int mu = m.at_ao0[a]; mu < m.at_ao0[a] + m.at_nao[a]; ++mu)
         s += P[(size_t)mu * m.nao + mu] * (-m.sh_kcn[m.ao_sh[mu]]) * EVTOAU;
@@ -173,7 +173,7 @@ __device__ void d_dhdcn_diag(DevMol m, const double* __restrict__ P, double* __r
 
 // ================================================================== isotropic electrostatics
 // getCoulombMatrixCluster with arithmetic hardness average (src/coulomb/klopmanohno.F90:257-312, 742-755)
-__device__ void d_jmat(DevMol m, double* __restrict__ J, long t) {
+__device__ inline void d_jmat(DevMol m, double* __restrict__ J, long t) {
     const int ns = m.nsh;
     const int s = (int)(t / ns), u = (int)(t % ns);
     const int a = m.sh_atom[s], b = m.sh_atom[u];
@@ -190,7 +190,7 @@ __device__ void d_jmat(DevMol m, double* __restrict__ J, long t) {
 
 // shift_s = (J qsh)_s + Gamma_s qsh_s^2 + v_D4[atom(s)]  (TxTBCoulomb%addShift, src/xtb/coulomb.f90:89-114,
 // src/xtb/thirdorder.f90:100-131); one warp per shell row
-__device__ void d_shell_shift(DevMol m, const double* __restrict__ J, const double* __restrict__ qsh,
+__device__ inline void d_shell_shift(DevMol m, const double* __restrict__ J, const double* __restrict__ qsh,
                               const double* __restrict__ vat, double* __restrict__ shift, double* __restrict__ Jq, int s, int lane) {
     const double* row = J + (size_t)s * m.nsh;
     double acc = 0.0;
@@ -205,14 +205,14 @@ __device__ void d_shell_shift(DevMol m, const double* __restrict__ J, const doub
 
 // ================================================================== anisotropic electrostatics
 // get_radcn + mmomgabzero (src/aespot.F90:1219-1281, 1309-1329)
-__device__ void d_radcn(DevMol m, const double* __restrict__ cn, double* __restrict__ radcn, int i) {
+__device__ inline void d_radcn(DevMol m, const double* __restrict__ cn, double* __restrict__ radcn, int i) {
     const double rco = m.mrad[i];
     const double t1 = cn[i] - m.valcn[i] - 1.2;
     radcn[i] = rco + (5.0 - rco) / (1.0 + exp(-4.0 * t1));
 }
 
 
-__device__ void d_gab(DevMol m, const double* __restrict__ radcn, double* __restrict__ gab3, double* __restrict__ gab5, long t) {
+__device__ inline void d_gab(DevMol m, const double* __restrict__ radcn, double* __restrict__ gab3, double* __restrict__ gab5, long t) {
     const int n = m.nat;
     const int i = (int)(t / n), j = (int)(t % n);
     if (i == j) { gab3[t] = 0.0; gab5[t] = 0.0; return; }
@@ -234,7 +234,7 @@ __device__ __forceinline__ int lin3(int a, int b) {  // packed index of (a,b): x
 
 
 // setvsdq (shifted = true, src/aespot.F90:727-848) / setdvsdq (src/aespot.F90:861-952); one warp per atom
-__device__ void d_aes_pot(DevMol m, const double* __restrict__ q, const double* __restrict__ dipm,
+__device__ inline void d_aes_pot(DevMol m, const double* __restrict__ q, const double* __restrict__ dipm,
                           const double* __restrict__ qp, const double* __restrict__ gab3, const double* __restrict__ gab5,
                           int shifted, double* __restrict__ vs, double* __restrict__ vd, double* __restrict__ vq, int i, int lane) {
     const int n = m.nat;
@@ -319,7 +319,7 @@ __device__ void d_aes_pot(DevMol m, const double* __restrict__ q, const double* 
 
 
 // aniso_electro_cpu (src/aespot.F90:566-664): e_part[i] = pair terms with j < i, e_part[n+i] = kernel term
-__device__ void d_aes_energy(DevMol m, const double* __restrict__ q, const double* __restrict__ dipm,
+__device__ inline void d_aes_energy(DevMol m, const double* __restrict__ q, const double* __restrict__ dipm,
                              const double* __restrict__ qp, const double* __restrict__ gab3,
                              const double* __restrict__ gab5, double* __restrict__ e_part, int i, int lane) {
     const int n = m.nat;
@@ -358,7 +358,7 @@ __device__ void d_aes_energy(DevMol m, const double* __restrict__ q, const doubl
 
 
 // aniso_grad (src/aespot.F90:1060-1165); tmp2[i] collects the radius-derivative prefactor
-__device__ void d_aes_grad(DevMol m, const double* __restrict__ q, const double* __restrict__ dipm,
+__device__ inline void d_aes_grad(DevMol m, const double* __restrict__ q, const double* __restrict__ dipm,
                            const double* __restrict__ qp, const double* __restrict__ radcn,
                            const double* __restrict__ gab3, const double* __restrict__ gab5, double* __restrict__ grad,
                            double* __restrict__ tmp2, int i, int lane) {
@@ -421,7 +421,7 @@ __device__ void d_aes_grad(DevMol m, const double* __restrict__ q, const double*
 
 
 // dradcn (src/aespot.F90:1292-1307): dhdcn[i] -= tmp2[i] * dR0_i/dCN_i (chain through the gfn CN)
-__device__ void d_aes_dradcn(DevMol m, const double* __restrict__ cn, const double* __restrict__ tmp2,
+__device__ inline void d_aes_dradcn(DevMol m, const double* __restrict__ cn, const double* __restrict__ tmp2,
                              double* __restrict__ dhdcn, int i) {
     const double rco = m.mrad[i];
     const double t1 = exp(-4.0 * (cn[i] - m.valcn[i] - 1.2));
@@ -433,7 +433,7 @@ __device__ void d_aes_dradcn(DevMol m, const double* __restrict__ cn, const doub
 
 // ================================================================== Hamiltonian build
 // buildIsoAnisotropicH1 (src/scc_core.f90:154-251) with the setdqlist screening (src/aespot.F90:34-85)
-__device__ void d_build_h(DevMol m, double neglect, const double* __restrict__ H0, const double* __restrict__ S,
+__device__ inline void d_build_h(DevMol m, double neglect, const double* __restrict__ H0, const double* __restrict__ S,
                           const double* __restrict__ D, const double* __restrict__ Q, const double* __restrict__ shift,
                           const double* __restrict__ vs, const double* __restrict__ vd, const double* __restrict__ vq,
                           double* __restrict__ H, size_t t) {
@@ -467,7 +467,7 @@ __device__ void d_build_h(DevMol m, double neglect, const double* __restrict__ H
 
 // ================================================================== Fermi smearing
 // fermismear (src/scc_core.f90:983-1064) for one spin channel; one block.
-__device__ void fermi_channel(int n, const double* emo, int nel, double etemp, double* occ, double* red,
+__device__ inline void fermi_channel(int n, const double* emo, int nel, double etemp, double* occ, double* red,
                               double& s_out, double& ef_out) {
     const double bkt = KB_AU * AUTOEV * etemp;
     const double thr = 1e-9;
@@ -514,7 +514,7 @@ __device__ void fermi_channel(int n, const double* emo, int nel, double etemp, d
 }
 
 
-__device__ void d_fermi(int n, const double* __restrict__ emo, int nel_a, int nel_b, double etemp,
+__device__ inline void d_fermi(int n, const double* __restrict__ emo, int nel_a, int nel_b, double etemp,
                         double* __restrict__ focc, double* __restrict__ fa, double* __restrict__ fb,
                         double* __restrict__ scal, int* __restrict__ kocc) {
     __shared__ double red[32];
@@ -546,7 +546,7 @@ __device__ void d_fermi(int n, const double* __restrict__ emo, int nel_a, int ne
 }
 
 
-__device__ void d_scale_cols(int n, const double* __restrict__ C, const double* __restrict__ f, double* __restrict__ Cf, size_t t) {
+__device__ inline void d_scale_cols(int n, const double* __restrict__ C, const double* __restrict__ f, double* __restrict__ Cf, size_t t) {
     const double fj = f[t % n];
     Cf[t] = (fj == 0.0) ? 0.0 : C[t] * fj;     // exact zeros for unoccupied columns
 }
@@ -555,7 +555,7 @@ __device__ void d_scale_cols(int n, const double* __restrict__ C, const double* 
 // ================================================================== populations
 // mpopsh + qsh2qat + mmompop_cpu + the H0 energy sum (src/scc_core.f90:1408-1444, src/aespot.F90:288-428,
 // src/scc_core.f90:686-722).  Pass 1: one warp per AO row computes 11 row sums.
-__device__ void d_rowsums(DevMol m, const double* __restrict__ P, const double* __restrict__ S,
+__device__ inline void d_rowsums(DevMol m, const double* __restrict__ P, const double* __restrict__ S,
                           const double* __restrict__ D, const double* __restrict__ Q, const double* __restrict__ H0,
                           double* __restrict__ rows, int mu, int lane) {
     const size_t nao = m.nao, nn = nao * nao, off = (size_t)mu * nao;
@@ -580,7 +580,7 @@ __device__ void d_rowsums(DevMol m, const double* __restrict__ P, const double* 
 
 
 // Pass 2: one thread per atom.
-__device__ void d_atom_pop(DevMol m, const double* __restrict__ rows, double* __restrict__ qsh, double* __restrict__ q,
+__device__ inline void d_atom_pop(DevMol m, const double* __restrict__ rows, double* __restrict__ qsh, double* __restrict__ q,
                            double* __restrict__ dipm, double* __restrict__ qp, double* __restrict__ eh0, int a) {
     const double R[3] = {m.xyz[3 * a], m.xyz[3 * a + 1], m.xyz[3 * a + 2]};
     double qa = 0.0, e = 0.0;
@@ -618,7 +618,7 @@ __device__ void d_atom_pop(DevMol m, const double* __restrict__ rows, double* __
 }
 
 
-__device__ void d_reduce(const double* __restrict__ x, int n, double* __restrict__ out) {
+__device__ inline void d_reduce(const double* __restrict__ x, int n, double* __restrict__ out) {
     __shared__ double red[32];
     double s = 0.0;
     for (int i = threadIdx.x; i < n; i += blockDim.x) s += x[i];
@@ -628,7 +628,7 @@ __device__ void d_reduce(const double* __restrict__ x, int n, double* __restrict
 
 
 // One block: dq = qout - qin, rms, Broyden update of qin in place.
-__device__ void d_broyden(int nbr, int it, int maxit, double alpha, double* __restrict__ qin,
+__device__ inline void d_broyden(int nbr, int it, int maxit, double alpha, double* __restrict__ qin,
                           const double* __restrict__ qout, double* __restrict__ dq, double* __restrict__ df,
                           double* __restrict__ u, double* __restrict__ amat, double* __restrict__ omega,
                           double* __restrict__ qlast, double* __restrict__ dqlast, double* __restrict__ work,
@@ -754,7 +754,7 @@ __device__ void d_broyden(int nbr, int it, int maxit, double alpha, double* __re
 
 // ================================================================== repulsion
 // repulsionEnGrad_latp, molecular case (src/xtb/repulsion.F90:41-158)
-__device__ void d_repulsion(DevMol m, double* __restrict__ e_atom, double* __restrict__ grad, int a) {
+__device__ inline void d_repulsion(DevMol m, double* __restrict__ e_atom, double* __restrict__ grad, int a) {
     double e = 0.0, g[3] = {0, 0, 0};
     for (int b = 0; b < m.nat; ++b) {
         if (b == a) continue;
@@ -780,7 +780,7 @@ __device__ void d_repulsion(DevMol m, double* __restrict__ e_atom, double* __res
 
 // ================================================================== Coulomb gradient
 // getCoulombDerivsCluster contracted with qsh (src/coulomb/klopmanohno.F90:471-573); warp per atom
-__device__ void d_coulomb_grad(DevMol m, const double* __restrict__ qsh, double* __restrict__ grad, int a, int lane) {
+__device__ inline void d_coulomb_grad(DevMol m, const double* __restrict__ qsh, double* __restrict__ grad, int a, int lane) {
     double g[3] = {0, 0, 0};
     for (int b = lane; b < m.nat; b += 32) {
         if (b == a) continue;
@@ -816,7 +816,7 @@ __device__ __forceinline__ double dzeta_fn(double a, double c, double qref, doub
 
 // Gaussian CN weights of the reference systems: d4 (src/disp/dftd4.F90:588-657) and
 // weight_references (:948-1065); gw[a*MAXREF + r], dgw = d gw / d CN
-__device__ void d_d4_weights(DevMol m, const double* __restrict__ cnv, double* __restrict__ gw, double* __restrict__ dgw, int a) {
+__device__ inline void d_d4_weights(DevMol m, const double* __restrict__ cnv, double* __restrict__ gw, double* __restrict__ dgw, int a) {
     const int e = m.eid[a];
     const int nref = m.d4_nref[e];
     const double wf = 6.0;
@@ -851,7 +851,7 @@ __device__ void d_d4_weights(DevMol m, const double* __restrict__ cnv, double* _
 
 
 // zeta / dzeta of the SCC dispersion (disppot, src/disp/dftd4.F90:735-818)
-__device__ void d_d4_zeta(DevMol m, const double* __restrict__ gw, const double* __restrict__ q,
+__device__ inline void d_d4_zeta(DevMol m, const double* __restrict__ gw, const double* __restrict__ q,
                           double* __restrict__ zeta, double* __restrict__ dzeta, int a) {
     const int e = m.eid[a];
     const double iz = m.d4_zeff[e], gi = m.d4_gam[e] * 2.0;
@@ -869,7 +869,7 @@ __device__ void d_d4_zeta(DevMol m, const double* __restrict__ gw, const double*
 
 
 // (W zeta) for atom a, W = build_wdispmat (src/disp/dftd4.F90:660-732) evaluated on the fly; warp per atom
-__device__ void d_d4_wz(DevMol m, const double* __restrict__ gw, const double* __restrict__ zeta,
+__device__ inline void d_d4_wz(DevMol m, const double* __restrict__ gw, const double* __restrict__ zeta,
                         const double* __restrict__ dzeta, double* __restrict__ Wz, double* __restrict__ vat,
                         double* __restrict__ e_atom, int a, int lane) {
     const int ea = m.eid[a], na = m.d4_nref[ea];
@@ -915,7 +915,7 @@ __device__ void d_d4_wz(DevMol m, const double* __restrict__ gw, const double* _
 
 
 // weight_references: zeta-weighted vectors for q and for q = 0 (src/disp/dftd4.F90:948-1065)
-__device__ void d_d4_refvec(DevMol m, const double* __restrict__ gw, const double* __restrict__ dgw,
+__device__ inline void d_d4_refvec(DevMol m, const double* __restrict__ gw, const double* __restrict__ dgw,
                             const double* __restrict__ q, double* __restrict__ zv, double* __restrict__ zr,
                             double* __restrict__ zdcn, double* __restrict__ zrdcn, int a) {
     const int e = m.eid[a];
@@ -935,7 +935,7 @@ __device__ void d_d4_refvec(DevMol m, const double* __restrict__ gw, const doubl
 
 
 // get_atomic_c6 (src/disp/dftd4.F90:1069-1147): c6[a][b], dc6[a][b] = d c6_ab / d CN_a
-__device__ void d_d4_c6(DevMol m, const double* __restrict__ zv, const double* __restrict__ zdcn,
+__device__ inline void d_d4_c6(DevMol m, const double* __restrict__ zv, const double* __restrict__ zdcn,
                         double* __restrict__ c6o, double* __restrict__ dc6o, long t) {
     const int n = m.nat;
     const int a = (int)(t / n), b = (int)(t % n);
@@ -954,7 +954,7 @@ __device__ void d_d4_c6(DevMol m, const double* __restrict__ zv, const double* _
 
 
 // two-body dispersion energy / gradient (disp_gradient_latp, src/disp/dftd4.F90:1832-1933); thread per atom
-__device__ void d_d4_2body(DevMol m, const double* __restrict__ c6, const double* __restrict__ dc6,
+__device__ inline void d_d4_2body(DevMol m, const double* __restrict__ c6, const double* __restrict__ dc6,
                            double* __restrict__ e_atom, double* __restrict__ dEdcn, double* __restrict__ grad, int a) {
     const int n = m.nat;
     double e = 0.0, dcn = 0.0, g[3] = {0, 0, 0};
@@ -980,6 +980,105 @@ __device__ void d_d4_2body(DevMol m, const double* __restrict__ c6, const double
     e_atom[a] = e;
     dEdcn[a] += dcn;
     for (int k = 0; k < 3; ++k) grad[3 * a + k] += g[k];
+}
+
+// Broyden vector [qsh; per atom (dipm 3, qp 6)] (gfn2broyden_*, src/aespot.F90:1360-1425)
+__device__ inline void d_broyden_pack(DevMol m, const double* __restrict__ qsh, const double* __restrict__ dipm,
+                               const double* __restrict__ qp, double* __restrict__ v, int t) {
+    if (t < m.nsh) v[t] = qsh[t];
+    if (t < m.nat) {
+        double* o = v + m.nsh + 9 * t;
+        for (int k = 0; k < 3; ++k) o[k] = dipm[3 * t + k];
+        for (int k = 0; k < 6; ++k) o[3 + k] = qp[6 * t + k];
+    }
+}
+
+__device__ inline void d_broyden_unpack(DevMol m, const double* __restrict__ v, double* __restrict__ qsh,
+                                 double* __restrict__ dipm, double* __restrict__ qp, double* __restrict__ q, int t) {
+    if (t < m.nsh) qsh[t] = v[t];
+    if (t < m.nat) {
+        const double* o = v + m.nsh + 9 * t;
+        for (int k = 0; k < 3; ++k) dipm[3 * t + k] = o[k];
+        for (int k = 0; k < 6; ++k) qp[6 * t + k] = o[3 + k];
+        double s = 0.0;
+        for (int sh = m.at_sh0[t]; sh < m.at_sh0[t] + m.at_nsh[t]; ++sh) s += v[sh];
+        q[t] = s;
+    }
+}
+
+// three-body (ATM) dispersion, atm_gradient_latp / deriv_atm_triple (src/disp/dftd4.F90:2023-2177, 2354-2433)
+__device__ inline void d_d4_atm(DevMol m, const double* __restrict__ c6, const double* __restrict__ dc6, long npair,
+                         double* __restrict__ e_pair, double* __restrict__ dEdcn, double* __restrict__ grad, long t) {
+    int ia, ja;
+    tri_pair(t, ia, ja);
+    if (ja >= ia) { e_pair[t] = 0.0; return; }
+    const int n = m.nat;
+    const double cut2 = 1600.0;
+    const double rij[3] = {m.xyz[3 * ja] - m.xyz[3 * ia], m.xyz[3 * ja + 1] - m.xyz[3 * ia + 1],
+                           m.xyz[3 * ja + 2] - m.xyz[3 * ia + 2]};
+    const double r2ij = rij[0] * rij[0] + rij[1] * rij[1] + rij[2] * rij[2];
+    double esum = 0.0;
+    if (r2ij <= cut2) {
+        double gi[3] = {0, 0, 0}, gj[3] = {0, 0, 0}, dci = 0.0, dcj = 0.0;
+        const double c6ij = c6[(size_t)ja * n + ia];
+        const double cij = 0.52 * sqrt(3.0 * m.r4r2[ia] * m.r4r2[ja]) + 5.0;
+        for (int ka = 0; ka < ja; ++ka) {
+            const double rik[3] = {m.xyz[3 * ka] - m.xyz[3 * ia], m.xyz[3 * ka + 1] - m.xyz[3 * ia + 1],
+                                   m.xyz[3 * ka + 2] - m.xyz[3 * ia + 2]};
+            const double r2ik = rik[0] * rik[0] + rik[1] * rik[1] + rik[2] * rik[2];
+            if (r2ik > cut2) continue;
+            const double rjk[3] = {m.xyz[3 * ka] - m.xyz[3 * ja], m.xyz[3 * ka + 1] - m.xyz[3 * ja + 1],
+                                   m.xyz[3 * ka + 2] - m.xyz[3 * ja + 2]};
+            const double r2jk = rjk[0] * rjk[0] + rjk[1] * rjk[1] + rjk[2] * rjk[2];
+            if (r2jk > cut2) continue;
+            const double c6ik = c6[(size_t)ka * n + ia], c6jk = c6[(size_t)ka * n + ja];
+            const double cik = 0.52 * sqrt(3.0 * m.r4r2[ia] * m.r4r2[ka]) + 5.0;
+            const double cjk = 0.52 * sqrt(3.0 * m.r4r2[ja] * m.r4r2[ka]) + 5.0;
+            const double c9 = -sqrt(c6ij * c6ik * c6jk);
+            const double ccc1 = cij * cjk * cik;
+            const double rrr2 = r2ij * r2jk * r2ik;
+            const double rrr1 = sqrt(rrr2);
+            const double rrr3 = rrr1 * rrr2;
+            const double ang_fact = 0.375 / (rrr2 * rrr3);
+            const double ang = ang_fact * (r2ij + r2jk - r2ik) * (r2ij - r2jk + r2ik) * (-r2ij + r2jk + r2ik) + 1.0 / rrr3;
+            const double cralp = pow(ccc1 / rrr1, 16.0 / 3.0);
+            const double fdmp = 1.0 / (1.0 + 6.0 * cralp);
+            const double dfdmp = -(2.0 * 16.0 * cralp) * fdmp * fdmp;
+            const double dE = -fdmp * ang * c9;
+            const double dang1 = -ang_fact * (r2ij * r2ij * r2ij + r2ij * r2ij * (r2jk + r2ik) +
+                                              r2ij * (3.0 * r2jk * r2jk + 2.0 * r2jk * r2ik + 3.0 * r2ik * r2ik) -
+                                              5.0 * sq(r2jk - r2ik) * (r2jk + r2ik));
+            const double dGr1 = (-dang1 * c9 * fdmp + dfdmp * c9 * ang) / r2ij;
+            const double dang2 = -ang_fact * (r2ik * r2ik * r2ik + r2ik * r2ik * (r2jk + r2ij) +
+                                              r2ik * (3.0 * r2jk * r2jk + 2.0 * r2jk * r2ij + 3.0 * r2ij * r2ij) -
+                                              5.0 * sq(r2jk - r2ij) * (r2jk + r2ij));
+            const double dGr2 = (-dang2 * c9 * fdmp + dfdmp * c9 * ang) / r2ik;
+            const double dang3 = -ang_fact * (r2jk * r2jk * r2jk + r2jk * r2jk * (r2ik + r2ij) +
+                                              r2jk * (3.0 * r2ik * r2ik + 2.0 * r2ik * r2ij + 3.0 * r2ij * r2ij) -
+                                              5.0 * sq(r2ik - r2ij) * (r2ik + r2ij));
+            const double dGr3 = (-dang3 * c9 * fdmp + dfdmp * c9 * ang) / r2jk;
+            const double s9 = 5.0;
+            esum += dE * s9;
+            for (int x = 0; x < 3; ++x) {
+                gi[x] += s9 * (-dGr1 * rij[x] - dGr2 * rik[x]);
+                gj[x] += s9 * (dGr1 * rij[x] - dGr3 * rjk[x]);
+                atomicAdd(&grad[3 * ka + x], s9 * (dGr2 * rik[x] + dGr3 * rjk[x]));
+            }
+            const double dc9i = 0.5 * c9 * (dc6[(size_t)ia * n + ja] / c6ij + dc6[(size_t)ia * n + ka] / c6ik);
+            const double dc9j = 0.5 * c9 * (dc6[(size_t)ja * n + ia] / c6ij + dc6[(size_t)ja * n + ka] / c6jk);
+            const double dc9k = 0.5 * c9 * (dc6[(size_t)ka * n + ia] / c6ik + dc6[(size_t)ka * n + ja] / c6jk);
+            dci += s9 * (-ang * fdmp * dc9i);
+            dcj += s9 * (-ang * fdmp * dc9j);
+            atomicAdd(&dEdcn[ka], s9 * (-ang * fdmp * dc9k));
+        }
+        for (int x = 0; x < 3; ++x) {
+            atomicAdd(&grad[3 * ia + x], gi[x]);
+            atomicAdd(&grad[3 * ja + x], gj[x]);
+        }
+        atomicAdd(&dEdcn[ia], dci);
+        atomicAdd(&dEdcn[ja], dcj);
+    }
+    e_pair[t] = esum;
 }
 
 }  // namespace xg

@@ -282,31 +282,16 @@ void add_vec(cudaStream_t st, int n, const double* a, double* b) {
 
 // ================================================================== Broyden mixing
 // broyden (src/broyden.f90:37-153) with gfn2broyden_save/diff/out packing (src/aespot.F90:1360-1425)
+
+
 __global__ void k_broyden_pack(DevMol m, const double* __restrict__ qsh, const double* __restrict__ dipm,
                                const double* __restrict__ qp, double* __restrict__ v) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < m.nsh) v[t] = qsh[t];
-    if (t < m.nat) {
-        double* o = v + m.nsh + 9 * t;
-        for (int k = 0; k < 3; ++k) o[k] = dipm[3 * t + k];
-        for (int k = 0; k < 6; ++k) o[3 + k] = qp[6 * t + k];
-    }
+    d_broyden_pack(m, qsh, dipm, qp, v, blockIdx.x * blockDim.x + threadIdx.x);
 }
-
 __global__ void k_broyden_unpack(DevMol m, const double* __restrict__ v, double* __restrict__ qsh,
                                  double* __restrict__ dipm, double* __restrict__ qp, double* __restrict__ q) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < m.nsh) qsh[t] = v[t];
-    if (t < m.nat) {
-        const double* o = v + m.nsh + 9 * t;
-        for (int k = 0; k < 3; ++k) dipm[3 * t + k] = o[k];
-        for (int k = 0; k < 6; ++k) qp[6 * t + k] = o[3 + k];
-        double s = 0.0;
-        for (int sh = m.at_sh0[t]; sh < m.at_sh0[t] + m.at_nsh[t]; ++sh) s += v[sh];
-        q[t] = s;
-    }
+    d_broyden_unpack(m, v, qsh, dipm, qp, q, blockIdx.x * blockDim.x + threadIdx.x);
 }
-
 void broyden_pack(cudaStream_t st, const DevMol& m, const double* qsh, const double* dipm, const double* qp, double* vec) {
     k_broyden_pack<<<ceil_div(std::max(m.nsh, m.nat), 256), 256, 0, st>>>(m, qsh, dipm, qp, vec);
     XG_LAUNCH_CHECK();
@@ -426,83 +411,14 @@ __global__ void k_d4_2body(DevMol m, const double* __restrict__ c6, const double
 
 // ATM three-body (atm_gradient_latp molecular branch + deriv_atm_triple, src/disp/dftd4.F90:2023-2177, 2354-2433);
 // one thread per pair (i > j), loop over k < j; gradient and dE/dCN of j, k by atomics.
+
+
 __global__ void k_d4_atm(DevMol m, const double* __restrict__ c6, const double* __restrict__ dc6, long npair,
                          double* __restrict__ e_pair, double* __restrict__ dEdcn, double* __restrict__ grad) {
     const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= npair) return;
-    int ia, ja;
-    tri_pair(t, ia, ja);
-    if (ja >= ia) { e_pair[t] = 0.0; return; }
-    const int n = m.nat;
-    const double cut2 = 1600.0;
-    const double rij[3] = {m.xyz[3 * ja] - m.xyz[3 * ia], m.xyz[3 * ja + 1] - m.xyz[3 * ia + 1],
-                           m.xyz[3 * ja + 2] - m.xyz[3 * ia + 2]};
-    const double r2ij = rij[0] * rij[0] + rij[1] * rij[1] + rij[2] * rij[2];
-    double esum = 0.0;
-    if (r2ij <= cut2) {
-        double gi[3] = {0, 0, 0}, gj[3] = {0, 0, 0}, dci = 0.0, dcj = 0.0;
-        const double c6ij = c6[(size_t)ja * n + ia];
-        const double cij = 0.52 * sqrt(3.0 * m.r4r2[ia] * m.r4r2[ja]) + 5.0;
-        for (int ka = 0; ka < ja; ++ka) {
-            const double rik[3] = {m.xyz[3 * ka] - m.xyz[3 * ia], m.xyz[3 * ka + 1] - m.xyz[3 * ia + 1],
-                                   m.xyz[3 * ka + 2] - m.xyz[3 * ia + 2]};
-            const double r2ik = rik[0] * rik[0] + rik[1] * rik[1] + rik[2] * rik[2];
-            if (r2ik > cut2) continue;
-            const double rjk[3] = {m.xyz[3 * ka] - m.xyz[3 * ja], m.xyz[3 * ka + 1] - m.xyz[3 * ja + 1],
-                                   m.xyz[3 * ka + 2] - m.xyz[3 * ja + 2]};
-            const double r2jk = rjk[0] * rjk[0] + rjk[1] * rjk[1] + rjk[2] * rjk[2];
-            if (r2jk > cut2) continue;
-            const double c6ik = c6[(size_t)ka * n + ia], c6jk = c6[(size_t)ka * n + ja];
-            const double cik = 0.52 * sqrt(3.0 * m.r4r2[ia] * m.r4r2[ka]) + 5.0;
-            const double cjk = 0.52 * sqrt(3.0 * m.r4r2[ja] * m.r4r2[ka]) + 5.0;
-            const double c9 = -sqrt(c6ij * c6ik * c6jk);
-            const double ccc1 = cij * cjk * cik;
-            const double rrr2 = r2ij * r2jk * r2ik;
-            const double rrr1 = sqrt(rrr2);
-            const double rrr3 = rrr1 * rrr2;
-            const double ang_fact = 0.375 / (rrr2 * rrr3);
-            const double ang = ang_fact * (r2ij + r2jk - r2ik) * (r2ij - r2jk + r2ik) * (-r2ij + r2jk + r2ik) + 1.0 / rrr3;
-            const double cralp = pow(ccc1 / rrr1, 16.0 / 3.0);
-            const double fdmp = 1.0 / (1.0 + 6.0 * cralp);
-            const double dfdmp = -(2.0 * 16.0 * cralp) * fdmp * fdmp;
-            const double dE = -fdmp * ang * c9;
-            const double dang1 = -ang_fact * (r2ij * r2ij * r2ij + r2ij * r2ij * (r2jk + r2ik) +
-                                              r2ij * (3.0 * r2jk * r2jk + 2.0 * r2jk * r2ik + 3.0 * r2ik * r2ik) -
-                                              5.0 * sq(r2jk - r2ik) * (r2jk + r2ik));
-            const double dGr1 = (-dang1 * c9 * fdmp + dfdmp * c9 * ang) / r2ij;
-            const double dang2 = -ang_fact * (r2ik * r2ik * r2ik + r2ik * r2ik * (r2jk + r2ij) +
-                                              r2ik * (3.0 * r2jk * r2jk + 2.0 * r2jk * r2ij + 3.0 * r2ij * r2ij) -
-                                              5.0 * sq(r2jk - r2ij) * (r2jk + r2ij));
-            const double dGr2 = (-dang2 * c9 * fdmp + dfdmp * c9 * ang) / r2ik;
-            const double dang3 = -ang_fact * (r2jk * r2jk * r2jk + r2jk * r2jk * (r2ik + r2ij) +
-                                              r2jk * (3.0 * r2ik * r2ik + 2.0 * r2ik * r2ij + 3.0 * r2ij * r2ij) -
-                                              5.0 * sq(r2ik - r2ij) * (r2ik + r2ij));
-            const double dGr3 = (-dang3 * c9 * fdmp + dfdmp * c9 * ang) / r2jk;
-            const double s9 = 5.0;
-            esum += dE * s9;
-            for (int x = 0; x < 3; ++x) {
-                gi[x] += s9 * (-dGr1 * rij[x] - dGr2 * rik[x]);
-                gj[x] += s9 * (dGr1 * rij[x] - dGr3 * rjk[x]);
-                atomicAdd(&grad[3 * ka + x], s9 * (dGr2 * rik[x] + dGr3 * rjk[x]));
-            }
-            const double dc9i = 0.5 * c9 * (dc6[(size_t)ia * n + ja] / c6ij + dc6[(size_t)ia * n + ka] / c6ik);
-            const double dc9j = 0.5 * c9 * (dc6[(size_t)ja * n + ia] / c6ij + dc6[(size_t)ja * n + ka] / c6jk);
-            const double dc9k = 0.5 * c9 * (dc6[(size_t)ka * n + ia] / c6ik + dc6[(size_t)ka * n + ja] / c6jk);
-            dci += s9 * (-ang * fdmp * dc9i);
-            dcj += s9 * (-ang * fdmp * dc9j);
-            atomicAdd(&dEdcn[ka], s9 * (-ang * fdmp * dc9k));
-        }
-        for (int x = 0; x < 3; ++x) {
-            atomicAdd(&grad[3 * ia + x], gi[x]);
-            atomicAdd(&grad[3 * ja + x], gj[x]);
-        }
-        atomicAdd(&dEdcn[ia], dci);
-        atomicAdd(&dEdcn[ja], dcj);
-    }
-    e_pair[t] = esum;
+    d_d4_atm(m, c6, dc6, npair, e_pair, dEdcn, grad, t);
 }
-
-
 void d4_grad(cudaStream_t st, const DevMol& m, const double* cnv, const double* q, double* gw, double* dgw,
              double* zv, double* zr, double* zdcn, double* zrdcn, double* c6, double* dc6, double* c6z, double* dc6z,
              double* e2_atom, double* e3_pair, double* dEdcn, double* grad) {

@@ -142,7 +142,7 @@ __device__ __forceinline__ double h0_factor(const DevMol& m, const double* se, i
 
 
 template <int LI, int LJ>
-__device__ void d_sdqh0(DevMol m, const double* __restrict__ se, double intcut, long npairs,
+__device__ inline void d_sdqh0(DevMol m, const double* __restrict__ se, double intcut, long npairs,
                                                double* __restrict__ S, double* __restrict__ D, double* __restrict__ Q,
                                                double* __restrict__ H0, long t) {
     int ish, jsh;
@@ -248,7 +248,7 @@ __device__ void d_sdqh0(DevMol m, const double* __restrict__ se, double intcut, 
 // shiftintg (src/intgrad.f90:607-728, 958-1035) and dshellPoly (src/grad_core.f90:40-72).  The derivative
 // integrals are contracted with their energy weights inside the primitive loop (fused kernel).
 template <int LI, int LJ>
-__device__ void d_grad_sdqh0(DevMol m, const double* __restrict__ se, double intcut, long npairs,
+__device__ inline void d_grad_sdqh0(DevMol m, const double* __restrict__ se, double intcut, long npairs,
                                                     const double* __restrict__ P, const double* __restrict__ Pew,
                                                     const double* __restrict__ shift, const double* __restrict__ vs,
                                                     const double* __restrict__ vd, const double* __restrict__ vq,

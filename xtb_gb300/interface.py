@@ -76,6 +76,17 @@ def load_library(path=LIBPATH):
         "xtbgb_setKeepOrbitals": (None, [vp, vp, C.c_int]),
         "xtbgb_fp64PeakTflops": (C.c_double, []),
         "xtbgb_repulsionNoAlloc": (C.c_int, [C.c_int, vp, vp, vp, vp, vp, C.c_char_p, C.c_int]),
+        "xtbgb_newBatch": (vp, [vp, C.c_int, ip, ip, dp, dp, ip]),
+        "xtbgb_delBatch": (None, [C.POINTER(vp)]),
+        "xtbgb_batchSinglepoint": (None, [vp, vp, C.c_double, C.c_double, C.c_int, C.c_int]),
+        "xtbgb_batchGetEnergies": (None, [vp, vp, dp]),
+        "xtbgb_batchGetGradients": (None, [vp, vp, dp]),
+        "xtbgb_batchGetCharges": (None, [vp, vp, dp]),
+        "xtbgb_batchGetDipoles": (None, [vp, vp, dp]),
+        "xtbgb_batchGetEnergyParts": (None, [vp, vp, dp]),
+        "xtbgb_batchGetStatus": (None, [vp, vp, ip, ip, ip, ip]),
+        "xtbgb_batchGetStats": (None, [vp, vp, dp, C.POINTER(C.c_longlong)]),
+        "xtbgb_batchNao": (None, [vp, vp, ip]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -199,3 +210,85 @@ class Results:
         lib.xtbgb_getTransferBytes(env.h, res, tb)
         self.h2d_bytes, self.d2h_bytes, self.launches = int(tb[0]), int(tb[1]), int(tb[2])
         env.check()
+
+
+class Batch:
+    """Many GFN2-xTB single points in one call of the batched engine (xtbgb_newBatch ...).
+
+    ``molecules`` is a list of (numbers, positions in Bohr); ``charges`` / ``uhf`` optional lists.
+    """
+
+    def __init__(self, molecules, charges=None, uhf=None, verbosity=0):
+        self.lib = load_library()
+        self.env = Environment(verbosity)
+        self.natoms = np.array([len(z) for z, _ in molecules], dtype=np.int32)
+        self.offsets = np.concatenate([[0], np.cumsum(self.natoms)])
+        self.numbers = np.ascontiguousarray(np.concatenate([np.asarray(z, dtype=np.int32) for z, _ in molecules]))
+        self.positions = np.ascontiguousarray(
+            np.concatenate([np.asarray(x, dtype=np.float64).reshape(-1, 3) for _, x in molecules]))
+        nmol = len(molecules)
+        ch = None if charges is None else np.ascontiguousarray(charges, dtype=np.float64)
+        uh = None if uhf is None else np.ascontiguousarray(uhf, dtype=np.int32)
+        self.h = C.c_void_p(self.lib.xtbgb_newBatch(
+            self.env.h, nmol, self.natoms.ctypes.data_as(C.POINTER(C.c_int)),
+            self.numbers.ctypes.data_as(C.POINTER(C.c_int)), _dptr(self.positions),
+            None if ch is None else _dptr(ch), None if uh is None else uh.ctypes.data_as(C.POINTER(C.c_int))))
+        self.env.check()
+        self.nmol = nmol
+        self.nao = np.zeros(nmol, dtype=np.int32)
+        self.lib.xtbgb_batchNao(self.env.h, self.h, self.nao.ctypes.data_as(C.POINTER(C.c_int)))
+
+    def run(self, accuracy=1.0, etemp=300.0, maxiter=250, gradient=True, check=True):
+        """Run every single point; returns a BatchResults.  With ``check`` an error on the
+        environment (failed or unconverged molecules) raises after the results are read."""
+        self.lib.xtbgb_batchSinglepoint(self.env.h, self.h, accuracy, etemp, maxiter, int(bool(gradient)))
+        failed = self.lib.xtb_checkEnvironment(self.env.h)
+        msg = None
+        if failed:
+            buf = C.create_string_buffer(4096)
+            n = C.c_int(4096)
+            self.lib.xtb_getError(self.env.h, buf, C.byref(n))
+            msg = buf.value.decode()
+            if "not available" in msg or "not allocated" in msg:
+                raise XTBException(msg)
+        r = BatchResults(self)
+        r.error = msg
+        if check and msg:
+            raise XTBException(msg)
+        return r
+
+    def __del__(self):
+        lib = getattr(self, "lib", None)
+        if lib is not None and getattr(self, "h", None) is not None:
+            lib.xtbgb_delBatch(C.byref(self.h))
+
+
+class BatchResults:
+    def __init__(self, b):
+        lib, env, h, n = b.lib, b.env, b.h, b.nmol
+        N = int(b.offsets[-1])
+        ip = C.POINTER(C.c_int)
+        self.energy = np.zeros(n)
+        lib.xtbgb_batchGetEnergies(env.h, h, _dptr(self.energy))
+        g = np.zeros((N, 3))
+        lib.xtbgb_batchGetGradients(env.h, h, _dptr(g))
+        q = np.zeros(N)
+        lib.xtbgb_batchGetCharges(env.h, h, _dptr(q))
+        self.gradients = [g[b.offsets[i]:b.offsets[i + 1]] for i in range(n)]
+        self.charges = [q[b.offsets[i]:b.offsets[i + 1]] for i in range(n)]
+        self.dipole = np.zeros((n, 3))
+        lib.xtbgb_batchGetDipoles(env.h, h, _dptr(self.dipole))
+        self.parts = np.zeros((n, 8))
+        lib.xtbgb_batchGetEnergyParts(env.h, h, _dptr(self.parts))
+        self.iterations = np.zeros(n, dtype=np.int32)
+        self.converged = np.zeros(n, dtype=np.int32)
+        self.status = np.zeros(n, dtype=np.int32)
+        self.engine = np.zeros(n, dtype=np.int32)
+        lib.xtbgb_batchGetStatus(env.h, h, self.iterations.ctypes.data_as(ip), self.converged.ctypes.data_as(ip),
+                                 self.status.ctypes.data_as(ip), self.engine.ctypes.data_as(ip))
+        t = np.zeros(2)
+        c = (C.c_longlong * 4)()
+        lib.xtbgb_batchGetStats(env.h, h, _dptr(t), c)
+        self.device_ms, self.wall_ms = float(t[0]), float(t[1])
+        self.h2d_bytes, self.d2h_bytes, self.launches, self.plain_count = (int(c[0]), int(c[1]), int(c[2]),
+                                                                          int(c[3]))
