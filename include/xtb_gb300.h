@@ -82,6 +82,33 @@ extern void xtbgb_batchGetStats(xtb_TEnvironment env, xtbgb_TBatch batch, double
 /* number of AOs of every molecule [nmol] */
 extern void xtbgb_batchNao(xtb_TEnvironment env, xtbgb_TBatch batch, int* nao);
 
+/* ---- Request loop (no counterpart in the reference).  A server owns a resident pool of
+ * molecules on the device (HBM budget pool_gib GiB, at most max_slots molecules) that is
+ * advanced iters_per_step SCC iterations per step with continuous batching: requests that
+ * arrive while others run join the next step.  Molecules above 512 AOs run on
+ * plain_workers concurrent plain-engine workers.  Submit and wait may be called from any
+ * thread, each thread with its own environment. */
+typedef struct _xtbgb_TServer* xtbgb_TServer;
+
+extern xtbgb_TServer xtbgb_newServer(xtb_TEnvironment env, double pool_gib, int max_slots, int plain_workers,
+                                     int iters_per_step, double accuracy, double etemp, int maxiter);
+/* Finishes all submitted work, then frees the server. */
+extern void xtbgb_delServer(xtbgb_TServer* server);
+/* Queue one GFN2-xTB single point (positions [natoms][3] Bohr); returns the request id, or
+ * -1 with an error on the environment. */
+extern long long xtbgb_serverSubmit(xtb_TEnvironment env, xtbgb_TServer server, int natoms, const int* numbers,
+                                    const double* positions, double charge, int uhf, int gradient);
+/* Wait for request `id` (timeout in seconds, < 0 waits forever).  Returns 1 and fills the
+ * outputs when the request is done, 0 on timeout.  energy[1]; gradient[natoms][3] and
+ * charges[natoms] may be NULL; info[10]: SCC iterations, converged, status, engine
+ * (0 pool, 1 plain), submit / start / done times (s since the server started), dipole[3].
+ * A failed or unconverged request also raises an error on the environment. */
+extern int xtbgb_serverWait(xtb_TEnvironment env, xtbgb_TServer server, long long id, double timeout,
+                            double* energy, double* gradient, double* charges, double* info);
+/* stats[6]: completed, run on the plain engine, pool steps, pool busy seconds, peak resident
+ * molecules, requests re-run on the plain engine. */
+extern void xtbgb_serverStats(xtb_TEnvironment env, xtbgb_TServer server, double* stats);
+
 /* Repulsion energy and gradient of one molecule, computed from and into DEVICE memory
  * without allocating anything.  No counterpart in the reference: it exists for callers
  * that own all device memory themselves (a serving loop that admits work against a fixed

@@ -11,6 +11,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -18,6 +19,7 @@
 #include "../../include/xtb_gb300.h"
 #include "batch.h"
 #include "engine.h"
+#include "serve.h"
 #include "host_model.h"
 #include "linalg.h"
 
@@ -654,6 +656,101 @@ void xtbgb_batchGetStats(xtb_TEnvironment env, xtbgb_TBatch batch, double* times
 void xtbgb_batchNao(xtb_TEnvironment env, xtbgb_TBatch batch, int* nao) {
     if (!check_env(env) || !batch || !nao) return;
     for (int i = 0; i < batch->nmol; ++i) nao[i] = batch->mols[i].nao;
+}
+
+
+// ------------------------------------------------------------------ request loop
+struct _xtbgb_TServer {
+    std::unique_ptr<xg::Server> srv;
+};
+
+xtbgb_TServer xtbgb_newServer(xtb_TEnvironment env, double pool_gib, int max_slots, int plain_workers,
+                              int iters_per_step, double accuracy, double etemp, int maxiter) {
+    static const char* src = "xtbgb_newServer";
+    if (!check_env(env)) return nullptr;
+    xg::ServeConfig cfg;
+    cfg.pool_bytes = (size_t)(std::max(pool_gib, 0.01) * (double)(size_t(1) << 30));
+    cfg.max_slots = std::max(1, max_slots);
+    cfg.plain_workers = std::max(1, plain_workers);
+    cfg.iters_per_step = std::max(1, iters_per_step);
+    cfg.set.accuracy = std::min(std::max(accuracy, 1.0e-4), 1.0e3);
+    cfg.set.etemp = std::max(etemp, 1.0e-6);
+    cfg.set.maxiter = std::max(maxiter, 1);
+    auto* s = new _xtbgb_TServer();
+    try {
+        s->srv = std::make_unique<xg::Server>(cfg);
+    } catch (const std::exception& e) {
+        env->error(e.what(), src);
+        delete s;
+        return nullptr;
+    }
+    return s;
+}
+
+void xtbgb_delServer(xtbgb_TServer* srv) {
+    if (srv && *srv) {
+        delete *srv;
+        *srv = nullptr;
+    }
+}
+
+long long xtbgb_serverSubmit(xtb_TEnvironment env, xtbgb_TServer srv, int natoms, const int* numbers,
+                             const double* positions, double charge, int uhf, int gradient) {
+    static const char* src = "xtbgb_serverSubmit";
+    if (!check_env(env)) return -1;
+    if (!srv || !srv->srv) {
+        env->error("Server is not allocated", src);
+        return -1;
+    }
+    if (natoms < 1 || !numbers || !positions) {
+        env->error("Invalid molecule", src);
+        return -1;
+    }
+    for (int a = 0; a < natoms; ++a)
+        if (numbers[a] < 1 || numbers[a] > kMaxElem) {
+            env->error("Element " + std::to_string(numbers[a]) + " is not parametrised in GFN2-xTB", src);
+            return -1;
+        }
+    std::string err;
+    const long long id = srv->srv->submit(natoms, numbers, positions, charge, uhf, gradient, err);
+    if (id < 0) env->error(err, src);
+    return id;
+}
+
+int xtbgb_serverWait(xtb_TEnvironment env, xtbgb_TServer srv, long long id, double timeout, double* energy,
+                     double* gradient, double* charges, double* info) {
+    static const char* src = "xtbgb_serverWait";
+    if (!check_env(env)) return 0;
+    if (!srv || !srv->srv) {
+        env->error("Server is not allocated", src);
+        return 0;
+    }
+    xg::Completed c;
+    if (!srv->srv->wait(id, c, timeout)) return 0;
+    if (energy) *energy = c.energy;
+    if (gradient) std::copy(c.gradient.begin(), c.gradient.end(), gradient);
+    if (charges) std::copy(c.charges.begin(), c.charges.end(), charges);
+    if (info) {
+        info[0] = c.iterations;
+        info[1] = c.converged;
+        info[2] = c.status;
+        info[3] = c.engine;
+        info[4] = c.t_submit;
+        info[5] = c.t_start;
+        info[6] = c.t_done;
+        info[7] = c.dipole[0];
+        info[8] = c.dipole[1];
+        info[9] = c.dipole[2];
+    }
+    if (!c.error.empty()) env->error(c.error, src);
+    else if (c.status != xg::BST_OK) env->error("Self consistent charge iterator did not converge", src);
+    return 1;
+}
+
+void xtbgb_serverStats(xtb_TEnvironment env, xtbgb_TServer srv, double* stats) {
+    if (!check_env(env) || !srv || !srv->srv || !stats) return;
+    const auto v = srv->srv->stats();
+    std::copy(v.begin(), v.end(), stats);
 }
 
 }  // extern "C"

@@ -510,6 +510,28 @@ __global__ void k_batch_gather(const BatchMol* __restrict__ mols, int nmol, cons
 }
 
 // ------------------------------------------------------------------ host side
+// Upload the recorded parameter arrays to base + offset, merged into contiguous runs
+// (the work arrays between them are small gaps); returns the bytes copied.
+long long upload_runs(const std::vector<Carver::Up>& ups, char* base, cudaStream_t st) {
+    long long bytes = 0;
+    std::vector<char> stage;
+    size_t i = 0;
+    while (i < ups.size()) {
+        size_t j = i, lo = ups[i].off, hi = ups[i].off + ups[i].bytes;
+        while (j + 1 < ups.size() && ups[j + 1].off - hi < 4096) {
+            ++j;
+            hi = ups[j].off + ups[j].bytes;
+        }
+        stage.assign(hi - lo, 0);
+        for (size_t k = i; k <= j; ++k) std::memcpy(stage.data() + (ups[k].off - lo), ups[k].src, ups[k].bytes);
+        XG_CUDA(cudaMemcpyAsync(base + lo, stage.data(), hi - lo, cudaMemcpyHostToDevice, st));
+        XG_CUDA(cudaStreamSynchronize(st));
+        bytes += (long long)(hi - lo);
+        i = j + 1;
+    }
+    return bytes;
+}
+
 DeviceBatch::~DeviceBatch() {
     if (base_) cudaFree(base_);
 }
@@ -556,47 +578,38 @@ void DeviceBatch::load(const std::vector<const HostMol*>& mols, const std::vecto
         h_mols_[i].want_grad = want_grad.empty() ? 1 : want_grad[i];
     }
     d_mols_ = reinterpret_cast<BatchMol*>(base_);
-    // parameter arrays lie between the work arrays; upload them as contiguous runs
-    std::vector<char> stage;
-    size_t i = 0;
-    while (i < ups.size()) {
-        size_t j = i, lo = ups[i].off, hi = ups[i].off + ups[i].bytes;
-        while (j + 1 < ups.size() && ups[j + 1].off - hi < 4096) {
-            ++j;
-            hi = ups[j].off + ups[j].bytes;
-        }
-        stage.assign(hi - lo, 0);
-        for (size_t k = i; k <= j; ++k) std::memcpy(stage.data() + (ups[k].off - lo), ups[k].src, ups[k].bytes);
-        XG_CUDA(cudaMemcpyAsync(base_ + lo, stage.data(), hi - lo, cudaMemcpyHostToDevice, st));
-        h2d_ += (long long)(hi - lo);
-        XG_CUDA(cudaStreamSynchronize(st));
-        i = j + 1;
-    }
+    h2d_ += upload_runs(ups, base_, st);
     XG_CUDA(cudaMemcpyAsync(d_mols_, h_mols_.data(), sizeof(BatchMol) * nmol_, cudaMemcpyHostToDevice, st));
     XG_CUDA(cudaStreamSynchronize(st));
 }
 
-int DeviceBatch::step(const BatchSettings& set, int max_iter, cudaStream_t st) {
-    if (nmol_ == 0) return 0;
-    const size_t smem = (size_t)std::max(12 * max_nao_ + 32, GEMM_SMEM) * sizeof(double);
+// The seven launches of one step over `nmol` slots.
+void launch_step(BatchMol* d_mols, int nmol, int max_nao, int max_nsh, const BatchSettings& set, int max_iter,
+                 cudaStream_t st) {
+    const size_t smem = (size_t)std::max(12 * max_nao + 32, GEMM_SMEM) * sizeof(double);
     static size_t smem_set = 0;
     if (smem > 48 * 1024 && smem > smem_set) {
         XG_CUDA(cudaFuncSetAttribute(k_batch_scc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         smem_set = smem;
     }
     const DevThresh th = thresholds(set.accuracy);
-    k_batch_setup_a<<<nmol_, BT, 0, st>>>(d_mols_, nmol_);
+    k_batch_setup_a<<<nmol, BT, 0, st>>>(d_mols, nmol);
     XG_LAUNCH_CHECK();
-    batch_integrals(st, d_mols_, nmol_, max_nsh_, th.intcut);
-    k_batch_setup_b<<<nmol_, BT, 0, st>>>(d_mols_, nmol_);
+    batch_integrals(st, d_mols, nmol, max_nsh, th.intcut);
+    k_batch_setup_b<<<nmol, BT, 0, st>>>(d_mols, nmol);
     XG_LAUNCH_CHECK();
-    k_batch_scc<<<nmol_, BT, smem, st>>>(d_mols_, nmol_, th, set.etemp, std::max(1, set.maxiter), max_iter);
+    k_batch_scc<<<nmol, BT, smem, st>>>(d_mols, nmol, th, set.etemp, std::max(1, set.maxiter), max_iter);
     XG_LAUNCH_CHECK();
-    k_batch_grad_a<<<nmol_, BT, 0, st>>>(d_mols_, nmol_);
+    k_batch_grad_a<<<nmol, BT, 0, st>>>(d_mols, nmol);
     XG_LAUNCH_CHECK();
-    batch_integral_gradient(st, d_mols_, nmol_, max_nsh_, th.intcut);
-    k_batch_grad_b<<<nmol_, BT, 0, st>>>(d_mols_, nmol_);
+    batch_integral_gradient(st, d_mols, nmol, max_nsh, th.intcut);
+    k_batch_grad_b<<<nmol, BT, 0, st>>>(d_mols, nmol);
     XG_LAUNCH_CHECK();
+}
+
+int DeviceBatch::step(const BatchSettings& set, int max_iter, cudaStream_t st) {
+    if (nmol_ == 0) return 0;
+    launch_step(d_mols_, nmol_, max_nao_, max_nsh_, set, max_iter, st);
     return nmol_;
 }
 
@@ -611,6 +624,122 @@ void DeviceBatch::gather(const long* d_off, double* d_grad, double* d_q, cudaStr
     if (nmol_ == 0) return;
     k_batch_gather<<<nmol_, 128, 0, st>>>(d_mols_, nmol_, d_off, d_grad, d_q);
     XG_LAUNCH_CHECK();
+}
+
+// ------------------------------------------------------------------ slot pool
+SlotPool::SlotPool(size_t budget_bytes, int max_slots) : max_slots_(std::max(1, max_slots)) {
+    desc_ = ((sizeof(BatchMol) * max_slots_ + 255) / 256) * 256;
+    cap_ = std::max(budget_bytes, desc_ + 4096);
+    XG_CUDA(cudaMalloc(&base_, cap_));
+    d_slots_ = reinterpret_cast<BatchMol*>(base_);
+    std::vector<BatchMol> empty(max_slots_);
+    for (auto& b : empty) {
+        b = BatchMol{};
+        b.stage = BS_DONE;
+    }
+    XG_CUDA(cudaMemcpy(d_slots_, empty.data(), sizeof(BatchMol) * max_slots_, cudaMemcpyHostToDevice));
+    slot_off_.assign(max_slots_, 0);
+    slot_size_.assign(max_slots_, 0);
+    slot_nao_.assign(max_slots_, 0);
+    slot_nsh_.assign(max_slots_, 0);
+    free_.push_back({desc_, cap_ - desc_});
+}
+
+SlotPool::~SlotPool() {
+    if (base_) cudaFree(base_);
+}
+
+size_t SlotPool::free_bytes() const {
+    size_t f = 0;
+    for (auto& r : free_) f += r.second;
+    return f;
+}
+
+int SlotPool::admit(const HostMol& hm, int want_grad, cudaStream_t st) {
+    if (hm.nao > BATCH_MAX_NAO) return -1;
+    int slot = -1;
+    for (int i = 0; i < max_slots_; ++i)
+        if (slot_size_[i] == 0) {
+            slot = i;
+            break;
+        }
+    if (slot < 0) return -1;
+    const size_t need = DeviceBatch::bytes_for(hm);
+    size_t k = 0;
+    while (k < free_.size() && free_[k].second < need) ++k;
+    if (k == free_.size()) return -1;
+    const size_t off = free_[k].first;
+    free_[k].first += need;
+    free_[k].second -= need;
+    if (free_[k].second == 0) free_.erase(free_.begin() + k);
+    BatchMol b{};
+    std::vector<Carver::Up> ups;
+    Carver cv;
+    cv.base = base_ + off;
+    cv.ups = &ups;
+    layout_mol(cv, hm, b);
+    b.want_grad = want_grad;
+    h2d_ += upload_runs(ups, base_ + off, st);
+    XG_CUDA(cudaMemcpyAsync(d_slots_ + slot, &b, sizeof(BatchMol), cudaMemcpyHostToDevice, st));
+    XG_CUDA(cudaStreamSynchronize(st));
+    h2d_ += sizeof(BatchMol);
+    slot_off_[slot] = off;
+    slot_size_[slot] = need;
+    slot_nao_[slot] = hm.nao;
+    slot_nsh_[slot] = hm.nsh;
+    ++resident_;
+    hi_ = std::max(hi_, slot + 1);
+    return slot;
+}
+
+void SlotPool::step(const BatchSettings& set, int max_iter, cudaStream_t st) {
+    if (resident_ == 0) return;
+    int max_nao = 1, max_nsh = 1;
+    for (int i = 0; i < hi_; ++i)
+        if (slot_size_[i]) {
+            max_nao = std::max(max_nao, slot_nao_[i]);
+            max_nsh = std::max(max_nsh, slot_nsh_[i]);
+        }
+    launch_step(d_slots_, hi_, max_nao, max_nsh, set, max_iter, st);
+}
+
+void SlotPool::finished(std::vector<int>& slots, std::vector<BatchMol>& states, cudaStream_t st) {
+    slots.clear();
+    states.clear();
+    if (resident_ == 0) return;
+    std::vector<BatchMol> all(hi_);
+    XG_CUDA(cudaMemcpyAsync(all.data(), d_slots_, sizeof(BatchMol) * hi_, cudaMemcpyDeviceToHost, st));
+    XG_CUDA(cudaStreamSynchronize(st));
+    for (int i = 0; i < hi_; ++i)
+        if (slot_size_[i] && all[i].stage == BS_DONE) {
+            slots.push_back(i);
+            states.push_back(all[i]);
+        }
+}
+
+void SlotPool::copy_results(const BatchMol& state, double* grad, double* q, cudaStream_t st) const {
+    const int nat = state.m.nat;
+    XG_CUDA(cudaMemcpyAsync(grad, state.grad, 3 * sizeof(double) * nat, cudaMemcpyDeviceToHost, st));
+    XG_CUDA(cudaMemcpyAsync(q, state.q, sizeof(double) * nat, cudaMemcpyDeviceToHost, st));
+}
+
+void SlotPool::release(int slot) {
+    if (slot < 0 || slot >= max_slots_ || slot_size_[slot] == 0) return;
+    // the descriptor on the device keeps stage BS_DONE, so later steps skip the slot
+    std::pair<size_t, size_t> r{slot_off_[slot], slot_size_[slot]};
+    auto it = std::lower_bound(free_.begin(), free_.end(), r);
+    it = free_.insert(it, r);
+    if (it + 1 != free_.end() && it->first + it->second == (it + 1)->first) {
+        it->second += (it + 1)->second;
+        free_.erase(it + 1);
+    }
+    if (it != free_.begin() && (it - 1)->first + (it - 1)->second == it->first) {
+        (it - 1)->second += it->second;
+        free_.erase(it);
+    }
+    slot_size_[slot] = 0;
+    --resident_;
+    while (hi_ > 0 && slot_size_[hi_ - 1] == 0) --hi_;
 }
 
 }  // namespace xg

@@ -98,6 +98,45 @@ private:
     long long h2d_ = 0;
 };
 
+// Resident molecule pool for continuous batching.  One device allocation of a fixed
+// budget holds a descriptor table of `max_slots` molecules followed by the molecules'
+// regions (parameters + work arrays), handed out first-fit as molecules are admitted and
+// returned when they finish.  Every step advances all resident molecules at once; a
+// molecule's state stays on the device from admission to completion.
+class SlotPool {
+public:
+    SlotPool(size_t budget_bytes, int max_slots);
+    SlotPool(const SlotPool&) = delete;
+    SlotPool& operator=(const SlotPool&) = delete;
+    ~SlotPool();
+    // Admit a molecule (nao <= BATCH_MAX_NAO): returns its slot, or -1 when no slot or no
+    // region of the needed size is free.  Uploads on `st` (the caller keeps hm alive until
+    // the next synchronisation of `st`).
+    int admit(const HostMol& hm, int want_grad, cudaStream_t st);
+    // Advance every resident molecule by at most max_iter SCC iterations.
+    void step(const BatchSettings& set, int max_iter, cudaStream_t st);
+    // Synchronise `st` and list the resident slots whose molecule is done, with their state.
+    void finished(std::vector<int>& slots, std::vector<BatchMol>& states, cudaStream_t st);
+    // Copy gradient [nat][3] and charges [nat] of a finished slot (asynchronous on `st`).
+    void copy_results(const BatchMol& state, double* grad, double* q, cudaStream_t st) const;
+    // Return the slot and its region to the pool.
+    void release(int slot);
+    int resident() const { return resident_; }
+    size_t free_bytes() const;
+    size_t capacity() const { return cap_; }
+    long long h2d_bytes() const { return h2d_; }
+
+private:
+    char* base_ = nullptr;
+    size_t cap_ = 0, desc_ = 0;
+    int max_slots_ = 0, resident_ = 0, hi_ = 0;
+    BatchMol* d_slots_ = nullptr;
+    std::vector<size_t> slot_off_, slot_size_;
+    std::vector<int> slot_nao_, slot_nsh_;
+    std::vector<std::pair<size_t, size_t>> free_;   // (offset, size), sorted by offset
+    long long h2d_ = 0;
+};
+
 // Results of run_batch, in input order.
 struct BatchResults {
     std::vector<double> energy;      // [nmol] Hartree

@@ -87,6 +87,11 @@ def load_library(path=LIBPATH):
         "xtbgb_batchGetStatus": (None, [vp, vp, ip, ip, ip, ip]),
         "xtbgb_batchGetStats": (None, [vp, vp, dp, C.POINTER(C.c_longlong)]),
         "xtbgb_batchNao": (None, [vp, vp, ip]),
+        "xtbgb_newServer": (vp, [vp, C.c_double, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int]),
+        "xtbgb_delServer": (None, [C.POINTER(vp)]),
+        "xtbgb_serverSubmit": (C.c_longlong, [vp, vp, C.c_int, ip, dp, C.c_double, C.c_int, C.c_int]),
+        "xtbgb_serverWait": (C.c_int, [vp, vp, C.c_longlong, C.c_double, dp, dp, dp, dp]),
+        "xtbgb_serverStats": (None, [vp, vp, dp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -292,3 +297,86 @@ class BatchResults:
         self.device_ms, self.wall_ms = float(t[0]), float(t[1])
         self.h2d_bytes, self.d2h_bytes, self.launches, self.plain_count = (int(c[0]), int(c[1]), int(c[2]),
                                                                           int(c[3]))
+
+
+class Server:
+    """Request loop with continuous batching (xtbgb_newServer ...).
+
+    ``submit`` returns a request id; ``wait`` returns a ServedResult.  Calls from several
+    Python threads are safe: every call uses an environment of its own thread.
+    """
+
+    def __init__(self, pool_gib=16.0, max_slots=1024, plain_workers=4, iters_per_step=4, accuracy=1.0,
+                 etemp=300.0, maxiter=250):
+        import threading
+        self.lib = load_library()
+        self._tls = threading.local()
+        env = self._env()
+        self.h = C.c_void_p(self.lib.xtbgb_newServer(env.h, pool_gib, max_slots, plain_workers, iters_per_step,
+                                                     accuracy, etemp, maxiter))
+        env.check()
+        self._natoms = {}
+
+    def _env(self):
+        e = getattr(self._tls, "env", None)
+        if e is None:
+            e = self._tls.env = Environment(0)
+        return e
+
+    def submit(self, numbers, positions, charge=0.0, uhf=0, gradient=True):
+        env = self._env()
+        z = np.ascontiguousarray(numbers, dtype=np.int32)
+        x = np.ascontiguousarray(positions, dtype=np.float64).reshape(-1, 3)
+        rid = self.lib.xtbgb_serverSubmit(env.h, self.h, len(z), z.ctypes.data_as(C.POINTER(C.c_int)), _dptr(x),
+                                          charge, uhf, int(bool(gradient)))
+        env.check()
+        self._natoms[rid] = len(z)
+        return rid
+
+    def wait(self, rid, timeout=-1.0, check=True):
+        env = self._env()
+        n = self._natoms[rid]
+        e = C.c_double()
+        g = np.zeros((n, 3))
+        q = np.zeros(n)
+        info = np.zeros(10)
+        ok = self.lib.xtbgb_serverWait(env.h, self.h, rid, timeout, C.byref(e), _dptr(g), _dptr(q), _dptr(info))
+        if not ok:
+            return None
+        err = None
+        if self.lib.xtb_checkEnvironment(env.h):
+            buf = C.create_string_buffer(4096)
+            nb = C.c_int(4096)
+            self.lib.xtb_getError(env.h, buf, C.byref(nb))
+            err = buf.value.decode()
+            if check:
+                raise XTBException(err)
+        del self._natoms[rid]
+        return ServedResult(rid, e.value, g, q, info, err)
+
+    def stats(self):
+        s = np.zeros(6)
+        self.lib.xtbgb_serverStats(self._env().h, self.h, _dptr(s))
+        keys = ("completed", "plain", "steps", "busy_s", "peak_resident", "reruns")
+        return dict(zip(keys, s.tolist()))
+
+    def close(self):
+        if getattr(self, "h", None) is not None and self.h.value is not None:
+            self.lib.xtbgb_delServer(C.byref(self.h))
+
+    def __del__(self):
+        if getattr(self, "lib", None) is not None:
+            self.close()
+
+
+class ServedResult:
+    def __init__(self, rid, energy, gradient, charges, info, error):
+        self.id = rid
+        self.energy = energy
+        self.gradient = gradient
+        self.charges = charges
+        self.iterations, self.converged, self.status, self.engine = (int(v) for v in info[:4])
+        self.t_submit, self.t_start, self.t_done = (float(v) for v in info[4:7])
+        self.dipole = np.array(info[7:10])
+        self.latency = self.t_done - self.t_submit
+        self.error = error

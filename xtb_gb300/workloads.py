@@ -104,3 +104,33 @@ def mixed_batch(count=4096, seed=0):
             m = int(rng.integers(2, 31))
             mols.append(water_cluster(m, seed=int(rng.integers(1 << 31))))
     return mols
+
+
+def served_stream(count=128, seed=0, rate=None, nmin=3, nmax=1500):
+    """Seeded request stream of the served benchmark.
+
+    Atom counts log-uniform in [nmin, nmax], rounded to the nearest size the generators
+    make (alkane C_nH_{2n+2}: 3n + 2 atoms; water cluster (H2O)_m: 3m atoms); alkane or
+    water with probability 1/2, gradient requested with probability 1/2.  ``rate`` (requests/s)
+    gives Poisson arrival times; None makes every request arrive at t = 0.
+    Returns a list of dicts: numbers, positions (Bohr), gradient, arrival, kind, size.
+    """
+    rng = np.random.default_rng(seed)
+    out = []
+    t = 0.0
+    for _ in range(count):
+        natoms = math.exp(rng.uniform(math.log(nmin), math.log(nmax)))
+        alk = rng.random() < 0.5
+        grad = bool(rng.random() < 0.5)
+        sub = int(rng.integers(1 << 31))
+        if alk:
+            n = max(1, int(round((natoms - 2) / 3.0)))
+            Z, xyz = alkane(n, 0.02, seed=sub)
+        else:
+            m = max(1, int(round(natoms / 3.0)))
+            Z, xyz = water_cluster(m, seed=sub)
+        if rate:
+            t += rng.exponential(1.0 / rate)
+        out.append({"numbers": Z, "positions": xyz, "gradient": grad, "arrival": t,
+                    "kind": "alkane" if alk else "water", "size": len(Z)})
+    return out
