@@ -100,13 +100,16 @@ extern long long xtbgb_serverSubmit(xtb_TEnvironment env, xtbgb_TServer server, 
                                     const double* positions, double charge, int uhf, int gradient);
 /* Wait for request `id` (timeout in seconds, < 0 waits forever).  Returns 1 and fills the
  * outputs when the request is done, 0 on timeout.  energy[1]; gradient[natoms][3] and
- * charges[natoms] may be NULL; info[10]: SCC iterations, converged, status, engine
- * (0 pool, 1 plain), submit / start / done times (s since the server started), dipole[3].
+ * charges[natoms] may be NULL; info[12]: SCC iterations, converged, status, engine
+ * (0 pool, 1 plain), submit / start / done times (s since the server started), dipole[3],
+ * number of AOs, device ms of the tridiagonalisations (plain engine only).
  * A failed or unconverged request also raises an error on the environment. */
 extern int xtbgb_serverWait(xtb_TEnvironment env, xtbgb_TServer server, long long id, double timeout,
                             double* energy, double* gradient, double* charges, double* info);
-/* stats[6]: completed, run on the plain engine, pool steps, pool busy seconds, peak resident
- * molecules, requests re-run on the plain engine. */
+/* stats[11]: completed, run on the plain engine, pool steps, pool busy seconds, peak resident
+ * molecules, requests re-run on the plain engine, host->device bytes, device->host bytes,
+ * kernel launches, device ms of the pool's SCC kernel, algorithmic FP64 flops of the pool's
+ * SCC iterations (n^3 + 4/3 n^3 + 2 n^3 + n^3 + 2 n^2 k per molecule and iteration). */
 extern void xtbgb_serverStats(xtb_TEnvironment env, xtbgb_TServer server, double* stats);
 
 /* Repulsion energy and gradient of one molecule, computed from and into DEVICE memory

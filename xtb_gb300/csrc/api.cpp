@@ -741,6 +741,8 @@ int xtbgb_serverWait(xtb_TEnvironment env, xtbgb_TServer srv, long long id, doub
         info[7] = c.dipole[0];
         info[8] = c.dipole[1];
         info[9] = c.dipole[2];
+        info[10] = c.nao;
+        info[11] = c.sytrd_ms;
     }
     if (!c.error.empty()) env->error(c.error, src);
     else if (c.status != xg::BST_OK) env->error("Self consistent charge iterator did not converge", src);

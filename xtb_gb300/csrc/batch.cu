@@ -278,14 +278,18 @@ __device__ void scc_iteration(BatchMol* b, const DevThresh& th, double etemp, in
     __syncthreads();
     d_tri_prep(nao, b->tri_d, b->tri_e, b->tri_e2, b->bounds);
     __syncthreads();
-    double* sd = sm;
-    double* se2 = sm + nao;
-    CTA_FOR(i, nao) {
-        sd[i] = b->tri_d[i];
-        se2[i] = (i < nao - 1) ? b->tri_e2[i] : 0.0;
-    }
+    stage_tridiag(nao, b->tri_d, b->tri_e2, sm);
     __syncthreads();
-    CTA_FOR(j, nao) b->emo[j] = d_bisect(nao, sd, se2, b->bounds, j);
+    {
+        const float* fsm = reinterpret_cast<const float*>(sm + 2 * nao);
+        const int per_pass = (int)(blockDim.x / BIS_G);
+        for (int j0 = 0; j0 < nao; j0 += per_pass) {   // uniform trip count: whole warps stay together
+            const int j = j0 + (int)(threadIdx.x / BIS_G);
+            const bool valid = j < nao;
+            const double v = d_bisect_group(nao, sm, sm + nao, fsm, fsm + nao, b->bounds, valid ? j : 0, valid);
+            if (valid && threadIdx.x % BIS_G == 0) b->emo[j] = v;
+        }
+    }
     __syncthreads();
     d_fermi(nao, b->emo, b->nel_a, b->nel_b, etemp, b->focc, b->focca, b->foccb, b->fscal, b->kocc);
     __syncthreads();
@@ -585,7 +589,7 @@ void DeviceBatch::load(const std::vector<const HostMol*>& mols, const std::vecto
 
 // The seven launches of one step over `nmol` slots.
 void launch_step(BatchMol* d_mols, int nmol, int max_nao, int max_nsh, const BatchSettings& set, int max_iter,
-                 cudaStream_t st) {
+                 cudaStream_t st, cudaEvent_t ev0 = nullptr, cudaEvent_t ev1 = nullptr) {
     const size_t smem = (size_t)std::max(12 * max_nao + 32, GEMM_SMEM) * sizeof(double);
     static size_t smem_set = 0;
     if (smem > 48 * 1024 && smem > smem_set) {
@@ -598,8 +602,10 @@ void launch_step(BatchMol* d_mols, int nmol, int max_nao, int max_nsh, const Bat
     batch_integrals(st, d_mols, nmol, max_nsh, th.intcut);
     k_batch_setup_b<<<nmol, BT, 0, st>>>(d_mols, nmol);
     XG_LAUNCH_CHECK();
+    if (ev0) XG_CUDA(cudaEventRecord(ev0, st));
     k_batch_scc<<<nmol, BT, smem, st>>>(d_mols, nmol, th, set.etemp, std::max(1, set.maxiter), max_iter);
     XG_LAUNCH_CHECK();
+    if (ev1) XG_CUDA(cudaEventRecord(ev1, st));
     k_batch_grad_a<<<nmol, BT, 0, st>>>(d_mols, nmol);
     XG_LAUNCH_CHECK();
     batch_integral_gradient(st, d_mols, nmol, max_nsh, th.intcut);
@@ -642,10 +648,16 @@ SlotPool::SlotPool(size_t budget_bytes, int max_slots) : max_slots_(std::max(1, 
     slot_size_.assign(max_slots_, 0);
     slot_nao_.assign(max_slots_, 0);
     slot_nsh_.assign(max_slots_, 0);
+    slot_iter_.assign(max_slots_, 0);
+    slot_nocc_.assign(max_slots_, 0);
+    XG_CUDA(cudaEventCreate(&ev0_));
+    XG_CUDA(cudaEventCreate(&ev1_));
     free_.push_back({desc_, cap_ - desc_});
 }
 
 SlotPool::~SlotPool() {
+    if (ev0_) cudaEventDestroy(ev0_);
+    if (ev1_) cudaEventDestroy(ev1_);
     if (base_) cudaFree(base_);
 }
 
@@ -687,6 +699,8 @@ int SlotPool::admit(const HostMol& hm, int want_grad, cudaStream_t st) {
     slot_size_[slot] = need;
     slot_nao_[slot] = hm.nao;
     slot_nsh_[slot] = hm.nsh;
+    slot_iter_[slot] = 0;
+    slot_nocc_[slot] = (hm.nel_a + hm.nel_b + 1) / 2;
     ++resident_;
     hi_ = std::max(hi_, slot + 1);
     return slot;
@@ -700,7 +714,7 @@ void SlotPool::step(const BatchSettings& set, int max_iter, cudaStream_t st) {
             max_nao = std::max(max_nao, slot_nao_[i]);
             max_nsh = std::max(max_nsh, slot_nsh_[i]);
         }
-    launch_step(d_slots_, hi_, max_nao, max_nsh, set, max_iter, st);
+    launch_step(d_slots_, hi_, max_nao, max_nsh, set, max_iter, st, ev0_, ev1_);
 }
 
 void SlotPool::finished(std::vector<int>& slots, std::vector<BatchMol>& states, cudaStream_t st) {
@@ -710,11 +724,21 @@ void SlotPool::finished(std::vector<int>& slots, std::vector<BatchMol>& states, 
     std::vector<BatchMol> all(hi_);
     XG_CUDA(cudaMemcpyAsync(all.data(), d_slots_, sizeof(BatchMol) * hi_, cudaMemcpyDeviceToHost, st));
     XG_CUDA(cudaStreamSynchronize(st));
-    for (int i = 0; i < hi_; ++i)
-        if (slot_size_[i] && all[i].stage == BS_DONE) {
+    last_state_bytes_ = sizeof(BatchMol) * hi_;
+    float ms = 0.0f;
+    if (cudaEventElapsedTime(&ms, ev0_, ev1_) == cudaSuccess) last_ms_ = ms;
+    else cudaGetLastError();
+    last_flops_ = 0.0;
+    for (int i = 0; i < hi_; ++i) {
+        if (!slot_size_[i]) continue;
+        const double n = slot_nao_[i], k = slot_nocc_[i];
+        last_flops_ += (double)(all[i].iter - slot_iter_[i]) * ((16.0 / 3.0) * n * n * n + 2.0 * n * n * k);
+        slot_iter_[i] = all[i].iter;
+        if (all[i].stage == BS_DONE) {
             slots.push_back(i);
             states.push_back(all[i]);
         }
+    }
 }
 
 void SlotPool::copy_results(const BatchMol& state, double* grad, double* q, cudaStream_t st) const {

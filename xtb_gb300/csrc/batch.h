@@ -122,6 +122,13 @@ public:
     // Return the slot and its region to the pool.
     void release(int slot);
     int resident() const { return resident_; }
+    // figures of the last step (valid after finished()): device ms of the SCC kernel (CUDA
+    // events on the pool's stream), algorithmic FP64 flops of the SCC iterations it ran
+    // (per molecule and iteration n^3 + 4/3 n^3 + 2 n^3 + n^3 + 2 n^2 k, the reference's
+    // LAPACK sequence), and the state bytes copied back
+    double last_scc_ms() const { return last_ms_; }
+    double last_scc_flops() const { return last_flops_; }
+    size_t last_state_bytes() const { return last_state_bytes_; }
     size_t free_bytes() const;
     size_t capacity() const { return cap_; }
     long long h2d_bytes() const { return h2d_; }
@@ -132,7 +139,10 @@ private:
     int max_slots_ = 0, resident_ = 0, hi_ = 0;
     BatchMol* d_slots_ = nullptr;
     std::vector<size_t> slot_off_, slot_size_;
-    std::vector<int> slot_nao_, slot_nsh_;
+    std::vector<int> slot_nao_, slot_nsh_, slot_iter_, slot_nocc_;
+    cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
+    double last_ms_ = 0.0, last_flops_ = 0.0;
+    size_t last_state_bytes_ = 0;
     std::vector<std::pair<size_t, size_t>> free_;   // (offset, size), sorted by offset
     long long h2d_ = 0;
 };

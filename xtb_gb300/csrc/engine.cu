@@ -132,14 +132,16 @@ struct Arena {
     char* base = nullptr;
     size_t cap = 0, used = 0;
     bool counting = false;
-    void reset(size_t need) {
+    // Stream-ordered (re)allocation on the engine stream: no device-wide synchronisation, so
+    // single points on other threads' streams keep running while this one grows its workspace.
+    void reset(size_t need, cudaStream_t st) {
         counting = false;
         need += 4096;
         if (need > cap) {
-            if (base) cudaFree(base);
+            if (base) XG_CUDA(cudaFreeAsync(base, st));
             base = nullptr;
             cap = 0;
-            XG_CUDA(cudaMalloc(&base, need));
+            XG_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&base), need, st));
             cap = need;
         }
         used = 0;
@@ -406,7 +408,7 @@ void run_singlepoint(const HostMol& hm, const SPSettings& set, Wavefunction& wfn
     ar.used = 0;
     layout();
     const size_t need = ar.used;
-    ar.reset(need);
+    ar.reset(need, st);
     layout();
 
     XG_CUDA(cudaMemsetAsync(grad, 0, 3 * (size_t)nat * sizeof(double), st));

@@ -193,22 +193,19 @@ __global__ void k_tri_prep(int n, const double* __restrict__ d, const double* __
     d_tri_prep(n, d, e, e2, bounds);
 }
 
-// One thread per eigenvalue and one warp per block, so the eigenvalues spread over as many
-// SMs as possible (the FP64 pipe of an SM is the limit); d and e^2 are staged in shared
-// memory (dynamic, 2n doubles).
+// One warp per block handles 32 / BIS_G eigenvalues, so the eigenvalues spread over as many
+// SMs as possible (FP64 latency, not throughput, is the limit); d, e^2 and their FP32 copies
+// are staged in shared memory (dynamic, 2n doubles + 2n floats).
 __global__ void __launch_bounds__(32) k_bisect(int n, const double* __restrict__ d, const double* __restrict__ e2,
                                                const double* __restrict__ bounds, double* __restrict__ w) {
     extern __shared__ double sde[];
-    double* sd = sde;
-    double* se = sde + n;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        sd[i] = d[i];
-        se[i] = (i < n - 1) ? e2[i] : 0.0;
-    }
+    stage_tridiag(n, d, e2, sde);
     __syncthreads();
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= n) return;
-    w[j] = d_bisect(n, sd, se, bounds, j);
+    const float* fsm = reinterpret_cast<const float*>(sde + 2 * n);
+    const int j = blockIdx.x * (32 / BIS_G) + (int)(threadIdx.x / BIS_G);
+    const bool valid = j < n;
+    const double v = d_bisect_group(n, sde, sde + n, fsm, fsm + n, bounds, valid ? j : 0, valid);
+    if (valid && threadIdx.x % BIS_G == 0) w[j] = v;
 }
 
 // ------------------------------------------------------------------ inverse iteration
@@ -235,10 +232,11 @@ void tridiag_eigvals(cudaStream_t st, int n, const double* d, const double* e, d
                      double* w) {
     k_tri_prep<<<1, 256, 0, st>>>(n, d, e, e2, bounds);
     XG_LAUNCH_CHECK();
-    const size_t smem = 2 * (size_t)n * sizeof(double);
+    const size_t smem = 2 * (size_t)n * (sizeof(double) + sizeof(float));
+    if (smem > 200 * 1024) throw CudaError("tridiag_eigvals: matrix too large for the shared-memory bisection");
     if (smem > 48 * 1024)
         XG_CUDA(cudaFuncSetAttribute(k_bisect, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_bisect<<<ceil_div(n, 32), 32, smem, st>>>(n, d, e2, bounds, w);
+    k_bisect<<<ceil_div(n, 32 / BIS_G), 32, smem, st>>>(n, d, e2, bounds, w);
     XG_LAUNCH_CHECK();
 }
 

@@ -266,28 +266,63 @@ __device__ inline void d_sytrd(int n, double* __restrict__ A, int lda, double* _
 
 // Number of eigenvalues of T below x, from the sign changes of the leading principal minors
 // p_i = (d_i - x) p_{i-1} - e_{i-1}^2 p_{i-2}, p_{-1} = 1 (Sturm sequence, three-term form).
-// Only one FMA per row sits on the dependent chain and no division is needed, which matters on
-// a part whose FP64 divide is a long multi-instruction sequence.  A minor that comes out exactly
-// zero is replaced by a tiny value of the sign opposite to its predecessor (the ratio p_i/p_{i-1}
-// becomes a tiny negative number, as the pivmin rule of the ratio form makes it); the pair
-// (p_i, p_{i-1}) is rescaled by an exact power of two whenever its larger exponent leaves
-// [2^-400, 2^400], so neither overflows nor underflows.  Sign and exponent tests use integer
-// operations on the bit pattern.  d and e2 are read from shared memory.
+// Only one FMA per row sits on the dependent chain: d_i - x and e_{i-1}^2 p_{i-2} are formed
+// off the chain, four rows at a time, and no division is needed (an FP64 divide costs about
+// nine dependent FP64 operations on this part).  The pair (p_{i-1}, p_i) is rescaled by an
+// exact power of two every four rows when its larger exponent leaves [2^-300, 2^300]; with
+// e^2 floored at 2^-100 (d_tri_prep) four rows cannot move it out of the normal range, and
+// no two consecutive minors can vanish, so a single zero minor gives exactly one sign change
+// whichever sign it carries.  Sign and exponent tests use integer operations on the bits.
 __device__ __forceinline__ int dexp_bits(double v) { return (__double2hiint(v) >> 20) & 0x7ff; }
+__device__ __forceinline__ int sgn_change(double a, double b) { return (__double2hiint(a) ^ __double2hiint(b)) < 0; }
+
+__device__ __forceinline__ void pair_rescale(double& pm, double& p) {
+    const int ex = max(dexp_bits(p), dexp_bits(pm));
+    if (ex > 1023 + 300) {
+        p *= 0x1p-300;
+        pm *= 0x1p-300;
+    } else if (ex < 1023 - 300) {
+        p *= 0x1p+300;
+        pm *= 0x1p+300;
+    }
+}
 
 __device__ inline int sturm_count(int n, const double* d, const double* e2, double x) {
     double pm = 1.0, p = d[0] - x;
-    if (p == 0.0) p = -0x1p-600;
     int cnt = __double2hiint(p) < 0;
-    for (int i = 1; i < n; ++i) {
-        double pn = fma(d[i] - x, p, -e2[i - 1] * pm);
-        if ((__double_as_longlong(pn) << 1) == 0) pn = -0x1p-600 * p;
-        cnt += (__double2hiint(pn) ^ __double2hiint(p)) < 0;
-        const int ex = max(dexp_bits(pn), dexp_bits(p));
-        if (ex > 1023 + 400) { pn *= 0x1p-400; p *= 0x1p-400; }
-        else if (ex < 1023 - 400) { pn *= 0x1p+400; p *= 0x1p+400; }
+    int i = 1;
+    for (; i + 3 < n; i += 4) {
+        const double t0 = d[i] - x, t1 = d[i + 1] - x, t2 = d[i + 2] - x, t3 = d[i + 3] - x;
+        const double f0 = e2[i - 1], f1 = e2[i], f2 = e2[i + 1], f3 = e2[i + 2];
+        const double p0 = fma(t0, p, -f0 * pm);
+        const double p1 = fma(t1, p0, -f1 * p);
+        const double p2 = fma(t2, p1, -f2 * p0);
+        const double p3 = fma(t3, p2, -f3 * p1);
+        cnt += sgn_change(p, p0) + sgn_change(p0, p1) + sgn_change(p1, p2) + sgn_change(p2, p3);
+        pm = p2;
+        p = p3;
+        pair_rescale(pm, p);
+    }
+    for (; i < n; ++i) {
+        const double pn = fma(d[i] - x, p, -e2[i - 1] * pm);
+        cnt += sgn_change(p, pn);
         pm = p;
         p = pn;
+        pair_rescale(pm, p);
+    }
+    return cnt;
+}
+
+// The same count in FP32 with the ratio form q_i = (d_i - x) - e_{i-1}^2 / q_{i-1} and the
+// pivmin guard; used only to narrow brackets that FP64 counts then verify.
+__device__ inline int sturm_count32(int n, const float* d, const float* e2, float x, float pivmin) {
+    float q = d[0] - x;
+    if (fabsf(q) < pivmin) q = -pivmin;
+    int cnt = q < 0.0f;
+    for (int i = 1; i < n; ++i) {
+        q = (d[i] - x) - __fdividef(e2[i - 1], q);
+        if (fabsf(q) < pivmin) q = -pivmin;
+        cnt += q < 0.0f;
     }
     return cnt;
 }
@@ -303,7 +338,7 @@ __device__ inline void d_tri_prep(int n, const double* __restrict__ d, const dou
         hi = fmax(hi, d[i] + el + er);
         tn = fmax(tn, fabs(d[i]) + el + er);
         if (i < n - 1) {
-            e2[i] = e[i] * e[i];
+            e2[i] = fmax(e[i] * e[i], 0x1p-100);   // floor: see sturm_count
             emax = fmax(emax, e[i] * e[i]);
         }
     }
@@ -332,17 +367,89 @@ __device__ inline void d_tri_prep(int n, const double* __restrict__ d, const dou
     }
 }
 
-// Eigenvalue j of T by bisection on Sturm counts (d, e2 already staged, e.g. in shared
-// memory), to an absolute accuracy of 2 eps ||T|| (the accuracy inverse iteration needs).
-__device__ inline double d_bisect(int n, const double* sd, const double* se, const double* __restrict__ bounds, int j) {
-    double lo = bounds[0], hi = bounds[1];
-    const double atol = 2.0 * 2.220446049250313e-16 * fmax(bounds[3], 1e-300);
-    for (int it = 0; it < 80; ++it) {
-        const double mid = 0.5 * (lo + hi);
-        if (hi - lo <= atol || mid <= lo || mid >= hi) break;
-        if (sturm_count(n, sd, se, mid) > j) hi = mid; else lo = mid;
+// Eigenvalue j of T to an absolute accuracy of 2 eps ||T|| (the accuracy inverse iteration
+// needs) by multisection: the BIS_G lanes of a group evaluate Sturm counts at BIS_G interior
+// points of the bracket, which shrinks (BIS_G + 1)-fold per round.  The bracket is first
+// narrowed with FP32 counts to about 1e-6 ||T||, widened by a margin far above the FP32
+// backward error, and verified with two FP64 counts (falling back to the Gershgorin bracket
+// if the check fails); FP64 rounds then finish it.  Must be called by all 32 lanes of a warp
+// (lanes of inactive groups pass valid = false); d, e2 (FP64) and fd, fe2 (FP32 copies) are
+// staged in shared memory.  Returns the eigenvalue in every lane of the group.
+constexpr int BIS_G = 4;
+
+__device__ inline double d_bisect_group(int n, const double* sd, const double* se2, const float* fd, const float* fe2,
+                                        const double* __restrict__ bounds, int j, bool valid) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31, gl = lane % BIS_G, gbase = lane - gl;
+    const unsigned gmask = ((1u << BIS_G) - 1u) << gbase;
+    const double glo = bounds[0], ghi = bounds[1];
+    const double tn = fmax(bounds[3], 1e-300);
+    const double atol = 2.0 * 2.220446049250313e-16 * tn;
+    // FP32 rounds
+    const float ftol = (float)(1.0e-6 * tn);
+    const float pivf = 1.0e-30f;
+    float flo = (float)glo, fhi = (float)ghi;
+    bool fact = valid;
+    for (int r = 0; r < 48; ++r) {
+        fact = fact && (fhi - flo > ftol);
+        if (!__any_sync(FULL, fact)) break;
+        const float h = (fhi - flo) / (float)(BIS_G + 1);
+        const float x = flo + h * (float)(gl + 1);
+        const int c = fact ? sturm_count32(n, fd, fe2, x, pivf) : 0;
+        const unsigned bits = (__ballot_sync(FULL, fact && c > j) & gmask) >> gbase;
+        if (fact) {
+            const int k = bits ? __ffs(bits) - 1 : BIS_G;
+            const float nlo = (k == 0) ? flo : flo + h * (float)k;
+            const float nhi = (k == BIS_G) ? fhi : flo + h * (float)(k + 1);
+            if (nlo == flo && nhi == fhi) fact = false;
+            flo = nlo;
+            fhi = nhi;
+        }
+    }
+    // widen, verify with FP64 counts
+    const double mar = 64.0 * 1.1920929e-7 * tn;
+    double lo = fmax(glo, (double)flo - mar), hi = fmin(ghi, (double)fhi + mar);
+    {
+        const double xv = (gl == 0) ? lo : hi;
+        const int c = (valid && gl < 2) ? sturm_count(n, sd, se2, xv) : 0;
+        const unsigned okb = __ballot_sync(FULL, valid && ((gl == 0 && c <= j) || (gl == 1 && c > j)));
+        const unsigned need = (3u << gbase);
+        if (valid && (okb & need) != need) {
+            lo = glo;
+            hi = ghi;
+        }
+    }
+    // FP64 rounds
+    bool act = valid;
+    for (int r = 0; r < 80; ++r) {
+        act = act && (hi - lo > atol);
+        if (!__any_sync(FULL, act)) break;
+        const double h = (hi - lo) / (double)(BIS_G + 1);
+        const double x = lo + h * (double)(gl + 1);
+        const int c = act ? sturm_count(n, sd, se2, x) : 0;
+        const unsigned bits = (__ballot_sync(FULL, act && c > j) & gmask) >> gbase;
+        if (act) {
+            const int k = bits ? __ffs(bits) - 1 : BIS_G;
+            const double nlo = (k == 0) ? lo : lo + h * (double)k;
+            const double nhi = (k == BIS_G) ? hi : lo + h * (double)(k + 1);
+            if (nlo == lo && nhi == hi) act = false;
+            lo = nlo;
+            hi = nhi;
+        }
     }
     return 0.5 * (lo + hi);
+}
+
+// Stage d, e^2 and their FP32 copies (2n doubles followed by 2n floats) in shared memory.
+__device__ inline void stage_tridiag(int n, const double* __restrict__ d, const double* __restrict__ e2, double* sm) {
+    float* fsm = reinterpret_cast<float*>(sm + 2 * n);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const double di = d[i], ei = (i < n - 1) ? e2[i] : 0.0;
+        sm[i] = di;
+        sm[n + i] = ei;
+        fsm[i] = (float)di;
+        fsm[n + i] = (float)ei;
+    }
 }
 
 // Eigenvector j of T for eigenvalue w[j]; output Y[i*n + j].  Scratch arrays are

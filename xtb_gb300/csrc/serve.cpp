@@ -69,7 +69,7 @@ bool Server::wait(long long id, Completed& out, double timeout) {
 
 std::vector<double> Server::stats() const {
     std::lock_guard<std::mutex> lk(mu_);
-    return {n_done_, n_plain_, n_steps_, busy_, peak_, n_rerun_};
+    return {n_done_, n_plain_, n_steps_, busy_, peak_, n_rerun_, h2d_, d2h_, launches_, scc_ms_, scc_flops_};
 }
 
 void Server::complete(Completed&& c) {
@@ -162,14 +162,21 @@ void Server::pool_body() {
             for (auto& r : to_plain) large_q_.push_back(std::move(r));
             cv_work_.notify_all();
         }
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            h2d_ += (double)(pool.h2d_bytes() - pool_h2d_seen_);
+            pool_h2d_seen_ = pool.h2d_bytes();
+        }
         if (pool.resident() == 0) continue;
         {
             std::lock_guard<std::mutex> lk(mu_);
             peak_ = std::max(peak_, (double)pool.resident());
         }
         const double t1 = now();
+        const long long l0 = launch_counter();
         pool.step(cfg_.set, std::max(1, cfg_.iters_per_step), st);
         pool.finished(slots, states, st);
+        double step_d2h = (double)pool.last_state_bytes();
         std::vector<Completed> out;
         std::vector<int> rel;
         for (size_t k = 0; k < slots.size(); ++k) {
@@ -199,8 +206,10 @@ void Server::pool_body() {
             c.t_start = req->t_start;
             c.gradient.assign(3 * (size_t)b.m.nat, 0.0);
             c.charges.assign(b.m.nat, 0.0);
+            c.nao = b.m.nao;
             out.push_back(std::move(c));
             pool.copy_results(b, out.back().gradient.data(), out.back().charges.data(), st);
+            step_d2h += 4.0 * sizeof(double) * b.m.nat;
         }
         XG_CUDA(cudaStreamSynchronize(st));
         for (int slot : rel) pool.release(slot);
@@ -208,6 +217,10 @@ void Server::pool_body() {
             std::lock_guard<std::mutex> lk(mu_);
             n_steps_ += 1;
             busy_ += now() - t1;
+            launches_ += (double)(launch_counter() - l0);
+            d2h_ += step_d2h;
+            scc_ms_ += pool.last_scc_ms();
+            scc_flops_ += pool.last_scc_flops();
         }
         for (auto& c : out) complete(std::move(c));
     }
@@ -239,6 +252,14 @@ void Server::plain_loop() {
             SPResult res;
             bool failed = false;
             run_singlepoint(r->hm, ps, wfn, res, false, failed);
+            {
+                std::lock_guard<std::mutex> lk(mu_);
+                h2d_ += (double)res.h2d_bytes;
+                d2h_ += (double)res.d2h_bytes;
+                launches_ += (double)res.launches;
+            }
+            c.nao = r->hm.nao;
+            c.sytrd_ms = res.phase_ms[PH_SYTRD];
             c.energy = res.energy;
             const double parts[8] = {res.e_elec, res.e_rep, res.e_es, res.e_aes, res.e_axc, res.e_disp, res.e_atm,
                                      res.hl_gap};

@@ -38,6 +38,8 @@ struct Completed {
     std::vector<double> gradient, charges;
     int iterations = 0, converged = 0, status = 0, engine = 0;   // engine: 0 pool, 1 plain
     double t_submit = 0.0, t_start = 0.0, t_done = 0.0;           // seconds since server start
+    int nao = 0;
+    double sytrd_ms = 0.0;   // plain engine: device time of the tridiagonalisations
     std::string error;
 };
 
@@ -52,7 +54,9 @@ public:
     bool wait(long long id, Completed& out, double timeout);
     double now() const;
     // [0] completed, [1] on the plain engine, [2] pool steps, [3] pool busy seconds,
-    // [4] peak resident molecules, [5] requests re-run on the plain engine
+    // [4] peak resident molecules, [5] requests re-run on the plain engine, [6] host->device
+    // bytes, [7] device->host bytes, [8] kernel launches, [9] pool SCC-kernel device ms,
+    // [10] FP64 flops of the pool's SCC iterations (algorithmic count)
     std::vector<double> stats() const;
 
 private:
@@ -77,6 +81,8 @@ private:
     bool stop_ = false, pool_done_ = false;
     int inflight_ = 0;
     double n_done_ = 0, n_plain_ = 0, n_steps_ = 0, busy_ = 0, peak_ = 0, n_rerun_ = 0;
+    double h2d_ = 0, d2h_ = 0, launches_ = 0, scc_ms_ = 0, scc_flops_ = 0;
+    long long pool_h2d_seen_ = 0;
     std::string pool_error_;
     std::vector<Completed> failed_resident_;
     std::thread pool_thread_;

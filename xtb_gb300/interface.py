@@ -339,7 +339,7 @@ class Server:
         e = C.c_double()
         g = np.zeros((n, 3))
         q = np.zeros(n)
-        info = np.zeros(10)
+        info = np.zeros(12)
         ok = self.lib.xtbgb_serverWait(env.h, self.h, rid, timeout, C.byref(e), _dptr(g), _dptr(q), _dptr(info))
         if not ok:
             return None
@@ -355,9 +355,10 @@ class Server:
         return ServedResult(rid, e.value, g, q, info, err)
 
     def stats(self):
-        s = np.zeros(6)
+        s = np.zeros(16)
         self.lib.xtbgb_serverStats(self._env().h, self.h, _dptr(s))
-        keys = ("completed", "plain", "steps", "busy_s", "peak_resident", "reruns")
+        keys = ("completed", "plain", "steps", "busy_s", "peak_resident", "reruns", "h2d_bytes", "d2h_bytes",
+                "launches", "pool_scc_ms", "pool_scc_flops")
         return dict(zip(keys, s.tolist()))
 
     def close(self):
@@ -379,4 +380,6 @@ class ServedResult:
         self.t_submit, self.t_start, self.t_done = (float(v) for v in info[4:7])
         self.dipole = np.array(info[7:10])
         self.latency = self.t_done - self.t_submit
+        self.nao = int(info[10])
+        self.sytrd_ms = float(info[11])
         self.error = error
