@@ -47,6 +47,11 @@ extern void xtbgb_setKeepOrbitals(xtb_TEnvironment env, xtb_TCalculator calc, in
  * returns 0 when no device is present. */
 extern double xtbgb_fp64PeakTflops(void);
 
+/* Dependent-operation latency of device 0 in clock cycles, measured with one warp:
+ * cycles[0] FP64 FMA, [1] FP64 add, [2] FP64 multiply, [3] FP64 divide, [4] FP32 FMA
+ * (all 0 when no device is present). */
+extern void xtbgb_fp64LatencyCycles(double* cycles);
+
 /* ---- Batched single points (no counterpart in the reference: the reference API runs one
  * molecule per call).  Many molecules of uneven size are solved together on the device, one
  * thread block per molecule with its whole SCC state resident; molecules above 512 AOs (or

@@ -455,6 +455,16 @@ extern "C" {
 
 int xtbgb_deviceCount(void) { return xg::device_count(); }
 
+void xtbgb_fp64LatencyCycles(double* cycles) {
+    if (!cycles) return;
+    for (int k = 0; k < 5; ++k) cycles[k] = 0.0;
+    if (xg::device_count() == 0) return;
+    try {
+        xg::fp64_latency_cycles(cycles);
+    } catch (const std::exception&) {
+    }
+}
+
 double xtbgb_fp64PeakTflops(void) {
     if (xg::device_count() == 0) return 0.0;
     try {

@@ -315,4 +315,52 @@ double fp64_peak_tflops() {
     const double flops = 2.0 * 8.0 * iters * (double)blocks * threads;
     return flops / (best * 1e-3) / 1e12;
 }
+// Dependent-chain latency probe, one warp: cycles per FP64 FMA, add, multiply, divide and
+// per FP32 FMA (clock64 around chains of `n` operations).
+__global__ void k_latency_probe(int n, double a, double b, float af, float bf, long long* out, double* sink,
+                                float* sinkf) {
+    double x = a;
+    float y = af;
+    const long long t0 = clock64();
+    for (int i = 0; i < n; ++i) x = fma(x, b, a);
+    const long long t1 = clock64();
+    for (int i = 0; i < n; ++i) x = x + b;
+    const long long t2 = clock64();
+    for (int i = 0; i < n; ++i) x = x * b;
+    const long long t3 = clock64();
+    for (int i = 0; i < n; ++i) x = a / x;
+    const long long t4 = clock64();
+    for (int i = 0; i < n; ++i) y = fmaf(y, bf, af);
+    const long long t5 = clock64();
+    if (threadIdx.x == 0) {
+        out[0] = t1 - t0;
+        out[1] = t2 - t1;
+        out[2] = t3 - t2;
+        out[3] = t4 - t3;
+        out[4] = t5 - t4;
+    }
+    sink[threadIdx.x] = x;
+    sinkf[threadIdx.x] = y;
+}
+
+void fp64_latency_cycles(double* cycles) {
+    long long* d_out = nullptr;
+    double* d_sink = nullptr;
+    float* d_sinkf = nullptr;
+    XG_CUDA(cudaMalloc(&d_out, 8 * sizeof(long long)));
+    XG_CUDA(cudaMalloc(&d_sink, 32 * sizeof(double)));
+    XG_CUDA(cudaMalloc(&d_sinkf, 32 * sizeof(float)));
+    const int n = 4096;
+    for (int rep = 0; rep < 2; ++rep) {   // the first pass warms the instruction cache
+        k_latency_probe<<<1, 32>>>(n, 1.0000001, 0.9999999, 1.0001f, 0.9999f, d_out, d_sink, d_sinkf);
+        XG_CUDA(cudaGetLastError());
+        XG_CUDA(cudaDeviceSynchronize());
+    }
+    long long h[5];
+    XG_CUDA(cudaMemcpy(h, d_out, sizeof(h), cudaMemcpyDeviceToHost));
+    for (int k = 0; k < 5; ++k) cycles[k] = (double)h[k] / n;
+    cudaFree(d_out);
+    cudaFree(d_sink);
+    cudaFree(d_sinkf);
+}
 }  // namespace xg

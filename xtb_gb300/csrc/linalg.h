@@ -31,5 +31,8 @@ void ormtr(cudaStream_t st, int n, const double* V, const double* tau, const dou
            const int* ncol = nullptr);
 // measured FP64 FMA throughput of the current device (TFLOP/s)
 double fp64_peak_tflops();
+// dependent-operation latency in cycles: [0] FP64 FMA, [1] FP64 add, [2] FP64 multiply,
+// [3] FP64 divide, [4] FP32 FMA
+void fp64_latency_cycles(double* cycles);
 
 }  // namespace xg

@@ -75,6 +75,7 @@ def load_library(path=LIBPATH):
         "xtbgb_getTransferBytes": (None, [vp, vp, C.POINTER(C.c_longlong)]),
         "xtbgb_setKeepOrbitals": (None, [vp, vp, C.c_int]),
         "xtbgb_fp64PeakTflops": (C.c_double, []),
+        "xtbgb_fp64LatencyCycles": (None, [dp]),
         "xtbgb_repulsionNoAlloc": (C.c_int, [C.c_int, vp, vp, vp, vp, vp, C.c_char_p, C.c_int]),
         "xtbgb_newBatch": (vp, [vp, C.c_int, ip, ip, dp, dp, ip]),
         "xtbgb_delBatch": (None, [C.POINTER(vp)]),
