@@ -181,7 +181,9 @@ void sytrd(cudaStream_t st, int n, double* A, int lda, double* V, double* tau, d
     XG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxblk, k_sytrd, 256, smem));
     if (maxblk < 1) throw CudaError("sytrd: kernel does not fit on an SM");
     // enough warps to cover the rows, at most one co-resident wave
-    int blocks = std::min(nsm * maxblk, std::max(1, ceil_div(n, 8)));
+    // at most one block per SM: every block repeats the O(n) per-column vector work, so fewer,
+    // fuller blocks spend less of the FP64 pipe on it
+    int blocks = std::min(std::min(nsm * maxblk, nsm), std::max(1, ceil_div(n, 8)));
     void* args[] = {&n, &A, &lda, &V, &tau, &d, &e, &p};
     XG_CUDA(cudaLaunchCooperativeKernel((void*)k_sytrd, blocks, 256, args, smem, st));
     ++launch_counter();

@@ -204,16 +204,33 @@ __device__ inline void d_sytrd(int n, double* __restrict__ A, int lda, double* _
         for (int r = gwarp; r < m; r += nwarps) {
             double* arow = A + (size_t)(k + 1 + r) * lda + k + 1;
             const double vr = pend ? vp[r + 1] : 0.0, wr = pend ? wp[r + 1] : 0.0;
-            double sdot = 0.0;
-            for (int c = lane; c < m; c += 32) {
-                double a = arow[c];
+            // two FMAs per element for the rank-2 update, two accumulators for the dot (FP64
+            // latency is long: independent chains keep the pipe busy)
+            double s0 = 0.0, s1 = 0.0;
+            int c = lane;
+            for (; c + 32 < m; c += 64) {
+                double a0 = arow[c], a1 = arow[c + 32];
                 if (pend) {
-                    a -= vr * wp[c + 1] + wr * vp[c + 1];
-                    arow[c] = a;
+                    a0 = fma(-vr, wp[c + 1], a0);
+                    a1 = fma(-vr, wp[c + 33], a1);
+                    a0 = fma(-wr, vp[c + 1], a0);
+                    a1 = fma(-wr, vp[c + 33], a1);
+                    arow[c] = a0;
+                    arow[c + 32] = a1;
                 }
-                sdot = fma(a, v[c], sdot);
+                s0 = fma(a0, v[c], s0);
+                s1 = fma(a1, v[c + 32], s1);
             }
-            sdot = warp_sum(sdot);
+            if (c < m) {
+                double a0 = arow[c];
+                if (pend) {
+                    a0 = fma(-vr, wp[c + 1], a0);
+                    a0 = fma(-wr, vp[c + 1], a0);
+                    arow[c] = a0;
+                }
+                s0 = fma(a0, v[c], s0);
+            }
+            const double sdot = warp_sum(s0 + s1);
             if (lane == 0) p[r] = tk * sdot;
         }
         if constexpr (CTA) __syncthreads();
