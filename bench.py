@@ -105,13 +105,20 @@ def dist_init(ws):
 
 
 def dist_max(x, ws):
+    """Max of x over the replicas (the slowest rank sets the whole job's time)."""
     if ws == 1:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_throughput(units_per_rank, seconds, ws):
+    """Whole-job throughput of `ws` independent replicas: all units over the slowest rank's time."""
+    return ws * units_per_rank / dist_max(seconds, ws)
 
 
 def dist_barrier(ws):

@@ -105,28 +105,54 @@ extern XTB_API_ENTRY void XTB_API_CALL xtb_setMaxIter(xtb_TEnvironment env, xtb_
 /* electronic temperature in K, at least 1e-6 [ref include/xtb.h:224-228] */
 extern XTB_API_ENTRY void XTB_API_CALL xtb_setElectronicTemp(xtb_TEnvironment env, xtb_TCalculator calc, double temperature);
 
-/* ---- single point [ref include/xtb.h:236-240] ---- */
+/* ---- single point [ref include/xtb.h:235-240] ---- */
 extern XTB_API_ENTRY void XTB_API_CALL
 xtb_singlepoint(xtb_TEnvironment env, xtb_TMolecule mol, xtb_TCalculator calc, xtb_TResults res);
 
-/* ---- results [ref include/xtb.h:259-344] ---- */
-extern XTB_API_ENTRY xtb_TResults XTB_API_CALL xtb_newResults(void);
-extern XTB_API_ENTRY void XTB_API_CALL xtb_delResults(xtb_TResults* res);
-extern XTB_API_ENTRY xtb_TResults XTB_API_CALL xtb_copyResults(xtb_TResults res);
+/* Numerical Hessian [3N][3N] (Hartree/Bohr^2) by central differences of analytic gradients,
+ * step 0.005 Bohr, every displaced point starting from the results object's wavefunction (a
+ * fresh object: the initial guess of the undisplaced molecule); the displaced single points
+ * run together on the batched engine.  dipole_gradient [3N][3] may be NULL.  The reference
+ * header declares atom_index_list and step_size in this order while its implementation reads
+ * a step and a list; both must be NULL here (all atoms, default step), as in the reference's
+ * own C test.  Polarizability gradients are not computed (non-NULL raises an error).
+ * [ref include/xtb.h:242-252] */
+extern XTB_API_ENTRY void XTB_API_CALL
+xtb_hessian(xtb_TEnvironment env, xtb_TMolecule mol, xtb_TCalculator calc, xtb_TResults res, double* hessian,
+            int* atom_index_list, int* step_size, double* dipole_gradient, double* polarizability_gradient);
+
+/* CPCM-X solvation: not supported, pushes an error [ref include/xtb.h:228-233] */
+extern XTB_API_ENTRY void XTB_API_CALL
+xtb_cpcmx_calc(xtb_TEnvironment env, xtb_TMolecule mol, xtb_TCalculator calc, xtb_TResults res);
+
+/* ---- results [ref include/xtb.h:258-344] ---- */
+extern XTB_API_ENTRY xtb_TResults XTB_API_CALL xtb_newResults(void);                       /* [ref :260] */
+extern XTB_API_ENTRY void XTB_API_CALL xtb_delResults(xtb_TResults* res);                  /* [ref :264] */
+extern XTB_API_ENTRY xtb_TResults XTB_API_CALL xtb_copyResults(xtb_TResults res);           /* [ref :268] */
+/* total energy in Hartree [ref include/xtb.h:272] */
 extern XTB_API_ENTRY void XTB_API_CALL xtb_getEnergy(xtb_TEnvironment env, xtb_TResults res, double* energy);
-/* gradient[natoms][3] */
+/* gas phase only: pushes "not available" like a reference results object without solvation
+ * [ref include/xtb.h:278] */
+extern XTB_API_ENTRY void XTB_API_CALL xtb_getSolvationEnergy(xtb_TEnvironment env, xtb_TResults res, double* energy);
+/* gradient[natoms][3] in Hartree/Bohr [ref include/xtb.h:284] */
 extern XTB_API_ENTRY void XTB_API_CALL xtb_getGradient(xtb_TEnvironment env, xtb_TResults res, double* grad);
-/* Mulliken partial charges[natoms] */
-extern XTB_API_ENTRY void XTB_API_CALL xtb_getCharges(xtb_TEnvironment env, xtb_TResults res, double* charges);
-/* dipole[3] in e*Bohr [ref include/xtb.h:277-280] */
+/* no external charges: pushes "not available" [ref include/xtb.h:290] */
+extern XTB_API_ENTRY void XTB_API_CALL xtb_getPCGradient(xtb_TEnvironment env, xtb_TResults res, double* grad);
+/* virial[3][3] in Hartree: dE/d(strain) = sum_A R_A g_A^T of the molecule [ref include/xtb.h:296] */
+extern XTB_API_ENTRY void XTB_API_CALL xtb_getVirial(xtb_TEnvironment env, xtb_TResults res, double* virial);
+/* dipole[3] in e*Bohr [ref include/xtb.h:302] */
 extern XTB_API_ENTRY void XTB_API_CALL xtb_getDipole(xtb_TEnvironment env, xtb_TResults res, double* dipole);
-/* Wiberg bond orders[natoms][natoms] [ref include/xtb.h:313-316] */
+/* Mulliken partial charges[natoms] [ref include/xtb.h:308] */
+extern XTB_API_ENTRY void XTB_API_CALL xtb_getCharges(xtb_TEnvironment env, xtb_TResults res, double* charges);
+/* Wiberg bond orders[natoms][natoms] [ref include/xtb.h:314] */
 extern XTB_API_ENTRY void XTB_API_CALL xtb_getBondOrders(xtb_TEnvironment env, xtb_TResults res, double* wbo);
+/* number of atomic orbitals [ref include/xtb.h:320] */
 extern XTB_API_ENTRY void XTB_API_CALL xtb_getNao(xtb_TEnvironment env, xtb_TResults res, int* nao);
-/* orbital energies[nao] in Hartree [ref include/xtb.h:325-328] */
+/* orbital energies[nao] in Hartree [ref include/xtb.h:326] */
 extern XTB_API_ENTRY void XTB_API_CALL xtb_getOrbitalEigenvalues(xtb_TEnvironment env, xtb_TResults res, double* emo);
+/* orbital occupations[nao] [ref include/xtb.h:332] */
 extern XTB_API_ENTRY void XTB_API_CALL xtb_getOrbitalOccupations(xtb_TEnvironment env, xtb_TResults res, double* focc);
-/* coefficients[nao][nao] [ref include/xtb.h:337-340] */
+/* coefficients[nao][nao] [ref include/xtb.h:338] */
 extern XTB_API_ENTRY void XTB_API_CALL xtb_getOrbitalCoefficients(xtb_TEnvironment env, xtb_TResults res, double* c);
 
 #ifdef __cplusplus

@@ -1056,3 +1056,35 @@ def singlepoint(Z, xyz, charge=0.0, uhf=0, etemp=300.0, accuracy=1.0, maxiter=25
     r.nshell = nsh
     r.basis = basis
     return r
+
+
+def hessian(Z, xyz, charge=0.0, uhf=0, step=0.005, atoms=None, **kw):
+    """Numerical Hessian (Eh/bohr^2) and dipole gradient by central differences of analytic
+    gradients, as xtb_hessian does for a fresh results object (hessian_api,
+    src/api/interface.f90:309-454; TCalculator%hessian, src/type/calculator.f90:116-199):
+    every displaced single point starts from the initial-guess wavefunction of the
+    undisplaced molecule (EEQ charges, iniqshell, zero multipoles), H[jj, ii] =
+    (g_jj(+h) - g_jj(-h)) / 2h for displaced coordinate ii, then H is symmetrised.
+    Returns (H [3N, 3N], dipgrad [3N, 3])."""
+    Z = np.asarray(Z, dtype=np.int64)
+    xyz = np.asarray(xyz, dtype=np.float64).reshape(-1, 3)
+    n = len(Z)
+    basis = I.Basis(Z)
+    q0 = eeq_guess(Z, xyz, charge)
+    qsh0 = ini_qshell(basis, valence_charge(Z), q0)
+    atoms = range(n) if atoms is None else atoms
+    H = np.zeros((3 * n, 3 * n))
+    dipgrad = np.zeros((3 * n, 3))
+    s2 = 0.5 / step
+    for iat in atoms:
+        for ic in range(3):
+            ii = 3 * iat + ic
+            res = []
+            for sgn in (1.0, -1.0):
+                x = xyz.copy()
+                x[iat, ic] += sgn * step
+                res.append(singlepoint(Z, x, charge=charge, uhf=uhf, qsh_init=qsh0, **kw))
+            H[:, ii] += (res[0].gradient - res[1].gradient).ravel() * s2
+            dipgrad[ii] = (res[0].dipole - res[1].dipole) * s2
+    H = 0.5 * (H + H.T)
+    return H, dipgrad

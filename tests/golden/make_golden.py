@@ -81,6 +81,14 @@ def main():
     for m in re.finditer(r"check\((\w+(?:\[\d+\])?),\s*(" + NUM + r"),\s*(" + NUM + r")", first):
         cks.append({"expr": m.group(1), "value": fnum(m.group(2)), "thr": fnum(m.group(3))})
     cases["capi"] = {"numbers": at, "positions": coord, "checks": cks[:4], "maxiter": 30, "guess": "eeq"}
+    # numerical Hessian of the same molecule (xtb_hessian, default step, fresh results object):
+    # hess[i] is element i of the flattened 3N x 3N matrix
+    hk = [c for c in cks if c["expr"].startswith("hess[")]
+    natsq = len(at) * len(at)
+    m = re.search(r"check\(hess\[\(9\*natsq\)-1\],\s*(" + NUM + r"),\s*(" + NUM + r")", first)
+    hk.append({"expr": f"hess[{9 * natsq - 1}]", "value": fnum(m.group(1)), "thr": fnum(m.group(2))})
+    cases["capi_hessian"] = {"numbers": at, "positions": coord, "checks": hk, "maxiter": 250, "guess": "eeq",
+                             "step": 0.005}
     json.dump(cases, open(OUT, "w"), indent=1)
     print("wrote", OUT)
 

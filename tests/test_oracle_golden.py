@@ -46,3 +46,16 @@ def test_oracle_gradient_matches_finite_difference():
         xm[a, k] -= h
         fd = (gfn2.singlepoint(Z, xp).energy - gfn2.singlepoint(Z, xm).energy) / (2 * h)
         assert abs(fd - g[a, k]) < 2e-6, (a, k, fd, g[a, k])
+
+
+def test_oracle_hessian_matches_reference_c_api_test():
+    """c_api_example.c:242-261: numerical Hessian of the propyne test molecule, fresh results
+    object, default step; the reference checks three elements at 1e-9."""
+    case = golden()["capi_hessian"]
+    Z, xyz = case_geometry(case)
+    H, _ = gfn2.hessian(Z, xyz, step=case["step"])
+    flat = H.T.ravel()                       # column-major, as the C array
+    for c in case["checks"]:
+        i = int(c["expr"][5:-1])
+        assert abs(flat[i] - c["value"]) <= c["thr"], (c["expr"], flat[i], c["value"])
+    assert np.max(np.abs(H - H.T)) == 0.0

@@ -63,6 +63,7 @@ struct _xtb_TResults {
     xg::Wavefunction wfn;
     xg::SPResult sp;
     int nat = 0;
+    std::vector<double> xyz;   // geometry of the last single point (virial)
 };
 
 namespace {
@@ -354,6 +355,7 @@ void xtb_singlepoint(xtb_TEnvironment env, xtb_TMolecule mol, xtb_TCalculator ca
     }
     res->has = true;
     res->nat = hm.nat;
+    res->xyz = mol->xyz;
     if (failed) env->error("Self consistent charge iterator did not converge", "scf");
     if (env->verbosity >= XTB_VERBOSITY_MINIMAL && env->out) {
         fprintf(env->out, "          | TOTAL ENERGY %28.12f Eh   |\n", res->sp.energy);
@@ -361,6 +363,106 @@ void xtb_singlepoint(xtb_TEnvironment env, xtb_TMolecule mol, xtb_TCalculator ca
         fprintf(env->out, "          | HOMO-LUMO GAP %27.12f eV   |\n", res->sp.hl_gap);
         fflush(env->out);
     }
+}
+
+// ------------------------------------------------------------------ Hessian
+void xtb_hessian(xtb_TEnvironment env, xtb_TMolecule mol, xtb_TCalculator calc, xtb_TResults res, double* hessian,
+                 int* atom_index_list, int* step_size, double* dipole_gradient, double* polarizability_gradient) {
+    static const char* src = "xtb_api_hessian";
+    if (!check_env(env)) return;
+    if (!mol) {
+        env->error("Molecular structure data is not allocated", src);
+        return;
+    }
+    if (!calc) {
+        env->error("Singlepoint calculator is not allocated", src);
+        return;
+    }
+    if (!calc->loaded) {
+        env->error("No calculator loaded for single point", src);
+        return;
+    }
+    if (!res) {
+        env->error("Calculation results are not allocated", src);
+        return;
+    }
+    if (!hessian) {
+        env->error("Hessian array is not allocated", src);
+        return;
+    }
+    if (atom_index_list || step_size) {
+        env->error("Atom lists and step sizes are not supported: pass NULL (all atoms, step 0.005 Bohr)", src);
+        return;
+    }
+    if (polarizability_gradient) {
+        env->error("Polarizability gradients are not available for GFN2-xTB here", src);
+        return;
+    }
+    const int n = mol->nat;
+    xg::HostMol hm0;
+    std::string err = xg::build_host_mol(n, mol->Z.data(), mol->xyz.data(), mol->charge, mol->uhf, hm0);
+    if (!err.empty()) {
+        env->error(err, src);
+        return;
+    }
+    const double step = 0.005, step2 = 0.5 / step;
+    try {
+        // every displaced point starts from the results object's wavefunction; a fresh object gets
+        // the initial guess of the undisplaced molecule (hessian_api, src/api/interface.f90:374-391)
+        if (!(res->wfn.valid() && res->wfn.nat == hm0.nat && res->wfn.nao == hm0.nao && res->wfn.nsh == hm0.nsh)) {
+            xg::Wavefunction g;
+            xg::SPResult dummy;
+            bool failed = false;
+            xg::run_singlepoint(hm0, calc->set, g, dummy, false, failed, true);
+            res->wfn = g;
+        }
+        const xg::Wavefunction* chk0 = &res->wfn;
+        std::vector<xg::HostMol> mols(6 * (size_t)n);
+        std::vector<const xg::Wavefunction*> guesses(mols.size(), chk0);
+        for (int iat = 0; iat < n; ++iat)
+            for (int ic = 0; ic < 3; ++ic)
+                for (int sg = 0; sg < 2; ++sg) {
+                    std::vector<double> xyz = mol->xyz;
+                    xyz[3 * iat + ic] += sg == 0 ? step : -step;
+                    err = xg::build_host_mol(n, mol->Z.data(), xyz.data(), mol->charge, mol->uhf,
+                                             mols[2 * (3 * iat + ic) + sg]);
+                    if (!err.empty()) throw std::runtime_error(err);
+                }
+        xg::BatchSettings set;
+        set.accuracy = calc->set.accuracy;
+        set.etemp = calc->set.etemp;
+        set.maxiter = calc->set.maxiter;
+        xg::BatchResults br;
+        xg::run_batch(mols, set, std::vector<int>(mols.size(), 1), br, &guesses);
+        const int N3 = 3 * n;
+        std::vector<double> H((size_t)N3 * N3, 0.0);
+        int bad = 0;
+        for (int ii = 0; ii < N3; ++ii) {
+            const int r = 2 * ii, l = 2 * ii + 1;
+            bad += (br.status[r] != xg::BST_OK) + (br.status[l] != xg::BST_OK);
+            const double* gr = br.gradient.data() + 3 * (size_t)n * r;   // all molecules have n atoms
+            const double* gl = br.gradient.data() + 3 * (size_t)n * l;
+            for (int jj = 0; jj < N3; ++jj) H[(size_t)ii * N3 + jj] = (gr[jj] - gl[jj]) * step2;
+            if (dipole_gradient)
+                for (int x = 0; x < 3; ++x)
+                    dipole_gradient[3 * ii + x] = (br.dipole[3 * (size_t)r + x] - br.dipole[3 * (size_t)l + x]) * step2;
+        }
+        for (int i = 0; i < N3; ++i)
+            for (int j = i + 1; j < N3; ++j) {
+                const double v = 0.5 * (H[(size_t)i * N3 + j] + H[(size_t)j * N3 + i]);
+                H[(size_t)i * N3 + j] = v;
+                H[(size_t)j * N3 + i] = v;
+            }
+        std::copy(H.begin(), H.end(), hessian);
+        if (bad) env->error("Self consistent charge iterator did not converge", "scf");
+    } catch (const std::exception& e) {
+        env->error(e.what(), src);
+    }
+}
+
+void xtb_cpcmx_calc(xtb_TEnvironment env, xtb_TMolecule, xtb_TCalculator, xtb_TResults) {
+    if (!check_env(env)) return;
+    env->error("CPCM-X solvation is not supported by this engine", "xtb_api_cpcmx_calc");
 }
 
 // ------------------------------------------------------------------ results
@@ -399,6 +501,34 @@ void xtb_getEnergy(xtb_TEnvironment env, xtb_TResults res, double* energy) {
 void xtb_getGradient(xtb_TEnvironment env, xtb_TResults res, double* grad) {
     if (!res_ready(env, res, "xtb_api_getGradient", "Gradient") || !grad) return;
     std::copy(res->sp.gradient.begin(), res->sp.gradient.end(), grad);
+}
+
+void xtb_getSolvationEnergy(xtb_TEnvironment env, xtb_TResults res, double* energy) {
+    if (!check_env(env)) return;
+    if (!res) {
+        env->error("Results object is not allocated", "xtb_api_getSolvationEnergy");
+        return;
+    }
+    (void)energy;
+    env->error("Solvation energy is not available in results", "xtb_api_getSolvationEnergy");
+}
+
+void xtb_getPCGradient(xtb_TEnvironment env, xtb_TResults res, double* grad) {
+    if (!check_env(env)) return;
+    if (!res) {
+        env->error("Results object is not allocated", "xtb_api_getPCGradient");
+        return;
+    }
+    (void)grad;
+    env->error("External charge gradients are not available in results", "xtb_api_getPCGradient");
+}
+
+void xtb_getVirial(xtb_TEnvironment env, xtb_TResults res, double* virial) {
+    if (!res_ready(env, res, "xtb_api_getVirial", "Virial") || !virial) return;
+    for (int k = 0; k < 9; ++k) virial[k] = 0.0;
+    for (int a = 0; a < res->nat; ++a)
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) virial[3 * i + j] += res->xyz[3 * a + i] * res->sp.gradient[3 * a + j];
 }
 
 void xtb_getCharges(xtb_TEnvironment env, xtb_TResults res, double* charges) {

@@ -46,7 +46,7 @@ struct Carver {
     }
 };
 
-void layout_mol(Carver& cv, const HostMol& hm, BatchMol& b) {
+void layout_mol(Carver& cv, const HostMol& hm, BatchMol& b, const std::vector<double>* guess = nullptr) {
     const int nat = hm.nat, nsh = hm.nsh, nao = hm.nao;
     const size_t nn = (size_t)nao * nao, aa = (size_t)nat * nat;
     DevMol& m = b.m;
@@ -70,6 +70,7 @@ void layout_mol(Carver& cv, const HostMol& hm, BatchMol& b) {
     m.sh_zsh = cv.upload(hm.sh_zsh);
     m.ao_sh = cv.upload(hm.ao_sh); m.ao_at = cv.upload(hm.ao_at);
     b.zval = cv.upload(hm.zval);
+    b.guess = guess ? cv.upload(*guess) : nullptr;
 
     b.S = cv.take<double>(nn); b.D = cv.take<double>(3 * nn); b.Q = cv.take<double>(6 * nn);
     b.H0 = cv.take<double>(nn); b.X = cv.take<double>(nn); b.H = cv.take<double>(nn); b.A = cv.take<double>(nn);
@@ -159,6 +160,14 @@ __device__ void stage_setup_a(BatchMol* b) {
     CTA_FOR(a, nat) d_cn(m, 0, b->cn_gfn, a);
     __syncthreads();
     CTA_FOR(s, nsh) b->se[s] = m.sh_se0[s] - m.sh_kcn[s] * b->cn_gfn[m.sh_atom[s]];
+    if (b->guess) {
+        // given initial wavefunction (warm start): [qsh; per atom (dipm 3, qp 6)] as packed for mixing
+        const int nbr = nsh + 9 * nat;
+        CTA_FOR(t, nbr) b->qin[t] = b->guess[t];
+        __syncthreads();
+        CTA_FOR(t, max(nsh, nat)) d_broyden_unpack(m, b->qin, b->qsh, b->dipm, b->qp, b->q, t);
+        __syncthreads();
+    } else {
     // EEQ guess (src/eeq_model.f90), iniqshell
     CTA_FOR(a, nat) d_cn(m, 2, b->cn_tmp, a);
     __syncthreads();
@@ -177,6 +186,7 @@ __device__ void stage_setup_a(BatchMol* b) {
     __syncthreads();
     CTA_FOR(t, max(nsh, nat)) d_broyden_unpack(m, b->qin, b->qsh, b->dipm, b->qp, b->q, t);
     __syncthreads();
+    }
     CTA_FOR(a, nat) d_repulsion(m, b->erep, b->grad, a);
     // integrals: zeroed here, filled by the batched integral kernels between the two set-up halves
     blk_zero(b->S, nn);
@@ -547,7 +557,23 @@ size_t DeviceBatch::bytes_for(const HostMol& hm) {
     return cv.used;
 }
 
-void DeviceBatch::load(const std::vector<const HostMol*>& mols, const std::vector<int>& want_grad, cudaStream_t st) {
+void DeviceBatch::load(const std::vector<const HostMol*>& mols, const std::vector<int>& want_grad, cudaStream_t st,
+                       const std::vector<const Wavefunction*>* guesses) {
+    // packed initial wavefunctions [qsh; per atom (dipm 3, qp 6)]
+    std::vector<std::vector<double>> packed(mols.size());
+    std::vector<const std::vector<double>*> gp(mols.size(), nullptr);
+    if (guesses)
+        for (size_t i = 0; i < mols.size(); ++i) {
+            const Wavefunction* w = (*guesses)[i];
+            if (!w || w->nat != mols[i]->nat || w->nsh != mols[i]->nsh) continue;
+            auto& v = packed[i];
+            v.assign(w->qsh.begin(), w->qsh.end());
+            for (int a = 0; a < w->nat; ++a) {
+                for (int k = 0; k < 3; ++k) v.push_back(w->dipm[3 * a + k]);
+                for (int k = 0; k < 6; ++k) v.push_back(w->qp[6 * a + k]);
+            }
+            gp[i] = &v;
+        }
     nmol_ = (int)mols.size();
     h_mols_.assign(nmol_, BatchMol{});
     max_nao_ = 1;
@@ -558,7 +584,7 @@ void DeviceBatch::load(const std::vector<const HostMol*>& mols, const std::vecto
     cv.used = desc;
     for (int i = 0; i < nmol_; ++i) {
         if (mols[i]->nao > BATCH_MAX_NAO) throw CudaError("batched engine: molecule exceeds the AO limit");
-        layout_mol(cv, *mols[i], h_mols_[i]);
+        layout_mol(cv, *mols[i], h_mols_[i], gp[i]);
         max_nao_ = std::max(max_nao_, mols[i]->nao);
         max_nsh_ = std::max(max_nsh_, mols[i]->nsh);
     }
@@ -578,7 +604,7 @@ void DeviceBatch::load(const std::vector<const HostMol*>& mols, const std::vecto
     cv2.used = desc;
     cv2.ups = &ups;
     for (int i = 0; i < nmol_; ++i) {
-        layout_mol(cv2, *mols[i], h_mols_[i]);
+        layout_mol(cv2, *mols[i], h_mols_[i], gp[i]);
         h_mols_[i].want_grad = want_grad.empty() ? 1 : want_grad[i];
     }
     d_mols_ = reinterpret_cast<BatchMol*>(base_);

@@ -45,6 +45,7 @@ struct BatchMol {
     int* kocc;
     BroydenState bs;
     const double* zval;
+    const double* guess;   // optional initial wavefunction [qsh; per atom (dipm 3, qp 6)], else EEQ
     int nel_a, nel_b;
     double charge;
     int want_grad;
@@ -73,7 +74,9 @@ public:
     DeviceBatch& operator=(const DeviceBatch&) = delete;
     ~DeviceBatch();
     // Lay out and upload the molecules (HostMol from build_host_mol); nao <= BATCH_MAX_NAO each.
-    void load(const std::vector<const HostMol*>& mols, const std::vector<int>& want_grad, cudaStream_t st);
+    // guesses (optional, per molecule, may hold nullptr): initial wavefunction instead of the EEQ guess.
+    void load(const std::vector<const HostMol*>& mols, const std::vector<int>& want_grad, cudaStream_t st,
+              const std::vector<const Wavefunction*>* guesses = nullptr);
     // Advance every unfinished molecule by at most `max_iter` SCC iterations (set-up and
     // gradient included); returns the number of molecules still unfinished.
     int step(const BatchSettings& set, int max_iter, cudaStream_t st);
@@ -162,7 +165,9 @@ struct BatchResults {
 
 // Single points of all molecules (batched engine, plain engine for the ones it cannot take).
 // want_grad[i] (empty: all) selects the gradient.  Throws on device errors.
+// guesses (optional): per molecule an initial wavefunction (qsh, dipm, qp of matching size) that
+// replaces the EEQ guess, as a warm start does.
 std::string run_batch(const std::vector<HostMol>& mols, const BatchSettings& set, const std::vector<int>& want_grad,
-                      BatchResults& out);
+                      BatchResults& out, const std::vector<const Wavefunction*>* guesses = nullptr);
 
 }  // namespace xg

@@ -19,7 +19,7 @@ thread_local DeviceBatch* g_batch = nullptr;
 }  // namespace
 
 std::string run_batch(const std::vector<HostMol>& mols, const BatchSettings& set, const std::vector<int>& want_grad,
-                      BatchResults& out) {
+                      BatchResults& out, const std::vector<const Wavefunction*>* guesses) {
     const auto t0 = std::chrono::steady_clock::now();
     if (device_count() == 0) throw CudaError("no CUDA device available for the GFN2 engine");
     if (!g_bstream) XG_CUDA(cudaStreamCreateWithFlags(&g_bstream, cudaStreamNonBlocking));
@@ -47,17 +47,19 @@ std::string run_batch(const std::vector<HostMol>& mols, const BatchSettings& set
     const long long launches0 = launch_counter();
     if (!batched.empty()) {
         std::vector<const HostMol*> hm;
+        std::vector<const Wavefunction*> gs;
         std::vector<int> wg;
         std::vector<long> off(batched.size());
         long o = 0;
         for (size_t k = 0; k < batched.size(); ++k) {
             hm.push_back(&mols[batched[k]]);
+            gs.push_back(guesses ? (*guesses)[batched[k]] : nullptr);
             wg.push_back(want_grad.empty() ? 1 : want_grad[batched[k]]);
             off[k] = o;
             o += mols[batched[k]].nat;
         }
         DeviceBatch& db = *g_batch;
-        db.load(hm, wg, st);
+        db.load(hm, wg, st, guesses ? &gs : nullptr);
         out.h2d += db.h2d_bytes() + (long long)(sizeof(long) * off.size());
         // outputs packed in batch order
         long* d_off = nullptr;
@@ -115,6 +117,7 @@ std::string run_batch(const std::vector<HostMol>& mols, const BatchSettings& set
         ps.etemp = set.etemp;
         ps.maxiter = set.maxiter;
         Wavefunction wfn;
+        if (guesses && (*guesses)[i]) wfn = *(*guesses)[i];   // warm start from the given guess
         SPResult r;
         bool failed = false;
         run_singlepoint(mols[i], ps, wfn, r, false, failed);

@@ -227,7 +227,7 @@ T* upload(Arena& ar, cudaStream_t st, const std::vector<T>& v) {
 }  // namespace
 
 void run_singlepoint(const HostMol& hm, const SPSettings& set, Wavefunction& wfn, SPResult& res, bool keep_orbitals,
-                     bool& scc_failed) {
+                     bool& scc_failed, bool guess_only) {
     if (device_count() == 0) throw CudaError("no CUDA device available for the GFN2 engine");
     if (!g_stream) XG_CUDA(cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking));
     cudaStream_t st = g_stream;
@@ -445,6 +445,20 @@ void run_singlepoint(const HostMol& hm, const SPSettings& set, Wavefunction& wfn
     }
     broyden_pack(st, m, qsh, dipm, qp, qin);
     broyden_unpack(st, m, qin, qsh, dipm, qp, q);   // q = sum of qsh (qsh2qat)
+    if (guess_only) {
+        // the initial-guess wavefunction only (newWavefunction, src/xtb/calculator.f90:432-496)
+        wfn = Wavefunction();
+        wfn.nat = nat; wfn.nao = nao; wfn.nsh = nsh;
+        wfn.q.resize(nat); wfn.qsh.resize(nsh); wfn.dipm.resize(3 * nat); wfn.qp.resize(6 * nat);
+        XG_CUDA(cudaMemcpyAsync(wfn.q.data(), q, nat * sizeof(double), cudaMemcpyDeviceToHost, st));
+        XG_CUDA(cudaMemcpyAsync(wfn.qsh.data(), qsh, nsh * sizeof(double), cudaMemcpyDeviceToHost, st));
+        XG_CUDA(cudaMemcpyAsync(wfn.dipm.data(), dipm, 3 * nat * sizeof(double), cudaMemcpyDeviceToHost, st));
+        XG_CUDA(cudaMemcpyAsync(wfn.qp.data(), qp, 6 * nat * sizeof(double), cudaMemcpyDeviceToHost, st));
+        tm.stop();
+        XG_CUDA(cudaStreamSynchronize(st));
+        scc_failed = false;
+        return;
+    }
 
     // ---- classical terms and integrals
     repulsion(st, m, erep, grad);

@@ -62,9 +62,11 @@ extern const char* const kPhaseNames[PH_COUNT];
 
 // Run the single point.  `wfn` is the warm-start wavefunction (used when sizes
 // match) and receives the converged one.  Throws std::runtime_error on failure;
-// `scc_failed` reports an unconverged SCC (results still filled).
+// `scc_failed` reports an unconverged SCC (results still filled).  With guess_only the
+// call stops after the initial guess and returns it in `wfn` (charges, shell charges,
+// zero or warm-start multipoles); `res` is not filled.
 void run_singlepoint(const HostMol& hm, const SPSettings& set, Wavefunction& wfn, SPResult& res, bool keep_orbitals,
-                     bool& scc_failed);
+                     bool& scc_failed, bool guess_only = false);
 
 // Number of CUDA devices visible (0 when none); never throws.
 int device_count();

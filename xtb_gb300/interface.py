@@ -66,6 +66,10 @@ def load_library(path=LIBPATH):
         "xtb_getOrbitalEigenvalues": (None, [vp, vp, dp]),
         "xtb_getOrbitalOccupations": (None, [vp, vp, dp]),
         "xtb_getOrbitalCoefficients": (None, [vp, vp, dp]),
+        "xtb_hessian": (None, [vp, vp, vp, vp, dp, ip, ip, dp, dp]),
+        "xtb_getVirial": (None, [vp, vp, dp]),
+        "xtb_getSolvationEnergy": (None, [vp, vp, dp]),
+        "xtb_getPCGradient": (None, [vp, vp, dp]),
         "xtbgb_deviceCount": (C.c_int, []),
         "xtbgb_getIterations": (None, [vp, vp, ip, ip]),
         "xtbgb_getEnergyParts": (None, [vp, vp, dp]),
@@ -160,6 +164,19 @@ class Calculator:
         self.lib.xtbgb_getShellCharges(self.env.h, self.res, _dptr(out))
         self.env.check()
         return out
+
+    def hessian(self, fresh=True):
+        """xtb_hessian: numerical Hessian [3N, 3N] (Eh/bohr^2) and dipole gradient [3N, 3];
+        ``fresh`` starts from a new results object, as the reference's C test does."""
+        if fresh:
+            self.lib.xtb_delResults(C.byref(self.res))
+            self.res = C.c_void_p(self.lib.xtb_newResults())
+        n3 = 3 * len(self.numbers)
+        hess = np.zeros((n3, n3))
+        dipgrad = np.zeros((n3, 3))
+        self.lib.xtb_hessian(self.env.h, self.mol, self.calc, self.res, _dptr(hess), None, None, _dptr(dipgrad), None)
+        self.env.check()
+        return hess, dipgrad
 
     def singlepoint(self, fresh=True):
         """Run xtb_singlepoint; ``fresh`` drops the warm-start wavefunction first."""
