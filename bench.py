@@ -175,7 +175,7 @@ def run_served(args, ws, rank):
     reqs = stream_requests(args)
     R = len(reqs)
     srv = X.Server(pool_gib=args.pool_gib, max_slots=1024, plain_workers=args.workers,
-                   iters_per_step=args.iters_per_step)
+                   iters_per_step=args.iters_per_step, precision=args.served_precision, slices=args.slices)
     for _ in range(args.warmup):
         served_pass(srv, reqs, args.rate)
     st0 = srv.stats()
@@ -247,6 +247,8 @@ def run_served(args, ws, rank):
         "config": {"workload": f"served stream: {R} requests, atoms log-uniform 3..1500 (alkanes C_nH_2n+2 and "
                                f"(H2O)_m, 1/2 each), gradient on 1/2, neutral, T_el 300 K, seed {args.seed}",
                    "arrival": f"Poisson {args.rate}/s" if args.rate else "all requests at t=0 (saturation)",
+                   "served_precision": (f"split products ({args.slices} bf16 digits) on the plain-engine workers"
+                                        if args.served_precision == "split" else "fp64"),
                    "pool_gib": args.pool_gib, "plain_workers": args.workers, "iters_per_step": args.iters_per_step,
                    "parallelism": f"replicas x{ws}",
                    "l2": "large requests hold n^2 matrices far above L2 (129 MB); no flush"},
@@ -277,11 +279,22 @@ def run_served(args, ws, rank):
 
 
 # ------------------------------------------------------------------ plain (H2O)300
+PLAIN_WORKLOADS = {
+    "h2o300": ("(H2O)300 seeded water cluster, 900 atoms, 1800 AOs, plain FP64 GPU single point",
+               lambda W: W.water_cluster(300, seed=1)),
+    "h2o1000": ("(H2O)1000 seeded water cluster, 3000 atoms, 6000 AOs, plain FP64 GPU single point",
+                lambda W: W.water_cluster(1000, seed=1)),
+    "c200h402": ("all-trans C200H402, sigma 0.02 A jitter, 602 atoms, 1202 AOs, plain FP64 GPU single point",
+                 lambda W: W.alkane(200, 0.02, seed=1)),
+}
+
+
 def run_plain(args, ws, rank):
     from xtb_gb300 import interface as X
     from xtb_gb300 import workloads as W
     dist_init(ws)
-    Z, xyz = W.water_cluster(300, seed=1)
+    desc, gen = PLAIN_WORKLOADS[args.workload]
+    Z, xyz = gen(W)
     lib = X.load_library()
     calc = X.Calculator(Z, xyz, keep_orbitals=False)
     for _ in range(args.warmup):
@@ -316,10 +329,10 @@ def run_plain(args, ws, rank):
         "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded generator, no public suite exists for this path)",
-        "config": {"workload": "(H2O)300 seeded water cluster, 900 atoms, 1800 AOs, plain FP64 GPU single point",
+        "config": {"workload": desc,
                    "atoms": int(len(Z)), "nao": int(nao), "scc_iterations": int(iters),
                    "parallelism": f"replicas x{ws}",
-                   "l2": "working set > L2 (n^2 matrices of ~26 MB each), no flush needed"},
+                   "l2": f"working set > L2 (n^2 matrices of {8 * nao * nao / 1e6:.0f} MB each), no flush needed"},
         "e2e": {"value": ws * args.steps / wall_s, "unit": "single points/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(launches),
@@ -338,6 +351,95 @@ def run_plain(args, ws, rank):
         out["cpu_baseline"] = cpu_baseline(args, [{"numbers": Zc, "positions": xc, "size": len(Zc)}],
                                            note="C10H22 (32 atoms) repeated")
     return out
+
+
+# ------------------------------------------------------------------ split precision vs FP64
+SPLIT_WORKLOADS = {
+    "split_c200h402": ("all-trans C200H402 (602 atoms, 1202 AOs), split-precision products vs FP64",
+                       lambda W: W.alkane(200, 0.02, seed=1)),
+    "split_h2o1000": ("(H2O)1000 seeded water cluster (3000 atoms, 6000 AOs), split-precision products vs FP64",
+                      lambda W: W.water_cluster(1000, seed=1)),
+}
+
+
+def run_split(args, ws, rank):
+    """Split-precision mode (back-transformation, P and W as BF16 tensor-core digit products) timed
+    over `steps` single points; the FP64 mode on the same molecule gives the reference for the
+    per-result errors |dE|, max |dq|, max |dg| and ||dP||_F / ||P||_F."""
+    from xtb_gb300 import interface as X
+    from xtb_gb300 import workloads as W
+    dist_init(ws)
+    desc, gen = SPLIT_WORKLOADS[args.workload]
+    Z, xyz = gen(W)
+    lib = X.load_library()
+    cs = X.Calculator(Z, xyz, keep_orbitals=False, precision="split", slices=args.slices)
+    for _ in range(args.warmup):
+        r = cs.singlepoint()
+    dist_barrier(ws)
+    clocks = ClockSampler(0)
+    clocks.start()
+    dev, wall = 0.0, 0.0
+    phase = np.zeros(len(PHASES))
+    launches = 0
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        r = cs.singlepoint()
+        wall += time.perf_counter() - t0
+        dev += r.phase_ms[-1] / 1e3
+        phase += r.phase_ms
+        launches += r.launches
+    dist_barrier(ws)
+    clk = clocks.stop()
+    dev = dist_max(dev, ws)
+    wall = dist_max(wall, ws)
+    if rank != 0:
+        return None
+    # FP64 mode and both densities (orbitals kept) for the error report
+
+    def density(calc, res):
+        """P = sum_j f_j c_j c_j^T from xtb_getOrbitalCoefficients (rows = orbitals)."""
+        import ctypes as C
+        nn = res.nao
+        c = np.zeros((nn, nn))
+        calc.lib.xtb_getOrbitalCoefficients(calc.env.h, calc.res, c.ctypes.data_as(C.POINTER(C.c_double)))
+        calc.env.check()
+        return (c.T * res.focc) @ c
+
+    cf = X.Calculator(Z, xyz, keep_orbitals=True)
+    f = cf.singlepoint()
+    csp = X.Calculator(Z, xyz, keep_orbitals=True, precision="split", slices=args.slices)
+    s = csp.singlepoint()
+    Pf, Ps = density(cf, f), density(csp, s)
+    err = {"max_abs_dE": abs(s.energy - f.energy), "max_abs_dq": float(np.max(np.abs(s.charges - f.charges))),
+           "max_abs_dg": float(np.max(np.abs(s.gradient - f.gradient))), "iterations": [f.iterations, s.iterations],
+           "rel_frobenius_dP": float(np.linalg.norm(Ps - Pf) / np.linalg.norm(Pf))}
+    per = phase / args.steps
+    peak = lib.xtbgb_fp64PeakTflops()
+    n = r.nao
+    sy = per[PHASES.index("sytrd")]
+    ach = (4.0 / 3.0) * float(n) ** 3 * r.iterations / (sy * 1e-3) / 1e12
+    return {
+        "metric": METRIC + ", split-precision products (BF16 tensor cores) vs FP64",
+        "value": ws * args.steps / dev, "unit": "single points/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * dev / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": f"f64 (products: bf16 digits x{args.slices}, fp32 accumulate)",
+        "data": "synthetic (seeded generator)",
+        "config": {"workload": desc, "atoms": int(len(Z)), "nao": int(n), "slices": args.slices,
+                   "parallelism": f"replicas x{ws}", "l2": "n^2 matrices above L2; no flush"},
+        "fp64_mode": {"value": 1e3 / f.phase_ms[-1], "unit": "single points/s"},
+        "error_vs_fp64": err,
+        "e2e": {"value": ws * args.steps / wall, "unit": "single points/s", "h2d_bytes_per_step": int(r.h2d_bytes),
+                "d2h_bytes_per_step": int(r.d2h_bytes)},
+        "gpu_launches": int(launches),
+        "phase_ms_per_step": {k: round(float(v), 3) for k, v in zip(PHASES, per)},
+        "roofline": {"bound": "fp64", "kernel": "k_sytrd", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
+                     "frac": ach / peak if peak else None,
+                     "traffic": SYTRD_BYTES_PER_ELEM * float(n) ** 2, "traffic_unit": "bytes per launch",
+                     "note": "the tridiagonalisation stays FP64 and dominates; split products are in "
+                             "backtransform/density/gradient",
+                     "peak_source": "measured FP64 FMA throughput of this GPU"},
+        "clocks": clk,
+    }
 
 
 # ------------------------------------------------------------------ batched 4096
@@ -429,7 +531,7 @@ def run_reference(args, ws, rank):
     if rank != 0:
         return None
     from xtb_gb300 import workloads as W
-    if args.workload == "h2o300":
+    if args.workload in PLAIN_WORKLOADS or args.workload in SPLIT_WORKLOADS:
         Zc, xc = W.alkane(10, 0.02, seed=1)
         reqs = [{"numbers": Zc, "positions": xc, "size": len(Zc)}] * 64
         wl = "C10H22 (32 atoms) single points on the CPU restatement (the (H2O)300 point takes minutes)"
@@ -465,7 +567,11 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="served", choices=["served", "h2o300", "batch4096"])
+    ap.add_argument("--workload", default="served",
+                    choices=["served", "batch4096"] + sorted(PLAIN_WORKLOADS) + sorted(SPLIT_WORKLOADS))
+    ap.add_argument("--slices", type=int, default=5, help="split workloads: digits per operand")
+    ap.add_argument("--served-precision", default="split", choices=["split", "fp64"],
+                    help="served: precision of the plain-engine workers' products")
     ap.add_argument("--requests", type=int, default=64, help="served: requests per pass")
     ap.add_argument("--seed", type=int, default=11, help="served: stream seed")
     ap.add_argument("--rate", type=float, default=None, help="served: Poisson arrival rate (default: saturation)")
@@ -480,7 +586,10 @@ def main():
     if args.impl == "reference":
         out = run_reference(args, ws, rank)
     else:
-        out = {"served": run_served, "h2o300": run_plain, "batch4096": run_batch}[args.workload](args, ws, rank)
+        run = {"served": run_served, "batch4096": run_batch}.get(args.workload)
+        if run is None:
+            run = run_split if args.workload in SPLIT_WORKLOADS else run_plain
+        out = run(args, ws, rank)
     if out is not None:
         print(json.dumps(out))
 

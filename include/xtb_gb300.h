@@ -43,6 +43,13 @@ extern void xtbgb_getTransferBytes(xtb_TEnvironment env, xtb_TResults res, long 
  * single point; needed by xtb_getOrbitalCoefficients.  Default 1 (as the reference). */
 extern void xtbgb_setKeepOrbitals(xtb_TEnvironment env, xtb_TCalculator calc, int keep);
 
+/* Precision of the calculator's dense products: split = 0 (default) keeps every product in
+ * FP64; split = 1 computes the back-transformation C = X Z, the density P = C f C^T and the
+ * energy-weighted density as split-precision products on the BF16 tensor cores with `slices`
+ * (4..7) digits of 8 bits per operand (5: about 2^-40 relative error per product term).  The
+ * Cholesky factorisation, the reduction to standard form and the eigensolver stay FP64. */
+extern void xtbgb_setPrecision(xtb_TEnvironment env, xtb_TCalculator calc, int split, int slices);
+
 /* Measured FP64 FMA throughput of device 0 in TFLOP/s (roofline denominator for FP64 kernels);
  * returns 0 when no device is present. */
 extern double xtbgb_fp64PeakTflops(void);
@@ -51,6 +58,13 @@ extern double xtbgb_fp64PeakTflops(void);
  * cycles[0] FP64 FMA, [1] FP64 add, [2] FP64 multiply, [3] FP64 divide, [4] FP32 FMA
  * (all 0 when no device is present). */
 extern void xtbgb_fp64LatencyCycles(double* cycles);
+
+/* Check and time the split-precision GEMM (FP64 results from BF16 tensor-core products of
+ * fixed-point digit slices) against the FP64 GEMM on seeded random M x K and K x N matrices
+ * with entries uniform(-1,1) * 2^-e, e in [0, exp_range].  out[0] max |dC| / (|A||B|),
+ * out[1] max |dC| / max |C|, out[2] split ms, out[3] FP64 ms, out[4] split TFLOP/s, out[5] FP64
+ * TFLOP/s.  slices 4..7.  Returns 0 on success. */
+extern int xtbgb_splitGemmCheck(int M, int N, int K, int slices, int seed, int exp_range, double* out);
 
 /* ---- Batched single points (no counterpart in the reference: the reference API runs one
  * molecule per call).  Many molecules of uneven size are solved together on the device, one
@@ -97,6 +111,11 @@ typedef struct _xtbgb_TServer* xtbgb_TServer;
 
 extern xtbgb_TServer xtbgb_newServer(xtb_TEnvironment env, double pool_gib, int max_slots, int plain_workers,
                                      int iters_per_step, double accuracy, double etemp, int maxiter);
+/* As xtbgb_newServer; split = 1 runs the plain-engine workers with split-precision products
+ * (xtbgb_setPrecision semantics, `slices` digits). */
+extern xtbgb_TServer xtbgb_newServerEx(xtb_TEnvironment env, double pool_gib, int max_slots, int plain_workers,
+                                       int iters_per_step, double accuracy, double etemp, int maxiter, int split,
+                                       int slices);
 /* Finishes all submitted work, then frees the server. */
 extern void xtbgb_delServer(xtbgb_TServer* server);
 /* Queue one GFN2-xTB single point (positions [natoms][3] Bohr); returns the request id, or

@@ -1,0 +1,47 @@
+"""Split-precision mode of the engine (back-transformation, density and energy-weighted
+density as BF16 tensor-core digit products) against the FP64 mode and the oracle.
+
+Bar: the benchmark spec's tolerances against the oracle (|dE| <= 1e-6 Eh, charges <= 1e-5 e,
+gradient <= 1e-5 Eh/bohr, iterations +-1); against the FP64 mode of the same engine the
+differences are reported and bounded tighter (1e-8 Eh, 1e-7).
+"""
+import numpy as np
+import pytest
+
+from helpers import TOL_E, TOL_G, TOL_ITER, TOL_Q, case_geometry, golden
+from oracle import gfn2
+from xtb_gb300 import interface as X
+from xtb_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def both(Z, xyz, slices=5):
+    f = X.Calculator(Z, xyz, keep_orbitals=False).singlepoint()
+    s = X.Calculator(Z, xyz, keep_orbitals=False, precision="split", slices=slices).singlepoint()
+    return f, s
+
+
+@pytest.mark.parametrize("mol", ["water30", "decane", "propyne"])
+def test_split_matches_fp64_and_oracle(mol):
+    if mol == "water30":
+        Z, xyz = W.water_cluster(30, seed=1)
+    elif mol == "decane":
+        Z, xyz = W.alkane(10, 0.02, seed=1)
+    else:
+        Z, xyz = case_geometry(golden()["capi"])
+    f, s = both(Z, xyz)
+    assert abs(s.energy - f.energy) <= 1e-8
+    assert np.max(np.abs(s.charges - f.charges)) <= 1e-7
+    assert np.max(np.abs(s.gradient - f.gradient)) <= 1e-7
+    assert abs(s.iterations - f.iterations) <= TOL_ITER
+    o = gfn2.singlepoint(np.asarray(Z), np.asarray(xyz, dtype=float))
+    assert abs(s.energy - o.energy) <= TOL_E
+    assert np.max(np.abs(s.charges - o.q)) <= TOL_Q
+    assert np.max(np.abs(s.gradient - o.gradient)) <= TOL_G
+
+
+def test_split_rejects_bad_slice_count():
+    Z, xyz = W.alkane(2, 0.02, seed=1)
+    with pytest.raises(X.XTBException, match="4..7"):
+        X.Calculator(Z, xyz, precision="split", slices=3)

@@ -20,6 +20,7 @@
 #include "batch.h"
 #include "engine.h"
 #include "serve.h"
+#include "splitgemm.h"
 #include "host_model.h"
 #include "linalg.h"
 
@@ -595,6 +596,17 @@ void xtbgb_fp64LatencyCycles(double* cycles) {
     }
 }
 
+int xtbgb_splitGemmCheck(int M, int N, int K, int slices, int seed, int exp_range, double* out) {
+    if (!out || M < 1 || N < 1 || K < 1 || slices < 4 || slices > 7) return 1;
+    if (xg::device_count() == 0) return 2;
+    try {
+        xg::split_gemm_check(M, N, K, slices, (unsigned)seed, exp_range, out);
+    } catch (const std::exception&) {
+        return 3;
+    }
+    return 0;
+}
+
 double xtbgb_fp64PeakTflops(void) {
     if (xg::device_count() == 0) return 0.0;
     try {
@@ -627,6 +639,20 @@ void xtbgb_getTransferBytes(xtb_TEnvironment env, xtb_TResults res, long long* b
     bytes[0] = res->sp.h2d_bytes;
     bytes[1] = res->sp.d2h_bytes;
     bytes[2] = res->sp.launches;
+}
+
+void xtbgb_setPrecision(xtb_TEnvironment env, xtb_TCalculator calc, int split, int slices) {
+    if (!check_env(env)) return;
+    if (!calc) {
+        env->error("Singlepoint calculator is not allocated", "xtbgb_setPrecision");
+        return;
+    }
+    if (split && (slices < 4 || slices > 7)) {
+        env->error("Split precision needs 4..7 slices", "xtbgb_setPrecision");
+        return;
+    }
+    calc->set.precision = split ? 1 : 0;
+    calc->set.slices = slices;
 }
 
 void xtbgb_setKeepOrbitals(xtb_TEnvironment env, xtb_TCalculator calc, int keep) {
@@ -806,6 +832,12 @@ struct _xtbgb_TServer {
 
 xtbgb_TServer xtbgb_newServer(xtb_TEnvironment env, double pool_gib, int max_slots, int plain_workers,
                               int iters_per_step, double accuracy, double etemp, int maxiter) {
+    return xtbgb_newServerEx(env, pool_gib, max_slots, plain_workers, iters_per_step, accuracy, etemp, maxiter, 0, 5);
+}
+
+xtbgb_TServer xtbgb_newServerEx(xtb_TEnvironment env, double pool_gib, int max_slots, int plain_workers,
+                                int iters_per_step, double accuracy, double etemp, int maxiter, int split,
+                                int slices) {
     static const char* src = "xtbgb_newServer";
     if (!check_env(env)) return nullptr;
     xg::ServeConfig cfg;
@@ -816,6 +848,12 @@ xtbgb_TServer xtbgb_newServer(xtb_TEnvironment env, double pool_gib, int max_slo
     cfg.set.accuracy = std::min(std::max(accuracy, 1.0e-4), 1.0e3);
     cfg.set.etemp = std::max(etemp, 1.0e-6);
     cfg.set.maxiter = std::max(maxiter, 1);
+    if (split && (slices < 4 || slices > 7)) {
+        env->error("Split precision needs 4..7 slices", src);
+        return nullptr;
+    }
+    cfg.precision = split ? 1 : 0;
+    cfg.slices = slices;
     auto* s = new _xtbgb_TServer();
     try {
         s->srv = std::make_unique<xg::Server>(cfg);

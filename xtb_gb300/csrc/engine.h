@@ -11,6 +11,11 @@ struct SPSettings {
     double accuracy = 1.0;     // xtb_setAccuracy
     double etemp = 300.0;      // xtb_setElectronicTemp (K)
     int maxiter = 250;         // xtb_setMaxIter
+    // 0: every product in FP64; 1: the back-transformation, density and energy-weighted density
+    // products as split-precision tensor-core GEMMs (`slices` digits of 8 bits); the Cholesky,
+    // the reduction to standard form and the eigensolver stay FP64
+    int precision = 0;
+    int slices = 5;
 };
 
 // Wavefunction kept between calls on the same results object (res%chk of the reference).

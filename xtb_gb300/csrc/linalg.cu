@@ -14,6 +14,7 @@
 
 #include "linalg.h"
 #include "linalg_device.cuh"
+#include "splitgemm.h"
 
 namespace cg = cooperative_groups;
 
@@ -37,6 +38,64 @@ void dgemm(cudaStream_t st, bool ta, bool tb, int M, int N, int K, double alpha,
     else if (ta && !tb) k_dgemm<true, false><<<grid, 256, 0, st>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, flags, dK, dN);
     else if (!ta && tb) k_dgemm<false, true><<<grid, 256, 0, st>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, flags, dK, dN);
     else k_dgemm<true, true><<<grid, 256, 0, st>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, flags, dK, dN);
+    XG_LAUNCH_CHECK();
+}
+
+// ------------------------------------------------------------------ split-K GEMM
+// Skinny products with a long K (the Gram matrix and the projections of the blocked
+// back-transformation) have few output tiles; grid.z splits K so that every SM gets work.
+// Slice z writes its partial product to P + z * M * N (row-major, ld N); k_reduce_slices sums
+// the slices in a fixed order (deterministic, no atomics).
+template <bool TA, bool TB>
+__global__ void __launch_bounds__(256) k_dgemm_slices(int M, int N, int K, int kc, const double* __restrict__ A,
+                                                      int lda, const double* __restrict__ B, int ldb,
+                                                      double* __restrict__ P, const int* __restrict__ dN) {
+    __shared__ double smem[GEMM_SMEM];
+    const int z = blockIdx.z, k0 = z * kc;
+    const int kn = min(kc, K - k0);
+    const double* Az = TA ? A + (size_t)k0 * lda : A + k0;
+    const double* Bz = TB ? B + k0 : B + (size_t)k0 * ldb;
+    double* Pz = P + (size_t)z * M * N;
+    if (kn <= 0) {
+        // empty slice: zero its tile so that the reduction can sum every slice
+        const int i0 = blockIdx.y * GBM, j0 = blockIdx.x * GBN;
+        for (int t = threadIdx.x; t < GBM * GBN; t += blockDim.x) {
+            const int i = i0 + t / GBN, j = j0 + t % GBN;
+            if (i < M && j < N) Pz[(size_t)i * N + j] = 0.0;
+        }
+        return;
+    }
+    dgemm_tile<TA, TB>(M, N, kn, 1.0, Az, lda, Bz, ldb, 0.0, Pz, N, 0, nullptr, dN, blockIdx.y * GBM,
+                       blockIdx.x * GBN, smem);
+}
+
+__global__ void k_reduce_slices(int M, int N, int nsplit, double alpha, const double* __restrict__ P, double beta,
+                                double* __restrict__ C, int ldc, const int* __restrict__ dN) {
+    const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long)M * N) return;
+    const int i = (int)(t / N), j = (int)(t % N);
+    if (dN && j >= *dN) return;
+    double s = 0.0;
+    for (int z = 0; z < nsplit; ++z) s += P[(size_t)z * M * N + t];
+    double v = alpha * s;
+    if (beta != 0.0) v += beta * C[(size_t)i * ldc + j];
+    C[(size_t)i * ldc + j] = v;
+}
+
+void dgemm_splitk(cudaStream_t st, bool ta, bool tb, int M, int N, int K, double alpha, const double* A, int lda,
+                  const double* B, int ldb, double beta, double* C, int ldc, int nsplit, double* partial,
+                  const int* dN) {
+    if (M <= 0 || N <= 0) return;
+    nsplit = std::max(1, std::min(nsplit, std::max(1, K / 64)));
+    const int kc = ((ceil_div(K, nsplit) + GBK - 1) / GBK) * GBK;
+    nsplit = ceil_div(K, kc);
+    dim3 grid(ceil_div(N, GBN), ceil_div(M, GBM), nsplit);
+    if (!ta && !tb) k_dgemm_slices<false, false><<<grid, 256, 0, st>>>(M, N, K, kc, A, lda, B, ldb, partial, dN);
+    else if (ta && !tb) k_dgemm_slices<true, false><<<grid, 256, 0, st>>>(M, N, K, kc, A, lda, B, ldb, partial, dN);
+    else if (!ta && tb) k_dgemm_slices<false, true><<<grid, 256, 0, st>>>(M, N, K, kc, A, lda, B, ldb, partial, dN);
+    else k_dgemm_slices<true, true><<<grid, 256, 0, st>>>(M, N, K, kc, A, lda, B, ldb, partial, dN);
+    XG_LAUNCH_CHECK();
+    k_reduce_slices<<<ceil_div((long)M * N, 256), 256, 0, st>>>(M, N, nsplit, alpha, partial, beta, C, ldc, dN);
     XG_LAUNCH_CHECK();
 }
 
@@ -261,6 +320,96 @@ __global__ void k_ormtr(int n, const double* __restrict__ V, const double* __res
     const int j = blockIdx.x * wpb + wib;
     if (j >= n || (ncol && j >= *ncol)) return;
     d_ormtr(n, V, tau, Y, Zt, j, lane, sm + (size_t)wib * n);
+}
+
+// ------------------------------------------------------------------ blocked back-transformation
+constexpr int ORM_NB = 128;     // reflectors per block
+constexpr int ORM_SPLIT = 16;   // K slices of the skinny products
+
+// T (kn x kn, upper) of the compact WY form H(0) ... H(kn-1) = I - V T V^T from the Gram matrix
+// S = V^T V and tau (dlarft, forward, columnwise: T(:i, i) = -tau_i T(:i, :i) S(:i, i)).
+__global__ void k_larft(int kn, const double* __restrict__ tau, const double* __restrict__ S, int lds,
+                        double* __restrict__ T, int ldt) {
+    __shared__ double w[ORM_NB];
+    for (int i = 0; i < kn; ++i) {
+        for (int j = threadIdx.x; j < i; j += blockDim.x) w[j] = S[(size_t)j * lds + i];
+        __syncthreads();
+        const double ti = tau[i];
+        for (int j = threadIdx.x; j < kn; j += blockDim.x) {
+            double v = 0.0;
+            if (j < i) {
+                double sum = 0.0;
+                for (int l = j; l < i; ++l) sum = fma(T[(size_t)j * ldt + l], w[l], sum);
+                v = -ti * sum;
+            } else if (j == i) {
+                v = ti;
+            }
+            T[(size_t)j * ldt + i] = v;
+        }
+        __syncthreads();
+    }
+}
+
+size_t ormtr_workspace(int n) {
+    return (size_t)ORM_SPLIT * ORM_NB * std::max(n, ORM_NB) + 2 * (size_t)ORM_NB * n + 2 * (size_t)ORM_NB * ORM_NB;
+}
+
+void ormtr_blocked(cudaStream_t st, int n, const double* V, const double* tau, double* Y, const int* d_ncol,
+                   double* work, int slices, void* split_work) {
+    if (n < 3) return;
+    double* partial = work;
+    double* G = partial + (size_t)ORM_SPLIT * ORM_NB * std::max(n, ORM_NB);
+    double* G2 = G + (size_t)ORM_NB * n;
+    double* S = G2 + (size_t)ORM_NB * n;
+    double* T = S + (size_t)ORM_NB * ORM_NB;
+    const int nref = n - 2;
+    for (int k0 = ((nref - 1) / ORM_NB) * ORM_NB; k0 >= 0; k0 -= ORM_NB) {
+        const int kn = std::min(ORM_NB, nref - k0);
+        const int r0 = k0 + 1, m = n - r0;
+        const double* Vb = V + (size_t)k0 * n + r0;   // kn rows of length m (zeros above each vector's start)
+        // S = Vb Vb^T, T from S and tau
+        dgemm_splitk(st, false, true, kn, kn, m, 1.0, Vb, n, Vb, n, 0.0, S, ORM_NB, ORM_SPLIT, partial, nullptr);
+        k_larft<<<1, 64, 0, st>>>(kn, tau + k0, S, ORM_NB, T, ORM_NB);
+        XG_LAUNCH_CHECK();
+        // G = Vb Y[r0:, :ncol];  G2 = T G;  Y[r0:, :ncol] -= Vb^T G2
+        if (slices) {
+            split_gemm(st, false, false, kn, n, m, 1.0, Vb, n, Y + (size_t)r0 * n, n, 0.0, G, n, slices, split_work,
+                       nullptr, d_ncol);
+        } else {
+            dgemm_splitk(st, false, false, kn, n, m, 1.0, Vb, n, Y + (size_t)r0 * n, n, 0.0, G, n, ORM_SPLIT,
+                         partial, d_ncol);
+        }
+        dgemm(st, false, false, kn, n, kn, 1.0, T, ORM_NB, G, n, 0.0, G2, n, GF_A_UPPER, nullptr, d_ncol);
+        if (slices)
+            split_gemm(st, true, false, m, n, kn, -1.0, Vb, n, G2, n, 1.0, Y + (size_t)r0 * n, n, slices, split_work,
+                       nullptr, d_ncol);
+        else
+            dgemm(st, true, false, m, n, kn, -1.0, Vb, n, G2, n, 1.0, Y + (size_t)r0 * n, n, 0, nullptr, d_ncol);
+    }
+}
+
+// Same as k_ormtr, but vector j is read from and written back to column j of Y.
+__global__ void k_ormtr_inplace(int n, const double* __restrict__ V, const double* __restrict__ tau,
+                                double* __restrict__ Y, const int* __restrict__ ncol) {
+    extern __shared__ double sm[];
+    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int wpb = blockDim.x >> 5;
+    const int j = blockIdx.x * wpb + wib;
+    if (j >= n || (ncol && j >= *ncol)) return;
+    double* y = sm + (size_t)wib * n;
+    d_ormtr_apply(n, V, tau, Y, j, lane, y);   // result in y (shared)
+    __syncwarp();
+    for (int i = lane; i < n; i += 32) Y[(size_t)i * n + j] = y[i];
+}
+
+void ormtr_inplace(cudaStream_t st, int n, const double* V, const double* tau, double* Y, const int* ncol) {
+    int wpb = 4;
+    size_t smem = (size_t)wpb * n * sizeof(double);
+    while (wpb > 1 && smem > 200 * 1024) { wpb >>= 1; smem = (size_t)wpb * n * sizeof(double); }
+    if (smem > 48 * 1024)
+        XG_CUDA(cudaFuncSetAttribute(k_ormtr_inplace, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_ormtr_inplace<<<ceil_div(n, wpb), wpb * 32, smem, st>>>(n, V, tau, Y, ncol);
+    XG_LAUNCH_CHECK();
 }
 
 void ormtr(cudaStream_t st, int n, const double* V, const double* tau, const double* Y, double* Zt, const int* ncol) {

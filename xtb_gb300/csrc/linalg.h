@@ -29,6 +29,19 @@ void tridiag_eigvecs(cudaStream_t st, int n, const double* d, const double* e, c
 // Zt[j][:] = Q Y[:, j] for j < *ncol (all if null)
 void ormtr(cudaStream_t st, int n, const double* V, const double* tau, const double* Y, double* Zt,
            const int* ncol = nullptr);
+// Y[:, j] = Q Y[:, j] in place for j < *ncol (all if null), Q = H(0) ... H(n-3): compact-WY blocks
+// of 128 reflectors applied as GEMMs; work: ormtr_workspace(n) doubles
+size_t ormtr_workspace(int n);
+// the same product, one warp per vector, in place (better below a few thousand AOs)
+void ormtr_inplace(cudaStream_t st, int n, const double* V, const double* tau, double* Y, const int* ncol);
+// slices > 0: the two large products per block as split-precision tensor-core GEMMs (split_work:
+// split_gemm_workspace(n, n, n, slices) bytes)
+void ormtr_blocked(cudaStream_t st, int n, const double* V, const double* tau, double* Y, const int* ncol,
+                   double* work, int slices = 0, void* split_work = nullptr);
+// C = alpha op(A) op(B) + beta C with K split into nsplit slices (partial: nsplit * M * N doubles)
+void dgemm_splitk(cudaStream_t st, bool ta, bool tb, int M, int N, int K, double alpha, const double* A, int lda,
+                  const double* B, int ldb, double beta, double* C, int ldc, int nsplit, double* partial,
+                  const int* dN = nullptr);
 // measured FP64 FMA throughput of the current device (TFLOP/s)
 double fp64_peak_tflops();
 // dependent-operation latency in cycles: [0] FP64 FMA, [1] FP64 add, [2] FP64 multiply,

@@ -19,45 +19,47 @@ constexpr int GBM = 64, GBN = 64, GBK = 16;
 //   GF_A_UPPER  op(A)[i,k] = 0 for k < i      (k >= i0 per tile)
 //   GF_SYM      C symmetric: only tiles touching the lower triangle are computed (mirror afterwards)
 // dK / dN (optional, device): K and N limited to *dK / *dN at run time.
-// One 64x64 tile (i0, j0) of the product, computed by a 256-thread block.
-template <bool TA, bool TB>
+// One TB x TB tile (i0, j0) of the product (TB = 64 or 32), computed by a 256-thread block: thread
+// (tx, ty) owns rows ty + 16 r and columns tx + 16 c, r, c < TB / 16.
+template <bool TA, bool TB, int TBS = GBM>
 __device__ inline void dgemm_tile(int M, int N, int K, double alpha, const double* __restrict__ A, int lda,
                            const double* __restrict__ B, int ldb, double beta, double* __restrict__ C, int ldc,
                            int flags, const int* __restrict__ dK, const int* __restrict__ dN, int i0, int j0,
                            double* smem) {
-    double (*As)[GBK][GBM + 1] = reinterpret_cast<double (*)[GBK][GBM + 1]>(smem);
-    double (*Bs)[GBK][GBN + 1] = reinterpret_cast<double (*)[GBK][GBN + 1]>(smem + 2 * GBK * (GBM + 1));
+    constexpr int TM = TBS, TN = TBS, R = TBS / 16;
+    double (*As)[GBK][TM + 1] = reinterpret_cast<double (*)[GBK][TM + 1]>(smem);
+    double (*Bs)[GBK][TN + 1] = reinterpret_cast<double (*)[GBK][TN + 1]>(smem + 2 * GBK * (TM + 1));
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
     if (dN) N = min(N, *dN);
     if (j0 >= N) return;
-    if ((flags & GF_SYM) && j0 >= i0 + GBM) return;
+    if ((flags & GF_SYM) && j0 >= i0 + TM) return;
     if (dK) K = min(K, *dK);
     int kbeg = 0, kend = K;
-    if (flags & GF_B_UPPER) kend = min(kend, j0 + GBN);
-    if (flags & GF_A_LOWER) kend = min(kend, i0 + GBM);
+    if (flags & GF_B_UPPER) kend = min(kend, j0 + TN);
+    if (flags & GF_A_LOWER) kend = min(kend, i0 + TM);
     if (flags & GF_A_UPPER) kbeg = (i0 / GBK) * GBK;
-    double acc[4][4];
+    double acc[R][R];
 #pragma unroll
-    for (int r = 0; r < 4; ++r)
+    for (int r = 0; r < R; ++r)
 #pragma unroll
-        for (int c = 0; c < 4; ++c) acc[r][c] = 0.0;
+        for (int c = 0; c < R; ++c) acc[r][c] = 0.0;
 
     auto load = [&](int buf, int k0) {
 #pragma unroll
-        for (int s = 0; s < (GBM * GBK) / 256; ++s) {
+        for (int s = 0; s < (TM * GBK) / 256; ++s) {
             const int t = threadIdx.x + s * 256;
             int ii, kk;
-            if (TA) { ii = t % GBM; kk = t / GBM; } else { kk = t % GBK; ii = t / GBK; }
+            if (TA) { ii = t % TM; kk = t / TM; } else { kk = t % GBK; ii = t / GBK; }
             const int gi = i0 + ii, gk = k0 + kk;
             double v = 0.0;
             if (gi < M && gk < kend) v = TA ? A[(size_t)gk * lda + gi] : A[(size_t)gi * lda + gk];
             As[buf][kk][ii] = v;
         }
 #pragma unroll
-        for (int s = 0; s < (GBN * GBK) / 256; ++s) {
+        for (int s = 0; s < (TN * GBK) / 256; ++s) {
             const int t = threadIdx.x + s * 256;
             int jj, kk;
-            if (TB) { kk = t % GBK; jj = t / GBK; } else { jj = t % GBN; kk = t / GBN; }
+            if (TB) { kk = t % GBK; jj = t / GBK; } else { jj = t % TN; kk = t / TN; }
             const int gj = j0 + jj, gk = k0 + kk;
             double v = 0.0;
             if (gj < N && gk < kend) v = TB ? B[(size_t)gj * ldb + gk] : B[(size_t)gk * ldb + gj];
@@ -72,25 +74,25 @@ __device__ inline void dgemm_tile(int M, int N, int K, double alpha, const doubl
         if (k0 + GBK < kend) load(buf ^ 1, k0 + GBK);
 #pragma unroll
         for (int kk = 0; kk < GBK; ++kk) {
-            double a[4], b[4];
+            double a[R], b[R];
 #pragma unroll
-            for (int r = 0; r < 4; ++r) a[r] = As[buf][kk][ty + 16 * r];
+            for (int r = 0; r < R; ++r) a[r] = As[buf][kk][ty + 16 * r];
 #pragma unroll
-            for (int c = 0; c < 4; ++c) b[c] = Bs[buf][kk][tx + 16 * c];
+            for (int c = 0; c < R; ++c) b[c] = Bs[buf][kk][tx + 16 * c];
 #pragma unroll
-            for (int r = 0; r < 4; ++r)
+            for (int r = 0; r < R; ++r)
 #pragma unroll
-                for (int c = 0; c < 4; ++c) acc[r][c] = fma(a[r], b[c], acc[r][c]);
+                for (int c = 0; c < R; ++c) acc[r][c] = fma(a[r], b[c], acc[r][c]);
         }
         __syncthreads();
         buf ^= 1;
     }
 #pragma unroll
-    for (int r = 0; r < 4; ++r) {
+    for (int r = 0; r < R; ++r) {
         const int i = i0 + ty + 16 * r;
         if (i >= M) continue;
 #pragma unroll
-        for (int c = 0; c < 4; ++c) {
+        for (int c = 0; c < R; ++c) {
             const int j = j0 + tx + 16 * c;
             if (j >= N) continue;
             double v = alpha * acc[r][c];
@@ -104,13 +106,16 @@ __device__ inline void dgemm_tile(int M, int N, int K, double alpha, const doubl
 constexpr int GEMM_SMEM = 2 * GBK * (GBM + 1) + 2 * GBK * (GBN + 1);
 
 // Whole product by one 256-thread block (tiles in sequence); used for small per-molecule matrices.
+// 32 x 32 tiles: for the few-hundred-AO matrices of a batch, 64 x 64 tiles would compute up to
+// 2.5x the needed products on padding (the FP64 pipe is the limit there).
 // smem: GEMM_SMEM doubles of shared memory.
 template <bool TA, bool TB>
 __device__ inline void cta_dgemm(int M, int N, int K, double alpha, const double* A, int lda, const double* B, int ldb,
                           double beta, double* C, int ldc, int flags, const int* dK, const int* dN, double* smem) {
-    for (int i0 = 0; i0 < M; i0 += GBM)
-        for (int j0 = 0; j0 < N; j0 += GBN) {
-            dgemm_tile<TA, TB>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, flags, dK, dN, i0, j0, smem);
+    constexpr int T = 32;
+    for (int i0 = 0; i0 < M; i0 += T)
+        for (int j0 = 0; j0 < N; j0 += T) {
+            dgemm_tile<TA, TB, T>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, flags, dK, dN, i0, j0, smem);
             __syncthreads();
         }
 }
@@ -614,8 +619,8 @@ __device__ inline void d_reorth(int n, const double* __restrict__ w, const doubl
 // ------------------------------------------------------------------ back-transformation
 // Zt[j][:] = Q * Y[:, j] for every eigenvector j (one warp per eigenvector, vector staged in shared memory).
 // y: n doubles of shared memory owned by the calling warp.
-__device__ inline void d_ormtr(int n, const double* __restrict__ V, const double* __restrict__ tau,
-                        const double* __restrict__ Y, double* __restrict__ Zt, int j, int lane, double* y) {
+__device__ inline void d_ormtr_apply(int n, const double* __restrict__ V, const double* __restrict__ tau,
+                                     const double* __restrict__ Y, int j, int lane, double* y) {
     for (int i = lane; i < n; i += 32) y[i] = Y[(size_t)i * n + j];
     __syncwarp();
     for (int k = n - 3; k >= 0; --k) {
@@ -628,6 +633,11 @@ __device__ inline void d_ormtr(int n, const double* __restrict__ V, const double
         for (int i = k + 1 + lane; i < n; i += 32) y[i] -= s * vk[i];
         __syncwarp();
     }
+}
+
+__device__ inline void d_ormtr(int n, const double* __restrict__ V, const double* __restrict__ tau,
+                        const double* __restrict__ Y, double* __restrict__ Zt, int j, int lane, double* y) {
+    d_ormtr_apply(n, V, tau, Y, j, lane, y);
     for (int i = lane; i < n; i += 32) Zt[(size_t)j * n + i] = y[i];
 }
 

@@ -248,6 +248,8 @@ void Server::plain_loop() {
             ps.accuracy = cfg_.set.accuracy;
             ps.etemp = cfg_.set.etemp;
             ps.maxiter = cfg_.set.maxiter;
+            ps.precision = cfg_.precision;
+            ps.slices = cfg_.slices;
             Wavefunction wfn;
             SPResult res;
             bool failed = false;

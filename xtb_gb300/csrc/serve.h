@@ -27,6 +27,7 @@ struct ServeConfig {
     int max_slots = 1024;                     // resident molecules at most
     int plain_workers = 4;                    // concurrent plain-engine single points
     int iters_per_step = 4;                   // SCC iterations per pool step
+    int precision = 0, slices = 5;            // plain-engine workers: 1 = split-precision products
     BatchSettings set;
 };
 

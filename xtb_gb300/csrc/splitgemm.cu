@@ -1,0 +1,327 @@
+// Split-precision GEMM on the BF16 tensor cores with FP64-level results.
+//
+// C = alpha op(A) op(B) + beta C for FP64 operands, computed from fixed-point slices:
+// every row of op(A) (column of op(B)) is scaled by a power of two s_i (t_j) so that
+// |x| < 1, and cut into S digits of 8 bits, x / s = sum_{p=1..S} d_p 2^(-8p) with integer
+// d_p in [-256, 256] -- exactly representable in BF16.  A digit product d_p e_q is exact in
+// FP32 (16 bits), and the tensor cores' FP32 sums of such products over a K chunk of 128
+// stay below 2^24, so they are exact too.  Products are grouped by level p + q <= S + 1
+// (the lower levels carry less than 2^(-8S) of the result and are dropped), each level is
+// summed exactly over a chunk, and the chunks are recombined in FP64 with the weights
+// 2^(-8(p+q)).  The only errors are the truncation to S digits and the FP64 additions:
+// with S = 5 the relative error per product term is about 2^-40.
+//
+// The products run as mma.sync.m16n8k16 (BF16 in, FP32 accumulate) from shared memory;
+// S(S+1)/2 tensor-core products replace one FP64 product.
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cstdint>
+
+#include "linalg.h"
+#include "splitgemm.h"
+
+namespace xg {
+
+namespace {
+
+constexpr int SG_BM = 64, SG_BN = 64;   // output tile per block (8 warps, each 32 x 16)
+constexpr int SG_KT = 32;               // K per shared-memory stage
+constexpr int SG_KC = 128;              // K per exact FP32 chunk
+constexpr int SG_LD = 40;               // shared row stride in bf16 (80 bytes: conflict-free fragments)
+
+// Digits of row r of X (element k = trans ? X[k*ldx + r] : X[r*ldx + k]), k < K (and k < *dK),
+// zero beyond; out[p][r][k] for k < Kp.  One warp per row.
+template <int S>
+__global__ void k_split_rows(int R, int K, int Kp, const double* __restrict__ X, int ldx, int trans,
+                             const int* __restrict__ dK, __nv_bfloat16* __restrict__ out, double* __restrict__ scale) {
+    const int r = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (r >= R) return;
+    const int kmax = dK ? min(K, *dK) : K;
+    auto at = [&](int k) { return trans ? X[(size_t)k * ldx + r] : X[(size_t)r * ldx + k]; };
+    double mx = 0.0;
+    for (int k = lane; k < kmax; k += 32) mx = fmax(mx, fabs(at(k)));
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    int e = 0;
+    if (mx > 0.0) {
+        frexp(mx, &e);                 // mx = f 2^e, f in [0.5, 1): |x| / 2^e < 1
+    }
+    if (lane == 0) scale[r] = (mx > 0.0) ? ldexp(1.0, e) : 1.0;
+    const size_t plane = (size_t)R * Kp;
+    for (int k = lane; k < Kp; k += 32) {
+        double x = (k < kmax && mx > 0.0) ? ldexp(at(k), -e) : 0.0;
+#pragma unroll
+        for (int p = 0; p < S; ++p) {
+            x *= 256.0;
+            const double d = rint(x);
+            x -= d;
+            out[p * plane + (size_t)r * Kp + k] = __double2bfloat16(d);
+        }
+    }
+}
+
+}  // namespace
+
+namespace {
+
+__device__ __forceinline__ void mma_bf16(float* c, const uint32_t* a, const uint32_t* b) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+// One 64 x 64 output tile per block of 8 warps (warp tile 32 x 16: 2 x 2 mma tiles).
+// As: S planes of M x Kp digits (rows of op(A)), Bs: S planes of N x Kp digits (columns of op(B)).
+// Dynamic shared memory: 2 * S * 64 * SG_LD bf16.
+template <int S>
+__global__ void __launch_bounds__(256) k_split_mma(int M, int N, int Kp, const __nv_bfloat16* __restrict__ As,
+                                                   const __nv_bfloat16* __restrict__ Bs, const double* __restrict__ sA,
+                                                   const double* __restrict__ sB, double alpha, double beta,
+                                                   double* __restrict__ C, int ldc, const int* __restrict__ dN) {
+    extern __shared__ __align__(16) unsigned char sg_raw[];
+    __nv_bfloat16* smA = reinterpret_cast<__nv_bfloat16*>(sg_raw);
+    __nv_bfloat16* smB = smA + S * SG_BM * SG_LD;
+    const int i0 = blockIdx.y * SG_BM, j0 = blockIdx.x * SG_BN;
+    const int Nl = dN ? min(N, *dN) : N;
+    if (j0 >= Nl) return;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, t = lane & 3;
+    const int wm = warp >> 2, wn = warp & 3;   // warp rows wm*32.., cols wn*16..
+    const size_t planeA = (size_t)M * Kp, planeB = (size_t)N * Kp;
+    float acc[S][2][2][4];
+    double acc64[2][2][4];
+    float low[2][2][4];
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+        for (int nt = 0; nt < 2; ++nt)
+#pragma unroll
+            for (int v = 0; v < 4; ++v) {
+                acc64[mt][nt][v] = 0.0;
+                low[mt][nt][v] = 0.0f;
+#pragma unroll
+                for (int L = 0; L < S; ++L) acc[L][mt][nt][v] = 0.0f;
+            }
+    const int srow = tid >> 2, scol = (tid & 3) * 8;   // staging: one 16-byte chunk per thread per plane
+    for (int k0 = 0; k0 < Kp; k0 += SG_KT) {
+#pragma unroll
+        for (int p = 0; p < S; ++p) {
+            const int gi = i0 + srow, gj = j0 + srow;
+            uint4 va = make_uint4(0u, 0u, 0u, 0u), vb = make_uint4(0u, 0u, 0u, 0u);
+            if (gi < M) va = *reinterpret_cast<const uint4*>(As + p * planeA + (size_t)gi * Kp + k0 + scol);
+            if (gj < N) vb = *reinterpret_cast<const uint4*>(Bs + p * planeB + (size_t)gj * Kp + k0 + scol);
+            *reinterpret_cast<uint4*>(smA + (p * SG_BM + srow) * SG_LD + scol) = va;
+            *reinterpret_cast<uint4*>(smB + (p * SG_BN + srow) * SG_LD + scol) = vb;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < SG_KT; kk += 16) {
+#pragma unroll
+            for (int p = 0; p < S; ++p) {
+                uint32_t a[2][4];
+#pragma unroll
+                for (int mt = 0; mt < 2; ++mt) {
+                    const __nv_bfloat16* base = smA + (p * SG_BM + wm * 32 + mt * 16 + g) * SG_LD + kk + 2 * t;
+                    a[mt][0] = *reinterpret_cast<const uint32_t*>(base);
+                    a[mt][1] = *reinterpret_cast<const uint32_t*>(base + 8 * SG_LD);
+                    a[mt][2] = *reinterpret_cast<const uint32_t*>(base + 8);
+                    a[mt][3] = *reinterpret_cast<const uint32_t*>(base + 8 * SG_LD + 8);
+                }
+#pragma unroll
+                for (int q = 0; q < S - p; ++q) {
+                    uint32_t b[2][2];
+#pragma unroll
+                    for (int nt = 0; nt < 2; ++nt) {
+                        const __nv_bfloat16* base = smB + (q * SG_BN + wn * 16 + nt * 8 + g) * SG_LD + kk + 2 * t;
+                        b[nt][0] = *reinterpret_cast<const uint32_t*>(base);
+                        b[nt][1] = *reinterpret_cast<const uint32_t*>(base + 8);
+                    }
+#pragma unroll
+                    for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+                        for (int nt = 0; nt < 2; ++nt) mma_bf16(acc[p + q][mt][nt], a[mt], b[nt]);
+                }
+            }
+        }
+        __syncthreads();
+        if ((k0 + SG_KT) % SG_KC == 0 || k0 + SG_KT >= Kp) {
+            // levels 0..2 (exact FP32 chunk sums) into FP64; lower levels into an FP32 sum at the
+            // scale of level 3, whose rounding is below 2^-48 of the result
+#pragma unroll
+            for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+                for (int nt = 0; nt < 2; ++nt)
+#pragma unroll
+                    for (int v = 0; v < 4; ++v) {
+                        acc64[mt][nt][v] += (double)acc[0][mt][nt][v] +
+                                            ((double)acc[1][mt][nt][v] + (double)acc[2][mt][nt][v] * 0x1p-8) * 0x1p-8;
+                        float lo = 0.0f;
+#pragma unroll
+                        for (int L = S - 1; L >= 3; --L) lo = lo * 0x1p-8f + acc[L][mt][nt][v];
+                        low[mt][nt][v] += lo;
+#pragma unroll
+                        for (int L = 0; L < S; ++L) acc[L][mt][nt][v] = 0.0f;
+                    }
+        }
+    }
+    // C = alpha sA sB 2^-16 (sum of levels) + beta C
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+        for (int nt = 0; nt < 2; ++nt)
+#pragma unroll
+            for (int v = 0; v < 4; ++v) {
+                const int i = i0 + wm * 32 + mt * 16 + g + ((v & 2) ? 8 : 0);
+                const int j = j0 + wn * 16 + nt * 8 + 2 * t + (v & 1);
+                if (i >= M || j >= Nl) continue;
+                const double sum = acc64[mt][nt][v] + (double)low[mt][nt][v] * 0x1p-24;
+                double r = alpha * sA[i] * sB[j] * (sum * 0x1p-16);
+                if (beta != 0.0) r += beta * C[(size_t)i * ldc + j];
+                C[(size_t)i * ldc + j] = r;
+            }
+}
+
+}  // namespace
+
+size_t split_gemm_workspace(int M, int N, int K, int slices) {
+    const size_t Kp = (size_t)((K + SG_KT - 1) / SG_KT) * SG_KT;
+    const size_t bf = (size_t)slices * ((size_t)M + N) * Kp * sizeof(__nv_bfloat16);
+    return (bf + 255) / 256 * 256 + ((size_t)M + N) * sizeof(double) + 256;
+}
+
+template <int S>
+static void split_gemm_s(cudaStream_t st, bool ta, bool tb, int M, int N, int K, double alpha, const double* A,
+                         int lda, const double* B, int ldb, double beta, double* C, int ldc, void* work,
+                         const int* dK, const int* dN) {
+    const int Kp = ((K + SG_KT - 1) / SG_KT) * SG_KT;
+    __nv_bfloat16* As = static_cast<__nv_bfloat16*>(work);
+    __nv_bfloat16* Bs = As + (size_t)S * M * Kp;
+    const size_t bf = (size_t)S * ((size_t)M + N) * Kp * sizeof(__nv_bfloat16);
+    double* sA = reinterpret_cast<double*>(static_cast<char*>(work) + (bf + 255) / 256 * 256);
+    double* sB = sA + M;
+    k_split_rows<S><<<ceil_div((long)M * 32, 256), 256, 0, st>>>(M, K, Kp, A, lda, ta ? 1 : 0, dK, As, sA);
+    XG_LAUNCH_CHECK();
+    k_split_rows<S><<<ceil_div((long)N * 32, 256), 256, 0, st>>>(N, K, Kp, B, ldb, tb ? 0 : 1, dK, Bs, sB);
+    XG_LAUNCH_CHECK();
+    const size_t smem = (size_t)2 * S * SG_BM * SG_LD * sizeof(__nv_bfloat16);
+    static bool attr = false;
+    if (!attr && smem > 48 * 1024) {
+        XG_CUDA(cudaFuncSetAttribute(k_split_mma<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        attr = true;
+    }
+    dim3 grid(ceil_div(N, SG_BN), ceil_div(M, SG_BM));
+    k_split_mma<S><<<grid, 256, smem, st>>>(M, N, Kp, As, Bs, sA, sB, alpha, beta, C, ldc, dN);
+    XG_LAUNCH_CHECK();
+}
+
+void split_gemm(cudaStream_t st, bool ta, bool tb, int M, int N, int K, double alpha, const double* A, int lda,
+                const double* B, int ldb, double beta, double* C, int ldc, int slices, void* work, const int* dK,
+                const int* dN) {
+    if (M <= 0 || N <= 0) return;
+    if (reinterpret_cast<uintptr_t>(work) % 256 != 0) throw CudaError("split_gemm: workspace must be 256-byte aligned");
+    switch (slices) {
+        case 4: split_gemm_s<4>(st, ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, work, dK, dN); break;
+        case 5: split_gemm_s<5>(st, ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, work, dK, dN); break;
+        case 6: split_gemm_s<6>(st, ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, work, dK, dN); break;
+        case 7: split_gemm_s<7>(st, ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, work, dK, dN); break;
+        default: throw CudaError("split_gemm: slices must be 4..7");
+    }
+}
+
+namespace {
+// deterministic pseudo-random fill: uniform(-1, 1) times 2^(e) with e uniform in [-ed, 0]
+__global__ void k_fill(size_t n, unsigned seed, int ed, double* __restrict__ x) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    unsigned long long h = (i + 1) * 0x9E3779B97F4A7C15ull ^ ((unsigned long long)seed << 32);
+    h ^= h >> 31; h *= 0xBF58476D1CE4E5B9ull; h ^= h >> 27; h *= 0x94D049BB133111EBull; h ^= h >> 31;
+    const double u = (double)(h >> 11) * 0x1p-53 * 2.0 - 1.0;
+    const int e = ed > 0 ? -(int)((h >> 3) % (unsigned)(ed + 1)) : 0;
+    x[i] = ldexp(u, e);
+}
+__global__ void k_abs(size_t n, const double* __restrict__ x, double* __restrict__ y) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = fabs(x[i]);
+}
+// out[0] = max |d - r| / b, out[1] = max |d - r| / max |r| (block 0 atomics-free: one block)
+__global__ void k_errmax(size_t n, const double* __restrict__ d, const double* __restrict__ r,
+                         const double* __restrict__ b, double* __restrict__ out) {
+    __shared__ double s0[256], s1[256], s2[256];
+    double e0 = 0.0, e1 = 0.0, mr = 0.0;
+    for (size_t i = threadIdx.x; i < n; i += blockDim.x) {
+        const double e = fabs(d[i] - r[i]);
+        e0 = fmax(e0, b[i] > 0.0 ? e / b[i] : e);
+        e1 = fmax(e1, e);
+        mr = fmax(mr, fabs(r[i]));
+    }
+    s0[threadIdx.x] = e0; s1[threadIdx.x] = e1; s2[threadIdx.x] = mr;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 1; k < (int)blockDim.x; ++k) { e0 = fmax(e0, s0[k]); e1 = fmax(e1, s1[k]); mr = fmax(mr, s2[k]); }
+        out[0] = e0;
+        out[1] = mr > 0.0 ? e1 / mr : e1;
+    }
+}
+}  // namespace
+
+void split_gemm_check(int M, int N, int K, int slices, unsigned seed, int exp_range, double* out) {
+    cudaStream_t st = nullptr;
+    XG_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    const size_t na = (size_t)M * K, nb = (size_t)K * N, nc = (size_t)M * N;
+    const size_t ws = split_gemm_workspace(M, N, K, slices);
+    char* buf = nullptr;
+    const size_t doubles = 2 * (na + nb) + 3 * nc + 8;
+    XG_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&buf), doubles * sizeof(double) + 256 + ws, st));
+    double* A = reinterpret_cast<double*>(buf);
+    double* B = A + na;
+    double* Aa = B + nb;
+    double* Ba = Aa + na;
+    double* Cs = Ba + nb;
+    double* Cr = Cs + nc;
+    double* Cb = Cr + nc;
+    double* res = Cb + nc;
+    // the digit planes are read with 16-byte loads: keep the workspace 256-byte aligned
+    const size_t off = (((doubles * sizeof(double)) + 255) / 256) * 256;
+    void* work = buf + off;
+    k_fill<<<ceil_div((long)na, 256), 256, 0, st>>>(na, seed, exp_range, A);
+    k_fill<<<ceil_div((long)nb, 256), 256, 0, st>>>(nb, seed + 1, exp_range, B);
+    k_abs<<<ceil_div((long)na, 256), 256, 0, st>>>(na, A, Aa);
+    k_abs<<<ceil_div((long)nb, 256), 256, 0, st>>>(nb, B, Ba);
+    XG_LAUNCH_CHECK();
+    dgemm(st, false, false, M, N, K, 1.0, Aa, K, Ba, N, 0.0, Cb, N);
+    cudaEvent_t e0, e1, e2;
+    XG_CUDA(cudaEventCreate(&e0));
+    XG_CUDA(cudaEventCreate(&e1));
+    XG_CUDA(cudaEventCreate(&e2));
+    split_gemm(st, false, false, M, N, K, 1.0, A, K, B, N, 0.0, Cs, N, slices, work);   // warm-up
+    dgemm(st, false, false, M, N, K, 1.0, A, K, B, N, 0.0, Cr, N);
+    XG_CUDA(cudaEventRecord(e0, st));
+    split_gemm(st, false, false, M, N, K, 1.0, A, K, B, N, 0.0, Cs, N, slices, work);
+    XG_CUDA(cudaEventRecord(e1, st));
+    dgemm(st, false, false, M, N, K, 1.0, A, K, B, N, 0.0, Cr, N);
+    XG_CUDA(cudaEventRecord(e2, st));
+    k_errmax<<<1, 256, 0, st>>>(nc, Cs, Cr, Cb, res);
+    XG_LAUNCH_CHECK();
+    double h[2];
+    XG_CUDA(cudaMemcpyAsync(h, res, sizeof(h), cudaMemcpyDeviceToHost, st));
+    XG_CUDA(cudaStreamSynchronize(st));
+    float ms_s = 0.0f, ms_d = 0.0f;
+    XG_CUDA(cudaEventElapsedTime(&ms_s, e0, e1));
+    XG_CUDA(cudaEventElapsedTime(&ms_d, e1, e2));
+    const double flops = 2.0 * M * N * (double)K;
+    out[0] = h[0];
+    out[1] = h[1];
+    out[2] = ms_s;
+    out[3] = ms_d;
+    out[4] = flops / (ms_s * 1e-3) / 1e12;
+    out[5] = flops / (ms_d * 1e-3) / 1e12;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaEventDestroy(e2);
+    XG_CUDA(cudaFreeAsync(buf, st));
+    XG_CUDA(cudaStreamSynchronize(st));
+    cudaStreamDestroy(st);
+}
+
+}  // namespace xg

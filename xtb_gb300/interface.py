@@ -78,8 +78,10 @@ def load_library(path=LIBPATH):
         "xtbgb_getPhaseTimes": (None, [vp, vp, dp]),
         "xtbgb_getTransferBytes": (None, [vp, vp, C.POINTER(C.c_longlong)]),
         "xtbgb_setKeepOrbitals": (None, [vp, vp, C.c_int]),
+        "xtbgb_setPrecision": (None, [vp, vp, C.c_int, C.c_int]),
         "xtbgb_fp64PeakTflops": (C.c_double, []),
         "xtbgb_fp64LatencyCycles": (None, [dp]),
+        "xtbgb_splitGemmCheck": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, dp]),
         "xtbgb_repulsionNoAlloc": (C.c_int, [C.c_int, vp, vp, vp, vp, vp, C.c_char_p, C.c_int]),
         "xtbgb_newBatch": (vp, [vp, C.c_int, ip, ip, dp, dp, ip]),
         "xtbgb_delBatch": (None, [C.POINTER(vp)]),
@@ -93,6 +95,8 @@ def load_library(path=LIBPATH):
         "xtbgb_batchGetStats": (None, [vp, vp, dp, C.POINTER(C.c_longlong)]),
         "xtbgb_batchNao": (None, [vp, vp, ip]),
         "xtbgb_newServer": (vp, [vp, C.c_double, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int]),
+        "xtbgb_newServerEx": (vp, [vp, C.c_double, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int,
+                                   C.c_int, C.c_int]),
         "xtbgb_delServer": (None, [C.POINTER(vp)]),
         "xtbgb_serverSubmit": (C.c_longlong, [vp, vp, C.c_int, ip, dp, C.c_double, C.c_int, C.c_int]),
         "xtbgb_serverWait": (C.c_int, [vp, vp, C.c_longlong, C.c_double, dp, dp, dp, dp]),
@@ -132,7 +136,7 @@ class Calculator:
     """GFN2-xTB single point through the C ABI (numbers, positions in Bohr)."""
 
     def __init__(self, numbers, positions, charge=0.0, uhf=0, accuracy=1.0, etemp=300.0, maxiter=250,
-                 verbosity=0, keep_orbitals=True):
+                 verbosity=0, keep_orbitals=True, precision="fp64", slices=5):
         self.lib = load_library()
         self.env = Environment(verbosity)
         self.numbers = np.ascontiguousarray(numbers, dtype=np.int32)
@@ -151,6 +155,7 @@ class Calculator:
         self.lib.xtb_setElectronicTemp(self.env.h, self.calc, etemp)
         self.lib.xtb_setMaxIter(self.env.h, self.calc, maxiter)
         self.lib.xtbgb_setKeepOrbitals(self.env.h, self.calc, int(bool(keep_orbitals)))
+        self.lib.xtbgb_setPrecision(self.env.h, self.calc, 1 if precision == "split" else 0, slices)
         self.env.check()
         self.res = C.c_void_p(self.lib.xtb_newResults())
 
@@ -325,13 +330,14 @@ class Server:
     """
 
     def __init__(self, pool_gib=16.0, max_slots=1024, plain_workers=4, iters_per_step=4, accuracy=1.0,
-                 etemp=300.0, maxiter=250):
+                 etemp=300.0, maxiter=250, precision="fp64", slices=5):
         import threading
         self.lib = load_library()
         self._tls = threading.local()
         env = self._env()
-        self.h = C.c_void_p(self.lib.xtbgb_newServer(env.h, pool_gib, max_slots, plain_workers, iters_per_step,
-                                                     accuracy, etemp, maxiter))
+        self.h = C.c_void_p(self.lib.xtbgb_newServerEx(env.h, pool_gib, max_slots, plain_workers, iters_per_step,
+                                                       accuracy, etemp, maxiter, 1 if precision == "split" else 0,
+                                                       slices))
         env.check()
         self._natoms = {}
 
