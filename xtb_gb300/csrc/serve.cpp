@@ -234,8 +234,13 @@ void Server::plain_loop() {
             std::unique_lock<std::mutex> lk(mu_);
             cv_work_.wait(lk, [&] { return (stop_ && pool_done_) || !large_q_.empty(); });
             if (large_q_.empty()) break;
-            r = std::move(large_q_.front());
-            large_q_.pop_front();
+            // largest first: the large requests dominate the makespan of a saturated stream
+            auto it = std::max_element(large_q_.begin(), large_q_.end(),
+                                       [](const std::unique_ptr<Req>& a, const std::unique_ptr<Req>& b) {
+                                           return a->hm.nao < b->hm.nao;
+                                       });
+            r = std::move(*it);
+            large_q_.erase(it);
         }
         r->t_start = now();
         Completed c;
