@@ -21,6 +21,11 @@ OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "gfn2_reference.j
 NUM = r"[-+]?(?:\d+\.\d*|\.\d+|\d+)(?:[eEdD][-+]?\d+)?"
 
 
+SYMBOLS = ("H He Li Be B C N O F Ne Na Mg Al Si P S Cl Ar K Ca Sc Ti V Cr Mn Fe Co Ni Cu Zn Ga Ge As Se Br "
+           "Kr Rb Sr Y Zr Nb Mo Tc Ru Rh Pd Ag Cd In Sn Sb Te I Xe Cs Ba La Ce Pr Nd Pm Sm Eu Gd Tb Dy Ho Er "
+           "Tm Yb Lu Hf Ta W Re Os Ir Pt Au Hg Tl Pb Bi Po At Rn").split()
+
+
 def fnum(t):
     return float(t.replace("_wp", "").replace("d", "e").replace("D", "e"))
 
@@ -89,6 +94,26 @@ def main():
     hk.append({"expr": f"hess[{9 * natsq - 1}]", "value": fnum(m.group(1)), "thr": fnum(m.group(2))})
     cases["capi_hessian"] = {"numbers": at, "positions": coord, "checks": hk, "maxiter": 250, "guess": "eeq",
                              "step": 0.005}
+    # mindless01-10 (test_gfn2.f90:667-742, geometries from test/unit/molstock.f90): energy,
+    # gradient norm and HOMO-LUMO gap at 1e-8 after a default single point from the EEQ guess
+    blk = sub(src, "test_gfn2_mindless_basic")
+    ref = {}
+    for key in ("ref_energies", "ref_gnorms", "ref_hlgaps"):
+        m = re.search(key + r"\(10\)\s*=[\s&]*\[(.*?)\]", blk, re.S)
+        ref[key] = [fnum(t) for t in re.findall(NUM, m.group(1))]
+    stock = open(os.path.join(REF, "test/unit/molstock.f90")).read()
+    mols = []
+    for i in range(1, 11):
+        name = f"mindless{i:02d}"
+        a = stock.index(f"subroutine {name}(mol)")
+        b = stock.index(f"end subroutine {name}", a)
+        body = stock[a:b]
+        syms = re.findall(r'"([A-Za-z]{1,2})\s*"', body[body.index("sym(nat)"):body.index("xyz(3, nat)")])
+        xyz = [fnum(t) for t in re.findall(NUM + r"(?=_wp)", body[body.index("xyz(3, nat)"):])]
+        mols.append({"name": name, "numbers": [SYMBOLS.index(x.capitalize()) + 1 for x in syms],
+                     "positions": xyz, "energy": ref["ref_energies"][i - 1], "gnorm": ref["ref_gnorms"][i - 1],
+                     "hl_gap": ref["ref_hlgaps"][i - 1], "thr": 1e-8})
+    cases["mindless"] = mols
     json.dump(cases, open(OUT, "w"), indent=1)
     print("wrote", OUT)
 

@@ -59,3 +59,15 @@ def test_oracle_hessian_matches_reference_c_api_test():
         i = int(c["expr"][5:-1])
         assert abs(flat[i] - c["value"]) <= c["thr"], (c["expr"], flat[i], c["value"])
     assert np.max(np.abs(H - H.T)) == 0.0
+
+
+def test_oracle_mindless_molecules():
+    """test_gfn2.f90:667-742: ten random 16-atom molecules over many elements (mindless01-10,
+    geometries of test/unit/molstock.f90), energy, gradient norm and gap at 1e-8."""
+    for m in golden()["mindless"]:
+        Z = np.array(m["numbers"])
+        xyz = np.array(m["positions"], dtype=float).reshape(-1, 3)
+        r = gfn2.singlepoint(Z, xyz)
+        assert abs(r.energy - m["energy"]) <= m["thr"], m["name"]
+        assert abs(np.linalg.norm(r.gradient) - m["gnorm"]) <= m["thr"], m["name"]
+        assert abs(r.hl_gap - m["hl_gap"]) <= m["thr"], m["name"]
