@@ -50,6 +50,11 @@ extern void xtbgb_setKeepOrbitals(xtb_TEnvironment env, xtb_TCalculator calc, in
  * Cholesky factorisation, the reduction to standard form and the eigensolver stay FP64. */
 extern void xtbgb_setPrecision(xtb_TEnvironment env, xtb_TCalculator calc, int split, int slices);
 
+/* AO count from which the eigenvector back-transformation runs as blocked compact-WY products
+ * (blocks of 128 reflectors) instead of one warp per eigenvector.  -1 (default) picks it by
+ * precision: 1500 AOs for FP64, 1000 for split precision. */
+extern void xtbgb_setBlockedBacktransform(xtb_TEnvironment env, xtb_TCalculator calc, int nao_min);
+
 /* Measured FP64 FMA throughput of device 0 in TFLOP/s (roofline denominator for FP64 kernels);
  * returns 0 when no device is present. */
 extern double xtbgb_fp64PeakTflops(void);
@@ -58,6 +63,12 @@ extern double xtbgb_fp64PeakTflops(void);
  * cycles[0] FP64 FMA, [1] FP64 add, [2] FP64 multiply, [3] FP64 divide, [4] FP32 FMA
  * (all 0 when no device is present). */
 extern void xtbgb_fp64LatencyCycles(double* cycles);
+
+/* Check the FP64 reciprocal used on the dependent chains of inverse iteration (an FP32 seed
+ * refined by one third-order Newton step) against the FP64 division on device 0: out[0] the
+ * largest difference in units of the last place, out[1] the number of values checked
+ * (+-(1 + t 2^-20) 2^k, k in [-1000, 1000]).  Returns 0 on success. */
+extern int xtbgb_reciprocalCheck(double* out);
 
 /* Check and time the split-precision GEMM (FP64 results from BF16 tensor-core products of
  * fixed-point digit slices) against the FP64 GEMM on seeded random M x K and K x N matrices

@@ -157,3 +157,31 @@ def test_mindless_molecules_reference_values():
             assert abs(e - m["energy"]) <= m["thr"], (m["name"], e, m["energy"])
             assert abs(g - m["gnorm"]) <= m["thr"], (m["name"], g, m["gnorm"])
             assert abs(gap - m["hl_gap"]) <= m["thr"], (m["name"], gap, m["hl_gap"])
+
+
+def test_fast_reciprocal_within_one_ulp():
+    """The reciprocal on the inverse-iteration chains (FP32 seed + one third-order Newton step)
+    against the FP64 division, over 6e8 values on both sides of the FP32 seed's range."""
+    import ctypes as C
+    lib = X.load_library()
+    out = np.zeros(2)
+    assert lib.xtbgb_reciprocalCheck(out.ctypes.data_as(C.POINTER(C.c_double))) == 0
+    assert out[1] == 2001 * 2 * 256 * 586
+    assert out[0] <= 1.0, out
+
+
+@pytest.mark.parametrize("precision", ["fp64", "split"])
+def test_blocked_backtransform(precision):
+    """The compact-WY back-transformation (blocks of 128 reflectors, all T factors in one launch)
+    forced below its default 3000-AO threshold: (H2O)50 has 300 AOs, so three blocks, the last
+    partial.  It must agree with the warp-per-vector form and with the oracle; with orbitals
+    kept, every eigenvector goes through it."""
+    Z, xyz = W.water_cluster(50, seed=8)
+    base = gpu(Z, xyz, keep_orbitals=False, precision=precision)
+    for keep in (False, True):
+        r = gpu(Z, xyz, keep_orbitals=keep, precision=precision, blocked_min=0)
+        assert abs(r.energy - base.energy) <= 1e-10
+        assert np.max(np.abs(r.charges - base.charges)) <= 1e-9
+        assert np.max(np.abs(r.gradient - base.gradient)) <= 1e-9
+        assert r.iterations == base.iterations
+    assert_parity(r, gfn2.singlepoint(Z, xyz))

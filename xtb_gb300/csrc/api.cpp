@@ -596,6 +596,18 @@ void xtbgb_fp64LatencyCycles(double* cycles) {
     }
 }
 
+int xtbgb_reciprocalCheck(double* out) {
+    if (!out) return 1;
+    out[0] = out[1] = 0.0;
+    if (xg::device_count() == 0) return 2;
+    try {
+        xg::reciprocal_check(out);
+    } catch (const std::exception&) {
+        return 3;
+    }
+    return 0;
+}
+
 int xtbgb_splitGemmCheck(int M, int N, int K, int slices, int seed, int exp_range, double* out) {
     if (!out || M < 1 || N < 1 || K < 1 || slices < 4 || slices > 7) return 1;
     if (xg::device_count() == 0) return 2;
@@ -653,6 +665,19 @@ void xtbgb_setPrecision(xtb_TEnvironment env, xtb_TCalculator calc, int split, i
     }
     calc->set.precision = split ? 1 : 0;
     calc->set.slices = slices;
+}
+
+void xtbgb_setBlockedBacktransform(xtb_TEnvironment env, xtb_TCalculator calc, int nao_min) {
+    if (!check_env(env)) return;
+    if (!calc) {
+        env->error("Singlepoint calculator is not allocated", "xtbgb_setBlockedBacktransform");
+        return;
+    }
+    if (nao_min < -1) {
+        env->error("AO threshold must be -1 (by precision) or >= 0", "xtbgb_setBlockedBacktransform");
+        return;
+    }
+    calc->set.blocked_min = nao_min;
 }
 
 void xtbgb_setKeepOrbitals(xtb_TEnvironment env, xtb_TCalculator calc, int keep) {

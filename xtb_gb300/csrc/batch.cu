@@ -305,7 +305,7 @@ __device__ void scc_iteration(BatchMol* b, const DevThresh& th, double etemp, in
     __syncthreads();
     const int kocc = *b->kocc;
     double* U1 = b->iscr;
-    CTA_FOR(j, kocc) d_inviter(nao, b->tri_d, b->tri_e, b->emo, b->bounds, b->Y, U1, U1 + nn, U1 + 2 * nn,
+    CTA_FOR(j, kocc) d_inviter<2>(nao, b->tri_d, b->tri_e, b->emo, b->bounds, b->Y, U1, U1 + nn, U1 + 2 * nn,
                                U1 + 3 * nn, b->piv, j);
     __syncthreads();
     WARP_FOR(j, kocc) d_reorth(nao, b->emo, b->bounds, 1.0e-7, b->Y, U1, U1 + nn, U1 + 2 * nn, U1 + 3 * nn, b->piv,

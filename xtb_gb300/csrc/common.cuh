@@ -42,6 +42,21 @@ __device__ __forceinline__ double warp_sum(double v) {
 }
 
 // Block-wide sum; every thread receives the result.  `red` needs blockDim.x/32 doubles.
+// 1/x from the FP32 reciprocal and one third-order Newton step for the reciprocal,
+// y = y0 (1 + e + e^2) with e = 1 - x y0: a seed of relative error d leaves d^3 + rounding,
+// and d <= 2^-23 here, so the result is within about one ulp of 1/x at roughly a third of
+// the dependent latency of an FP64 division.  Outside [2^-120, 2^120] the FP32 seed would
+// leave the normal range, so the division is used there.
+__device__ __forceinline__ double rcp_fast(double x) {
+    const int ex = (__double2hiint(x) >> 20) & 0x7ff;
+    if (ex > 1023 - 120 && ex < 1023 + 120) {
+        const double y0 = (double)__frcp_rn((float)x);
+        const double e = fma(-x, y0, 1.0);
+        return fma(y0, fma(e, e, e), y0);
+    }
+    return 1.0 / x;
+}
+
 __device__ __forceinline__ double block_sum(double v, double* red) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
     v = warp_sum(v);

@@ -36,10 +36,6 @@ int device_count() {
 
 namespace {
 
-// AO count from which the back-transformation runs as compact-WY GEMMs (measured on GB300:
-// 172 ms vs 234 ms per (H2O)300 single point below, 10.6 s vs 3.7 s per (H2O)1000 above)
-constexpr int kBlockedBacktransform = 3000;
-
 // --------------------------------------------------------------- small kernels
 __global__ void k_self_energy(int nsh, const int* __restrict__ sh_atom, const double* __restrict__ se0,
                               const double* __restrict__ kcn, const double* __restrict__ cn, double* __restrict__ se) {
@@ -393,7 +389,7 @@ void run_singlepoint(const HostMol& hm, const SPSettings& set, Wavefunction& wfn
     tri_e = ar.take<double>(nao);
     tri_e2 = ar.take<double>(nao);
     tri_tau = ar.take<double>(nao);
-    tri_p = ar.take<double>(2 * (size_t)nao);
+    tri_p = ar.take<double>(sytrd_workspace(nao));
     bounds = ar.take<double>(8);
     fscal = ar.take<double>(8 + (size_t)nao);
     escal = ar.take<double>(16);
@@ -516,7 +512,7 @@ void run_singlepoint(const HostMol& hm, const SPSettings& set, Wavefunction& wfn
         tridiag_eigvecs(st, nao, tri_d, tri_e, bounds, emo, Y, iscr, piv, info + 1);
         tm.mark(PH_BACKTR);
         // Y[:, :kocc] = Q Y: compact-WY GEMMs pay off for large n, one warp per vector below
-        if (nao >= kBlockedBacktransform)
+        if (nao >= set.blocked_threshold())
             ormtr_blocked(st, nao, V, tri_tau, Y, info + 1, ormw, split ? set.slices : 0, sgw);
         else
             ormtr_inplace(st, nao, V, tri_tau, Y, info + 1);
@@ -564,7 +560,7 @@ void run_singlepoint(const HostMol& hm, const SPSettings& set, Wavefunction& wfn
     if (keep_orbitals) {
         // all MO coefficients of the last iteration (only occupied ones were needed inside the SCC)
         tridiag_eigvecs(st, nao, tri_d, tri_e, bounds, emo, Y, iscr, piv, nullptr);
-        if (nao >= kBlockedBacktransform) ormtr_blocked(st, nao, V, tri_tau, Y, nullptr, ormw);
+        if (nao >= set.blocked_threshold()) ormtr_blocked(st, nao, V, tri_tau, Y, nullptr, ormw);
         else ormtr_inplace(st, nao, V, tri_tau, Y, nullptr);
         dgemm(st, false, false, nao, nao, nao, 1.0, X, nao, Y, nao, 0.0, C, nao, GF_A_UPPER);
     }
@@ -588,7 +584,7 @@ void run_singlepoint(const HostMol& hm, const SPSettings& set, Wavefunction& wfn
     // D4 two-body and ATM at the final charges, covalent CN
     cn(st, m, 1, cn_tmp);
     XG_CUDA(cudaMemsetAsync(tmp2, 0, nat * sizeof(double), st));
-    d4_grad(st, m, cn_tmp, q, gw, dgw, zv, zr, zdcn, zrdcn, c6, dc6, c6z, dc6z, e2, e3, tmp2, grad);
+    d4_grad(st, m, cn_tmp, q, gw, dgw, zv, zr, zdcn, zrdcn, c6, dc6, c6z, dc6z, e2, e3, tmp2, grad, iscr);
     cn_chain(st, m, 1, tmp2, grad);
     coulomb_grad(st, m, qsh, grad);
     k_dipole<<<1, 256, 0, st>>>(nat, nao, m.xyz, d_zval, rows, dip);

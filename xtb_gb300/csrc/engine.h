@@ -16,6 +16,12 @@ struct SPSettings {
     // the reduction to standard form and the eigensolver stay FP64
     int precision = 0;
     int slices = 5;
+    // AO count from which the back-transformation of the eigenvectors runs as compact-WY
+    // GEMMs instead of one warp per vector; -1 picks it by precision (measured on GB300 per
+    // single point: FP64 at (H2O)150, 900 AOs, warp form 41 ms vs 50 ms; at (H2O)300, 1800 AOs,
+    // 178 ms vs 165 ms; split precision 32 ms vs 34 ms and 149 ms vs 101 ms)
+    int blocked_min = -1;
+    int blocked_threshold() const { return blocked_min >= 0 ? blocked_min : (precision == 1 ? 1000 : 1500); }
 };
 
 // Wavefunction kept between calls on the same results object (res%chk of the reference).

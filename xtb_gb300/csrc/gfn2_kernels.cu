@@ -409,19 +409,113 @@ __global__ void k_d4_2body(DevMol m, const double* __restrict__ c6, const double
 }
 
 
-// ATM three-body (atm_gradient_latp molecular branch + deriv_atm_triple, src/disp/dftd4.F90:2023-2177, 2354-2433);
-// one thread per pair (i > j), loop over k < j; gradient and dE/dCN of j, k by atomics.
+// ATM three-body (atm_gradient_latp molecular branch + deriv_atm_triple, src/disp/dftd4.F90:2023-2177, 2354-2433).
+// The triple terms factor into pair quantities: the damping base (C_ijk / R_ijk)^(16/3) with
+// C_ijk = c_ij c_ik c_jk and R_ijk = R_ij R_ik R_jk is tp_ij tp_ik tp_jk, tp = (c / R)^(16/3);
+// sqrt(C6_ij C6_ik C6_jk) is s6_ij s6_ik s6_jk; 1/R_ijk is ir_ij ir_ik ir_jk.  k_atm_pairs
+// forms them once per pair (t = a*n + b), so the O(N^3) loop has no power, square root or
+// division other than the damping's reciprocal.  ga[a*n + b] = (dC6_ab/dCN_a) / C6_ab and its
+// transpose gt serve the C6 derivatives with coalesced loads for either index order.
+__global__ void k_atm_pairs(DevMol m, const double* __restrict__ c6, const double* __restrict__ dc6,
+                            double* __restrict__ ir, double* __restrict__ tp, double* __restrict__ s6,
+                            double* __restrict__ ga, double* __restrict__ gt) {
+    const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = m.nat;
+    if (t >= (long)n * n) return;
+    const int a = (int)(t / n), b = (int)(t % n);
+    const size_t tt = (size_t)b * n + a;
+    if (a == b) {
+        ir[t] = 0.0; tp[t] = 0.0; s6[t] = 0.0; ga[t] = 0.0; gt[t] = 0.0;
+        return;
+    }
+    const double dx = m.xyz[3 * b] - m.xyz[3 * a], dy = m.xyz[3 * b + 1] - m.xyz[3 * a + 1],
+                 dz = m.xyz[3 * b + 2] - m.xyz[3 * a + 2];
+    const double irr = 1.0 / sqrt(dx * dx + dy * dy + dz * dz);
+    const double cab = 0.52 * sqrt(3.0 * m.r4r2[a] * m.r4r2[b]) + 5.0;
+    ir[t] = irr;
+    tp[t] = pow(cab * irr, 16.0 / 3.0);
+    s6[t] = sqrt(c6[t]);
+    const double g = dc6[t] / c6[tt];
+    ga[t] = g;
+    gt[tt] = g;
+}
 
-
-__global__ void k_d4_atm(DevMol m, const double* __restrict__ c6, const double* __restrict__ dc6, long npair,
-                         double* __restrict__ e_pair, double* __restrict__ dEdcn, double* __restrict__ grad) {
+// One thread per pair (i > j), loop over k < j; gradient and dE/dCN of k by atomics.
+__global__ void k_d4_atm(DevMol m, const double* __restrict__ ir, const double* __restrict__ tp,
+                         const double* __restrict__ s6, const double* __restrict__ ga, const double* __restrict__ gt,
+                         long npair, double* __restrict__ e_pair, double* __restrict__ dEdcn,
+                         double* __restrict__ grad) {
     const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= npair) return;
-    d_d4_atm(m, c6, dc6, npair, e_pair, dEdcn, grad, t);
+    int ia, ja;
+    tri_pair(t, ia, ja);
+    if (ja >= ia) { e_pair[t] = 0.0; return; }
+    const int n = m.nat;
+    const double cut2 = 1600.0, s9 = 5.0;
+    const double* x = m.xyz;
+    const double rij[3] = {x[3 * ja] - x[3 * ia], x[3 * ja + 1] - x[3 * ia + 1], x[3 * ja + 2] - x[3 * ia + 2]};
+    const double r2ij = rij[0] * rij[0] + rij[1] * rij[1] + rij[2] * rij[2];
+    double esum = 0.0;
+    if (r2ij <= cut2) {
+        double gi[3] = {0, 0, 0}, gj[3] = {0, 0, 0}, dci = 0.0, dcj = 0.0;
+        const size_t pij = (size_t)ja * n + ia;
+        const double irij = ir[pij], tij = tp[pij], sij = s6[pij];
+        const double gi_j = ga[(size_t)ia * n + ja], gj_i = ga[pij];
+        for (int ka = 0; ka < ja; ++ka) {
+            const double rik[3] = {x[3 * ka] - x[3 * ia], x[3 * ka + 1] - x[3 * ia + 1], x[3 * ka + 2] - x[3 * ia + 2]};
+            const double r2ik = rik[0] * rik[0] + rik[1] * rik[1] + rik[2] * rik[2];
+            if (r2ik > cut2) continue;
+            const double rjk[3] = {x[3 * ka] - x[3 * ja], x[3 * ka + 1] - x[3 * ja + 1], x[3 * ka + 2] - x[3 * ja + 2]};
+            const double r2jk = rjk[0] * rjk[0] + rjk[1] * rjk[1] + rjk[2] * rjk[2];
+            if (r2jk > cut2) continue;
+            const size_t pik = (size_t)ka * n + ia, pjk = (size_t)ka * n + ja;
+            const double irik = ir[pik], irjk = ir[pjk];
+            const double c9 = -(sij * s6[pik] * s6[pjk]);
+            const double cralp = tij * tp[pik] * tp[pjk];
+            const double irrr1 = irij * irik * irjk;
+            const double irrr2 = irrr1 * irrr1, irrr3 = irrr2 * irrr1;
+            const double ang_fact = 0.375 * irrr2 * irrr3;
+            const double ang = ang_fact * (r2ij + r2jk - r2ik) * (r2ij - r2jk + r2ik) * (-r2ij + r2jk + r2ik) + irrr3;
+            const double fdmp = rcp_fast(1.0 + 6.0 * cralp);
+            const double dfdmp = -(2.0 * 16.0 * cralp) * fdmp * fdmp;
+            const double c9f = c9 * fdmp, c9d = dfdmp * c9 * ang;
+            const double dE = -ang * c9f;
+            const double dang1 = -ang_fact * (r2ij * r2ij * r2ij + r2ij * r2ij * (r2jk + r2ik) +
+                                              r2ij * (3.0 * r2jk * r2jk + 2.0 * r2jk * r2ik + 3.0 * r2ik * r2ik) -
+                                              5.0 * sq(r2jk - r2ik) * (r2jk + r2ik));
+            const double dang2 = -ang_fact * (r2ik * r2ik * r2ik + r2ik * r2ik * (r2jk + r2ij) +
+                                              r2ik * (3.0 * r2jk * r2jk + 2.0 * r2jk * r2ij + 3.0 * r2ij * r2ij) -
+                                              5.0 * sq(r2jk - r2ij) * (r2jk + r2ij));
+            const double dang3 = -ang_fact * (r2jk * r2jk * r2jk + r2jk * r2jk * (r2ik + r2ij) +
+                                              r2jk * (3.0 * r2ik * r2ik + 2.0 * r2ik * r2ij + 3.0 * r2ij * r2ij) -
+                                              5.0 * sq(r2ik - r2ij) * (r2ik + r2ij));
+            const double dGr1 = s9 * (c9d - dang1 * c9f) * (irij * irij);
+            const double dGr2 = s9 * (c9d - dang2 * c9f) * (irik * irik);
+            const double dGr3 = s9 * (c9d - dang3 * c9f) * (irjk * irjk);
+            esum += dE * s9;
+            for (int q = 0; q < 3; ++q) {
+                gi[q] -= dGr1 * rij[q] + dGr2 * rik[q];
+                gj[q] += dGr1 * rij[q] - dGr3 * rjk[q];
+                atomicAdd(&grad[3 * ka + q], dGr2 * rik[q] + dGr3 * rjk[q]);
+            }
+            const double h = -0.5 * s9 * ang * fdmp * c9;
+            dci += h * (gi_j + gt[pik]);
+            dcj += h * (gj_i + gt[pjk]);
+            atomicAdd(&dEdcn[ka], h * (ga[pik] + ga[pjk]));
+        }
+        for (int q = 0; q < 3; ++q) {
+            atomicAdd(&grad[3 * ia + q], gi[q]);
+            atomicAdd(&grad[3 * ja + q], gj[q]);
+        }
+        atomicAdd(&dEdcn[ia], dci);
+        atomicAdd(&dEdcn[ja], dcj);
+    }
+    e_pair[t] = esum;
 }
+
 void d4_grad(cudaStream_t st, const DevMol& m, const double* cnv, const double* q, double* gw, double* dgw,
              double* zv, double* zr, double* zdcn, double* zrdcn, double* c6, double* dc6, double* c6z, double* dc6z,
-             double* e2_atom, double* e3_pair, double* dEdcn, double* grad) {
+             double* e2_atom, double* e3_pair, double* dEdcn, double* grad, double* pair_work) {
     k_d4_weights<<<ceil_div(m.nat, 128), 128, 0, st>>>(m, cnv, gw, dgw);
     XG_LAUNCH_CHECK();
     k_d4_refvec<<<ceil_div(m.nat, 128), 128, 0, st>>>(m, gw, dgw, q, zv, zr, zdcn, zrdcn);
@@ -433,8 +527,16 @@ void d4_grad(cudaStream_t st, const DevMol& m, const double* cnv, const double* 
     XG_LAUNCH_CHECK();
     k_d4_2body<<<ceil_div(m.nat, 128), 128, 0, st>>>(m, c6, dc6, e2_atom, dEdcn, grad);
     XG_LAUNCH_CHECK();
+    // ATM pair factors: c6 and dc6 are free once the two-body term is done
+    double* ir = c6;
+    double* tp = dc6;
+    double* s6 = pair_work;
+    double* ga = pair_work + nn;
+    double* gt = pair_work + 2 * nn;
+    k_atm_pairs<<<ceil_div(nn, 256), 256, 0, st>>>(m, c6z, dc6z, ir, tp, s6, ga, gt);
+    XG_LAUNCH_CHECK();
     const long np = (long)m.nat * (m.nat + 1) / 2;
-    k_d4_atm<<<ceil_div(np, 128), 128, 0, st>>>(m, c6z, dc6z, np, e3_pair, dEdcn, grad);
+    k_d4_atm<<<ceil_div(np, 128), 128, 0, st>>>(m, ir, tp, s6, ga, gt, np, e3_pair, dEdcn, grad);
     XG_LAUNCH_CHECK();
 }
 

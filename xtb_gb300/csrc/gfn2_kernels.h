@@ -119,10 +119,11 @@ void coulomb_grad(cudaStream_t st, const DevMol& m, const double* qsh, double* g
 void aes_grad(cudaStream_t st, const DevMol& m, const double* q, const double* dipm, const double* qp,
               const double* radcn, const double* gab3, const double* gab5, double* grad, double* tmp2);
 void aes_dradcn(cudaStream_t st, const DevMol& m, const double* cn, const double* tmp2, double* dhdcn);
-// D4 dispersion energy and gradient at fixed charges (2-body + ATM); dEdcn accumulated
+// D4 dispersion energy and gradient at fixed charges (2-body + ATM); dEdcn accumulated.
+// c6 and dc6 are overwritten (ATM pair factors); pair_work: 3 nat^2 doubles of scratch.
 void d4_grad(cudaStream_t st, const DevMol& m, const double* cn, const double* q, double* gw, double* dgw,
              double* zv, double* zr, double* zdcn, double* zrdcn, double* c6, double* dc6, double* c6z, double* dc6z, double* e2_atom,
-             double* e3_atom, double* dEdcn, double* grad);
+             double* e3_atom, double* dEdcn, double* grad, double* pair_work);
 void add_vec(cudaStream_t st, int n, const double* a, double* b);
 
 }  // namespace xg

@@ -225,7 +225,7 @@ __global__ void __launch_bounds__(1024) k_sytrd(int n, double* __restrict__ A, i
 
 void sytrd(cudaStream_t st, int n, double* A, int lda, double* V, double* tau, double* d, double* e, double* p) {
     static int nsm = 0, maxblk = 0;
-    const size_t smem = (size_t)(4 * n + 32) * sizeof(double);
+    const size_t smem = (size_t)(4 * n + 72) * sizeof(double);
     if (n <= 2) {
         // trivial: copy diagonal / off-diagonal
         k_sytrd<<<1, 256, smem, st>>>(n, A, lda, V, tau, d, e, p);
@@ -244,6 +244,7 @@ void sytrd(cudaStream_t st, int n, double* A, int lda, double* V, double* tau, d
     XG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxblk, k_sytrd, threads, smem));
     if (maxblk < 1) throw CudaError("sytrd: kernel does not fit on an SM");
     int blocks = std::min(std::min(nsm * maxblk, nsm), std::max(1, ceil_div(n, threads / 32)));
+    blocks = std::min(blocks, SYTRD_SLOTS);
     void* args[] = {&n, &A, &lda, &V, &tau, &d, &e, &p};
     XG_CUDA(cudaLaunchCooperativeKernel((void*)k_sytrd, blocks, threads, args, smem, st));
     ++launch_counter();
@@ -271,13 +272,13 @@ __global__ void __launch_bounds__(32) k_bisect(int n, const double* __restrict__
 }
 
 // ------------------------------------------------------------------ inverse iteration
-__global__ void k_inviter(int n, const double* __restrict__ d, const double* __restrict__ e,
+__global__ void __launch_bounds__(64) k_inviter(int n, const double* __restrict__ d, const double* __restrict__ e,
                           const double* __restrict__ w, const double* __restrict__ bounds, double* __restrict__ Y,
                           double* __restrict__ U1, double* __restrict__ U2, double* __restrict__ U3,
                           double* __restrict__ ML, unsigned char* __restrict__ piv, const int* __restrict__ ncol) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n || (ncol && j >= *ncol)) return;
-    d_inviter(n, d, e, w, bounds, Y, U1, U2, U3, ML, piv, j);
+    d_inviter<8>(n, d, e, w, bounds, Y, U1, U2, U3, ML, piv, j);
 }
 
 __global__ void k_reorth(int n, const double* __restrict__ w, const double* __restrict__ bounds, double ctol,
@@ -328,50 +329,75 @@ constexpr int ORM_NB = 128;     // reflectors per block
 constexpr int ORM_SPLIT = 16;   // K slices of the skinny products
 
 // T (kn x kn, upper) of the compact WY form H(0) ... H(kn-1) = I - V T V^T from the Gram matrix
-// S = V^T V and tau (dlarft, forward, columnwise: T(:i, i) = -tau_i T(:i, :i) S(:i, i)).
-__global__ void k_larft(int kn, const double* __restrict__ tau, const double* __restrict__ S, int lds,
-                        double* __restrict__ T, int ldt) {
-    __shared__ double w[ORM_NB];
+// S = V^T V and tau (dlarft, forward, columnwise: T(:i, i) = -tau_i T(:i, :i) S(:i, i)), for
+// every block of reflectors at once: thread block b handles reflectors b*ORM_NB ... .  The
+// recurrence is sequential in i, so each block keeps T in shared memory (S's strict upper
+// triangle is loaded into the same array and column i of S is overwritten by column i of T
+// once it has been used) and eight threads share each row's dot product.
+constexpr int LARFT_LD = ORM_NB + 1;
+__global__ void __launch_bounds__(8 * ORM_NB) k_larft_all(int nref, const double* __restrict__ tau,
+                                                          const double* __restrict__ Sall, double* __restrict__ Tall) {
+    extern __shared__ double Ts[];   // [ORM_NB][LARFT_LD]
+    const int k0 = blockIdx.x * ORM_NB, kn = min(ORM_NB, nref - k0);
+    const double* S = Sall + (size_t)blockIdx.x * ORM_NB * ORM_NB;
+    double* T = Tall + (size_t)blockIdx.x * ORM_NB * ORM_NB;
+    for (int t = threadIdx.x; t < ORM_NB * ORM_NB; t += blockDim.x) {
+        const int j = t / ORM_NB, l = t % ORM_NB;
+        Ts[j * LARFT_LD + l] = (j < l && l < kn) ? S[t] : 0.0;
+    }
+    __syncthreads();
+    const int j = threadIdx.x >> 3, sub = threadIdx.x & 7;
     for (int i = 0; i < kn; ++i) {
-        for (int j = threadIdx.x; j < i; j += blockDim.x) w[j] = S[(size_t)j * lds + i];
+        double sum = 0.0;
+        if (j < i)
+            for (int l = j + sub; l < i; l += 8) sum = fma(Ts[j * LARFT_LD + l], Ts[l * LARFT_LD + i], sum);
+        sum += __shfl_xor_sync(0xffffffffu, sum, 4);
+        sum += __shfl_xor_sync(0xffffffffu, sum, 2);
+        sum += __shfl_xor_sync(0xffffffffu, sum, 1);
+        const double ti = tau[k0 + i];
         __syncthreads();
-        const double ti = tau[i];
-        for (int j = threadIdx.x; j < kn; j += blockDim.x) {
-            double v = 0.0;
-            if (j < i) {
-                double sum = 0.0;
-                for (int l = j; l < i; ++l) sum = fma(T[(size_t)j * ldt + l], w[l], sum);
-                v = -ti * sum;
-            } else if (j == i) {
-                v = ti;
-            }
-            T[(size_t)j * ldt + i] = v;
-        }
+        if (sub == 0 && j <= i) Ts[j * LARFT_LD + i] = (j < i) ? -ti * sum : ti;
         __syncthreads();
+    }
+    for (int t = threadIdx.x; t < ORM_NB * ORM_NB; t += blockDim.x) {
+        const int r = t / ORM_NB, c = t % ORM_NB;
+        T[t] = Ts[r * LARFT_LD + c];
     }
 }
 
 size_t ormtr_workspace(int n) {
-    return (size_t)ORM_SPLIT * ORM_NB * std::max(n, ORM_NB) + 2 * (size_t)ORM_NB * n + 2 * (size_t)ORM_NB * ORM_NB;
+    const size_t nblk = (size_t)std::max(1, ceil_div(std::max(n - 2, 1), ORM_NB));
+    return (size_t)ORM_SPLIT * ORM_NB * std::max(n, ORM_NB) + 2 * (size_t)ORM_NB * n +
+           2 * nblk * ORM_NB * ORM_NB;
 }
 
 void ormtr_blocked(cudaStream_t st, int n, const double* V, const double* tau, double* Y, const int* d_ncol,
                    double* work, int slices, void* split_work) {
     if (n < 3) return;
+    const int nref = n - 2;
+    const int nblk = ceil_div(nref, ORM_NB);
     double* partial = work;
     double* G = partial + (size_t)ORM_SPLIT * ORM_NB * std::max(n, ORM_NB);
     double* G2 = G + (size_t)ORM_NB * n;
-    double* S = G2 + (size_t)ORM_NB * n;
-    double* T = S + (size_t)ORM_NB * ORM_NB;
-    const int nref = n - 2;
-    for (int k0 = ((nref - 1) / ORM_NB) * ORM_NB; k0 >= 0; k0 -= ORM_NB) {
-        const int kn = std::min(ORM_NB, nref - k0);
+    double* Sall = G2 + (size_t)ORM_NB * n;
+    double* Tall = Sall + (size_t)nblk * ORM_NB * ORM_NB;
+    // Gram matrices S_b = V_b V_b^T of every block, then all T factors in one launch
+    for (int b = 0; b < nblk; ++b) {
+        const int k0 = b * ORM_NB, kn = std::min(ORM_NB, nref - k0);
         const int r0 = k0 + 1, m = n - r0;
         const double* Vb = V + (size_t)k0 * n + r0;   // kn rows of length m (zeros above each vector's start)
-        // S = Vb Vb^T, T from S and tau
-        dgemm_splitk(st, false, true, kn, kn, m, 1.0, Vb, n, Vb, n, 0.0, S, ORM_NB, ORM_SPLIT, partial, nullptr);
-        k_larft<<<1, 64, 0, st>>>(kn, tau + k0, S, ORM_NB, T, ORM_NB);
-        XG_LAUNCH_CHECK();
+        dgemm_splitk(st, false, true, kn, kn, m, 1.0, Vb, n, Vb, n, 0.0, Sall + (size_t)b * ORM_NB * ORM_NB, ORM_NB,
+                     ORM_SPLIT, partial, nullptr);
+    }
+    const size_t smem = (size_t)ORM_NB * LARFT_LD * sizeof(double);
+    XG_CUDA(cudaFuncSetAttribute(k_larft_all, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_larft_all<<<nblk, 8 * ORM_NB, smem, st>>>(nref, tau, Sall, Tall);
+    XG_LAUNCH_CHECK();
+    for (int b = nblk - 1; b >= 0; --b) {
+        const int k0 = b * ORM_NB, kn = std::min(ORM_NB, nref - k0);
+        const int r0 = k0 + 1, m = n - r0;
+        const double* Vb = V + (size_t)k0 * n + r0;
+        const double* T = Tall + (size_t)b * ORM_NB * ORM_NB;
         // G = Vb Y[r0:, :ncol];  G2 = T G;  Y[r0:, :ncol] -= Vb^T G2
         if (slices) {
             split_gemm(st, false, false, kn, n, m, 1.0, Vb, n, Y + (size_t)r0 * n, n, 0.0, G, n, slices, split_work,
@@ -514,5 +540,38 @@ void fp64_latency_cycles(double* cycles) {
     cudaFree(d_out);
     cudaFree(d_sink);
     cudaFree(d_sinkf);
+}
+// rcp_fast against the FP64 division: x = +-(1 + t/2^20) 2^k for k in [-1000, 1000] (both
+// sides of the FP32-seed range) and every t of a stride through [0, 2^20).  out[0] = largest
+// |rcp_fast(x) - 1/x| in units of the last place of 1/x, out[1] = values checked.
+__global__ void k_rcp_check(unsigned long long* __restrict__ worst, unsigned long long* __restrict__ count) {
+    const int k = (int)blockIdx.x - 1000;
+    unsigned long long w = 0, c = 0;
+    for (int t = threadIdx.x; t < (1 << 20); t += 7 * blockDim.x) {
+        const double m = 1.0 + (double)t * 0x1p-20;
+        for (int sgn = 0; sgn < 2; ++sgn) {
+            const double x = ldexp(sgn ? -m : m, k);
+            const double ref = 1.0 / x, got = rcp_fast(x);
+            const long long a = __double_as_longlong(ref), b = __double_as_longlong(got);
+            const unsigned long long d = (unsigned long long)(a > b ? a - b : b - a);
+            w = d > w ? d : w;
+            ++c;
+        }
+    }
+    atomicMax(worst, w);
+    atomicAdd(count, c);
+}
+
+void reciprocal_check(double* out) {
+    unsigned long long* d = nullptr;
+    XG_CUDA(cudaMalloc(&d, 2 * sizeof(unsigned long long)));
+    XG_CUDA(cudaMemset(d, 0, 2 * sizeof(unsigned long long)));
+    k_rcp_check<<<2001, 256>>>(d, d + 1);
+    XG_CUDA(cudaGetLastError());
+    unsigned long long h[2];
+    XG_CUDA(cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost));
+    cudaFree(d);
+    out[0] = (double)h[0];
+    out[1] = (double)h[1];
 }
 }  // namespace xg

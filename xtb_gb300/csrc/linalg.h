@@ -19,6 +19,10 @@ void potrf_upper(cudaStream_t st, int n, double* A, int lda, int* d_info);
 // X = U^-1
 void trinv_upper(cudaStream_t st, int n, const double* U, int ldu, double* X, int ldx);
 // Householder reduction to tridiagonal form (A destroyed); V[n*n], tau[n], d[n], e[n]; p[2n] scratch
+// Householder tridiagonalisation of the symmetric n x n matrix A (one cooperative launch).
+// p: sytrd_workspace(n) doubles of device scratch.
+constexpr int SYTRD_SLOTS = 256;   // most blocks of the cooperative tridiagonalisation
+inline size_t sytrd_workspace(int n) { return 2 * (size_t)n + 2 * (size_t)SYTRD_SLOTS; }
 void sytrd(cudaStream_t st, int n, double* A, int lda, double* V, double* tau, double* d, double* e, double* p);
 // eigenvalues of the tridiagonal (d, e): w[n] ascending; e2: n, bounds: 4
 void tridiag_eigvals(cudaStream_t st, int n, const double* d, const double* e, double* e2, double* bounds, double* w);
@@ -47,5 +51,7 @@ double fp64_peak_tflops();
 // dependent-operation latency in cycles: [0] FP64 FMA, [1] FP64 add, [2] FP64 multiply,
 // [3] FP64 divide, [4] FP32 FMA
 void fp64_latency_cycles(double* cycles);
+// Largest error of the fast FP64 reciprocal in ulps (out[0]) over out[1] checked values.
+void reciprocal_check(double* out);
 
 }  // namespace xg

@@ -149,21 +149,58 @@ __device__ inline void d_trinv_col(int n, const double* __restrict__ U, int ldu,
 // pending vectors it keeps in shared memory.  p alternates between two buffers
 // (p[0..n) and p[n..2n)), so one grid-wide barrier per column suffices: a block
 // still reading p of step k cannot meet a writer of the same buffer before the
-// barrier of step k+1.
+// barrier of step k+1.  The grid form also leaves each block's share of p.v in
+// two alternating slot arrays (after p: 2 x SYTRD_SLOTS doubles), which every block
+// sums in the same order after the barrier.
+//
+// Each warp streams its row in chunks of 32 x RT elements with the next chunk's loads
+// issued before the current chunk is processed: the trailing matrix lives in L2, and a
+// row pass that waits for every load is bound by L2 latency, not by the FP64 pipe.
 //
 // CTA = true: the whole reduction by one thread block (__syncthreads for the barrier),
-// used by the batched engine; CTA = false: all blocks of a cooperative launch.
-// sm: 4n + 32 doubles of shared memory.
+// used by the batched engine; CTA = false: all blocks of a cooperative launch (at most
+// SYTRD_SLOTS blocks).  sm: 4n + 68 doubles of shared memory (4n + 32 for CTA = true
+// with at most 32 warps).
+
+// Sum of red[0..nw) in four interleaved chains (nw a multiple of 4; FP64 additions have a
+// long dependent latency, so a serial sum over the warps of a block is slow).
+__device__ __forceinline__ double sum_slots4(const double* red, int nw) {
+    double t0 = 0.0, t1 = 0.0, t2 = 0.0, t3 = 0.0;
+    for (int k = 0; k < nw; k += 4) {
+        t0 += red[k];
+        t1 += red[k + 1];
+        t2 += red[k + 2];
+        t3 += red[k + 3];
+    }
+    return (t0 + t1) + (t2 + t3);
+}
+
+__device__ __forceinline__ double block_sum4(double v, double* red) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    v = warp_sum(v);
+    __syncthreads();
+    if (lane == 0) red[wid] = v;
+    if (threadIdx.x < 4 && nw + (int)threadIdx.x < ((nw + 3) & ~3)) red[nw + threadIdx.x] = 0.0;
+    __syncthreads();
+    return sum_slots4(red, (nw + 3) & ~3);
+}
+
 template <bool CTA>
 __device__ inline void d_sytrd(int n, double* __restrict__ A, int lda, double* __restrict__ V, double* __restrict__ tau,
-                        double* __restrict__ d, double* __restrict__ e, double* __restrict__ p2, double* sm) {
+                               double* __restrict__ d, double* __restrict__ e, double* __restrict__ p2, double* sm) {
+    constexpr int RT = CTA ? 2 : 8;   // chunk of a row pass: RT elements per lane
     double* v = sm;            // [n] current reflector, offset k+1
     double* w = sm + n;        // [n]
     double* vp = sm + 2 * n;   // [n] pending update (previous step), offset k
     double* wp = sm + 3 * n;   // [n]
-    double* red = sm + 4 * n;  // [32]
-    const int lane = threadIdx.x & 31;
-    const int gwarp = CTA ? (int)(threadIdx.x >> 5) : (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    double* red = sm + 4 * n;  // [36] block reductions
+    double* wred = red + 36;   // [32] per-warp p.v of the grid form
+    double* slots = p2 + 2 * (size_t)n;   // grid form: [2][SYTRD_SLOTS] per-block p.v
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    // grid form: consecutive rows go to consecutive blocks (warp w of block b takes rows
+    // w*G + b (mod G*warps)), so that every SM's FP64 pipe gets a share of the trailing rows
+    // even when there are fewer rows than warps
+    const int gwarp = CTA ? wid : (int)(wid * gridDim.x + blockIdx.x);
     const int nwarps = CTA ? (int)(blockDim.x >> 5) : (int)((gridDim.x * blockDim.x) >> 5);
     const bool lead = CTA || blockIdx.x == 0;
     double tprev = 0.0;        // tau of the pending update (0: nothing pending)
@@ -171,6 +208,7 @@ __device__ inline void d_sytrd(int n, double* __restrict__ A, int lda, double* _
     for (int k = 0; k < n - 2; ++k) {
         const int m = n - k - 1;
         double* p = p2 + (size_t)(k & 1) * n;
+        double* slot = slots + (size_t)(k & 1) * SYTRD_SLOTS;
         const double* xk = A + (size_t)k * lda + k + 1;   // row k, pending update of step k-1 missing
         const bool pend = tprev != 0.0;
         const double v0 = pend ? vp[0] : 0.0, w0 = pend ? wp[0] : 0.0;
@@ -181,7 +219,7 @@ __device__ inline void d_sytrd(int n, double* __restrict__ A, int lda, double* _
             v[i] = xv;
             if (i > 0) ss += xv * xv;
         }
-        const double xnorm2 = block_sum(ss, red);
+        const double xnorm2 = block_sum4(ss, red);
         const double alpha = v[0];
         double beta, tk, scale;
         if (xnorm2 == 0.0) {
@@ -205,50 +243,76 @@ __device__ inline void d_sytrd(int n, double* __restrict__ A, int lda, double* _
             }
         }
         // rows k+1 .. n-1: apply the pending update of step k-1 (cols >= k+1) and form
-        // p = tau A22 v
+        // p = tau A22 v; the grid form also accumulates this warp's share of p.v
+        double pvw = 0.0;
         for (int r = gwarp; r < m; r += nwarps) {
             double* arow = A + (size_t)(k + 1 + r) * lda + k + 1;
             const double vr = pend ? vp[r + 1] : 0.0, wr = pend ? wp[r + 1] : 0.0;
             // two FMAs per element for the rank-2 update, two accumulators for the dot (FP64
             // latency is long: independent chains keep the pipe busy)
             double s0 = 0.0, s1 = 0.0;
-            int c = lane;
-            for (; c + 32 < m; c += 64) {
-                double a0 = arow[c], a1 = arow[c + 32];
-                if (pend) {
-                    a0 = fma(-vr, wp[c + 1], a0);
-                    a1 = fma(-vr, wp[c + 33], a1);
-                    a0 = fma(-wr, vp[c + 1], a0);
-                    a1 = fma(-wr, vp[c + 33], a1);
-                    arow[c] = a0;
-                    arow[c + 32] = a1;
-                }
-                s0 = fma(a0, v[c], s0);
-                s1 = fma(a1, v[c + 32], s1);
+            double nx[RT];
+#pragma unroll
+            for (int t = 0; t < RT; ++t) {
+                const int c = lane + 32 * t;
+                nx[t] = c < m ? arow[c] : 0.0;
             }
-            if (c < m) {
-                double a0 = arow[c];
-                if (pend) {
-                    a0 = fma(-vr, wp[c + 1], a0);
-                    a0 = fma(-wr, vp[c + 1], a0);
-                    arow[c] = a0;
+            for (int c0 = 0; c0 < m; c0 += 32 * RT) {
+                double cu[RT];
+#pragma unroll
+                for (int t = 0; t < RT; ++t) cu[t] = nx[t];
+#pragma unroll
+                for (int t = 0; t < RT; ++t) {
+                    const int c = c0 + 32 * RT + lane + 32 * t;
+                    nx[t] = c < m ? arow[c] : 0.0;
                 }
-                s0 = fma(a0, v[c], s0);
+#pragma unroll
+                for (int t = 0; t < RT; ++t) {
+                    const int c = c0 + lane + 32 * t;
+                    if (c < m) {
+                        double a = cu[t];
+                        if (pend) {
+                            a = fma(-vr, wp[c + 1], a);
+                            a = fma(-wr, vp[c + 1], a);
+                            arow[c] = a;
+                        }
+                        if (t & 1) s1 = fma(a, v[c], s1);
+                        else s0 = fma(a, v[c], s0);
+                    }
+                }
             }
             const double sdot = warp_sum(s0 + s1);
-            if (lane == 0) p[r] = tk * sdot;
+            const double pr = tk * sdot;
+            if (lane == 0) p[r] = pr;
+            if constexpr (!CTA) pvw = fma(pr, v[r], pvw);
         }
-        if constexpr (CTA) __syncthreads();
-        else cg::this_grid().sync();
+        if constexpr (CTA) {
+            __syncthreads();
+        } else {
+            // this block's share of p.v: one value per warp, summed in warp order
+            if (lane == 0) wred[wid] = pvw;
+            __syncthreads();
+            if (threadIdx.x == 0) slot[blockIdx.x] = sum_slots4(wred, (int)(blockDim.x >> 5));
+            cg::this_grid().sync();
+        }
         // w = p - (tau/2)(p.v) v; it becomes the pending update (offset k+1)
         if (tk != 0.0) {
-            double pv = 0.0;
-            for (int i = threadIdx.x; i < m; i += blockDim.x) {
-                const double pi = p[i];
-                w[i] = pi;
-                pv += pi * v[i];
+            double pv;
+            if constexpr (CTA) {
+                pv = 0.0;
+                for (int i = threadIdx.x; i < m; i += blockDim.x) {
+                    const double pi = p[i];
+                    w[i] = pi;
+                    pv += pi * v[i];
+                }
+                pv = block_sum4(pv, red);
+            } else {
+                // copy p (its loads overlap the slot sum), then the slot sum in block order
+                for (int i = threadIdx.x; i < m; i += blockDim.x) w[i] = p[i];
+                double t = 0.0;
+                for (int b = lane; b < (int)gridDim.x; b += 32) t += slot[b];
+                pv = warp_sum(t);
             }
-            pv = block_sum(pv, red);
             const double kk = -0.5 * tk * pv;
             for (int i = threadIdx.x; i < m; i += blockDim.x) w[i] += kk * v[i];
         }
@@ -284,7 +348,6 @@ __device__ inline void d_sytrd(int n, double* __restrict__ A, int lda, double* _
         tau[n - 1] = 0.0;
     }
 }
-
 
 // Number of eigenvalues of T below x, from the sign changes of the leading principal minors
 // p_i = (d_i - x) p_{i-1} - e_{i-1}^2 p_{i-2}, p_{-1} = 1 (Sturm sequence, three-term form).
@@ -474,12 +537,134 @@ __device__ inline void stage_tridiag(int n, const double* __restrict__ d, const 
     }
 }
 
+// |a| < |b| for doubles that are not NaN, by comparing the magnitude bits as integers.
+__device__ __forceinline__ bool abs_less(double a, double b) {
+    const unsigned long long m = 0x7fffffffffffffffULL;
+    return ((unsigned long long)__double_as_longlong(a) & m) < ((unsigned long long)__double_as_longlong(b) & m);
+}
+
+// LU factors of T - lam I with partial pivoting, row i of U scaled by its pivot:
+// U1 = 1/u_ii, U2 = u_i,i+1/u_ii, U3 = u_i,i+2/u_ii, ML = multiplier, piv = rows i, i+1
+// interchanged.  The solve of (T - lam I) x = b is then
+//   forward:  b_i <-> b_i+1 if piv_i; b_i+1 -= ML_i b_i
+//   backward: x_i = U1_i b_i - U2_i x_i+1 - U3_i x_i+2
+// so that one FMA per row sits on the dependent chain of the back substitution.
+
+// Forward elimination of column j of Y in place, with the right-hand side scaled by `scale`
+// as it is read (or, with gen != nullptr, generated on the fly).  Returns the last element,
+// which is not stored.  Loads run CH rows ahead of the dependent chain.
+template <int CH>
+__device__ __forceinline__ double lu_forward(int n, double* __restrict__ y, size_t sn, const double* __restrict__ ml,
+                                             const unsigned char* __restrict__ pv, double scale, uint32_t* gen) {
+    auto rhs = [&](int i, double loaded) -> double {
+        if (gen) {
+            uint32_t s = *gen;
+            s ^= s << 13; s ^= s >> 17; s ^= s << 5;
+            *gen = s;
+            return 0.5 + (double)(s & 0xffffff) / (double)0x1000000;
+        }
+        return loaded * scale;
+    };
+    double cur = rhs(0, gen ? 0.0 : y[0]);
+    double nb[CH], nm[CH];
+    unsigned char np[CH];
+#pragma unroll
+    for (int t = 0; t < CH; ++t) {
+        const int i = t;
+        const bool ok = i < n - 1;
+        nb[t] = (ok && !gen) ? y[(size_t)(i + 1) * sn] : 0.0;
+        nm[t] = ok ? ml[(size_t)i * sn] : 0.0;
+        np[t] = ok ? pv[(size_t)i * sn] : 0;
+    }
+    for (int i0 = 0; i0 < n - 1; i0 += CH) {
+        double cb[CH], cm[CH];
+        unsigned char cp[CH];
+#pragma unroll
+        for (int t = 0; t < CH; ++t) { cb[t] = nb[t]; cm[t] = nm[t]; cp[t] = np[t]; }
+#pragma unroll
+        for (int t = 0; t < CH; ++t) {
+            const int i = i0 + CH + t;
+            const bool ok = i < n - 1;
+            nb[t] = (ok && !gen) ? y[(size_t)(i + 1) * sn] : 0.0;
+            nm[t] = ok ? ml[(size_t)i * sn] : 0.0;
+            np[t] = ok ? pv[(size_t)i * sn] : 0;
+        }
+#pragma unroll
+        for (int t = 0; t < CH; ++t) {
+            const int i = i0 + t;
+            if (i < n - 1) {
+                const double bn = rhs(i + 1, cb[t]);
+                const double bi = cp[t] ? bn : cur;
+                const double bo = cp[t] ? cur : bn;
+                y[(size_t)i * sn] = bi;
+                cur = fma(-cm[t], bi, bo);
+            }
+        }
+    }
+    return cur;
+}
+
+// Back substitution of column j of Y in place; `last` is the forward result of row n-1.
+// Returns max |x_i| and accumulates sum x_i^2 into *nrm2.
+template <int CH>
+__device__ __forceinline__ double lu_backward(int n, double* __restrict__ y, size_t sn, const double* __restrict__ u1,
+                                              const double* __restrict__ u2, const double* __restrict__ u3,
+                                              double last, double* nrm2) {
+    double x1 = last * u1[(size_t)(n - 1) * sn], x2 = 0.0;
+    y[(size_t)(n - 1) * sn] = x1;
+    double mx = fabs(x1), s2 = x1 * x1;
+    double nb[CH], n1[CH], n2[CH], n3[CH];
+#pragma unroll
+    for (int t = 0; t < CH; ++t) {
+        const int i = n - 2 - t;
+        const bool ok = i >= 0;
+        const size_t o = ok ? (size_t)i * sn : 0;
+        nb[t] = ok ? y[o] : 0.0;
+        n1[t] = ok ? u1[o] : 0.0;
+        n2[t] = ok ? u2[o] : 0.0;
+        n3[t] = ok ? u3[o] : 0.0;
+    }
+    for (int i0 = n - 2; i0 >= 0; i0 -= CH) {
+        double cb[CH], c1[CH], c2[CH], c3[CH];
+#pragma unroll
+        for (int t = 0; t < CH; ++t) { cb[t] = nb[t]; c1[t] = n1[t]; c2[t] = n2[t]; c3[t] = n3[t]; }
+#pragma unroll
+        for (int t = 0; t < CH; ++t) {
+            const int i = i0 - CH - t;
+            const bool ok = i >= 0;
+            const size_t o = ok ? (size_t)i * sn : 0;
+            nb[t] = ok ? y[o] : 0.0;
+            n1[t] = ok ? u1[o] : 0.0;
+            n2[t] = ok ? u2[o] : 0.0;
+            n3[t] = ok ? u3[o] : 0.0;
+        }
+#pragma unroll
+        for (int t = 0; t < CH; ++t) {
+            const int i = i0 - t;
+            if (i >= 0) {
+                const double x = fma(-c2[t], x1, fma(-c3[t], x2, cb[t] * c1[t]));
+                y[(size_t)i * sn] = x;
+                x2 = x1;
+                x1 = x;
+                mx = fmax(mx, fabs(x));
+                s2 = fma(x, x, s2);
+            }
+        }
+    }
+    *nrm2 = s2;
+    return mx;
+}
+
 // Eigenvector j of T for eigenvalue w[j]; output Y[i*n + j].  Scratch arrays are
 // [i*n + j] so that the threads of a warp (consecutive j) access consecutive words.
+// Three steps of inverse iteration from a deterministic pseudo-random start (dstein's
+// scheme without its convergence test); each step's right-hand side is the previous
+// solution scaled by its largest element, and the result is normalised to unit length.
+template <int CH = 8>
 __device__ inline void d_inviter(int n, const double* __restrict__ d, const double* __restrict__ e,
-                          const double* __restrict__ w, const double* __restrict__ bounds, double* __restrict__ Y,
-                          double* __restrict__ U1, double* __restrict__ U2, double* __restrict__ U3,
-                          double* __restrict__ ML, unsigned char* __restrict__ piv, int j) {
+                                 const double* __restrict__ w, const double* __restrict__ bounds, double* __restrict__ Y,
+                                 double* __restrict__ U1, double* __restrict__ U2, double* __restrict__ U3,
+                                 double* __restrict__ ML, unsigned char* __restrict__ piv, int j) {
     const double tnorm = fmax(bounds[3], 1e-300);
     const double eps = 2.220446049250313e-16;
     double lam = w[j];
@@ -490,88 +675,58 @@ __device__ inline void d_inviter(int n, const double* __restrict__ d, const doub
         lam += (double)(j - k) * 10.0 * eps * tnorm;
     }
     const double pert = eps * tnorm;
-    auto at = [n, j](int i) { return (size_t)i * n + j; };
-    if (n == 1) { Y[at(0)] = 1.0; return; }
-    // LU with partial pivoting of T - lam I
+    const size_t sn = (size_t)n;
+    if (n == 1) { Y[j] = 1.0; return; }
+    double* y = Y + j;
+    double* u1 = U1 + j;
+    double* u2 = U2 + j;
+    double* u3 = U3 + j;
+    double* ml = ML + j;
+    unsigned char* pv = piv + j;
+    // LU with partial pivoting of T - lam I.  Rows i (current: w0, w1, 0) and i+1
+    // (e_i, d_i+1 - lam, e_i+1): the larger first entry becomes the pivot row.
     double w0 = d[0] - lam, w1 = e[0];
     for (int i = 0; i < n - 1; ++i) {
         const double sub = e[i];
         const double nd = d[i + 1] - lam;
         const double ns = (i + 1 < n - 1) ? e[i + 1] : 0.0;
-        if (fabs(w0) >= fabs(sub)) {
-            double u0 = w0;
-            if (fabs(u0) < pert) u0 = copysign(pert, u0 == 0.0 ? 1.0 : u0);
-            const double r0 = 1.0 / u0;
-            const double m = sub * r0;
-            U1[at(i)] = r0; U2[at(i)] = w1; U3[at(i)] = 0.0; ML[at(i)] = m; piv[at(i)] = 0;
-            w0 = nd - m * w1;
-            w1 = ns;
-        } else {
-            const double r0 = 1.0 / sub;
-            const double m = w0 * r0;
-            U1[at(i)] = r0; U2[at(i)] = nd; U3[at(i)] = ns; ML[at(i)] = m; piv[at(i)] = 1;
-            w0 = w1 - m * nd;
-            w1 = -m * ns;
-        }
+        const bool sw = abs_less(w0, sub);
+        double u0 = w0;
+        if (!sw && abs_less(u0, pert)) u0 = copysign(pert, u0 == 0.0 ? 1.0 : u0);
+        const double p0 = sw ? sub : u0, p1 = sw ? nd : w1, p2 = sw ? ns : 0.0;   // pivot row
+        const double o0 = sw ? w0 : sub, o1 = sw ? w1 : nd, o2 = sw ? 0.0 : ns;   // eliminated row
+        const double r0 = rcp_fast(p0);
+        const double m = o0 * r0;
+        const size_t o = (size_t)i * sn;
+        u1[o] = r0;
+        u2[o] = p1 * r0;
+        u3[o] = p2 * r0;
+        ml[o] = m;
+        pv[o] = sw ? 1 : 0;
+        w0 = fma(-o0 * p1, r0, o1);
+        w1 = fma(-m, p2, o2);
     }
-    if (fabs(w0) < pert) w0 = copysign(pert, w0 == 0.0 ? 1.0 : w0);
-    U1[at(n - 1)] = 1.0 / w0;   // U1 holds reciprocal pivots
-    // start vector: deterministic pseudo-random
-    uint32_t s = 0x9e3779b9u ^ (uint32_t)(j * 2654435761u);
-    for (int i = 0; i < n; ++i) {
-        s ^= s << 13; s ^= s >> 17; s ^= s << 5;
-        Y[at(i)] = 0.5 + (double)(s & 0xffffff) / (double)0x1000000;
-    }
+    if (abs_less(w0, pert)) w0 = copysign(pert, w0 == 0.0 ? 1.0 : w0);
+    u1[(size_t)(n - 1) * sn] = rcp_fast(w0);
+    uint32_t seed = 0x9e3779b9u ^ (uint32_t)(j * 2654435761u);
+    double scale = 1.0, nrm2 = 1.0;
     for (int iter = 0; iter < 3; ++iter) {
-        // forward: apply row interchanges and multipliers
-        for (int i = 0; i < n - 1; ++i) {
-            double bi = Y[at(i)], bn = Y[at(i + 1)];
-            if (piv[at(i)]) { const double t = bi; bi = bn; bn = t; Y[at(i)] = bi; }
-            Y[at(i + 1)] = bn - ML[at(i)] * bi;
-        }
-        // back substitution
-        double x2 = 0.0, x1 = Y[at(n - 1)] * U1[at(n - 1)];
-        Y[at(n - 1)] = x1;
-        double mx = fabs(x1);
-        for (int i = n - 2; i >= 0; --i) {
-            const double x = (Y[at(i)] - U2[at(i)] * x1 - U3[at(i)] * x2) * U1[at(i)];
-            Y[at(i)] = x;
-            x2 = x1;
-            x1 = x;
-            mx = fmax(mx, fabs(x));
-        }
-        // normalise (scale by max first to avoid overflow)
-        const double inv = 1.0 / mx;
-        double nrm = 0.0;
-        for (int i = 0; i < n; ++i) {
-            const double x = Y[at(i)] * inv;
-            Y[at(i)] = x;
-            nrm += x * x;
-        }
-        const double sc = 1.0 / sqrt(nrm);
-        for (int i = 0; i < n; ++i) Y[at(i)] *= sc;
+        const double last = lu_forward<CH>(n, y, sn, ml, pv, scale, iter == 0 ? &seed : nullptr);
+        const double mx = lu_backward<CH>(n, y, sn, u1, u2, u3, last, &nrm2);
+        scale = 1.0 / mx;
     }
+    const double sc = 1.0 / sqrt(nrm2);
+    for (int i = 0; i < n; ++i) y[(size_t)i * sn] *= sc;
 }
 
-
-// Solve (T - lam_j I) x = b in place on column j of Y with the stored LU factors (one thread).
+// One solve of (T - lam I) x = b for column j of Y with the factors of d_inviter (used by the
+// cluster re-orthogonalisation).
 __device__ inline void tri_solve_col(int n, int j, const double* __restrict__ U1, const double* __restrict__ U2,
-                              const double* __restrict__ U3, const double* __restrict__ ML,
-                              const unsigned char* __restrict__ piv, double* __restrict__ Y) {
-    auto at = [n, j](int i) { return (size_t)i * n + j; };
-    for (int i = 0; i < n - 1; ++i) {
-        double bi = Y[at(i)], bn = Y[at(i + 1)];
-        if (piv[at(i)]) { const double t = bi; bi = bn; bn = t; Y[at(i)] = bi; }
-        Y[at(i + 1)] = bn - ML[at(i)] * bi;
-    }
-    double x2 = 0.0, x1 = Y[at(n - 1)] * U1[at(n - 1)];
-    Y[at(n - 1)] = x1;
-    for (int i = n - 2; i >= 0; --i) {
-        const double x = (Y[at(i)] - U2[at(i)] * x1 - U3[at(i)] * x2) * U1[at(i)];
-        Y[at(i)] = x;
-        x2 = x1;
-        x1 = x;
-    }
+                                     const double* __restrict__ U3, const double* __restrict__ ML,
+                                     const unsigned char* __restrict__ piv, double* __restrict__ Y) {
+    double nrm2;
+    const double last = lu_forward<2>(n, Y + j, (size_t)n, ML + j, piv + j, 1.0, nullptr);
+    lu_backward<2>(n, Y + j, (size_t)n, U1 + j, U2 + j, U3 + j, last, &nrm2);
 }
 
 // Clusters of (near-)degenerate eigenvalues (gap < ctol*||T||): inverse iteration with

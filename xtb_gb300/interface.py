@@ -79,8 +79,10 @@ def load_library(path=LIBPATH):
         "xtbgb_getTransferBytes": (None, [vp, vp, C.POINTER(C.c_longlong)]),
         "xtbgb_setKeepOrbitals": (None, [vp, vp, C.c_int]),
         "xtbgb_setPrecision": (None, [vp, vp, C.c_int, C.c_int]),
+        "xtbgb_setBlockedBacktransform": (None, [vp, vp, C.c_int]),
         "xtbgb_fp64PeakTflops": (C.c_double, []),
         "xtbgb_fp64LatencyCycles": (None, [dp]),
+        "xtbgb_reciprocalCheck": (C.c_int, [dp]),
         "xtbgb_splitGemmCheck": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, dp]),
         "xtbgb_repulsionNoAlloc": (C.c_int, [C.c_int, vp, vp, vp, vp, vp, C.c_char_p, C.c_int]),
         "xtbgb_newBatch": (vp, [vp, C.c_int, ip, ip, dp, dp, ip]),
@@ -136,7 +138,7 @@ class Calculator:
     """GFN2-xTB single point through the C ABI (numbers, positions in Bohr)."""
 
     def __init__(self, numbers, positions, charge=0.0, uhf=0, accuracy=1.0, etemp=300.0, maxiter=250,
-                 verbosity=0, keep_orbitals=True, precision="fp64", slices=5):
+                 verbosity=0, keep_orbitals=True, precision="fp64", slices=5, blocked_min=None):
         self.lib = load_library()
         self.env = Environment(verbosity)
         self.numbers = np.ascontiguousarray(numbers, dtype=np.int32)
@@ -156,6 +158,8 @@ class Calculator:
         self.lib.xtb_setMaxIter(self.env.h, self.calc, maxiter)
         self.lib.xtbgb_setKeepOrbitals(self.env.h, self.calc, int(bool(keep_orbitals)))
         self.lib.xtbgb_setPrecision(self.env.h, self.calc, 1 if precision == "split" else 0, slices)
+        if blocked_min is not None:
+            self.lib.xtbgb_setBlockedBacktransform(self.env.h, self.calc, int(blocked_min))
         self.env.check()
         self.res = C.c_void_p(self.lib.xtb_newResults())
 
