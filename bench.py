@@ -258,7 +258,8 @@ def run_served(args, ws, rank):
                   "path": "xtb_singlepoint per request, one after another"},
         "speedup_vs_plain": (ws * args.steps * R / wall) / (R / plain_wall),
         "parity_vs_plain": {"max_abs_dE": dE, "max_abs_dq": dq, "max_abs_dg": dg, "max_iter_diff": iters_diff,
-                            "failed_requests": len(bad)},
+                            "failed_requests": len(bad),
+                            "errors": sorted({f"nao {x.nao}: {x.error}" for x in bad})[:5]},
         "e2e": {"value": ws * args.steps * R / wall, "unit": "single points/s",
                 "h2d_bytes_per_step": int(d["h2d_bytes"] / args.steps),
                 "d2h_bytes_per_step": int(d["d2h_bytes"] / args.steps)},
@@ -576,7 +577,7 @@ def main():
     ap.add_argument("--seed", type=int, default=11, help="served: stream seed")
     ap.add_argument("--rate", type=float, default=None, help="served: Poisson arrival rate (default: saturation)")
     ap.add_argument("--workers", type=int, default=6, help="served: plain-engine workers")
-    ap.add_argument("--iters-per-step", type=int, default=4, help="served: SCC iterations per pool step")
+    ap.add_argument("--iters-per-step", type=int, default=1, help="served: SCC iterations per pool step")
     ap.add_argument("--pool-gib", type=float, default=24.0, help="served: HBM budget of the resident pool")
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="CPU restatement: seconds of work")
     ap.add_argument("--cpu-max-atoms", type=int, default=120)

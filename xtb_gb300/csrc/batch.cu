@@ -617,11 +617,7 @@ void DeviceBatch::load(const std::vector<const HostMol*>& mols, const std::vecto
 void launch_step(BatchMol* d_mols, int nmol, int max_nao, int max_nsh, const BatchSettings& set, int max_iter,
                  cudaStream_t st, cudaEvent_t ev0 = nullptr, cudaEvent_t ev1 = nullptr) {
     const size_t smem = (size_t)std::max(12 * max_nao + 32, GEMM_SMEM) * sizeof(double);
-    static size_t smem_set = 0;
-    if (smem > 48 * 1024 && smem > smem_set) {
-        XG_CUDA(cudaFuncSetAttribute(k_batch_scc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        smem_set = smem;
-    }
+    if (smem > 48 * 1024) allow_max_dynamic_smem((const void*)k_batch_scc);
     const DevThresh th = thresholds(set.accuracy);
     k_batch_setup_a<<<nmol, BT, 0, st>>>(d_mols, nmol);
     XG_LAUNCH_CHECK();

@@ -3,8 +3,11 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <cstdio>
+#include <mutex>
+#include <set>
 #include <stdexcept>
 #include <string>
+#include <utility>
 
 namespace xg {
 
@@ -18,6 +21,26 @@ struct CudaError : std::runtime_error {
         if (e_ != cudaSuccess)                                                             \
             throw ::xg::CudaError(std::string(#call) + ": " + cudaGetErrorString(e_));     \
     } while (0)
+
+// Allow `kernel` the device's largest opt-in dynamic shared memory, once per device.  The
+// limit is a process-wide property of the function: setting it before each launch to that
+// launch's own size races with host threads that launch the same kernel with a larger size
+// (a launch that falls between the other thread's two calls fails), so every launcher sets
+// the same, largest value.
+inline void allow_max_dynamic_smem(const void* kernel) {
+    static std::mutex mu;
+    static std::set<std::pair<const void*, int>> done;
+    int dev = 0;
+    XG_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(mu);
+    if (done.count({kernel, dev})) return;
+    int mx = 0;
+    XG_CUDA(cudaDeviceGetAttribute(&mx, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    cudaFuncAttributes fa;
+    XG_CUDA(cudaFuncGetAttributes(&fa, kernel));
+    XG_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, mx - (int)fa.sharedSizeBytes));
+    done.insert({kernel, dev});
+}
 
 // kernel launches issued by this thread (every launch is followed by XG_LAUNCH_CHECK)
 long long& launch_counter();

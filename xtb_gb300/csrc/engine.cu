@@ -168,7 +168,18 @@ struct Sizer {
 };
 
 thread_local Arena g_arena;
-thread_local cudaStream_t g_stream = nullptr;
+// engine streams of this thread, one per stream priority (slot = least priority - priority)
+constexpr int kPrioritySlots = 16;
+thread_local cudaStream_t g_streams[kPrioritySlots] = {};
+
+cudaStream_t engine_stream(int priority) {
+    int least = 0, greatest = 0;
+    XG_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    const int p = std::max(greatest, std::min(least, priority));
+    const int slot = std::min(kPrioritySlots - 1, least - p);
+    if (!g_streams[slot]) XG_CUDA(cudaStreamCreateWithPriority(&g_streams[slot], cudaStreamNonBlocking, p));
+    return g_streams[slot];
+}
 
 // CUDA-event phase timer on the engine stream; elapsed times are read after the final sync.
 struct PhaseTimer {
@@ -230,8 +241,9 @@ T* upload(Arena& ar, cudaStream_t st, const std::vector<T>& v) {
 void run_singlepoint(const HostMol& hm, const SPSettings& set, Wavefunction& wfn, SPResult& res, bool keep_orbitals,
                      bool& scc_failed, bool guess_only) {
     if (device_count() == 0) throw CudaError("no CUDA device available for the GFN2 engine");
-    if (!g_stream) XG_CUDA(cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking));
-    cudaStream_t st = g_stream;
+    // every earlier single point of this thread has been synchronised, so the workspace may
+    // move to a stream of another priority
+    cudaStream_t st = engine_stream(set.stream_priority);
     const int nat = hm.nat, nsh = hm.nsh, nao = hm.nao, ne = hm.nelem;
     const size_t nn = (size_t)nao * nao;
     const size_t aa = (size_t)nat * nat;

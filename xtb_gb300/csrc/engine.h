@@ -22,6 +22,9 @@ struct SPSettings {
     // 178 ms vs 165 ms; split precision 32 ms vs 34 ms and 149 ms vs 101 ms)
     int blocked_min = -1;
     int blocked_threshold() const { return blocked_min >= 0 ? blocked_min : (precision == 1 ? 1000 : 1500); }
+    // CUDA stream priority of the single point's stream (lower is more urgent; clamped to the
+    // device's range; 0 is the default priority)
+    int stream_priority = 0;
 };
 
 // Wavefunction kept between calls on the same results object (res%chk of the reference).

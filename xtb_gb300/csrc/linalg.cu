@@ -216,38 +216,43 @@ void trinv_upper(cudaStream_t st, int n, const double* U, int ldu, double* X, in
     XG_LAUNCH_CHECK();
 }
 
-__global__ void __launch_bounds__(1024) k_sytrd(int n, double* __restrict__ A, int lda, double* __restrict__ V,
+template <int NT>
+__global__ void __launch_bounds__(NT) k_sytrd(int n, double* __restrict__ A, int lda, double* __restrict__ V,
                                                double* __restrict__ tau, double* __restrict__ d, double* __restrict__ e,
                                                double* __restrict__ p2) {
     extern __shared__ double sm[];
     d_sytrd<false>(n, A, lda, V, tau, d, e, p2, sm);
 }
 
+template <int NT>
+static void sytrd_launch(cudaStream_t st, int n, double* A, int lda, double* V, double* tau, double* d, double* e,
+                         double* p, size_t smem) {
+    int dev = 0, nsm = 0, maxblk = 0;
+    XG_CUDA(cudaGetDevice(&dev));
+    XG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    if (smem > 48 * 1024) allow_max_dynamic_smem((const void*)k_sytrd<NT>);
+    XG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxblk, k_sytrd<NT>, NT, smem));
+    if (maxblk < 1) throw CudaError("sytrd: kernel does not fit on an SM");
+    int blocks = std::min(std::min(nsm * maxblk, nsm), std::max(1, ceil_div(n, NT / 32)));
+    blocks = std::min(blocks, SYTRD_SLOTS);
+    void* args[] = {&n, &A, &lda, &V, &tau, &d, &e, &p};
+    XG_CUDA(cudaLaunchCooperativeKernel((void*)k_sytrd<NT>, blocks, NT, args, smem, st));
+    ++launch_counter();
+}
+
 void sytrd(cudaStream_t st, int n, double* A, int lda, double* V, double* tau, double* d, double* e, double* p) {
-    static int nsm = 0, maxblk = 0;
     const size_t smem = (size_t)(4 * n + 72) * sizeof(double);
     if (n <= 2) {
         // trivial: copy diagonal / off-diagonal
-        k_sytrd<<<1, 256, smem, st>>>(n, A, lda, V, tau, d, e, p);
+        k_sytrd<256><<<1, 256, smem, st>>>(n, A, lda, V, tau, d, e, p);
         XG_LAUNCH_CHECK();
         return;
     }
-    int dev;
-    XG_CUDA(cudaGetDevice(&dev));
-    XG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    if (smem > 48 * 1024)
-        XG_CUDA(cudaFuncSetAttribute(k_sytrd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     // More warps per block only for the largest matrices (measured: 1024 threads gain 7% at
     // n = 6000, 512 threads lose 19% at n = 1800 and 47% at n = 1202); at most one block per
     // SM, because every block repeats the O(n) per-column vector work.
-    const int threads = n >= 4000 ? 1024 : 256;
-    XG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxblk, k_sytrd, threads, smem));
-    if (maxblk < 1) throw CudaError("sytrd: kernel does not fit on an SM");
-    int blocks = std::min(std::min(nsm * maxblk, nsm), std::max(1, ceil_div(n, threads / 32)));
-    blocks = std::min(blocks, SYTRD_SLOTS);
-    void* args[] = {&n, &A, &lda, &V, &tau, &d, &e, &p};
-    XG_CUDA(cudaLaunchCooperativeKernel((void*)k_sytrd, blocks, threads, args, smem, st));
-    ++launch_counter();
+    if (n >= 4000) sytrd_launch<1024>(st, n, A, lda, V, tau, d, e, p, smem);
+    else sytrd_launch<256>(st, n, A, lda, V, tau, d, e, p, smem);
 }
 
 // ------------------------------------------------------------------ bisection
@@ -298,7 +303,7 @@ void tridiag_eigvals(cudaStream_t st, int n, const double* d, const double* e, d
     const size_t smem = 2 * (size_t)n * (sizeof(double) + sizeof(float));
     if (smem > 200 * 1024) throw CudaError("tridiag_eigvals: matrix too large for the shared-memory bisection");
     if (smem > 48 * 1024)
-        XG_CUDA(cudaFuncSetAttribute(k_bisect, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        allow_max_dynamic_smem((const void*)k_bisect);
     k_bisect<<<ceil_div(n, 32 / BIS_G), 32, smem, st>>>(n, d, e2, bounds, w);
     XG_LAUNCH_CHECK();
 }
@@ -390,7 +395,7 @@ void ormtr_blocked(cudaStream_t st, int n, const double* V, const double* tau, d
                      ORM_SPLIT, partial, nullptr);
     }
     const size_t smem = (size_t)ORM_NB * LARFT_LD * sizeof(double);
-    XG_CUDA(cudaFuncSetAttribute(k_larft_all, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    allow_max_dynamic_smem((const void*)k_larft_all);
     k_larft_all<<<nblk, 8 * ORM_NB, smem, st>>>(nref, tau, Sall, Tall);
     XG_LAUNCH_CHECK();
     for (int b = nblk - 1; b >= 0; --b) {
@@ -434,7 +439,7 @@ void ormtr_inplace(cudaStream_t st, int n, const double* V, const double* tau, d
     size_t smem = (size_t)wpb * n * sizeof(double);
     while (wpb > 1 && smem > 200 * 1024) { wpb >>= 1; smem = (size_t)wpb * n * sizeof(double); }
     if (smem > 48 * 1024)
-        XG_CUDA(cudaFuncSetAttribute(k_ormtr_inplace, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        allow_max_dynamic_smem((const void*)k_ormtr_inplace);
     k_ormtr_inplace<<<ceil_div(n, wpb), wpb * 32, smem, st>>>(n, V, tau, Y, ncol);
     XG_LAUNCH_CHECK();
 }
@@ -443,7 +448,7 @@ void ormtr(cudaStream_t st, int n, const double* V, const double* tau, const dou
     int wpb = 4;
     size_t smem = (size_t)wpb * n * sizeof(double);
     while (wpb > 1 && smem > 200 * 1024) { wpb >>= 1; smem = (size_t)wpb * n * sizeof(double); }
-    if (smem > 48 * 1024) XG_CUDA(cudaFuncSetAttribute(k_ormtr, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (smem > 48 * 1024) allow_max_dynamic_smem((const void*)k_ormtr);
     k_ormtr<<<ceil_div(n, wpb), wpb * 32, smem, st>>>(n, V, tau, Y, Zt, ncol);
     XG_LAUNCH_CHECK();
 }

@@ -189,10 +189,9 @@ template <bool CTA>
 __device__ inline void d_sytrd(int n, double* __restrict__ A, int lda, double* __restrict__ V, double* __restrict__ tau,
                                double* __restrict__ d, double* __restrict__ e, double* __restrict__ p2, double* sm) {
     constexpr int RT = CTA ? 2 : 8;   // chunk of a row pass: RT elements per lane
-    double* v = sm;            // [n] current reflector, offset k+1
-    double* w = sm + n;        // [n]
-    double* vp = sm + 2 * n;   // [n] pending update (previous step), offset k
-    double* wp = sm + 3 * n;   // [n]
+    // two sets of (reflector v, update vector w), offset k+1 at step k: set `cur` holds step
+    // k's, the other the pending update of step k-1; the roles swap every column, and the
+    // pending set's v buffer receives the next pivot row once step k's row pass is done
     double* red = sm + 4 * n;  // [36] block reductions
     double* wred = red + 36;   // [32] per-warp p.v of the grid form
     double* slots = p2 + 2 * (size_t)n;   // grid form: [2][SYTRD_SLOTS] per-block p.v
@@ -203,24 +202,23 @@ __device__ inline void d_sytrd(int n, double* __restrict__ A, int lda, double* _
     const int gwarp = CTA ? wid : (int)(wid * gridDim.x + blockIdx.x);
     const int nwarps = CTA ? (int)(blockDim.x >> 5) : (int)((gridDim.x * blockDim.x) >> 5);
     const bool lead = CTA || blockIdx.x == 0;
-    double tprev = 0.0;        // tau of the pending update (0: nothing pending)
 
-    for (int k = 0; k < n - 2; ++k) {
+    // Householder reflector of step k from row k's trailing part, already in x[0..m) with the
+    // pending update (pv, pw: step k-1's v, w; ptau = 0 when there is none) still missing.
+    // Leaves v_k in x and returns tau_k; the lead block stores v_k, tau_k, d_k, e_k.
+    auto reflector = [&](int k, double* x, const double* pv, const double* pw, double ptau) -> double {
         const int m = n - k - 1;
-        double* p = p2 + (size_t)(k & 1) * n;
-        double* slot = slots + (size_t)(k & 1) * SYTRD_SLOTS;
-        const double* xk = A + (size_t)k * lda + k + 1;   // row k, pending update of step k-1 missing
-        const bool pend = tprev != 0.0;
-        const double v0 = pend ? vp[0] : 0.0, w0 = pend ? wp[0] : 0.0;
+        const bool pend = ptau != 0.0;
+        const double v0 = pend ? pv[0] : 0.0, w0 = pend ? pw[0] : 0.0;
         double ss = 0.0;
         for (int i = threadIdx.x; i < m; i += blockDim.x) {
-            double xv = xk[i];
-            if (pend) xv -= v0 * wp[i + 1] + w0 * vp[i + 1];
-            v[i] = xv;
+            double xv = x[i];
+            if (pend) xv -= v0 * pw[i + 1] + w0 * pv[i + 1];
+            x[i] = xv;
             if (i > 0) ss += xv * xv;
         }
         const double xnorm2 = block_sum4(ss, red);
-        const double alpha = v[0];
+        const double alpha = x[0];
         double beta, tk, scale;
         if (xnorm2 == 0.0) {
             tk = 0.0;
@@ -232,16 +230,35 @@ __device__ inline void d_sytrd(int n, double* __restrict__ A, int lda, double* _
             scale = 1.0 / (alpha - beta);
         }
         __syncthreads();
-        for (int i = threadIdx.x; i < m; i += blockDim.x) v[i] = (i == 0) ? 1.0 : v[i] * scale;
+        for (int i = threadIdx.x; i < m; i += blockDim.x) x[i] = (i == 0) ? 1.0 : x[i] * scale;
         __syncthreads();
         if (lead) {
-            for (int i = threadIdx.x; i < n; i += blockDim.x) V[(size_t)k * n + i] = (i <= k) ? 0.0 : v[i - k - 1];
+            for (int i = threadIdx.x; i < n; i += blockDim.x) V[(size_t)k * n + i] = (i <= k) ? 0.0 : x[i - k - 1];
             if (threadIdx.x == 0) {
                 tau[k] = tk;
                 d[k] = A[(size_t)k * lda + k] - 2.0 * v0 * w0;
                 e[k] = beta;
             }
         }
+        return tk;
+    };
+
+    int cur = 0;
+    double tprev = 0.0;        // tau of the pending update (0: nothing pending)
+    double tk = 0.0;
+    if (n > 2) {
+        for (int i = threadIdx.x; i < n - 1; i += blockDim.x) sm[i] = A[i + 1];
+        tk = reflector(0, sm, nullptr, nullptr, 0.0);
+    }
+    for (int k = 0; k < n - 2; ++k) {
+        const int m = n - k - 1;
+        double* v = sm + (size_t)(2 * cur) * n;
+        double* w = v + n;
+        double* vp = sm + (size_t)(2 * (cur ^ 1)) * n;
+        const double* wp = vp + n;
+        double* p = p2 + (size_t)(k & 1) * n;
+        double* slot = slots + (size_t)(k & 1) * SYTRD_SLOTS;
+        const bool pend = tprev != 0.0;
         // rows k+1 .. n-1: apply the pending update of step k-1 (cols >= k+1) and form
         // p = tau A22 v; the grid form also accumulates this warp's share of p.v
         double pvw = 0.0;
@@ -295,20 +312,22 @@ __device__ inline void d_sytrd(int n, double* __restrict__ A, int lda, double* _
             if (threadIdx.x == 0) slot[blockIdx.x] = sum_slots4(wred, (int)(blockDim.x >> 5));
             cg::this_grid().sync();
         }
-        // w = p - (tau/2)(p.v) v; it becomes the pending update (offset k+1)
+        // p (for w = p - (tau/2)(p.v) v) and the next pivot row (row k+1, cols k+2..) are
+        // loaded together: the pending buffers are free now, and the two loads share one trip
+        // to L2
+        const bool next = k + 1 < n - 2;
+        double* xn = vp;
+        for (int i = threadIdx.x; i < m; i += blockDim.x) {
+            if (tk != 0.0) w[i] = p[i];
+            if (next && i < m - 1) xn[i] = A[(size_t)(k + 1) * lda + k + 2 + i];
+        }
         if (tk != 0.0) {
             double pv;
             if constexpr (CTA) {
                 pv = 0.0;
-                for (int i = threadIdx.x; i < m; i += blockDim.x) {
-                    const double pi = p[i];
-                    w[i] = pi;
-                    pv += pi * v[i];
-                }
+                for (int i = threadIdx.x; i < m; i += blockDim.x) pv += w[i] * v[i];
                 pv = block_sum4(pv, red);
             } else {
-                // copy p (its loads overlap the slot sum), then the slot sum in block order
-                for (int i = threadIdx.x; i < m; i += blockDim.x) w[i] = p[i];
                 double t = 0.0;
                 for (int b = lane; b < (int)gridDim.x; b += 32) t += slot[b];
                 pv = warp_sum(t);
@@ -317,14 +336,15 @@ __device__ inline void d_sytrd(int n, double* __restrict__ A, int lda, double* _
             for (int i = threadIdx.x; i < m; i += blockDim.x) w[i] += kk * v[i];
         }
         __syncthreads();
-        if (tk != 0.0)
-            for (int i = threadIdx.x; i < m; i += blockDim.x) { vp[i] = v[i]; wp[i] = w[i]; }
         tprev = tk;
-        __syncthreads();
+        if (next) tk = reflector(k + 1, xn, v, w, tprev);
+        cur ^= 1;
     }
     if (lead && threadIdx.x == 0) {
         if (n >= 3) {
             // rows n-2 and n-1 still carry the pending update of step n-3 (offset n-2)
+            const double* vp = sm + (size_t)(2 * (cur ^ 1)) * n;
+            const double* wp = vp + n;
             double a11 = A[(size_t)(n - 2) * lda + n - 2];
             double a21 = A[(size_t)(n - 1) * lda + n - 2];
             double a22 = A[(size_t)(n - 1) * lda + n - 1];

@@ -230,6 +230,7 @@ void Server::pool_body() {
 void Server::plain_loop() {
     for (;;) {
         std::unique_ptr<Req> r;
+        int rank = 0;
         {
             std::unique_lock<std::mutex> lk(mu_);
             cv_work_.wait(lk, [&] { return (stop_ && pool_done_) || !large_q_.empty(); });
@@ -241,6 +242,11 @@ void Server::plain_loop() {
                                        });
             r = std::move(*it);
             large_q_.erase(it);
+            // the critical path of a saturated stream runs through the largest requests: the
+            // k-th largest of those in flight gets the k-th most urgent stream priority, so its
+            // blocks are dispatched before those of smaller requests and of the pool
+            rank = (int)std::distance(running_nao_.upper_bound(r->hm.nao), running_nao_.end());
+            running_nao_.insert(r->hm.nao);
         }
         r->t_start = now();
         Completed c;
@@ -255,6 +261,9 @@ void Server::plain_loop() {
             ps.maxiter = cfg_.set.maxiter;
             ps.precision = cfg_.precision;
             ps.slices = cfg_.slices;
+            int least = 0, greatest = 0;
+            XG_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+            ps.stream_priority = std::min(least, greatest + rank);
             Wavefunction wfn;
             SPResult res;
             bool failed = false;
@@ -280,6 +289,10 @@ void Server::plain_loop() {
         } catch (const std::exception& e) {
             c.error = e.what();
             c.status = BST_NONFINITE;
+        }
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            running_nao_.erase(running_nao_.find(r->hm.nao));
         }
         complete(std::move(c));
     }

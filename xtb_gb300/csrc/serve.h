@@ -14,6 +14,7 @@
 #include <map>
 #include <memory>
 #include <mutex>
+#include <set>
 #include <string>
 #include <thread>
 #include <vector>
@@ -77,6 +78,7 @@ private:
     mutable std::mutex mu_;
     std::condition_variable cv_work_, cv_done_;
     std::deque<std::unique_ptr<Req>> small_q_, large_q_;
+    std::multiset<int> running_nao_;   // AO counts of the requests on the plain workers
     std::map<long long, Completed> done_;
     long long next_id_ = 0;
     bool stop_ = false, pool_done_ = false;

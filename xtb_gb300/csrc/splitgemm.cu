@@ -205,11 +205,7 @@ static void split_gemm_s(cudaStream_t st, bool ta, bool tb, int M, int N, int K,
     k_split_rows<S><<<ceil_div((long)N * 32, 256), 256, 0, st>>>(N, K, Kp, B, ldb, tb ? 0 : 1, dK, Bs, sB);
     XG_LAUNCH_CHECK();
     const size_t smem = (size_t)2 * S * SG_BM * SG_LD * sizeof(__nv_bfloat16);
-    static bool attr = false;
-    if (!attr && smem > 48 * 1024) {
-        XG_CUDA(cudaFuncSetAttribute(k_split_mma<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        attr = true;
-    }
+    if (smem > 48 * 1024) allow_max_dynamic_smem((const void*)k_split_mma<S>);
     dim3 grid(ceil_div(N, SG_BN), ceil_div(M, SG_BM));
     k_split_mma<S><<<grid, 256, smem, st>>>(M, N, Kp, As, Bs, sA, sB, alpha, beta, C, ldc, dN);
     XG_LAUNCH_CHECK();
