@@ -20,20 +20,56 @@ namespace cg = cooperative_groups;
 
 namespace xg {
 
+// Output tile of linear block b in a heaviest-first order, so that the short tiles of a
+// triangular product fill the end of the launch instead of the long ones trailing alone:
+// GF_B_UPPER tiles need K up to j0 + 64 (descending columns first), GF_A_LOWER up to
+// i0 + 64 (descending rows first); GF_SYM enumerates only the tiles on or below the diagonal.
+__device__ __forceinline__ void dgemm_tile_order(int b, int tm, int tn, int flags, int& it, int& jt) {
+    if (flags & GF_SYM) {
+        // rows tm-1, tm-2, ...; row r holds tiles jt = 0..min(r, tn-1)
+        int r = tm - 1;
+        for (;;) {
+            const int cnt = min(r, tn - 1) + 1;
+            if (b < cnt || r == 0) break;
+            b -= cnt;
+            --r;
+        }
+        it = r;
+        jt = b;
+    } else if (flags & GF_B_UPPER) {
+        jt = tn - 1 - b / tm;
+        it = b % tm;
+    } else if (flags & GF_A_LOWER) {
+        it = tm - 1 - b / tn;
+        jt = b % tn;
+    } else {
+        it = b / tn;
+        jt = b % tn;
+    }
+}
+
+inline int dgemm_tile_count(int tm, int tn, int flags) {
+    if (!(flags & GF_SYM)) return tm * tn;
+    int c = 0;
+    for (int r = 0; r < tm; ++r) c += std::min(r, tn - 1) + 1;
+    return c;
+}
+
 template <bool TA, bool TB>
 __global__ void __launch_bounds__(256) k_dgemm(int M, int N, int K, double alpha, const double* __restrict__ A,
                                                int lda, const double* __restrict__ B, int ldb, double beta,
                                                double* __restrict__ C, int ldc, int flags, const int* __restrict__ dK,
                                                const int* __restrict__ dN) {
     __shared__ double smem[GEMM_SMEM];
-    dgemm_tile<TA, TB>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, flags, dK, dN, blockIdx.y * GBM,
-                       blockIdx.x * GBN, smem);
+    int it, jt;
+    dgemm_tile_order((int)blockIdx.x, (M + GBM - 1) / GBM, (N + GBN - 1) / GBN, flags, it, jt);
+    dgemm_tile<TA, TB>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, flags, dK, dN, it * GBM, jt * GBN, smem);
 }
 
 void dgemm(cudaStream_t st, bool ta, bool tb, int M, int N, int K, double alpha, const double* A, int lda,
            const double* B, int ldb, double beta, double* C, int ldc, int flags, const int* dK, const int* dN) {
     if (M <= 0 || N <= 0) return;
-    dim3 grid(ceil_div(N, GBN), ceil_div(M, GBM));
+    const dim3 grid(dgemm_tile_count(ceil_div(M, GBM), ceil_div(N, GBN), flags));
     if (!ta && !tb) k_dgemm<false, false><<<grid, 256, 0, st>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, flags, dK, dN);
     else if (ta && !tb) k_dgemm<true, false><<<grid, 256, 0, st>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, flags, dK, dN);
     else if (!ta && tb) k_dgemm<false, true><<<grid, 256, 0, st>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, flags, dK, dN);
