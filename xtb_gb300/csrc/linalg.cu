@@ -257,7 +257,7 @@ __global__ void __launch_bounds__(NT) k_sytrd(int n, double* __restrict__ A, int
                                                double* __restrict__ tau, double* __restrict__ d, double* __restrict__ e,
                                                double* __restrict__ p2) {
     extern __shared__ double sm[];
-    d_sytrd<false>(n, A, lda, V, tau, d, e, p2, sm);
+    d_sytrd<false, (NT <= 256)>(n, A, lda, V, tau, d, e, p2, sm);
 }
 
 template <int NT>

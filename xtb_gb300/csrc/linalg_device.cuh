@@ -185,7 +185,7 @@ __device__ __forceinline__ double block_sum4(double v, double* red) {
     return sum_slots4(red, (nw + 3) & ~3);
 }
 
-template <bool CTA>
+template <bool CTA, bool PREFETCH = false>
 __device__ inline void d_sytrd(int n, double* __restrict__ A, int lda, double* __restrict__ V, double* __restrict__ tau,
                                double* __restrict__ d, double* __restrict__ e, double* __restrict__ p2, double* sm) {
     constexpr int RT = CTA ? 2 : 8;   // chunk of a row pass: RT elements per lane
@@ -226,8 +226,8 @@ __device__ inline void d_sytrd(int n, double* __restrict__ A, int lda, double* _
             scale = 0.0;
         } else {
             beta = -copysign(sqrt(alpha * alpha + xnorm2), alpha);
-            tk = (beta - alpha) / beta;
-            scale = 1.0 / (alpha - beta);
+            tk = (beta - alpha) * rcp_fast(beta);
+            scale = rcp_fast(alpha - beta);
         }
         __syncthreads();
         for (int i = threadIdx.x; i < m; i += blockDim.x) x[i] = (i == 0) ? 1.0 : x[i] * scale;
@@ -246,6 +246,11 @@ __device__ inline void d_sytrd(int n, double* __restrict__ A, int lda, double* _
     int cur = 0;
     double tprev = 0.0;        // tau of the pending update (0: nothing pending)
     double tk = 0.0;
+    // PREFETCH: the first chunk of this warp's first row of the coming step is loaded right
+    // after the barrier, so that its L2 latency overlaps the reflector (the row is final once
+    // the barrier is passed); it costs RT registers held across the reflector
+    double pre[RT];
+    bool pre_ok = false;
     if (n > 2) {
         for (int i = threadIdx.x; i < n - 1; i += blockDim.x) sm[i] = A[i + 1];
         tk = reflector(0, sm, nullptr, nullptr, 0.0);
@@ -269,10 +274,15 @@ __device__ inline void d_sytrd(int n, double* __restrict__ A, int lda, double* _
             // latency is long: independent chains keep the pipe busy)
             double s0 = 0.0, s1 = 0.0;
             double nx[RT];
+            if (PREFETCH && r == gwarp && pre_ok) {
 #pragma unroll
-            for (int t = 0; t < RT; ++t) {
-                const int c = lane + 32 * t;
-                nx[t] = c < m ? arow[c] : 0.0;
+                for (int t = 0; t < RT; ++t) nx[t] = pre[t];
+            } else {
+#pragma unroll
+                for (int t = 0; t < RT; ++t) {
+                    const int c = lane + 32 * t;
+                    nx[t] = c < m ? arow[c] : 0.0;
+                }
             }
             for (int c0 = 0; c0 < m; c0 += 32 * RT) {
                 double cu[RT];
@@ -316,6 +326,15 @@ __device__ inline void d_sytrd(int n, double* __restrict__ A, int lda, double* _
         // loaded together: the pending buffers are free now, and the two loads share one trip
         // to L2
         const bool next = k + 1 < n - 2;
+        pre_ok = PREFETCH && next && gwarp < m - 1;
+        if (PREFETCH && pre_ok) {
+            const double* arow = A + (size_t)(k + 2 + gwarp) * lda + k + 2;
+#pragma unroll
+            for (int t = 0; t < RT; ++t) {
+                const int c = lane + 32 * t;
+                pre[t] = c < m - 1 ? arow[c] : 0.0;
+            }
+        }
         double* xn = vp;
         for (int i = threadIdx.x; i < m; i += blockDim.x) {
             if (tk != 0.0) w[i] = p[i];

@@ -60,6 +60,70 @@ __global__ void k_split_rows(int R, int K, int Kp, const double* __restrict__ X,
     }
 }
 
+// The same digits for the transposed case (element k of row r is X[k*ldx + r]), in two passes
+// that read X along its rows: k_col_max takes the largest magnitude of each column over one
+// 256-long K block (integer max on the magnitude bits, so the result does not depend on the
+// order of the blocks), and k_col_digits cuts one 32 x 32 (r, k) tile per block, read with the
+// lanes along r and written through shared memory with the lanes along k.
+__global__ void __launch_bounds__(256) k_col_max(int R, int K, const double* __restrict__ X, int ldx,
+                                                 const int* __restrict__ dK, unsigned long long* __restrict__ mbits) {
+    __shared__ unsigned long long red[8][32];
+    const int l = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int r = blockIdx.x * 32 + l;
+    const int kmax = dK ? min(K, *dK) : K;
+    const int k0 = blockIdx.y * 256, k1 = min(kmax, k0 + 256);
+    unsigned long long m = 0;
+    if (r < R)
+        for (int k = k0 + w; k < k1; k += 8) {
+            const unsigned long long b = (unsigned long long)__double_as_longlong(X[(size_t)k * ldx + r]) &
+                                         0x7fffffffffffffffULL;
+            m = b > m ? b : m;
+        }
+    red[w][l] = m;
+    __syncthreads();
+    if (w == 0 && r < R) {
+        for (int q = 1; q < 8; ++q) m = red[q][l] > m ? red[q][l] : m;
+        if (m) atomicMax(&mbits[r], m);
+    }
+}
+
+template <int S>
+__global__ void __launch_bounds__(256) k_col_digits(int R, int K, int Kp, const double* __restrict__ X, int ldx,
+                                                    const int* __restrict__ dK,
+                                                    const unsigned long long* __restrict__ mbits,
+                                                    __nv_bfloat16* __restrict__ out, double* __restrict__ scale) {
+    constexpr int LD = 34;   // bf16 per staged row: 17 words, so the 32 lanes hit 32 banks
+    __shared__ __align__(16) __nv_bfloat16 dig[S][32][LD];
+    const int l = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int r0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
+    const int r = r0 + l;
+    const int kmax = dK ? min(K, *dK) : K;
+    const double mx = r < R ? __longlong_as_double((long long)mbits[r]) : 0.0;
+    int e = 0;
+    if (mx > 0.0) frexp(mx, &e);
+    if (blockIdx.y == 0 && w == 0 && r < R) scale[r] = (mx > 0.0) ? ldexp(1.0, e) : 1.0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const int kk = w + 8 * j, k = k0 + kk;
+        double x = (r < R && k < kmax && mx > 0.0) ? ldexp(X[(size_t)k * ldx + r], -e) : 0.0;
+#pragma unroll
+        for (int p = 0; p < S; ++p) {
+            x *= 256.0;
+            const double d = rint(x);
+            x -= d;
+            dig[p][l][kk] = __double2bfloat16(d);
+        }
+    }
+    __syncthreads();
+    const size_t plane = (size_t)R * Kp;
+    for (int idx = threadIdx.x; idx < S * 32 * 16; idx += 256) {
+        const int p = idx / 512, row = (idx / 16) % 32, wd = idx % 16;
+        if (r0 + row >= R) continue;
+        const uint32_t v = *reinterpret_cast<const uint32_t*>(&dig[p][row][2 * wd]);
+        *reinterpret_cast<uint32_t*>(out + p * plane + (size_t)(r0 + row) * Kp + k0 + 2 * wd) = v;
+    }
+}
+
 }  // namespace
 
 namespace {
@@ -187,7 +251,24 @@ __global__ void __launch_bounds__(256) k_split_mma(int M, int N, int Kp, const _
 size_t split_gemm_workspace(int M, int N, int K, int slices) {
     const size_t Kp = (size_t)((K + SG_KT - 1) / SG_KT) * SG_KT;
     const size_t bf = (size_t)slices * ((size_t)M + N) * Kp * sizeof(__nv_bfloat16);
-    return (bf + 255) / 256 * 256 + ((size_t)M + N) * sizeof(double) + 256;
+    return (bf + 255) / 256 * 256 + 2 * ((size_t)M + N) * sizeof(double) + 256;
+}
+
+// Digits and scales of the rows of op(X) (R rows, K long): along memory rows when !trans,
+// through the column kernels when trans.
+template <int S>
+static void split_operand(cudaStream_t st, int R, int K, int Kp, const double* X, int ldx, bool trans, const int* dK,
+                          __nv_bfloat16* out, double* scale, unsigned long long* mbits) {
+    if (!trans) {
+        k_split_rows<S><<<ceil_div((long)R * 32, 256), 256, 0, st>>>(R, K, Kp, X, ldx, 0, dK, out, scale);
+        XG_LAUNCH_CHECK();
+        return;
+    }
+    XG_CUDA(cudaMemsetAsync(mbits, 0, (size_t)R * sizeof(unsigned long long), st));
+    k_col_max<<<dim3(ceil_div(R, 32), std::max(1, ceil_div(K, 256))), 256, 0, st>>>(R, K, X, ldx, dK, mbits);
+    XG_LAUNCH_CHECK();
+    k_col_digits<S><<<dim3(ceil_div(R, 32), Kp / 32), 256, 0, st>>>(R, K, Kp, X, ldx, dK, mbits, out, scale);
+    XG_LAUNCH_CHECK();
 }
 
 template <int S>
@@ -200,10 +281,10 @@ static void split_gemm_s(cudaStream_t st, bool ta, bool tb, int M, int N, int K,
     const size_t bf = (size_t)S * ((size_t)M + N) * Kp * sizeof(__nv_bfloat16);
     double* sA = reinterpret_cast<double*>(static_cast<char*>(work) + (bf + 255) / 256 * 256);
     double* sB = sA + M;
-    k_split_rows<S><<<ceil_div((long)M * 32, 256), 256, 0, st>>>(M, K, Kp, A, lda, ta ? 1 : 0, dK, As, sA);
-    XG_LAUNCH_CHECK();
-    k_split_rows<S><<<ceil_div((long)N * 32, 256), 256, 0, st>>>(N, K, Kp, B, ldb, tb ? 0 : 1, dK, Bs, sB);
-    XG_LAUNCH_CHECK();
+    unsigned long long* mA = reinterpret_cast<unsigned long long*>(sB + N);
+    unsigned long long* mB = mA + M;
+    split_operand<S>(st, M, K, Kp, A, lda, ta, dK, As, sA, mA);
+    split_operand<S>(st, N, K, Kp, B, ldb, !tb, dK, Bs, sB, mB);
     const size_t smem = (size_t)2 * S * SG_BM * SG_LD * sizeof(__nv_bfloat16);
     if (smem > 48 * 1024) allow_max_dynamic_smem((const void*)k_split_mma<S>);
     dim3 grid(ceil_div(N, SG_BN), ceil_div(M, SG_BM));
