@@ -178,10 +178,47 @@ def test_blocked_backtransform(precision):
     kept, every eigenvector goes through it."""
     Z, xyz = W.water_cluster(50, seed=8)
     base = gpu(Z, xyz, keep_orbitals=False, precision=precision)
+    # FP64: both forms are FP64 products in a different order.  Split precision: the two forms
+    # feed differently shaped split products (about 2^-40 relative error per product term).
+    tol_e, tol = (1e-10, 1e-9) if precision == "fp64" else (1e-8, 1e-8)
     for keep in (False, True):
         r = gpu(Z, xyz, keep_orbitals=keep, precision=precision, blocked_min=0)
-        assert abs(r.energy - base.energy) <= 1e-10
-        assert np.max(np.abs(r.charges - base.charges)) <= 1e-9
-        assert np.max(np.abs(r.gradient - base.gradient)) <= 1e-9
+        assert abs(r.energy - base.energy) <= tol_e, (r.energy - base.energy)
+        assert np.max(np.abs(r.charges - base.charges)) <= tol
+        assert np.max(np.abs(r.gradient - base.gradient)) <= tol
         assert r.iterations == base.iterations
     assert_parity(r, gfn2.singlepoint(Z, xyz))
+
+
+def test_concurrent_threads_match_sequential():
+    """Single points on several host threads at once (each thread has its own engine stream and
+    workspace) give the sequential results.  The molecules differ in size, so the launches of one
+    kernel ask for different dynamic shared-memory sizes at the same time (above 48 KB from 1536
+    AOs): the per-kernel limit is process-wide and must never be lowered under another thread."""
+    import threading
+    mols = [W.water_cluster(270, seed=31), W.water_cluster(40, seed=32), W.alkane(270, 0.02, seed=33),
+            W.water_cluster(12, seed=34)]
+    seq = [gpu(Z, xyz, keep_orbitals=False) for Z, xyz in mols]
+    out = [[None] * len(mols) for _ in range(2)]
+    errs = []
+
+    def work(slot, order):
+        try:
+            for i in order:
+                Z, xyz = mols[i]
+                out[slot][i] = gpu(Z, xyz, keep_orbitals=False)
+        except Exception as e:          # re-raised below on the test's thread
+            errs.append(e)
+
+    threads = [threading.Thread(target=work, args=(0, [0, 1, 2, 3])),
+               threading.Thread(target=work, args=(1, [2, 3, 0, 1]))]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errs, errs
+    for slot in range(2):
+        for r, s in zip(out[slot], seq):
+            assert abs(r.energy - s.energy) <= 1e-9
+            assert np.max(np.abs(r.gradient - s.gradient)) <= 1e-9
+            assert r.iterations == s.iterations

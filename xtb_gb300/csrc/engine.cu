@@ -447,7 +447,7 @@ void run_singlepoint(const HostMol& hm, const SPSettings& set, Wavefunction& wfn
         cn(st, m, 2, cn_tmp);
         eeq_setup(st, m, cn_tmp, eeqA, eeqX);
         potrf_upper(st, nat, eeqA, nat, info);
-        eeq_finish(st, nat, eeqA, eeqX, hm.charge, q, nullptr);
+        eeq_finish(st, nat, eeqA, eeqX, hm.charge, q, iscr);   // iscr: free until the first eigenvectors
         int hinfo = 0;
         XG_CUDA(cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, st));
         XG_CUDA(cudaStreamSynchronize(st));

@@ -7,6 +7,21 @@ namespace xg {
 
 
 __device__ __forceinline__ double sq(double x) { return x * x; }
+// x^N for the small integer exponents of the pair terms, by multiplication (the reference's
+// Fortran x**n with an integer n is evaluated the same way), instead of the general pow
+template <int N>
+__device__ __forceinline__ double powi(double x) {
+    static_assert(N >= 1 && N <= 8, "small integer powers only");
+    const double x2 = x * x;
+    if constexpr (N == 1) return x;
+    else if constexpr (N == 2) return x2;
+    else if constexpr (N == 3) return x2 * x;
+    else if constexpr (N == 4) return x2 * x2;
+    else if constexpr (N == 5) return x2 * x2 * x;
+    else if constexpr (N == 6) return x2 * x2 * x2;
+    else if constexpr (N == 7) return x2 * x2 * x2 * x;
+    else return (x2 * x2) * (x2 * x2);
+}
 
 
 // linear index t -> (a, b) with a >= b of a packed lower triangle
@@ -78,6 +93,22 @@ __device__ inline void d_cn(DevMol m, int mode, double* __restrict__ cn, int i) 
 }
 
 
+// Warp-cooperative form of d_cn (one warp per atom, lanes over the partner atoms): the plain
+// engine's molecules have hundreds to thousands of atoms, and one thread per atom would leave
+// most SMs idle.
+__device__ inline void d_cn_warp(DevMol m, int mode, double* __restrict__ cn, int i, int lane) {
+    const double xi = m.xyz[3 * i], yi = m.xyz[3 * i + 1], zi = m.xyz[3 * i + 2];
+    double s = 0.0;
+    for (int j = lane; j < m.nat; j += 32) {
+        if (j == i) continue;
+        const double r2 = sq(m.xyz[3 * j] - xi) + sq(m.xyz[3 * j + 1] - yi) + sq(m.xyz[3 * j + 2] - zi);
+        CNTerm t;
+        if (cn_term(m, mode, i, j, r2, t)) s += t.cf;
+    }
+    s = warp_sum(s);
+    if (lane == 0) cn[i] = s;
+}
+
 // g[a] += sum_b den*dcount(r_ab)*(R_a - R_b)/r_ab * (v_a + v_b)  ==  sum_b dCN_b/dR_a v_b
 __device__ inline void d_cn_chain(DevMol m, int mode, const double* __restrict__ v, double* __restrict__ g, int a) {
     const double xa = m.xyz[3 * a], ya = m.xyz[3 * a + 1], za = m.xyz[3 * a + 2];
@@ -92,6 +123,25 @@ __device__ inline void d_cn_chain(DevMol m, int mode, const double* __restrict__
         gx += f * dx; gy += f * dy; gz += f * dz;
     }
     g[3 * a] += gx; g[3 * a + 1] += gy; g[3 * a + 2] += gz;
+}
+
+
+// Warp-cooperative form of d_cn_chain (one warp per atom, lanes over the partner atoms).
+__device__ inline void d_cn_chain_warp(DevMol m, int mode, const double* __restrict__ v, double* __restrict__ g, int a,
+                                       int lane) {
+    const double xa = m.xyz[3 * a], ya = m.xyz[3 * a + 1], za = m.xyz[3 * a + 2];
+    double gx = 0, gy = 0, gz = 0;
+    for (int b = lane; b < m.nat; b += 32) {
+        if (b == a) continue;
+        const double dx = xa - m.xyz[3 * b], dy = ya - m.xyz[3 * b + 1], dz = za - m.xyz[3 * b + 2];
+        const double r2 = dx * dx + dy * dy + dz * dz;
+        CNTerm t;
+        if (!cn_term(m, mode, a, b, r2, t)) continue;
+        const double f = t.df / sqrt(r2) * (v[a] + v[b]);
+        gx += f * dx; gy += f * dy; gz += f * dz;
+    }
+    gx = warp_sum(gx); gy = warp_sum(gy); gz = warp_sum(gz);
+    if (lane == 0) { g[3 * a] += gx; g[3 * a + 1] += gy; g[3 * a + 2] += gz; }
 }
 
 
@@ -220,10 +270,10 @@ __device__ inline void d_gab(DevMol m, const double* __restrict__ radcn, double*
                           sq(m.xyz[3 * j + 2] - m.xyz[3 * i + 2]));
     const double ri = 1.0 / r;
     const double rco = 0.5 * (radcn[i] + radcn[j]);
-    const double d3 = 1.0 / (1.0 + 6.0 * pow(rco * ri, 3.0));
-    const double d5 = 1.0 / (1.0 + 6.0 * pow(rco * ri, 4.0));
-    gab3[t] = d3 * pow(ri, 3.0);
-    gab5[t] = d5 * pow(ri, 5.0);
+    const double d3 = 1.0 / (1.0 + 6.0 * powi<3>(rco * ri));
+    const double d5 = 1.0 / (1.0 + 6.0 * powi<4>(rco * ri));
+    gab3[t] = d3 * powi<3>(ri);
+    gab5[t] = d5 * powi<5>(ri);
 }
 
 
@@ -373,12 +423,13 @@ __device__ inline void d_aes_grad(DevMol m, const double* __restrict__ q, const 
         const double r2 = rij[0] * rij[0] + rij[1] * rij[1] + rij[2] * rij[2];
         const double rabi = 1.0 / sqrt(r2);
         const double rco = 0.5 * (radcn[i] + radcn[j]);
-        const double damp1 = 1.0 / (1.0 + 6.0 * pow(rco * rabi, 3.0));
+        const double damp1 = 1.0 / (1.0 + 6.0 * powi<3>(rco * rabi));
         const double dd1 = -3.0 * rabi * (damp1 * damp1 - damp1);
-        const double dgab3 = (-3.0 * rabi * pow(rabi, 3.0)) * damp1 + dd1 * pow(rabi, 3.0);
-        const double damp2 = 1.0 / (1.0 + 6.0 * pow(rco * rabi, 4.0));
+        const double r3 = powi<3>(rabi), r5 = powi<5>(rabi);
+        const double dgab3 = (-3.0 * rabi * r3) * damp1 + dd1 * r3;
+        const double damp2 = 1.0 / (1.0 + 6.0 * powi<4>(rco * rabi));
         const double dd2 = -4.0 * rabi * (damp2 * damp2 - damp2);
-        const double dgab5 = (-5.0 * rabi * pow(rabi, 5.0)) * damp2 + dd2 * pow(rabi, 5.0);
+        const double dgab5 = (-5.0 * rabi * r5) * damp2 + dd2 * r5;
         const double G3 = gab3[(size_t)j * n + i], G5 = gab5[(size_t)j * n + i];
         const double* dj = dipm + 3 * j;
         const double* Qj = qp + 6 * j;
@@ -407,7 +458,7 @@ __device__ inline void d_aes_grad(DevMol m, const double* __restrict__ q, const 
             g[k] -= ed * dgab3 * dxi + (eq + edd) * dgab5 * dxi;
         }
         const double rab = 0.5 * (radcn[i] + radcn[j]);
-        t2 += ed * 3.0 * G3 * (damp1 / rab) * pow(rab * rabi, 3.0) + (eq + edd) * 4.0 * G5 * (damp2 / rab) * pow(rab * rabi, 4.0);
+        t2 += ed * 3.0 * G3 * (damp1 / rab) * powi<3>(rab * rabi) + (eq + edd) * 4.0 * G5 * (damp2 / rab) * powi<4>(rab * rabi);
     }
     for (int k = 0; k < 3; ++k) g[k] = warp_sum(g[k]);
     t2 = warp_sum(t2);
@@ -778,6 +829,36 @@ __device__ inline void d_repulsion(DevMol m, double* __restrict__ e_atom, double
 }
 
 
+// Warp-cooperative form of d_repulsion for the plain engine (one warp per atom).
+__device__ inline void d_repulsion_warp(DevMol m, double* __restrict__ e_atom, double* __restrict__ grad, int a,
+                                        int lane) {
+    double e = 0.0, g[3] = {0, 0, 0};
+    for (int b = lane; b < m.nat; b += 32) {
+        if (b == a) continue;
+        const double rij[3] = {m.xyz[3 * a] - m.xyz[3 * b], m.xyz[3 * a + 1] - m.xyz[3 * b + 1],
+                               m.xyz[3 * a + 2] - m.xyz[3 * b + 2]};
+        const double r2 = rij[0] * rij[0] + rij[1] * rij[1] + rij[2] * rij[2];
+        if (r2 > 1600.0 || r2 < 1e-8) continue;
+        const double r1 = sqrt(r2);
+        const double alpha = sqrt(m.rep_alpha[a] * m.rep_alpha[b]);
+        const double zeff = m.rep_zeff[a] * m.rep_zeff[b];
+        const double kexp = (m.Z[a] > 2 || m.Z[b] > 2) ? 1.5 : 1.0;
+        const double t16 = (m.Z[a] > 2 || m.Z[b] > 2) ? r1 * sqrt(r1) : r1;   // r^kexp
+        const double t26 = exp(-alpha * t16);
+        const double dE = zeff * t26 / r1;
+        const double f = -(alpha * t16 * kexp + 1.0) * dE / r2;
+        e += 0.5 * dE;
+        for (int k = 0; k < 3; ++k) g[k] += f * rij[k];
+    }
+    e = warp_sum(e);
+    for (int k = 0; k < 3; ++k) g[k] = warp_sum(g[k]);
+    if (lane == 0) {
+        e_atom[a] = e;
+        for (int k = 0; k < 3; ++k) grad[3 * a + k] += g[k];
+    }
+}
+
+
 // ================================================================== Coulomb gradient
 // getCoulombDerivsCluster contracted with qsh (src/coulomb/klopmanohno.F90:471-573); warp per atom
 __device__ inline void d_coulomb_grad(DevMol m, const double* __restrict__ qsh, double* __restrict__ grad, int a, int lane) {
@@ -882,8 +963,10 @@ __device__ inline void d_d4_wz(DevMol m, const double* __restrict__ gw, const do
         if (r2 > 72.0 * 72.0) continue;
         const double r4r2 = 3.0 * m.r4r2[a] * m.r4r2[b];
         const double cut = 0.52 * sqrt(r4r2) + 5.0;
-        const double oor6 = 1.0 / (r2 * r2 * r2 + pow(cut, 6.0));
-        const double oor8 = 1.0 / (r2 * r2 * r2 * r2 + pow(cut, 8.0));
+        const double cut2 = cut * cut, cut6 = cut2 * cut2 * cut2, r6 = r2 * r2 * r2;
+        const double oor6 = rcp_fast(r6 + cut6);
+        const double oor8 = rcp_fast(r6 * r2 + cut6 * cut2);
+        const double h = oor6 + 2.7 * r4r2 * oor8;   // -(C6 oor6 + 2.7 r4r2 C6 oor8) = -C6 h
         const int eb = m.eid[b], nb = m.d4_nref[eb];
         const double* c6 = m.d4_c6 + ((size_t)(ea * m.nelem + eb) * MAXREF) * MAXREF;
         for (int r = 0; r < na; ++r) {
@@ -892,10 +975,9 @@ __device__ inline void d_d4_wz(DevMol m, const double* __restrict__ gw, const do
             for (int u = 0; u < nb; ++u) {
                 const double gg = gr * gw[b * MAXREF + u];
                 if (gg < 1e-7) continue;
-                const double c = c6[r * MAXREF + u];
-                s += gg * (-1.0 * (c * oor6) - 2.7 * (r4r2 * c * oor8)) * zeta[b * MAXREF + u];
+                s = fma(gg * c6[r * MAXREF + u], zeta[b * MAXREF + u], s);
             }
-            acc[r] += s;
+            acc[r] -= h * s;
         }
     }
     double v = 0.0, e = 0.0;
@@ -966,8 +1048,8 @@ __device__ inline void d_d4_2body(DevMol m, const double* __restrict__ c6, const
         if (r2 > 3600.0 || r2 < 1e-10) continue;
         const double r4r2 = 3.0 * m.r4r2[a] * m.r4r2[b];
         const double r0 = 0.52 * sqrt(r4r2) + 5.0;
-        const double t6 = 1.0 / (r2 * r2 * r2 + pow(r0, 6.0));
-        const double t8 = 1.0 / (r2 * r2 * r2 * r2 + pow(r0, 8.0));
+        const double t6 = 1.0 / (r2 * r2 * r2 + powi<6>(r0));
+        const double t8 = 1.0 / (r2 * r2 * r2 * r2 + powi<8>(r0));
         const double d6 = -6.0 * r2 * r2 * t6 * t6;
         const double d8 = -8.0 * r2 * r2 * r2 * t8 * t8;
         const double disp = 1.0 * t6 + 2.7 * r4r2 * t8;
@@ -980,6 +1062,41 @@ __device__ inline void d_d4_2body(DevMol m, const double* __restrict__ c6, const
     e_atom[a] = e;
     dEdcn[a] += dcn;
     for (int k = 0; k < 3; ++k) grad[3 * a + k] += g[k];
+}
+
+// Warp-cooperative form of d_d4_2body for the plain engine (one warp per atom).
+__device__ inline void d_d4_2body_warp(DevMol m, const double* __restrict__ c6, const double* __restrict__ dc6,
+                                       double* __restrict__ e_atom, double* __restrict__ dEdcn,
+                                       double* __restrict__ grad, int a, int lane) {
+    const int n = m.nat;
+    double e = 0.0, dcn = 0.0, g[3] = {0, 0, 0};
+    for (int b = lane; b < n; b += 32) {
+        if (b == a) continue;
+        const double rij[3] = {m.xyz[3 * a] - m.xyz[3 * b], m.xyz[3 * a + 1] - m.xyz[3 * b + 1],
+                               m.xyz[3 * a + 2] - m.xyz[3 * b + 2]};
+        const double r2 = rij[0] * rij[0] + rij[1] * rij[1] + rij[2] * rij[2];
+        if (r2 > 3600.0 || r2 < 1e-10) continue;
+        const double r4r2 = 3.0 * m.r4r2[a] * m.r4r2[b];
+        const double r0 = 0.52 * sqrt(r4r2) + 5.0;
+        const double t6 = 1.0 / (r2 * r2 * r2 + powi<6>(r0));
+        const double t8 = 1.0 / (r2 * r2 * r2 * r2 + powi<8>(r0));
+        const double d6 = -6.0 * r2 * r2 * t6 * t6;
+        const double d8 = -8.0 * r2 * r2 * r2 * t8 * t8;
+        const double disp = 1.0 * t6 + 2.7 * r4r2 * t8;
+        const double ddisp = 1.0 * d6 + 2.7 * r4r2 * d8;
+        const double cab = c6[(size_t)a * n + b];
+        e += -cab * disp * 0.5;
+        dcn += -dc6[(size_t)a * n + b] * disp;
+        for (int k = 0; k < 3; ++k) g[k] += -cab * ddisp * rij[k];
+    }
+    e = warp_sum(e);
+    dcn = warp_sum(dcn);
+    for (int k = 0; k < 3; ++k) g[k] = warp_sum(g[k]);
+    if (lane == 0) {
+        e_atom[a] = e;
+        dEdcn[a] += dcn;
+        for (int k = 0; k < 3; ++k) grad[3 * a + k] += g[k];
+    }
 }
 
 // Broyden vector [qsh; per atom (dipm 3, qp 6)] (gfn2broyden_*, src/aespot.F90:1360-1425)

@@ -14,27 +14,27 @@ namespace xg {
 
 
 __global__ void k_cn(DevMol m, int mode, double* __restrict__ cn) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
     if (i >= m.nat) return;
-    d_cn(m, mode, cn, i);
+    d_cn_warp(m, mode, cn, i, threadIdx.x & 31);
 }
 
 
 void cn(cudaStream_t st, const DevMol& m, int mode, double* out) {
-    k_cn<<<ceil_div(m.nat, 128), 128, 0, st>>>(m, mode, out);
+    k_cn<<<ceil_div((long)m.nat * 32, 128), 128, 0, st>>>(m, mode, out);
     XG_LAUNCH_CHECK();
 }
 
 
 __global__ void k_cn_chain(DevMol m, int mode, const double* __restrict__ v, double* __restrict__ g) {
-    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    const int a = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
     if (a >= m.nat) return;
-    d_cn_chain(m, mode, v, g, a);
+    d_cn_chain_warp(m, mode, v, g, a, threadIdx.x & 31);
 }
 
 
 void cn_chain(cudaStream_t st, const DevMol& m, int mode, const double* v, double* grad) {
-    k_cn_chain<<<ceil_div(m.nat, 128), 128, 0, st>>>(m, mode, v, grad);
+    k_cn_chain<<<ceil_div((long)m.nat * 32, 128), 128, 0, st>>>(m, mode, v, grad);
     XG_LAUNCH_CHECK();
 }
 
@@ -57,7 +57,82 @@ __global__ void k_eeq_solve(int n, const double* __restrict__ U, double* __restr
                             double* __restrict__ q) { d_eeq_solve(n, U, X, charge, q); }
 
 
-void eeq_finish(cudaStream_t st, int nat, const double* Uf, double* X, double charge, double* q, double*) {
+// UT = U^T (n x n, 32 x 32 tiles through shared memory).
+__global__ void k_transpose(int n, const double* __restrict__ U, double* __restrict__ UT) {
+    __shared__ double tile[32][33];
+    const int x = blockIdx.x * 32 + threadIdx.x;
+    for (int yy = threadIdx.y; yy < 32; yy += blockDim.y) {
+        const int y = blockIdx.y * 32 + yy;
+        if (x < n && y < n) tile[yy][threadIdx.x] = U[(size_t)y * n + x];
+    }
+    __syncthreads();
+    const int xo = blockIdx.y * 32 + threadIdx.x;
+    for (int yy = threadIdx.y; yy < 32; yy += blockDim.y) {
+        const int yo = blockIdx.x * 32 + yy;
+        if (xo < n && yo < n) UT[(size_t)yo * n + xo] = tile[threadIdx.x][yy];
+    }
+}
+
+// The two EEQ right-hand sides through U^T y = b and U x = y by one block, both as column
+// sweeps (row i of U, then row i of U^T): one barrier per step and no reductions, with the
+// right-hand sides and the reciprocal diagonal in shared memory (3 n doubles).  Then the
+// charge constraint as in d_eeq_solve.
+__global__ void __launch_bounds__(1024) k_eeq_solve_smem(int n, const double* __restrict__ U,
+                                                         const double* __restrict__ UT, const double* __restrict__ X,
+                                                         double charge, double* __restrict__ q) {
+    extern __shared__ double es[];
+    double* b0 = es;
+    double* b1 = es + n;
+    double* rd = es + 2 * n;
+    __shared__ double red[32];
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        b0[k] = X[k];
+        b1[k] = X[n + k];
+        rd[k] = 1.0 / U[(size_t)k * n + k];
+    }
+    __syncthreads();
+    for (int i = 0; i < n; ++i) {
+        const double y0 = b0[i] * rd[i], y1 = b1[i] * rd[i];
+        const double* ur = U + (size_t)i * n;
+        for (int k = i + 1 + threadIdx.x; k < n; k += blockDim.x) {
+            const double u = ur[k];
+            b0[k] = fma(-u, y0, b0[k]);
+            b1[k] = fma(-u, y1, b1[k]);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) { b0[i] = y0; b1[i] = y1; }
+    }
+    __syncthreads();
+    for (int i = n - 1; i >= 0; --i) {
+        const double x0 = b0[i] * rd[i], x1 = b1[i] * rd[i];
+        const double* uc = UT + (size_t)i * n;   // column i of U
+        for (int k = threadIdx.x; k < i; k += blockDim.x) {
+            const double u = uc[k];
+            b0[k] = fma(-u, x0, b0[k]);
+            b1[k] = fma(-u, x1, b1[k]);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) { b0[i] = x0; b1[i] = x1; }
+    }
+    __syncthreads();
+    double sx0 = 0.0, sx1 = 0.0;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) { sx0 += b0[k]; sx1 += b1[k]; }
+    sx0 = block_sum(sx0, red);
+    sx1 = block_sum(sx1, red);
+    const double lam = (sx0 - charge) / sx1;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) q[k] = b0[k] - lam * b1[k];
+}
+
+void eeq_finish(cudaStream_t st, int nat, const double* Uf, double* X, double charge, double* q, double* work) {
+    const size_t smem = 3 * (size_t)nat * sizeof(double);
+    if (work && smem <= 200 * 1024) {
+        k_transpose<<<dim3(ceil_div(nat, 32), ceil_div(nat, 32)), dim3(32, 8), 0, st>>>(nat, Uf, work);
+        XG_LAUNCH_CHECK();
+        if (smem > 48 * 1024) allow_max_dynamic_smem((const void*)k_eeq_solve_smem);
+        k_eeq_solve_smem<<<1, 1024, smem, st>>>(nat, Uf, work, X, charge, q);
+        XG_LAUNCH_CHECK();
+        return;
+    }
     k_eeq_solve<<<1, 1024, 0, st>>>(nat, Uf, X, charge, q);
     XG_LAUNCH_CHECK();
 }
@@ -319,14 +394,14 @@ void broyden_step(cudaStream_t st, BroydenState& bs, int it, double alpha, doubl
 
 
 __global__ void k_repulsion(DevMol m, double* __restrict__ e_atom, double* __restrict__ grad) {
-    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    const int a = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
     if (a >= m.nat) return;
-    d_repulsion(m, e_atom, grad, a);
+    d_repulsion_warp(m, e_atom, grad, a, threadIdx.x & 31);
 }
 
 
 void repulsion(cudaStream_t st, const DevMol& m, double* e_atom, double* grad) {
-    k_repulsion<<<ceil_div(m.nat, 128), 128, 0, st>>>(m, e_atom, grad);
+    k_repulsion<<<ceil_div((long)m.nat * 32, 128), 128, 0, st>>>(m, e_atom, grad);
     XG_LAUNCH_CHECK();
 }
 
@@ -403,9 +478,9 @@ __global__ void k_d4_c6(DevMol m, const double* __restrict__ zv, const double* _
 
 __global__ void k_d4_2body(DevMol m, const double* __restrict__ c6, const double* __restrict__ dc6,
                            double* __restrict__ e_atom, double* __restrict__ dEdcn, double* __restrict__ grad) {
-    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    const int a = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
     if (a >= m.nat) return;
-    d_d4_2body(m, c6, dc6, e_atom, dEdcn, grad, a);
+    d_d4_2body_warp(m, c6, dc6, e_atom, dEdcn, grad, a, threadIdx.x & 31);
 }
 
 
@@ -525,7 +600,7 @@ void d4_grad(cudaStream_t st, const DevMol& m, const double* cnv, const double* 
     XG_LAUNCH_CHECK();
     k_d4_c6<<<ceil_div(nn, 256), 256, 0, st>>>(m, zr, zrdcn, c6z, dc6z);
     XG_LAUNCH_CHECK();
-    k_d4_2body<<<ceil_div(m.nat, 128), 128, 0, st>>>(m, c6, dc6, e2_atom, dEdcn, grad);
+    k_d4_2body<<<ceil_div((long)m.nat * 32, 128), 128, 0, st>>>(m, c6, dc6, e2_atom, dEdcn, grad);
     XG_LAUNCH_CHECK();
     // ATM pair factors: c6 and dc6 are free once the two-body term is done
     double* ir = c6;

@@ -247,7 +247,43 @@ __global__ void k_trinv_upper(int n, const double* __restrict__ U, int ldu, doub
     d_trinv_col(n, U, ldu, X, ldx, j, lane);
 }
 
+// Same result with column j of X built in the warp's shared memory (d_trinv_col reads it back
+// from global memory with a row stride on every step), the longest columns first, and the
+// diagonal reciprocal off the dependent chain.  smem: wpb * n doubles.
+__global__ void k_trinv_upper_smem(int n, const double* __restrict__ U, int ldu, double* __restrict__ X, int ldx) {
+    extern __shared__ double xs[];
+    const int wpb = blockDim.x >> 5, wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int j = n - 1 - (int)(blockIdx.x * wpb + wib);
+    if (j < 0) return;   // warps are independent: no block barrier below
+    double* x = xs + (size_t)wib * n;
+    if (lane == 0) x[j] = 1.0 / U[(size_t)j * ldu + j];
+    __syncwarp();
+    for (int i = j - 1; i >= 0; --i) {
+        const double* urow = U + (size_t)i * ldu;
+        const double r = rcp_fast(urow[i]);
+        double s0 = 0.0, s1 = 0.0;
+        int k = i + 1 + lane;
+        for (; k + 32 <= j; k += 64) {
+            s0 = fma(urow[k], x[k], s0);
+            s1 = fma(urow[k + 32], x[k + 32], s1);
+        }
+        if (k <= j) s0 = fma(urow[k], x[k], s0);
+        const double sum = warp_sum(s0 + s1);
+        if (lane == 0) x[i] = -sum * r;
+        __syncwarp();
+    }
+    for (int i = lane; i < n; i += 32) X[(size_t)i * ldx + j] = (i <= j) ? x[i] : 0.0;
+}
+
 void trinv_upper(cudaStream_t st, int n, const double* U, int ldu, double* X, int ldx) {
+    int wpb = n <= 3500 ? 4 : 2;
+    const size_t smem = (size_t)wpb * n * sizeof(double);
+    if (smem <= 200 * 1024) {
+        if (smem > 48 * 1024) allow_max_dynamic_smem((const void*)k_trinv_upper_smem);
+        k_trinv_upper_smem<<<ceil_div(n, wpb), wpb * 32, smem, st>>>(n, U, ldu, X, ldx);
+        XG_LAUNCH_CHECK();
+        return;
+    }
     k_trinv_upper<<<ceil_div((long)n * 32, 256), 256, 0, st>>>(n, U, ldu, X, ldx);
     XG_LAUNCH_CHECK();
 }
