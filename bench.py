@@ -186,6 +186,22 @@ def run_served(args, ws, rank):
     dist_barrier(ws)
     clk = clocks.stop()
     st1 = srv.stats()
+    # the same requests once more with Poisson arrivals at 80% of the measured saturation
+    # throughput (arrival times from their own seeded generator, so the molecules are the same):
+    # throughput and latency under load below capacity, next to the capacity itself
+    poisson = None
+    if not args.rate:
+        sat = sum(len(p[0]) for p in passes) / max(1e-9, sum(p[2] for p in passes))
+        prate = 0.8 * sat
+        arr = np.cumsum(np.random.default_rng(args.seed + 1).exponential(1.0 / prate, R)) - 1.0 / prate
+        preqs = [dict(r, arrival=float(a)) for r, a in zip(reqs, arr)]
+        pres, pwall, _ = served_pass(srv, preqs, prate)
+        plat = np.array([x.latency for x in pres]) * 1e3
+        poisson = {"rate": prate, "value": R / pwall, "unit": "single points/s",
+                   "latency_ms": {"p50": float(np.percentile(plat, 50)), "p99": float(np.percentile(plat, 99)),
+                                  "max": float(plat.max())},
+                   "failed_requests": int(sum(1 for x in pres if x.status != 0)),
+                   "note": "one pass, arrivals exponential at 0.8x the saturation throughput"}
     srv.close()
     span = dist_max(sum(p[2] for p in passes), ws)
     wall = dist_max(sum(p[1] for p in passes), ws)
@@ -266,6 +282,7 @@ def run_served(args, ws, rank):
                 "h2d_bytes_per_step": int(d["h2d_bytes"] / args.steps),
                 "d2h_bytes_per_step": int(d["d2h_bytes"] / args.steps)},
         "gpu_launches": int(d["launches"]),
+        "poisson": poisson,
         "served_mix": {"pool": int(sum(1 for x in served if x.engine == 0)),
                        "plain_engine": int(sum(1 for x in served if x.engine == 1)),
                        "peak_resident": int(st1["peak_resident"])},
