@@ -296,7 +296,7 @@ __device__ void scc_iteration(BatchMol* b, const DevThresh& th, double etemp, in
         for (int j0 = 0; j0 < nao; j0 += per_pass) {   // uniform trip count: whole warps stay together
             const int j = j0 + (int)(threadIdx.x / BIS_G);
             const bool valid = j < nao;
-            const double v = d_bisect_group(nao, sm, sm + nao, fsm, fsm + nao, b->bounds, valid ? j : 0, valid);
+            const double v = d_bisect_group<true>(nao, sm, sm + nao, fsm, fsm + nao, b->bounds, valid ? j : 0, valid);
             if (valid && threadIdx.x % BIS_G == 0) b->emo[j] = v;
         }
     }

@@ -344,7 +344,7 @@ __global__ void __launch_bounds__(32) k_bisect(int n, const double* __restrict__
     const float* fsm = reinterpret_cast<const float*>(sde + 2 * n);
     const int j = blockIdx.x * (32 / BIS_G) + (int)(threadIdx.x / BIS_G);
     const bool valid = j < n;
-    const double v = d_bisect_group(n, sde, sde + n, fsm, fsm + n, bounds, valid ? j : 0, valid);
+    const double v = d_bisect_group<false>(n, sde, sde + n, fsm, fsm + n, bounds, valid ? j : 0, valid);
     if (valid && threadIdx.x % BIS_G == 0) w[j] = v;
 }
 

@@ -437,6 +437,42 @@ __device__ inline int sturm_count(int n, const double* d, const double* e2, doub
     return cnt;
 }
 
+// Newton correction -f(x)/f'(x) for f(x) = det(T - x I): the leading minors p_i and their
+// derivatives p'_i follow p_i = (d_i - x) p_i-1 - e_i-1^2 p_i-2 and
+// p'_i = (d_i - x) p'_i-1 - p_i-1 - e_i-1^2 p'_i-2.  The four running values are rescaled
+// together by an exact power of two every four rows (the ratio is unchanged).
+__device__ __forceinline__ void quad_rescale(double& pm, double& p, double& qm, double& q) {
+    const int ex = max(max(dexp_bits(p), dexp_bits(pm)), max(dexp_bits(q), dexp_bits(qm)));
+    if (ex > 1023 + 300) {
+        p *= 0x1p-300; pm *= 0x1p-300; q *= 0x1p-300; qm *= 0x1p-300;
+    } else if (ex < 1023 - 300) {
+        p *= 0x1p+300; pm *= 0x1p+300; q *= 0x1p+300; qm *= 0x1p+300;
+    }
+}
+
+__device__ inline double newton_dx(int n, const double* d, const double* e2, double x) {
+    double pm = 1.0, p = d[0] - x, qm = 0.0, q = -1.0;
+    int i = 1;
+    for (; i + 3 < n; i += 4) {
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const double t = d[i + u] - x, f = e2[i + u - 1];
+            const double pn = fma(t, p, -f * pm);
+            const double qn = fma(t, q, -fma(f, qm, p));
+            pm = p; p = pn; qm = q; q = qn;
+        }
+        quad_rescale(pm, p, qm, q);
+    }
+    for (; i < n; ++i) {
+        const double t = d[i] - x, f = e2[i - 1];
+        const double pn = fma(t, p, -f * pm);
+        const double qn = fma(t, q, -fma(f, qm, p));
+        pm = p; p = pn; qm = q; q = qn;
+        quad_rescale(pm, p, qm, q);
+    }
+    return -p / q;
+}
+
 // The same count in FP32 with the ratio form q_i = (d_i - x) - e_{i-1}^2 / q_{i-1} and the
 // pivmin guard; used only to narrow brackets that FP64 counts then verify.
 __device__ inline int sturm_count32(int n, const float* d, const float* e2, float x, float pivmin) {
@@ -501,6 +537,12 @@ __device__ inline void d_tri_prep(int n, const double* __restrict__ d, const dou
 // staged in shared memory.  Returns the eigenvalue in every lane of the group.
 constexpr int BIS_G = 4;
 
+// NEWTON: the FP64 phase starts with Newton steps (below).  It cuts the FP64 work about
+// eightfold where the eigenvalues are well separated, which pays where FP64 throughput is the
+// limit (the batched engine: +9% single points/s on the mixed set); on the plain engine's
+// large clusters (many near-degenerate levels) Newton often falls back to multisection, and the
+// latency-bound launch measured slower, so it is off there.
+template <bool NEWTON>
 __device__ inline double d_bisect_group(int n, const double* sd, const double* se2, const float* fd, const float* fe2,
                                         const double* __restrict__ bounds, int j, bool valid) {
     const unsigned FULL = 0xffffffffu;
@@ -543,8 +585,44 @@ __device__ inline double d_bisect_group(int n, const double* sd, const double* s
             hi = ghi;
         }
     }
-    // FP64 rounds
-    bool act = valid;
+    // FP64: Newton steps from the bracket's midpoint (lane 0 of the group), then two Sturm counts
+    // confirm that eigenvalue j lies within eps*||T|| of x.  Quadratic convergence from the FP32
+    // bracket takes about three steps; a cluster inside the bracket or a step that leaves it
+    // falls back to multisection on the bracket.
+    const double delta = 0.5 * atol;
+    double x = 0.5 * (lo + hi);
+    bool nwt = NEWTON && valid, nfail = !NEWTON;
+    for (int it = 0; it < 6; ++it) {
+        if (!__any_sync(FULL, nwt)) break;
+        double dx = 0.0;
+        if (nwt && gl == 0) dx = newton_dx(n, sd, se2, x);
+        dx = __shfl_sync(FULL, dx, gbase);
+        if (nwt) {
+            const double xn = x + dx;
+            if (!(xn > lo && xn < hi)) {
+                nwt = false;
+                nfail = true;
+            } else {
+                x = xn;
+                if (fabs(dx) <= 0.25 * delta) nwt = false;
+            }
+        }
+    }
+    if (nwt) nfail = true;   // not converged within the step limit
+    bool confirmed = false;
+    {
+        const bool chk = valid && !nfail && gl < 2;
+        const int c = chk ? sturm_count(n, sd, se2, gl == 0 ? x - delta : x + delta) : 0;
+        const unsigned okb = __ballot_sync(FULL, chk && ((gl == 0 && c <= j) || (gl == 1 && c > j)));
+        const unsigned need = (3u << gbase);
+        confirmed = valid && !nfail && (okb & need) == need;
+        if (confirmed) {
+            lo = x - delta;
+            hi = x + delta;
+        }
+    }
+    // FP64 multisection (only where Newton was not confirmed)
+    bool act = valid && !confirmed;
     for (int r = 0; r < 80; ++r) {
         act = act && (hi - lo > atol);
         if (!__any_sync(FULL, act)) break;
