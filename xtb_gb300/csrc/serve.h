@@ -26,8 +26,9 @@ namespace xg {
 struct ServeConfig {
     size_t pool_bytes = size_t(16) << 30;   // HBM budget of the resident pool
     int max_slots = 1024;                     // resident molecules at most
-    int plain_workers = 4;                    // concurrent plain-engine single points
-    int iters_per_step = 4;                   // SCC iterations per pool step
+    int plain_workers = 6;                    // concurrent plain-engine single points
+    int iters_per_step = 1;                   // SCC iterations per pool step (a pool launch holds
+                                              // its SMs for that long; one measured best)
     int precision = 0, slices = 5;            // plain-engine workers: 1 = split-precision products
     BatchSettings set;
 };

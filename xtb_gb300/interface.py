@@ -330,10 +330,12 @@ class Server:
     """Request loop with continuous batching (xtbgb_newServer ...).
 
     ``submit`` returns a request id; ``wait`` returns a ServedResult.  Calls from several
-    Python threads are safe: every call uses an environment of its own thread.
+    Python threads are safe: every call uses an environment of its own thread.  The defaults
+    (six plain-engine workers, one SCC iteration per pool step) measured best on the mixed
+    request stream of 3..1500 atoms.
     """
 
-    def __init__(self, pool_gib=16.0, max_slots=1024, plain_workers=4, iters_per_step=4, accuracy=1.0,
+    def __init__(self, pool_gib=16.0, max_slots=1024, plain_workers=6, iters_per_step=1, accuracy=1.0,
                  etemp=300.0, maxiter=250, precision="fp64", slices=5):
         import threading
         self.lib = load_library()
