@@ -509,12 +509,15 @@ void run_singlepoint(const HostMol& hm, const SPSettings& set, Wavefunction& wfn
         d4_scc(st, m, gw, q, zeta, dzeta, Wz, vat, ed4);
         shell_shift(st, m, J, qsh, vat, shift, Jq);
         aes_potential(st, m, q, dipm, qp, gab3, gab5, true, vs, vd, vq);
-        build_h(st, m, th, H0, S, D, Q, shift, vs, vd, vq, H);
-        // standard form A = X^T H X (X = U^-1 upper triangular, A symmetric)
+        build_hu(st, m, th, H0, S, D, Q, shift, vs, vd, vq, H);
+        // standard form A = X^T H X (X = U^-1 upper triangular) as B + B^T with B = X^T (Hu X):
+        // Hu X is a product of two upper triangular matrices (n^3/3 flops) and X^T (Hu X) needs
+        // only k < min(i, j) (2 n^3/3), so n^3 flops in all against 5/3 n^3 for X^T (H X) --
+        // the count of LAPACK's dsygst
         tm.mark(PH_STDFORM);
-        dgemm(st, false, false, nao, nao, nao, 1.0, H, nao, X, nao, 0.0, T1, nao, GF_B_UPPER);
-        dgemm(st, true, false, nao, nao, nao, 1.0, X, nao, T1, nao, 0.0, A, nao, GF_A_LOWER | GF_SYM);
-        mirror_lower(st, nao, A, nao);
+        dgemm(st, false, false, nao, nao, nao, 1.0, H, nao, X, nao, 0.0, T1, nao, GF_A_UPPER | GF_B_UPPER);
+        dgemm(st, true, false, nao, nao, nao, 1.0, X, nao, T1, nao, 0.0, A, nao, GF_A_LOWER | GF_B_UPPER);
+        sym_add(st, nao, A, nao);
         tm.mark(PH_SYTRD);
         sytrd(st, nao, A, nao, V, tri_tau, tri_d, tri_e, tri_p);
         // eigenvalues, occupations, then eigenvectors of the occupied orbitals only

@@ -271,13 +271,20 @@ __global__ void k_build_h(DevMol m, double neglect, const double* __restrict__ H
                           const double* __restrict__ vs, const double* __restrict__ vd, const double* __restrict__ vq,
                           double* __restrict__ H) {
     const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= (size_t)m.nao * m.nao) return;
+    const int n = m.nao;
+    if (t >= (size_t)n * n) return;
+    const int i = (int)(t / n), j = (int)(t % n);
+    if (i > j) {
+        H[t] = 0.0;
+        return;
+    }
     d_build_h(m, neglect, H0, S, D, Q, shift, vs, vd, vq, H, t);
+    if (i == j) H[t] *= 0.5;
 }
 
 
-void build_h(cudaStream_t st, const DevMol& m, Thresholds th, const double* H0, const double* S, const double* D,
-             const double* Q, const double* shift, const double* vs, const double* vd, const double* vq, double* H) {
+void build_hu(cudaStream_t st, const DevMol& m, Thresholds th, const double* H0, const double* S, const double* D,
+              const double* Q, const double* shift, const double* vs, const double* vd, const double* vq, double* H) {
     const size_t nn = (size_t)m.nao * m.nao;
     k_build_h<<<ceil_div((long)nn, 256), 256, 0, st>>>(m, th.neglect, H0, S, D, Q, shift, vs, vd, vq, H);
     XG_LAUNCH_CHECK();

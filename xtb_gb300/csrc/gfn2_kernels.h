@@ -77,8 +77,10 @@ void shell_shift(cudaStream_t st, const DevMol& m, const double* J, const double
                  double* shift, double* Jq);
 void aes_potential(cudaStream_t st, const DevMol& m, const double* q, const double* dipm, const double* qp,
                    const double* gab3, const double* gab5, bool shifted, double* vs, double* vd, double* vq);
-void build_h(cudaStream_t st, const DevMol& m, Thresholds th, const double* H0, const double* S, const double* D,
-             const double* Q, const double* shift, const double* vs, const double* vd, const double* vq, double* H);
+// Hu, the upper triangle of the Hamiltonian with half its diagonal (H = Hu + Hu^T); the lower
+// triangle is set to zero without being computed
+void build_hu(cudaStream_t st, const DevMol& m, Thresholds th, const double* H0, const double* S, const double* D,
+              const double* Q, const double* shift, const double* vs, const double* vd, const double* vq, double* H);
 // Fermi smearing (one block): focc = fa + fb (alpha, beta occupations), scal = {entropy term, e_fermi_a, e_fermi_b}
 // kocc[0] = number of leading orbitals with non-zero occupation
 void fermi(cudaStream_t st, int n, const double* emo, int nel_a, int nel_b, double etemp, double* focc, double* fa,

@@ -148,6 +148,27 @@ void mirror_lower(cudaStream_t st, int n, double* C, int ldc) {
     XG_LAUNCH_CHECK();
 }
 
+// C <- C + C^T (both triangles written); the thread of element (i, j), i >= j, owns the pair.
+__global__ void k_sym_add(int n, double* __restrict__ C, int ldc) {
+    const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long)n * n) return;
+    const int i = (int)(t / n), j = (int)(t % n);
+    if (i < j) return;
+    const size_t a = (size_t)i * ldc + j, b = (size_t)j * ldc + i;
+    if (i == j) {
+        C[a] *= 2.0;
+    } else {
+        const double s = C[a] + C[b];
+        C[a] = s;
+        C[b] = s;
+    }
+}
+
+void sym_add(cudaStream_t st, int n, double* C, int ldc) {
+    k_sym_add<<<ceil_div((long)n * n, 256), 256, 0, st>>>(n, C, ldc);
+    XG_LAUNCH_CHECK();
+}
+
 // ------------------------------------------------------------------ Cholesky (upper)
 constexpr int CNB = 32;
 

@@ -14,6 +14,8 @@ void dgemm(cudaStream_t st, bool ta, bool tb, int M, int N, int K, double alpha,
            const int* dN = nullptr);
 // copy the lower triangle of C onto its upper triangle
 void mirror_lower(cudaStream_t st, int n, double* C, int ldc);
+// C <- C + C^T
+void sym_add(cudaStream_t st, int n, double* C, int ldc);
 // A = U^T U, U upper (lower triangle zeroed); d_info[0] = failing column + 1 or 0
 void potrf_upper(cudaStream_t st, int n, double* A, int lda, int* d_info);
 // X = U^-1
