@@ -247,7 +247,7 @@ def run_served(args, ws, rank):
         dom, ach = "k_sytrd", kernels["k_sytrd"]["tflops"]
         traffic = sum(SYTRD_BYTES_PER_ELEM * float(x.nao) ** 2 * x.iterations for x in plain_res) / max(1, sy_launches)
         note = "4/3 n^3 FP64 flops per tridiagonalisation / CUDA-event time of the tridiagonalisation phase"
-    fp64_flops = sum(3.0 * float(x.nao) ** 3 * x.iterations for x in plain_res) + pool_flops
+    fp64_flops = sum((7.0 / 3.0) * float(x.nao) ** 3 * x.iterations for x in plain_res) + pool_flops
     fp64_job = fp64_flops / span / 1e12 if span > 0 else None   # rank 0 against one GPU
     out = {
         "metric": METRIC + ", served request stream (continuous batching) vs plain GPU SCC",
@@ -293,8 +293,9 @@ def run_served(args, ws, rank):
                      "peak_source": "measured FP64 FMA throughput of this GPU (MEASURED_PEAKS.json has no FP64 figure)"},
         # the whole run against the FP64 pipe: the per-launch roofline above is measured under
         # contention (concurrent requests share the SMs), so also report the FP64-only
-        # algorithmic work of all requests (plain engine: standard form 5/3 n^3 + tridiagonal
-        # reduction 4/3 n^3 per SCC iteration; pool: its counted SCC flops) over the span
+        # algorithmic work of all requests (plain engine: standard form n^3 + tridiagonal
+        # reduction 4/3 n^3 per SCC iteration, the counts of LAPACK's dsygst and dsytrd; pool:
+        # its counted SCC flops) over the span
         "fp64_job": {"achieved": fp64_job, "peak": peak, "unit": "TFLOP/s",
                      "frac": (fp64_job / peak) if peak else None,
                      "note": "FP64-only algorithmic flops of every request / served span (split-precision "
