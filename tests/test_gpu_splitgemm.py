@@ -21,7 +21,8 @@ def check(M, N, K, slices, seed=1, exp_range=0):
     return out
 
 
-@pytest.mark.parametrize("shape", [(64, 64, 64), (100, 77, 300), (257, 129, 4097), (1000, 1000, 1000)])
+@pytest.mark.parametrize("shape", [(64, 64, 64), (100, 77, 300), (257, 129, 4097), (1000, 1000, 1000),
+                                   (128, 3000, 3000)])   # the third and the last split K (few output tiles)
 def test_split_gemm_accuracy(shape):
     M, N, K = shape
     out5 = check(M, N, K, 5)

@@ -143,7 +143,8 @@ template <int S>
 __global__ void __launch_bounds__(256) k_split_mma(int M, int N, int Kp, const __nv_bfloat16* __restrict__ As,
                                                    const __nv_bfloat16* __restrict__ Bs, const double* __restrict__ sA,
                                                    const double* __restrict__ sB, double alpha, double beta,
-                                                   double* __restrict__ C, int ldc, const int* __restrict__ dN) {
+                                                   double* __restrict__ C, int ldc, const int* __restrict__ dN,
+                                                   int kchunk, double* __restrict__ P) {
     extern __shared__ __align__(16) unsigned char sg_raw[];
     __nv_bfloat16* smA = reinterpret_cast<__nv_bfloat16*>(sg_raw);
     __nv_bfloat16* smB = smA + S * SG_BM * SG_LD;
@@ -168,7 +169,11 @@ __global__ void __launch_bounds__(256) k_split_mma(int M, int N, int Kp, const _
                 for (int L = 0; L < S; ++L) acc[L][mt][nt][v] = 0.0f;
             }
     const int srow = tid >> 2, scol = (tid & 3) * 8;   // staging: one 16-byte chunk per thread per plane
-    for (int k0 = 0; k0 < Kp; k0 += SG_KT) {
+    // split K (P != nullptr): slice blockIdx.z covers [z kchunk, (z+1) kchunk), a whole number of
+    // exact chunks, and leaves alpha sA sB (its sum) in P[z][i][j] for k_split_reduce
+    const int kb = P ? (int)blockIdx.z * kchunk : 0;
+    const int ke = P ? min(Kp, kb + kchunk) : Kp;
+    for (int k0 = kb; k0 < ke; k0 += SG_KT) {
 #pragma unroll
         for (int p = 0; p < S; ++p) {
             const int gi = i0 + srow, gj = j0 + srow;
@@ -209,7 +214,7 @@ __global__ void __launch_bounds__(256) k_split_mma(int M, int N, int Kp, const _
             }
         }
         __syncthreads();
-        if ((k0 + SG_KT) % SG_KC == 0 || k0 + SG_KT >= Kp) {
+        if ((k0 + SG_KT) % SG_KC == 0 || k0 + SG_KT >= ke) {
             // levels 0..2 (exact FP32 chunk sums) into FP64; lower levels into an FP32 sum at the
             // scale of level 3, whose rounding is below 2^-48 of the result
 #pragma unroll
@@ -241,6 +246,10 @@ __global__ void __launch_bounds__(256) k_split_mma(int M, int N, int Kp, const _
                 if (i >= M || j >= Nl) continue;
                 const double sum = acc64[mt][nt][v] + (double)low[mt][nt][v] * 0x1p-24;
                 double r = alpha * sA[i] * sB[j] * (sum * 0x1p-16);
+                if (P) {
+                    P[((size_t)blockIdx.z * M + i) * N + j] = r;
+                    continue;
+                }
                 if (beta != 0.0) r += beta * C[(size_t)i * ldc + j];
                 C[(size_t)i * ldc + j] = r;
             }
@@ -248,10 +257,39 @@ __global__ void __launch_bounds__(256) k_split_mma(int M, int N, int Kp, const _
 
 }  // namespace
 
+// Split K for products with few output tiles (the skinny products of the blocked
+// back-transformation): up to SG_KS slices of whole exact chunks, when the tile grid would leave
+// SMs idle.  Partials need at most SG_KS x min(M N, SG_SPLIT_ELEMS) doubles.
+constexpr int SG_KS = 8;
+constexpr long SG_SPLIT_TILES = 304;
+constexpr size_t SG_SPLIT_ELEMS = (size_t)SG_SPLIT_TILES * SG_BM * SG_BN;
+
+static int split_k_slices(int M, int N, int Kp) {
+    const long tiles = (long)((M + SG_BM - 1) / SG_BM) * ((N + SG_BN - 1) / SG_BN);
+    if (tiles >= SG_SPLIT_TILES) return 1;
+    const int by_chunks = Kp / (2 * SG_KC);   // at least two exact chunks per slice
+    const int want = (int)std::min<long>(SG_KS, std::max<long>(1, (2 * SG_SPLIT_TILES / 2) / tiles));
+    return std::max(1, std::min(want, by_chunks));
+}
+
+// C[i][j] = sum_z P[z][i][j] (in slice order) + beta C[i][j], j < N (and < *dN)
+__global__ void k_split_reduce(int M, int N, int KS, const double* __restrict__ P, double beta,
+                               double* __restrict__ C, int ldc, const int* __restrict__ dN) {
+    const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long)M * N) return;
+    const int i = (int)(t / N), j = (int)(t % N);
+    if (dN && j >= *dN) return;
+    double r = 0.0;
+    for (int z = 0; z < KS; ++z) r += P[((size_t)z * M + i) * N + j];
+    if (beta != 0.0) r += beta * C[(size_t)i * ldc + j];
+    C[(size_t)i * ldc + j] = r;
+}
+
 size_t split_gemm_workspace(int M, int N, int K, int slices) {
     const size_t Kp = (size_t)((K + SG_KT - 1) / SG_KT) * SG_KT;
     const size_t bf = (size_t)slices * ((size_t)M + N) * Kp * sizeof(__nv_bfloat16);
-    return (bf + 255) / 256 * 256 + 2 * ((size_t)M + N) * sizeof(double) + 256;
+    const size_t split = (size_t)SG_KS * std::min((size_t)M * N, SG_SPLIT_ELEMS);
+    return (bf + 255) / 256 * 256 + 2 * ((size_t)M + N) * sizeof(double) + split * sizeof(double) + 512;
 }
 
 // Digits and scales of the rows of op(X) (R rows, K long): along memory rows when !trans,
@@ -287,8 +325,21 @@ static void split_gemm_s(cudaStream_t st, bool ta, bool tb, int M, int N, int K,
     split_operand<S>(st, N, K, Kp, B, ldb, !tb, dK, Bs, sB, mB);
     const size_t smem = (size_t)2 * S * SG_BM * SG_LD * sizeof(__nv_bfloat16);
     if (smem > 48 * 1024) allow_max_dynamic_smem((const void*)k_split_mma<S>);
+    const int ks = split_k_slices(M, N, Kp);
+    if (ks > 1) {
+        const int kchunk = ((Kp / ks + SG_KC - 1) / SG_KC) * SG_KC;
+        const int kz = (Kp + kchunk - 1) / kchunk;
+        double* P = reinterpret_cast<double*>(
+            (reinterpret_cast<uintptr_t>(mB + N) + 255) / 256 * 256);   // after the scales and maxima
+        dim3 grid(ceil_div(N, SG_BN), ceil_div(M, SG_BM), kz);
+        k_split_mma<S><<<grid, 256, smem, st>>>(M, N, Kp, As, Bs, sA, sB, alpha, beta, C, ldc, dN, kchunk, P);
+        XG_LAUNCH_CHECK();
+        k_split_reduce<<<ceil_div((long)M * N, 256), 256, 0, st>>>(M, N, kz, P, beta, C, ldc, dN);
+        XG_LAUNCH_CHECK();
+        return;
+    }
     dim3 grid(ceil_div(N, SG_BN), ceil_div(M, SG_BM));
-    k_split_mma<S><<<grid, 256, smem, st>>>(M, N, Kp, As, Bs, sA, sB, alpha, beta, C, ldc, dN);
+    k_split_mma<S><<<grid, 256, smem, st>>>(M, N, Kp, As, Bs, sA, sB, alpha, beta, C, ldc, dN, Kp, nullptr);
     XG_LAUNCH_CHECK();
 }
 
