@@ -13,13 +13,20 @@ Workloads (``--workload``):
   h2o300   plain FP64 single point of the seeded (H2O)300 cluster (900 atoms, 1800 AOs).
   batch4096 one launch set of the batched engine over 4096 seeded molecules (alkanes
            C1..C20, water clusters 2..30).
+  split_c200h402 / split_h2o1000  split-precision products vs the FP64 mode.
 
 ``value`` counts device-side time (for served: from the first request's start on the
 device to the last completion); ``e2e`` is wall clock through the C ABI with host buffers
 (geometry in, energy/gradient/charges out, every copy inside the timing).
 
-``--impl reference`` times the CPU restatement of the reference (oracle/, NumPy + SciPy
-LAPACK on all host cores) on a bounded sample of the same workload.
+``--impl reference`` times the reference's CPU algorithm on the host cores: the C++/OpenMP +
+LAPACK restatement of the oracle (oracle/twin.cpp, pinned to the reference's known-answer
+tests and to the oracle fixtures), over the same requests as the GPU arm.  The K timed steps
+split the workload between them, so the run covers every request once.
+
+The default line also carries, under ``configs``, the three single-GPU configurations beside
+the served stream: the (H2O)300 plain FP64 single point, the 4096-molecule batched set and the
+C200H402 split-precision single point, each with its own timing, parity and clocks.
 """
 import argparse
 import json
@@ -36,6 +43,8 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+# the headline metric, word for word in both arms
+SERVED_METRIC = "single points/s + p99 latency, served vs plain GPU SCC, at |ΔE|≤1e-6 Eh"
 METRIC = "GFN2-xTB single points/s (energy + Mulliken charges + gradient on request)"
 PHASES = ("setup", "integrals", "cholesky", "hbuild", "stdform", "sytrd", "trieig", "backtransform", "density",
           "popmix", "gradient", "total")
@@ -128,7 +137,7 @@ def dist_barrier(ws):
 
 
 def host_info():
-    model = platform.processor() or platform.machine()
+    model = ""
     try:
         for line in open("/proc/cpuinfo"):
             if line.lower().startswith(("model name", "cpu model")):
@@ -136,7 +145,16 @@ def host_info():
                 break
     except OSError:
         pass
-    return model
+    if not model:
+        try:
+            out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+            for line in out.splitlines():
+                if line.startswith("Model name"):
+                    model = line.split(":", 1)[1].strip()
+                    break
+        except (OSError, subprocess.SubprocessError):
+            pass
+    return f"{model or 'unknown CPU'} ({platform.machine()}, {os.cpu_count()} cores)"
 
 
 def stream_requests(args):
@@ -150,6 +168,70 @@ def sp_flops(nao, nocc, iters):
     + 2 n^2 k (density)."""
     n = float(nao)
     return iters * ((16.0 / 3.0) * n ** 3 + 2.0 * n * n * nocc)
+
+
+_PEAK = None
+
+
+def fp64_peak(lib):
+    """Roofline denominator for the FP64 kernels: the largest of two FMA-throughput probes and
+    the engine's own FP64 GEMM at 4096^3, measured once per process on this GPU
+    (MEASURED_PEAKS.json holds no FP64 figure)."""
+    global _PEAK
+    if _PEAK is None:
+        import ctypes as C
+        d = np.zeros(3)
+        lib.xtbgb_fp64PeakDetail(d.ctypes.data_as(C.POINTER(C.c_double)))
+        _PEAK = (float(np.max(d)), {"fma_probe": float(d[0]), "accumulator_probe": float(d[1]),
+                                    "fp64_gemm_4096": float(d[2]),
+                                    "source": "measured on this GPU in this run: the largest of the three"})
+    return _PEAK
+
+
+# ------------------------------------------------------------------ workloads, named once for both arms
+PLAIN_WORKLOADS = {
+    "h2o300": ("(H2O)300 seeded water cluster, 900 atoms, 1800 AOs, plain FP64 GPU single point",
+               lambda W: W.water_cluster(300, seed=1)),
+    "h2o1000": ("(H2O)1000 seeded water cluster, 3000 atoms, 6000 AOs, plain FP64 GPU single point",
+                lambda W: W.water_cluster(1000, seed=1)),
+    "c200h402": ("all-trans C200H402, sigma 0.02 A jitter, 602 atoms, 1202 AOs, plain FP64 GPU single point",
+                 lambda W: W.alkane(200, 0.02, seed=1)),
+}
+SPLIT_WORKLOADS = {
+    "split_c200h402": ("all-trans C200H402 (602 atoms, 1202 AOs), split-precision products vs FP64",
+                       lambda W: W.alkane(200, 0.02, seed=1)),
+    "split_h2o1000": ("(H2O)1000 seeded water cluster (3000 atoms, 6000 AOs), split-precision products vs FP64",
+                      lambda W: W.water_cluster(1000, seed=1)),
+}
+BATCH_DESC = "4096 molecules: 2048 alkanes C_nH_2n+2 n~U{1..20}, 2048 water clusters m~U{2..30}, seed 7"
+
+
+def served_desc(args):
+    return (f"served stream: {args.requests} requests, atoms log-uniform 3..1500 (alkanes C_nH_2n+2 and "
+            f"(H2O)_m, 1/2 each), gradient on 1/2, neutral, T_el 300 K, seed {args.seed}")
+
+
+def workload_spec(args):
+    """(metric, config.workload) of the selected workload: the same strings in both arms."""
+    if args.workload == "served":
+        return SERVED_METRIC, served_desc(args)
+    if args.workload == "batch4096":
+        return METRIC + ", batched engine (one thread block per molecule) vs plain GPU SCC", BATCH_DESC
+    if args.workload in SPLIT_WORKLOADS:
+        return METRIC + ", split-precision products (BF16 tensor cores) vs FP64", SPLIT_WORKLOADS[args.workload][0]
+    return METRIC + ", plain FP64 GPU SCC", PLAIN_WORKLOADS[args.workload][0]
+
+
+def workload_requests(args):
+    """The workload as a list of requests (numbers, positions, gradient)."""
+    from xtb_gb300 import workloads as W
+    if args.workload == "served":
+        return stream_requests(args)
+    if args.workload == "batch4096":
+        return [{"numbers": z, "positions": x, "gradient": True} for z, x in W.mixed_batch(4096, seed=7)]
+    gen = (SPLIT_WORKLOADS.get(args.workload) or PLAIN_WORKLOADS[args.workload])[1]
+    Z, xyz = gen(W)
+    return [{"numbers": Z, "positions": xyz, "gradient": True}]
 
 
 # ------------------------------------------------------------------ served stream
@@ -170,10 +252,10 @@ def served_pass(srv, reqs, rate):
 
 def run_served(args, ws, rank):
     from xtb_gb300 import interface as X
-    dist_init(ws)
     lib = X.load_library()
     reqs = stream_requests(args)
     R = len(reqs)
+    metric, wdesc = workload_spec(args)
     srv = X.Server(pool_gib=args.pool_gib, max_slots=1024, plain_workers=args.workers,
                    iters_per_step=args.iters_per_step, precision=args.served_precision, slices=args.slices)
     for _ in range(args.warmup):
@@ -215,42 +297,44 @@ def run_served(args, ws, rank):
     plain_wall, plain_dev = 0.0, 0.0
     dE = dq = dg = 0.0
     iters_diff = 0
+    plain = []
     for r, s in zip(reqs, served):
         t1 = time.perf_counter()
         p = X.Calculator(r["numbers"], r["positions"], keep_orbitals=False).singlepoint()
         plain_wall += time.perf_counter() - t1
         plain_dev += p.phase_ms[-1] / 1e3
+        plain.append(p)
         dE = max(dE, abs(s.energy - p.energy))
         dq = max(dq, float(np.max(np.abs(s.charges - p.charges))))
         if r["gradient"]:
             dg = max(dg, float(np.max(np.abs(s.gradient - p.gradient))))
         iters_diff = max(iters_diff, abs(s.iterations - p.iterations))
-    # roofline of the dominant kernel: the pool's SCC kernel or the plain engine's tridiagonalisation
+    peak, peak_detail = fp64_peak(lib)
+    # Roofline of the dominant kernel, the FP64 tridiagonalisation, from the sequential plain
+    # pass: one request at a time, so its CUDA-event time is the kernel's own, not time spent
+    # queued behind concurrent requests.  Taken on the largest request (the one that sets the
+    # served makespan); 4/3 n^3 algorithmic flops per launch, one launch per SCC iteration.
+    big = max(plain, key=lambda p: p.nao)
+    sy_ms = big.phase_ms[PHASES.index("sytrd")] / big.iterations
+    ach = (4.0 / 3.0) * float(big.nao) ** 3 / (sy_ms * 1e-3) / 1e12
+    # the same kernel inside the served timed region (concurrent requests share the SMs, so
+    # these event times include queueing) and the pool's SCC kernel
     plain_res = [x for p in passes for x in p[0] if x.engine == 1]
-    sy_ms = sum(x.sytrd_ms for x in plain_res)
-    sy_flops = sum((4.0 / 3.0) * float(x.nao) ** 3 * x.iterations for x in plain_res)
-    sy_launches = sum(x.iterations for x in plain_res)
-    peak = lib.xtbgb_fp64PeakTflops()
+    ssy_ms = sum(x.sytrd_ms for x in plain_res)
+    ssy_flops = sum((4.0 / 3.0) * float(x.nao) ** 3 * x.iterations for x in plain_res)
     pool_ms, pool_flops = d["pool_scc_ms"], d["pool_scc_flops"]
-    kernels = {
+    served_kernels = {
         "k_batch_scc": {"device_ms": round(pool_ms, 2), "tflops": (pool_flops / (pool_ms * 1e-3) / 1e12)
                         if pool_ms > 0 else None, "launches": int(d["steps"])},
-        "k_sytrd": {"device_ms": round(sy_ms, 2), "tflops": (sy_flops / (sy_ms * 1e-3) / 1e12) if sy_ms > 0 else None,
-                    "launches": int(sy_launches)},
+        "k_sytrd": {"device_ms": round(ssy_ms, 2), "tflops": (ssy_flops / (ssy_ms * 1e-3) / 1e12)
+                    if ssy_ms > 0 else None, "launches": int(sum(x.iterations for x in plain_res))},
+        "note": "CUDA-event times inside the served timed region, summed over concurrent requests "
+                "(they overlap, and include time queued behind other requests' kernels)",
     }
-    if pool_ms >= sy_ms:
-        dom, ach = "k_batch_scc", kernels["k_batch_scc"]["tflops"]
-        traffic = None
-        note = ("algorithmic FP64 flops of the SCC iterations the pool ran (n^3 + 4/3 n^3 + 2 n^3 + n^3 + 2 n^2 k "
-                "per molecule and iteration) / CUDA-event time of the pool's SCC kernel")
-    else:
-        dom, ach = "k_sytrd", kernels["k_sytrd"]["tflops"]
-        traffic = sum(SYTRD_BYTES_PER_ELEM * float(x.nao) ** 2 * x.iterations for x in plain_res) / max(1, sy_launches)
-        note = "4/3 n^3 FP64 flops per tridiagonalisation / CUDA-event time of the tridiagonalisation phase"
     fp64_flops = sum((7.0 / 3.0) * float(x.nao) ** 3 * x.iterations for x in plain_res) + pool_flops
     fp64_job = fp64_flops / span / 1e12 if span > 0 else None   # rank 0 against one GPU
     out = {
-        "metric": METRIC + ", served request stream (continuous batching) vs plain GPU SCC",
+        "metric": metric,
         "value": ws * args.steps * R / span,
         "unit": "single points/s",
         "n_gpus": ws,
@@ -262,8 +346,7 @@ def run_served(args, ws, rank):
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic (seeded request stream; no public suite exists for this path)",
-        "config": {"workload": f"served stream: {R} requests, atoms log-uniform 3..1500 (alkanes C_nH_2n+2 and "
-                               f"(H2O)_m, 1/2 each), gradient on 1/2, neutral, T_el 300 K, seed {args.seed}",
+        "config": {"workload": wdesc,
                    "arrival": f"Poisson {args.rate}/s" if args.rate else "all requests at t=0 (saturation)",
                    "served_precision": (f"split products ({args.slices} bf16 digits) on the plain-engine workers"
                                         if args.served_precision == "split" else "fp64"),
@@ -286,44 +369,64 @@ def run_served(args, ws, rank):
         "served_mix": {"pool": int(sum(1 for x in served if x.engine == 0)),
                        "plain_engine": int(sum(1 for x in served if x.engine == 1)),
                        "peak_resident": int(st1["peak_resident"])},
-        "kernels": kernels,
-        "roofline": {"bound": "fp64", "kernel": dom, "achieved": ach, "peak": peak, "unit": "TFLOP/s",
-                     "frac": (ach / peak) if (ach and peak) else None, "traffic": traffic,
-                     "traffic_unit": "bytes per launch" if traffic else None, "note": note,
-                     "peak_source": "measured FP64 FMA throughput of this GPU (MEASURED_PEAKS.json has no FP64 figure)"},
-        # the whole run against the FP64 pipe: the per-launch roofline above is measured under
-        # contention (concurrent requests share the SMs), so also report the FP64-only
-        # algorithmic work of all requests (plain engine: standard form n^3 + tridiagonal
-        # reduction 4/3 n^3 per SCC iteration, the counts of LAPACK's dsygst and dsytrd; pool:
-        # its counted SCC flops) over the span
+        "served_kernels": served_kernels,
+        "roofline": {"bound": "fp64", "kernel": "k_sytrd", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
+                     "frac": ach / peak if peak else None,
+                     "traffic": SYTRD_BYTES_PER_ELEM * float(big.nao) ** 2, "traffic_unit": "bytes per launch",
+                     "launch_ms": sy_ms, "nao": int(big.nao), "launches": int(big.iterations),
+                     "note": "4/3 n^3 FP64 flops per launch / CUDA-event time per launch, largest request of the "
+                             "stream in the sequential plain pass (no concurrent work); traffic scaled as n^2 from "
+                             "the ncu capture at n = 1800",
+                     "peak_detail": peak_detail},
+        # the whole run against the FP64 pipe: FP64-only algorithmic work of all requests (plain
+        # engine: standard form n^3 + tridiagonal reduction 4/3 n^3 per SCC iteration, the counts
+        # of LAPACK's dsygst and dsytrd; pool: its counted SCC flops) over the span
         "fp64_job": {"achieved": fp64_job, "peak": peak, "unit": "TFLOP/s",
                      "frac": (fp64_job / peak) if peak else None,
                      "note": "FP64-only algorithmic flops of every request / served span (split-precision "
                              "products on the tensor cores not counted)"},
         "clocks": clk,
     }
+    if not args.no_configs and ws == 1:
+        out["configs"] = run_configs(args)
     if not args.no_cpu_baseline and ws == 1:
         out["cpu_baseline"] = cpu_baseline(args, reqs)
     return out
 
 
-# ------------------------------------------------------------------ plain (H2O)300
-PLAIN_WORKLOADS = {
-    "h2o300": ("(H2O)300 seeded water cluster, 900 atoms, 1800 AOs, plain FP64 GPU single point",
-               lambda W: W.water_cluster(300, seed=1)),
-    "h2o1000": ("(H2O)1000 seeded water cluster, 3000 atoms, 6000 AOs, plain FP64 GPU single point",
-                lambda W: W.water_cluster(1000, seed=1)),
-    "c200h402": ("all-trans C200H402, sigma 0.02 A jitter, 602 atoms, 1202 AOs, plain FP64 GPU single point",
-                 lambda W: W.alkane(200, 0.02, seed=1)),
-}
+def run_configs(args):
+    """The three other single-GPU configurations, timed after the served passes, each with
+    its own steps, timing, parity and clocks (3 timed steps after 3 warm-up steps)."""
+    sub = argparse.Namespace(**vars(args))
+    sub.steps, sub.warmup, sub.no_cpu_baseline = 3, 3, True
+    keep = ("metric", "value", "unit", "steps", "warmup", "ms_per_step", "config", "e2e", "gpu_launches",
+            "parity", "error_vs_fp64", "fp64_mode", "plain", "roofline", "phase_ms_per_step", "clocks")
+    out = {}
+    for name, fn in (("h2o300", run_plain), ("batch4096", run_batch), ("split_c200h402", run_split)):
+        sub.workload = name
+        r = fn(sub, 1, 0)
+        out[name] = {k: r[k] for k in keep if k in r}
+    return out
+
+
+# ------------------------------------------------------------------ plain single point
+def fixture_parity(name, res):
+    """Largest differences of a GPU result against the committed oracle fixture of the geometry."""
+    path = os.path.join(ROOT, "tests", "golden", f"{name}.npz")
+    if not name or not os.path.exists(path):
+        return None
+    f = np.load(path)
+    return {"vs": f"oracle fixture tests/golden/{name}.npz", "abs_dE": abs(res.energy - float(f["energy"])),
+            "max_abs_dq": float(np.max(np.abs(res.charges - f["charges"]))),
+            "max_abs_dg": float(np.max(np.abs(res.gradient - f["gradient"]))),
+            "iterations": [int(res.iterations), int(f["iterations"])]}
 
 
 def run_plain(args, ws, rank):
     from xtb_gb300 import interface as X
     from xtb_gb300 import workloads as W
-    dist_init(ws)
-    desc, gen = PLAIN_WORKLOADS[args.workload]
-    Z, xyz = gen(W)
+    metric, desc = workload_spec(args)
+    Z, xyz = PLAIN_WORKLOADS[args.workload][1](W)
     lib = X.load_library()
     calc = X.Calculator(Z, xyz, keep_orbitals=False)
     for _ in range(args.warmup):
@@ -349,11 +452,11 @@ def run_plain(args, ws, rank):
     if rank != 0:
         return None
     per_step = phase / args.steps
-    sy_ms = per_step[PHASES.index("sytrd")]
-    ach = (4.0 / 3.0) * float(nao) ** 3 * iters / (sy_ms * 1e-3) / 1e12
-    peak = lib.xtbgb_fp64PeakTflops()
+    sy_ms = per_step[PHASES.index("sytrd")] / iters
+    ach = (4.0 / 3.0) * float(nao) ** 3 / (sy_ms * 1e-3) / 1e12
+    peak, peak_detail = fp64_peak(lib)
     out = {
-        "metric": METRIC + ", plain FP64 GPU SCC",
+        "metric": metric,
         "value": ws * args.steps / dev_s, "unit": "single points/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64",
@@ -365,41 +468,30 @@ def run_plain(args, ws, rank):
         "e2e": {"value": ws * args.steps / wall_s, "unit": "single points/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(launches),
+        "parity": fixture_parity({"h2o300": "h2o_300_seed1"}.get(args.workload, ""), r),
         "phase_ms_per_step": {k: round(float(v), 3) for k, v in zip(PHASES, per_step)},
         "algorithmic_tflops_per_sp": sp_flops(nao, nocc, iters) / 1e12,
         "roofline": {"bound": "fp64", "kernel": "k_sytrd", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
-                     "frac": ach / peak if peak else None,
+                     "frac": ach / peak if peak else None, "launch_ms": sy_ms,
                      "traffic": SYTRD_BYTES_PER_ELEM * float(nao) ** 2, "traffic_unit": "bytes per launch",
-                     "note": "4/3 n^3 FP64 flops per tridiagonalisation / CUDA-event time of that phase",
-                     "peak_source": "measured FP64 FMA throughput of this GPU (MEASURED_PEAKS.json has no FP64 figure)"},
+                     "note": "4/3 n^3 FP64 flops per launch / CUDA-event time per launch",
+                     "peak_detail": peak_detail},
         "clocks": clk,
     }
     if not args.no_cpu_baseline and ws == 1:
-        from xtb_gb300 import workloads as W2
-        Zc, xc = W2.alkane(10, 0.02, seed=1)
-        out["cpu_baseline"] = cpu_baseline(args, [{"numbers": Zc, "positions": xc, "size": len(Zc)}],
-                                           note="C10H22 (32 atoms) repeated")
+        out["cpu_baseline"] = cpu_baseline(args, workload_requests(args))
     return out
 
 
 # ------------------------------------------------------------------ split precision vs FP64
-SPLIT_WORKLOADS = {
-    "split_c200h402": ("all-trans C200H402 (602 atoms, 1202 AOs), split-precision products vs FP64",
-                       lambda W: W.alkane(200, 0.02, seed=1)),
-    "split_h2o1000": ("(H2O)1000 seeded water cluster (3000 atoms, 6000 AOs), split-precision products vs FP64",
-                      lambda W: W.water_cluster(1000, seed=1)),
-}
-
-
 def run_split(args, ws, rank):
     """Split-precision mode (back-transformation, P and W as BF16 tensor-core digit products) timed
     over `steps` single points; the FP64 mode on the same molecule gives the reference for the
     per-result errors |dE|, max |dq|, max |dg| and ||dP||_F / ||P||_F."""
     from xtb_gb300 import interface as X
     from xtb_gb300 import workloads as W
-    dist_init(ws)
-    desc, gen = SPLIT_WORKLOADS[args.workload]
-    Z, xyz = gen(W)
+    metric, desc = workload_spec(args)
+    Z, xyz = SPLIT_WORKLOADS[args.workload][1](W)
     lib = X.load_library()
     cs = X.Calculator(Z, xyz, keep_orbitals=False, precision="split", slices=args.slices)
     for _ in range(args.warmup):
@@ -443,12 +535,12 @@ def run_split(args, ws, rank):
            "max_abs_dg": float(np.max(np.abs(s.gradient - f.gradient))), "iterations": [f.iterations, s.iterations],
            "rel_frobenius_dP": float(np.linalg.norm(Ps - Pf) / np.linalg.norm(Pf))}
     per = phase / args.steps
-    peak = lib.xtbgb_fp64PeakTflops()
+    peak, peak_detail = fp64_peak(lib)
     n = r.nao
-    sy = per[PHASES.index("sytrd")]
-    ach = (4.0 / 3.0) * float(n) ** 3 * r.iterations / (sy * 1e-3) / 1e12
+    sy = per[PHASES.index("sytrd")] / r.iterations
+    ach = (4.0 / 3.0) * float(n) ** 3 / (sy * 1e-3) / 1e12
     return {
-        "metric": METRIC + ", split-precision products (BF16 tensor cores) vs FP64",
+        "metric": metric,
         "value": ws * args.steps / dev, "unit": "single points/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * dev / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": f"f64 (products: bf16 digits x{args.slices}, fp32 accumulate)",
@@ -462,11 +554,11 @@ def run_split(args, ws, rank):
         "gpu_launches": int(launches),
         "phase_ms_per_step": {k: round(float(v), 3) for k, v in zip(PHASES, per)},
         "roofline": {"bound": "fp64", "kernel": "k_sytrd", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
-                     "frac": ach / peak if peak else None,
+                     "frac": ach / peak if peak else None, "launch_ms": sy,
                      "traffic": SYTRD_BYTES_PER_ELEM * float(n) ** 2, "traffic_unit": "bytes per launch",
                      "note": "the tridiagonalisation stays FP64 and dominates; split products are in "
                              "backtransform/density/gradient",
-                     "peak_source": "measured FP64 FMA throughput of this GPU"},
+                     "peak_detail": peak_detail},
         "clocks": clk,
     }
 
@@ -475,7 +567,7 @@ def run_split(args, ws, rank):
 def run_batch(args, ws, rank):
     from xtb_gb300 import interface as X
     from xtb_gb300 import workloads as W
-    dist_init(ws)
+    metric, desc = workload_spec(args)
     mols = W.mixed_batch(4096, seed=7)
     lib = X.load_library()
     b = X.Batch(mols)
@@ -492,10 +584,9 @@ def run_batch(args, ws, rank):
     if rank != 0:
         return None
     r = runs[-1]
-    nocc = [None] * len(mols)
     flops = sum(sp_flops(b.nao[i], b.nao[i] // 2, r.iterations[i]) for i in range(len(mols)))
     ach = flops / (r.device_ms * 1e-3) / 1e12
-    peak = lib.xtbgb_fp64PeakTflops()
+    peak, peak_detail = fp64_peak(lib)
     idx = np.random.default_rng(0).choice(len(mols), 32, replace=False)
     pw = pd = 0.0
     dE = 0.0
@@ -506,87 +597,110 @@ def run_batch(args, ws, rank):
         pd += p.phase_ms[-1] / 1e3
         dE = max(dE, abs(p.energy - r.energy[i]))
     n = len(mols)
-    return {
-        "metric": METRIC + ", batched engine (one thread block per molecule) vs plain GPU SCC",
+    out = {
+        "metric": metric,
         "value": ws * args.steps * n / dev, "unit": "single points/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * dev / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generators)",
-        "config": {"workload": "4096 molecules: 2048 alkanes C_nH_2n+2 n~U{1..20}, 2048 water clusters m~U{2..30}, "
-                               "seed 7", "nao_mean": float(np.mean(b.nao)), "nao_max": int(np.max(b.nao)),
+        "config": {"workload": desc, "nao_mean": float(np.mean(b.nao)), "nao_max": int(np.max(b.nao)),
                    "parallelism": f"replicas x{ws}", "l2": "6+ GB resident state, far above L2; no flush"},
         "e2e": {"value": ws * args.steps * n / wall, "unit": "single points/s",
                 "h2d_bytes_per_step": int(r.h2d_bytes), "d2h_bytes_per_step": int(r.d2h_bytes)},
         "gpu_launches": int(sum(x.launches for x in runs)),
         "plain": {"value": len(idx) / pd, "e2e": len(idx) / pw, "unit": "single points/s",
-                  "sample": "32 random molecules of the set, xtb_singlepoint one after another",
-                  "max_abs_dE_vs_batched": dE},
+                  "sample": "32 random molecules of the set, xtb_singlepoint one after another"},
+        "parity": {"vs": "plain engine on 32 random molecules of the set", "max_abs_dE": dE,
+                   "failed": int(np.sum(r.status != 0))},
         "roofline": {"bound": "fp64", "kernel": "batched step (all kernels)", "achieved": ach, "peak": peak,
                      "unit": "TFLOP/s", "frac": ach / peak if peak else None, "traffic": None,
                      "note": "algorithmic FP64 flops of all SCC iterations / CUDA-event time of the launch set",
-                     "peak_source": "measured FP64 FMA throughput of this GPU"},
+                     "peak_detail": peak_detail},
         "clocks": clk,
     }
+    if not args.no_cpu_baseline and ws == 1:
+        out["cpu_baseline"] = cpu_baseline(args, workload_requests(args))
+    return out
 
 
-# ------------------------------------------------------------------ CPU restatement
-def cpu_sample(reqs, budget, max_atoms):
-    """Oracle single points on the requests in stream order (skipping those above max_atoms)
-    until `budget` seconds are spent; returns (count, seconds, atoms done)."""
-    from oracle import gfn2
-    done, spent, atoms = 0, 0.0, []
+# ------------------------------------------------------------------ CPU: the reference's algorithm
+def blas_info():
+    try:
+        import scipy
+        b = scipy.show_config(mode="dicts")["Build Dependencies"]["lapack"]
+        return f"{b.get('name')} {b.get('version')}"
+    except Exception:   # noqa: BLE001 -- a description only
+        return "SciPy's bundled OpenBLAS"
+
+
+def cpu_threads():
+    return int(os.environ.get("OMP_NUM_THREADS", "0") or 0) or os.cpu_count()
+
+
+def twin_run(reqs):
+    """The C++/OpenMP + LAPACK restatement on `reqs`, one after another; (seconds, count)."""
+    from oracle import twin
+    spent = 0.0
     for r in reqs:
-        if r["size"] > max_atoms:
-            continue
         t0 = time.perf_counter()
-        gfn2.singlepoint(np.asarray(r["numbers"]), np.asarray(r["positions"], dtype=float))
+        twin.singlepoint(np.asarray(r["numbers"]), np.asarray(r["positions"], dtype=float))
         spent += time.perf_counter() - t0
-        done += 1
-        atoms.append(int(r["size"]))
-        if spent > budget:
-            break
-    return done, spent, atoms
+    return spent, len(reqs)
 
 
-def cpu_baseline(args, reqs, note=None):
-    n, t, atoms = cpu_sample(reqs * 64 if len(reqs) == 1 else reqs, args.cpu_budget, args.cpu_max_atoms)
-    return {"value": n / t if t > 0 else None, "unit": "single points/s", "cores": os.cpu_count(), "kind": "port",
-            "host": host_info(),
-            "sample": (note or "requests of the stream in order, those above "
-                       f"{args.cpu_max_atoms} atoms skipped") + f": {n} single points ({min(atoms)}..{max(atoms)} "
-                       f"atoms) in {t:.1f} s on the NumPy/SciPy-LAPACK restatement"}
+def cpu_desc(sample):
+    return (f"{sample}; C++/OpenMP restatement of the reference's algorithm (oracle/twin.cpp: dpotrf once, "
+            f"dsygst + dsyevd + dtrsm per SCC iteration, the density as a full dgemm, OpenMP loops elsewhere) with "
+            f"{cpu_threads()} OpenMP threads and {blas_info()} on all cores of {host_info()}; the reference binary "
+            "itself cannot be built here (no Fortran compiler, no meson)")
+
+
+def cpu_baseline(args, reqs):
+    """The reference's CPU algorithm on the same requests as the GPU arm, each once."""
+    from oracle import twin
+    twin.build()
+    twin.singlepoint(np.asarray(reqs[0]["numbers"]), np.asarray(reqs[0]["positions"], dtype=float))   # load
+    if args.workload == "batch4096":
+        reqs = reqs[:args.cpu_batch_sample]
+        what = f"the first {len(reqs)} molecules of the 4096-molecule set"
+    else:
+        what = "every request of the workload once"
+    t, n = twin_run(reqs)
+    return {"value": n / t, "unit": "single points/s", "cores": cpu_threads(), "kind": "port",
+            "sample": cpu_desc(f"{n} single points ({what}) in {t:.1f} s")}
 
 
 def run_reference(args, ws, rank):
+    """The reference arm: the reference's CPU algorithm on the host cores, on this arm's workload.
+    The K timed steps partition the workload's requests (request j goes to step j mod K), so the
+    run covers every request once; warm-up steps run the smallest request."""
     if rank != 0:
         return None
-    from xtb_gb300 import workloads as W
-    if args.workload in PLAIN_WORKLOADS or args.workload in SPLIT_WORKLOADS:
-        Zc, xc = W.alkane(10, 0.02, seed=1)
-        reqs = [{"numbers": Zc, "positions": xc, "size": len(Zc)}] * 64
-        wl = "C10H22 (32 atoms) single points on the CPU restatement (the (H2O)300 point takes minutes)"
-    elif args.workload == "batch4096":
-        reqs = [{"numbers": z, "positions": x, "size": len(z)} for z, x in W.mixed_batch(4096, seed=7)]
-        wl = "molecules of the 4096-molecule set in order"
-    else:
-        reqs = stream_requests(args)
-        wl = f"requests of the served stream (seed {args.seed}) in order, above {args.cpu_max_atoms} atoms skipped"
-    cpu_sample(reqs[:1], 0.0, args.cpu_max_atoms)       # warm-up: imports, first LAPACK calls
-    budget = max(5.0, args.cpu_budget / max(1, args.steps))
-    tot_n, tot_t = 0, 0.0
-    for _ in range(args.steps):
-        n, t, _ = cpu_sample(reqs, budget, args.cpu_max_atoms)
-        tot_n += n
+    from oracle import twin
+    twin.build()
+    metric, wdesc = workload_spec(args)
+    reqs = workload_requests(args)
+    if args.workload == "batch4096":
+        reqs = reqs[:args.cpu_batch_sample]
+    small = min(reqs, key=lambda r: len(r["numbers"]))
+    for _ in range(max(1, args.warmup)):
+        twin_run([small])
+    K = args.steps
+    parts = [reqs[s::K] for s in range(K)] if len(reqs) >= K else [[reqs[s % len(reqs)]] for s in range(K)]
+    tot_t, tot_n = 0.0, 0
+    for part in parts:
+        t, n = twin_run(part)
         tot_t += t
+        tot_n += n
     value = tot_n / tot_t
-    return {"metric": METRIC, "impl": "reference", "value": value, "unit": "single points/s", "n_gpus": ws,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_t / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": wl},
-            "cpu_baseline": {"value": value, "unit": "single points/s", "cores": os.cpu_count(), "kind": "port",
-                             "host": host_info(),
-                             "sample": f"{tot_n} single points in {tot_t:.1f} s; the reference binary cannot be "
-                                       "built (Fortran + meson, not installable with pip), so the oracle "
-                                       "restatement stands in for it"},
+    what = ("every request of the workload once, split over the timed steps" if args.workload != "batch4096"
+            else f"the first {args.cpu_batch_sample} molecules of the 4096-molecule set")
+    return {"metric": metric, "impl": "reference", "value": value, "unit": "single points/s", "n_gpus": ws,
+            "steps": K, "warmup": args.warmup, "ms_per_step": 1e3 * tot_t / K,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (the same seeded requests as the GPU arm)",
+            "config": {"workload": wdesc},
+            "cpu_baseline": {"value": value, "unit": "single points/s", "cores": cpu_threads(), "kind": "port",
+                             "sample": cpu_desc(f"{tot_n} single points ({what}) in {tot_t:.1f} s")},
             "e2e": {"value": value, "unit": "single points/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
@@ -607,14 +721,16 @@ def main():
     ap.add_argument("--workers", type=int, default=6, help="served: plain-engine workers")
     ap.add_argument("--iters-per-step", type=int, default=1, help="served: SCC iterations per pool step")
     ap.add_argument("--pool-gib", type=float, default=24.0, help="served: HBM budget of the resident pool")
-    ap.add_argument("--cpu-budget", type=float, default=20.0, help="CPU restatement: seconds of work")
-    ap.add_argument("--cpu-max-atoms", type=int, default=120)
+    ap.add_argument("--cpu-batch-sample", type=int, default=512,
+                    help="batch4096: molecules of the set the CPU restatement runs")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-configs", action="store_true", help="served: skip the three other configurations")
     args = ap.parse_args()
     ws, rank, _ = dist_setup()
     if args.impl == "reference":
         out = run_reference(args, ws, rank)
     else:
+        dist_init(ws)
         run = {"served": run_served, "batch4096": run_batch}.get(args.workload)
         if run is None:
             run = run_split if args.workload in SPLIT_WORKLOADS else run_plain

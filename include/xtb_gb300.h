@@ -55,9 +55,14 @@ extern void xtbgb_setPrecision(xtb_TEnvironment env, xtb_TCalculator calc, int s
  * precision: 1500 AOs for FP64, 1000 for split precision. */
 extern void xtbgb_setBlockedBacktransform(xtb_TEnvironment env, xtb_TCalculator calc, int nao_min);
 
-/* Measured FP64 FMA throughput of device 0 in TFLOP/s (roofline denominator for FP64 kernels);
- * returns 0 when no device is present. */
+/* Measured FP64 throughput of device 0 in TFLOP/s (roofline denominator for FP64 kernels): the
+ * largest of two FMA-throughput probes and the engine's own FP64 GEMM at 4096^3; returns 0 when
+ * no device is present. */
 extern double xtbgb_fp64PeakTflops(void);
+
+/* The three figures behind xtbgb_fp64PeakTflops, measured anew (TFLOP/s): out[0] FMA chains with
+ * uniform operands, out[1] GEMM-style accumulator chains, out[2] FP64 GEMM C = A B at 4096^3. */
+extern void xtbgb_fp64PeakDetail(double* out);
 
 /* Dependent-operation latency of device 0 in clock cycles, measured with one warp:
  * cycles[0] FP64 FMA, [1] FP64 add, [2] FP64 multiply, [3] FP64 divide, [4] FP32 FMA

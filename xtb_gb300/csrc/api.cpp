@@ -628,6 +628,17 @@ double xtbgb_fp64PeakTflops(void) {
     }
 }
 
+void xtbgb_fp64PeakDetail(double* out) {
+    if (!out) return;
+    for (int k = 0; k < 3; ++k) out[k] = 0.0;
+    if (xg::device_count() == 0) return;
+    try {
+        xg::fp64_peak_tflops();
+        xg::fp64_peak_detail(out);
+    } catch (const std::exception&) {
+    }
+}
+
 void xtbgb_getIterations(xtb_TEnvironment env, xtb_TResults res, int* iterations, int* converged) {
     if (!res_ready(env, res, "xtbgb_getIterations", "SCC information")) return;
     if (iterations) *iterations = res->sp.iterations;

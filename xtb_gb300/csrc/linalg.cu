@@ -549,7 +549,9 @@ void ormtr(cudaStream_t st, int n, const double* V, const double* tau, const dou
 }  // namespace xg
 
 namespace xg {
-// FP64 FMA throughput probe: 8 independent chains per thread, all SMs busy.
+// FP64 FMA throughput probes, all SMs busy.  Probe 1: 8 independent chains a = a * b + c per
+// thread with uniform b, c.  Probe 2: the accumulator pattern of a GEMM, a_k += x_k y_k with 8
+// distinct register operands per thread.
 __global__ void k_fp64_probe(int iters, double* out) {
     double a[8];
     const double b = 1.0000000001, c = 1e-12;
@@ -564,6 +566,27 @@ __global__ void k_fp64_probe(int iters, double* out) {
     if (s == 12345.678) out[0] = s;   // keep the chains alive
 }
 
+__global__ void k_fp64_probe_acc(int iters, double* out) {
+    double x[8], y[8], a[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        x[k] = 1.0 + (threadIdx.x + k) * 1e-9;
+        y[k] = 1.0 - (blockIdx.x + k) * 1e-9;
+        a[k] = 0.0;
+    }
+    for (int i = 0; i < iters; ++i)
+#pragma unroll
+        for (int k = 0; k < 8; ++k) a[k] = fma(x[k], y[k], a[k]);
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) s += a[k];
+    if (s == 12345.678) out[0] = s;
+}
+
+namespace {
+double g_fp64_detail[3] = {0.0, 0.0, 0.0};   // FMA probe, accumulator probe, FP64 GEMM (TFLOP/s)
+}
+
 double fp64_peak_tflops() {
     int dev = 0, nsm = 0;
     XG_CUDA(cudaGetDevice(&dev));
@@ -574,22 +597,43 @@ double fp64_peak_tflops() {
     cudaEvent_t e0, e1;
     XG_CUDA(cudaEventCreate(&e0));
     XG_CUDA(cudaEventCreate(&e1));
-    k_fp64_probe<<<blocks, threads>>>(iters, d);   // warm-up
-    float best = 1e30f;
-    for (int r = 0; r < 5; ++r) {
-        XG_CUDA(cudaEventRecord(e0));
-        k_fp64_probe<<<blocks, threads>>>(iters, d);
-        XG_CUDA(cudaEventRecord(e1));
-        XG_CUDA(cudaEventSynchronize(e1));
-        float ms;
-        XG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-        best = std::min(best, ms);
-    }
+    auto best_ms = [&](auto launch) {
+        launch();   // warm-up
+        float best = 1e30f;
+        for (int r = 0; r < 5; ++r) {
+            XG_CUDA(cudaEventRecord(e0));
+            launch();
+            XG_CUDA(cudaEventRecord(e1));
+            XG_CUDA(cudaEventSynchronize(e1));
+            float ms;
+            XG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            best = std::min(best, ms);
+        }
+        return (double)best;
+    };
+    const double probe_flops = 2.0 * 8.0 * iters * (double)blocks * threads;
+    double t1 = best_ms([&] { k_fp64_probe<<<blocks, threads>>>(iters, d); });
+    double t2 = best_ms([&] { k_fp64_probe_acc<<<blocks, threads>>>(iters, d); });
+    XG_LAUNCH_CHECK();
+    g_fp64_detail[0] = probe_flops / (t1 * 1e-3) / 1e12;
+    g_fp64_detail[1] = probe_flops / (t2 * 1e-3) / 1e12;
+    // the engine's own FP64 GEMM, C = A B at 4096^3 (2 n^3 flops)
+    const int n = 4096;
+    double* m = nullptr;
+    XG_CUDA(cudaMalloc(&m, 3 * sizeof(double) * n * n));
+    XG_CUDA(cudaMemset(m, 0, 3 * sizeof(double) * n * n));
+    double t3 = best_ms([&] { dgemm(0, false, false, n, n, n, 1.0, m, n, m + (size_t)n * n, n, 0.0,
+                                    m + 2 * (size_t)n * n, n); });
+    g_fp64_detail[2] = 2.0 * (double)n * n * n / (t3 * 1e-3) / 1e12;
+    XG_CUDA(cudaFree(m));
     XG_CUDA(cudaEventDestroy(e0));
     XG_CUDA(cudaEventDestroy(e1));
     XG_CUDA(cudaFree(d));
-    const double flops = 2.0 * 8.0 * iters * (double)blocks * threads;
-    return flops / (best * 1e-3) / 1e12;
+    return std::max(g_fp64_detail[0], std::max(g_fp64_detail[1], g_fp64_detail[2]));
+}
+
+void fp64_peak_detail(double* out) {
+    for (int k = 0; k < 3; ++k) out[k] = g_fp64_detail[k];
 }
 // Dependent-chain latency probe, one warp: cycles per FP64 FMA, add, multiply, divide and
 // per FP32 FMA (clock64 around chains of `n` operations).

@@ -48,8 +48,10 @@ void ormtr_blocked(cudaStream_t st, int n, const double* V, const double* tau, d
 void dgemm_splitk(cudaStream_t st, bool ta, bool tb, int M, int N, int K, double alpha, const double* A, int lda,
                   const double* B, int ldb, double beta, double* C, int ldc, int nsplit, double* partial,
                   const int* dN = nullptr);
-// measured FP64 FMA throughput of the current device (TFLOP/s)
+// measured FP64 throughput of the current device (TFLOP/s): the largest of two FMA probes and
+// the FP64 GEMM at 4096^3; fp64_peak_detail gives the three figures of the last measurement
 double fp64_peak_tflops();
+void fp64_peak_detail(double* out);
 // dependent-operation latency in cycles: [0] FP64 FMA, [1] FP64 add, [2] FP64 multiply,
 // [3] FP64 divide, [4] FP32 FMA
 void fp64_latency_cycles(double* cycles);

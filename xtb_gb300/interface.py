@@ -81,6 +81,7 @@ def load_library(path=LIBPATH):
         "xtbgb_setPrecision": (None, [vp, vp, C.c_int, C.c_int]),
         "xtbgb_setBlockedBacktransform": (None, [vp, vp, C.c_int]),
         "xtbgb_fp64PeakTflops": (C.c_double, []),
+        "xtbgb_fp64PeakDetail": (None, [C.POINTER(C.c_double)]),
         "xtbgb_fp64LatencyCycles": (None, [dp]),
         "xtbgb_reciprocalCheck": (C.c_int, [dp]),
         "xtbgb_splitGemmCheck": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, dp]),
