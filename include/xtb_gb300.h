@@ -151,6 +151,10 @@ extern int xtbgb_serverWait(xtb_TEnvironment env, xtbgb_TServer server, long lon
  * kernel launches, device ms of the pool's SCC kernel, algorithmic FP64 flops of the pool's
  * SCC iterations (n^3 + 4/3 n^3 + 2 n^3 + n^3 + 2 n^2 k per molecule and iteration). */
 extern void xtbgb_serverStats(xtb_TEnvironment env, xtbgb_TServer server, double* stats);
+/* Test hook (no counterpart in the reference), host side only: the next `count` admissions to
+ * the resident pool fail as if the device had run out of memory.  Each such request completes
+ * with status 3 and the error on the waiting environment; the pool keeps serving the others. */
+extern void xtbgb_serverInjectAdmissionFailures(xtb_TEnvironment env, xtbgb_TServer server, int count);
 
 /* Repulsion energy and gradient of one molecule, computed from and into DEVICE memory
  * without allocating anything.  No counterpart in the reference: it exists for callers
@@ -164,7 +168,10 @@ extern void xtbgb_serverStats(xtb_TEnvironment env, xtbgb_TServer server, double
  * rejected.  The first call on each device looks up that array (cudaGetSymbolAddress) and
  * should come before any stream capture.  Calls that overlap in time share the scratch
  * and race: serialise them.  Returns 0 on success, else a nonzero code with a message in
- * errbuf[errlen] (errbuf may be NULL); an element outside 1..86 yields a NaN energy. */
+ * errbuf[errlen] (errbuf may be NULL).  The atomic numbers are device data and are not checked on
+ * the host: an element outside 1..86 still returns 0, with a NaN energy.  The scratch address is
+ * cached per device at the first call; resetting the device (cudaDeviceReset) between calls is
+ * not supported. */
 extern int xtbgb_repulsionNoAlloc(int natoms, const int* numbers, const double* positions, double* energy,
                                   double* gradient, void* stream, char* errbuf, int errlen);
 

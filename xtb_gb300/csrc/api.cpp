@@ -959,8 +959,20 @@ int xtbgb_serverWait(xtb_TEnvironment env, xtbgb_TServer srv, long long id, doub
         info[11] = c.sytrd_ms;
     }
     if (!c.error.empty()) env->error(c.error, src);
+    else if (c.status == xg::BST_CHOLESKY) env->error("Overlap matrix is not positive definite", src);
+    else if (c.status == xg::BST_NONFINITE) env->error("Energy or gradient is not finite", src);
     else if (c.status != xg::BST_OK) env->error("Self consistent charge iterator did not converge", src);
     return 1;
+}
+
+void xtbgb_serverInjectAdmissionFailures(xtb_TEnvironment env, xtbgb_TServer srv, int count) {
+    static const char* src = "xtbgb_serverInjectAdmissionFailures";
+    if (!check_env(env)) return;
+    if (!srv || !srv->srv) {
+        env->error("Server is not allocated", src);
+        return;
+    }
+    srv->srv->inject_admission_failures(count);
 }
 
 void xtbgb_serverStats(xtb_TEnvironment env, xtbgb_TServer srv, double* stats) {

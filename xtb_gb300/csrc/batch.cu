@@ -734,9 +734,28 @@ int SlotPool::admit(const HostMol& hm, int want_grad, cudaStream_t st) {
     cv.ups = &ups;
     layout_mol(cv, hm, b);
     b.want_grad = want_grad;
-    h2d_ += upload_runs(ups, base_ + off, st);
-    XG_CUDA(cudaMemcpyAsync(d_slots_ + slot, &b, sizeof(BatchMol), cudaMemcpyHostToDevice, st));
-    XG_CUDA(cudaStreamSynchronize(st));
+    try {
+        if (fail_admissions_ > 0) {
+            --fail_admissions_;
+            throw CudaError("admission failed: out of device memory (injected)");
+        }
+        h2d_ += upload_runs(ups, base_ + off, st);
+        XG_CUDA(cudaMemcpyAsync(d_slots_ + slot, &b, sizeof(BatchMol), cudaMemcpyHostToDevice, st));
+        XG_CUDA(cudaStreamSynchronize(st));
+    } catch (...) {
+        // hand the region back, so a failed admission costs only its own request
+        std::pair<size_t, size_t> r{off, need};
+        free_.insert(std::lower_bound(free_.begin(), free_.end(), r), r);
+        for (size_t k = 0; k + 1 < free_.size();) {
+            if (free_[k].first + free_[k].second == free_[k + 1].first) {
+                free_[k].second += free_[k + 1].second;
+                free_.erase(free_.begin() + k + 1);
+            } else {
+                ++k;
+            }
+        }
+        throw;
+    }
     h2d_ += sizeof(BatchMol);
     slot_off_[slot] = off;
     slot_size_[slot] = need;

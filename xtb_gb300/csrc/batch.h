@@ -135,6 +135,9 @@ public:
     size_t free_bytes() const;
     size_t capacity() const { return cap_; }
     long long h2d_bytes() const { return h2d_; }
+    // Host-side fault injection for tests: the next n admissions throw as if the device had run
+    // out of memory, after the slot search and before any upload (the region is handed back).
+    void fail_next_admissions(int n) { fail_admissions_ = n; }
 
 private:
     char* base_ = nullptr;
@@ -147,6 +150,7 @@ private:
     double last_ms_ = 0.0, last_flops_ = 0.0;
     size_t last_state_bytes_ = 0;
     std::vector<std::pair<size_t, size_t>> free_;   // (offset, size), sorted by offset
+    int fail_admissions_ = 0;
     long long h2d_ = 0;
 };
 

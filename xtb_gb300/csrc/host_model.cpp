@@ -120,6 +120,17 @@ std::string build_host_mol(int nat, const int* Zin, const double* xyzin, double 
         }
     }
     hm.nelem = (int)elem.size();
+    // every later stage divides by interatomic distances: reject non-finite coordinates and
+    // atoms that sit on top of each other (closer than 1e-3 bohr) before any device work
+    for (int i = 0; i < 3 * nat; ++i)
+        if (!std::isfinite(hm.xyz[i])) return "atom " + std::to_string(i / 3 + 1) + " has a non-finite coordinate";
+    for (int i = 0; i < nat; ++i)
+        for (int j = 0; j < i; ++j) {
+            const double dx = hm.xyz[3 * i] - hm.xyz[3 * j], dy = hm.xyz[3 * i + 1] - hm.xyz[3 * j + 1],
+                         dz = hm.xyz[3 * i + 2] - hm.xyz[3 * j + 2];
+            if (dx * dx + dy * dy + dz * dz < 1e-6)
+                return "atoms " + std::to_string(j + 1) + " and " + std::to_string(i + 1) + " coincide";
+        }
     // per-atom data
     double zsum = 0.0;
     for (int i = 0; i < nat; ++i) {

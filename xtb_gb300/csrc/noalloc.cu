@@ -48,8 +48,9 @@ RepTables make_tables() {
     return t;
 }
 
-// Thread per atom, the same pair loop and summation order as the engine's repulsion
-// kernel; the last block to finish sums the per-atom energies in the engine's order.
+// Thread per atom (the engine's kernel runs a warp per atom with a warp reduction and forms
+// r^1.5 as r sqrt(r); this one loops over the pairs serially and calls pow), so the two agree to
+// rounding, not bit for bit.  The last block to finish sums the per-atom energies in atom order.
 __global__ void __launch_bounds__(NOALLOC_BLOCK)
     k_repulsion_noalloc(int nat, const int* __restrict__ Z, const double* __restrict__ xyz, RepTables tab,
                         RepScratch* __restrict__ sc, double* __restrict__ energy, double* __restrict__ grad) {

@@ -72,6 +72,11 @@ std::vector<double> Server::stats() const {
     return {n_done_, n_plain_, n_steps_, busy_, peak_, n_rerun_, h2d_, d2h_, launches_, scc_ms_, scc_flops_};
 }
 
+void Server::inject_admission_failures(int n) {
+    std::lock_guard<std::mutex> lk(mu_);
+    inject_admissions_ = std::max(0, n);
+}
+
 void Server::complete(Completed&& c) {
     std::lock_guard<std::mutex> lk(mu_);
     c.t_done = now();
@@ -140,12 +145,30 @@ void Server::pool_body() {
                 incoming.push_back(std::move(small_q_.front()));
                 small_q_.pop_front();
             }
+            if (inject_admissions_ > 0) {
+                pool.fail_next_admissions(inject_admissions_);
+                inject_admissions_ = 0;
+            }
         }
-        // admission: in arrival order while slots and HBM budget last
+        // admission: in arrival order while slots and HBM budget last; a request whose
+        // admission fails (its upload threw) completes with the error, the others go on
         std::vector<std::unique_ptr<Req>> back, to_plain;
+        std::vector<Completed> rejected;
         bool full = false;
         for (auto& r : incoming) {
-            int slot = full ? -1 : pool.admit(r->hm, r->want_grad, st);
+            int slot = -1;
+            try {
+                slot = full ? -1 : pool.admit(r->hm, r->want_grad, st);
+            } catch (const std::exception& e) {
+                Completed c;
+                c.id = r->id;
+                c.status = BST_NONFINITE;
+                c.error = e.what();
+                c.t_submit = r->t_submit;
+                c.nao = r->hm.nao;
+                rejected.push_back(std::move(c));
+                continue;
+            }
             if (slot >= 0) {
                 r->t_start = now();
                 resident[slot] = std::move(r);
@@ -162,6 +185,7 @@ void Server::pool_body() {
             for (auto& r : to_plain) large_q_.push_back(std::move(r));
             cv_work_.notify_all();
         }
+        for (auto& c : rejected) complete(std::move(c));
         {
             std::lock_guard<std::mutex> lk(mu_);
             h2d_ += (double)(pool.h2d_bytes() - pool_h2d_seen_);

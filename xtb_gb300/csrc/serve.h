@@ -61,6 +61,10 @@ public:
     // bytes, [7] device->host bytes, [8] kernel launches, [9] pool SCC-kernel device ms,
     // [10] FP64 flops of the pool's SCC iterations (algorithmic count)
     std::vector<double> stats() const;
+    // Test hook, host side only: the next n admissions to the resident pool fail as if the
+    // device had run out of memory; each such request completes with an error and the pool
+    // keeps serving the others.
+    void inject_admission_failures(int n);
 
 private:
     struct Req {
@@ -84,6 +88,7 @@ private:
     long long next_id_ = 0;
     bool stop_ = false, pool_done_ = false;
     int inflight_ = 0;
+    int inject_admissions_ = 0;
     double n_done_ = 0, n_plain_ = 0, n_steps_ = 0, busy_ = 0, peak_ = 0, n_rerun_ = 0;
     double h2d_ = 0, d2h_ = 0, launches_ = 0, scc_ms_ = 0, scc_flops_ = 0;
     long long pool_h2d_seen_ = 0;

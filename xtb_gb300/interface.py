@@ -104,6 +104,7 @@ def load_library(path=LIBPATH):
         "xtbgb_serverSubmit": (C.c_longlong, [vp, vp, C.c_int, ip, dp, C.c_double, C.c_int, C.c_int]),
         "xtbgb_serverWait": (C.c_int, [vp, vp, C.c_longlong, C.c_double, dp, dp, dp, dp]),
         "xtbgb_serverStats": (None, [vp, vp, dp]),
+        "xtbgb_serverInjectAdmissionFailures": (None, [vp, vp, C.c_int]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -384,6 +385,13 @@ class Server:
                 raise XTBException(err)
         del self._natoms[rid]
         return ServedResult(rid, e.value, g, q, info, err)
+
+    def inject_admission_failures(self, count):
+        """Test hook: the next `count` admissions to the resident pool fail on the host as if the
+        device had run out of memory (xtbgb_serverInjectAdmissionFailures)."""
+        env = self._env()
+        self.lib.xtbgb_serverInjectAdmissionFailures(env.h, self.h, int(count))
+        env.check()
 
     def stats(self):
         s = np.zeros(16)
