@@ -250,12 +250,29 @@ def served_pass(srv, reqs, rate):
     return res, wall, span
 
 
+def autotune_served(args, reqs):
+    """The engine's autotuner, before any timing: the kernel-form crossovers of this device, then
+    the request loop's schedule on this stream (unless given on the command line)."""
+    from xtb_gb300 import tuning
+    forms = tuning.kernel_forms()
+    out = {"kernel_forms": forms}
+    if args.workers is None or args.iters_per_step is None:
+        sched = tuning.schedule(reqs, pool_gib=args.pool_gib, precision=args.served_precision, slices=args.slices)
+        out["schedule"] = sched
+        if args.workers is None:
+            args.workers = sched["plain_workers"]
+        if args.iters_per_step is None:
+            args.iters_per_step = sched["iters_per_step"]
+    return out
+
+
 def run_served(args, ws, rank):
     from xtb_gb300 import interface as X
     lib = X.load_library()
     reqs = stream_requests(args)
     R = len(reqs)
     metric, wdesc = workload_spec(args)
+    tuned = autotune_served(args, reqs)
     srv = X.Server(pool_gib=args.pool_gib, max_slots=1024, plain_workers=args.workers,
                    iters_per_step=args.iters_per_step, precision=args.served_precision, slices=args.slices)
     for _ in range(args.warmup):
@@ -370,6 +387,7 @@ def run_served(args, ws, rank):
                        "plain_engine": int(sum(1 for x in served if x.engine == 1)),
                        "peak_resident": int(st1["peak_resident"])},
         "served_kernels": served_kernels,
+        "autotune": tuned,
         "roofline": {"bound": "fp64", "kernel": "k_sytrd", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
                      "frac": ach / peak if peak else None,
                      "traffic": SYTRD_BYTES_PER_ELEM * float(big.nao) ** 2, "traffic_unit": "bytes per launch",
@@ -718,8 +736,9 @@ def main():
     ap.add_argument("--requests", type=int, default=64, help="served: requests per pass")
     ap.add_argument("--seed", type=int, default=11, help="served: stream seed")
     ap.add_argument("--rate", type=float, default=None, help="served: Poisson arrival rate (default: saturation)")
-    ap.add_argument("--workers", type=int, default=6, help="served: plain-engine workers")
-    ap.add_argument("--iters-per-step", type=int, default=1, help="served: SCC iterations per pool step")
+    ap.add_argument("--workers", type=int, default=None, help="served: plain-engine workers (default: autotuned)")
+    ap.add_argument("--iters-per-step", type=int, default=None,
+                    help="served: SCC iterations per pool step (default: autotuned)")
     ap.add_argument("--pool-gib", type=float, default=24.0, help="served: HBM budget of the resident pool")
     ap.add_argument("--cpu-batch-sample", type=int, default=512,
                     help="batch4096: molecules of the set the CPU restatement runs")

@@ -1,0 +1,59 @@
+"""The autotuner (needs a GB300).
+
+Its choices only select between kernel forms that compute the same single point, so the
+results must not depend on them: a molecule whose size sits where the forms cross over gives
+the same energy, charges and gradient with every form pinned (to the rounding of the
+different summation orders), and the request loop gives the same results under every schedule.
+"""
+import numpy as np
+import pytest
+
+from xtb_gb300 import interface as X
+from xtb_gb300 import tuning
+from xtb_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def test_kernel_forms_measured_and_kept():
+    t = tuning.kernel_forms()
+    assert t["seconds"] > 0.0
+    assert len(t["sytrd_ms"]) >= 5 and len(t["backtransform_ms"]) >= 4
+    for row in t["sytrd_ms"]:
+        assert row["row_form"] > 0.0 and row["upper_triangle_form"] > 0.0
+    g = X.get_tuning()
+    assert g["measured"]
+    assert (g["sytrd_sym_min"], g["blocked_min_fp64"], g["blocked_min_split"]) == \
+        (t["sytrd_sym_min"], t["blocked_min_fp64"], t["blocked_min_split"])
+    assert tuning.kernel_forms()["seconds"] == t["seconds"]      # kept, not measured again
+
+
+@pytest.mark.parametrize("precision", ["fp64", "split"])
+def test_results_do_not_depend_on_the_forms(precision):
+    Z, xyz = W.water_cluster(110, seed=3)             # 660 AOs
+    saved = X.get_tuning()
+    try:
+        X.set_tuning(3, 0, 0)                          # upper-triangle form, blocked back-transformation
+        a = X.Calculator(Z, xyz, keep_orbitals=False, precision=precision).singlepoint()
+        X.set_tuning(1 << 30, 1 << 30, 1 << 30)        # row form, one warp per vector
+        b = X.Calculator(Z, xyz, keep_orbitals=False, precision=precision).singlepoint()
+    finally:
+        X.set_tuning(saved["sytrd_sym_min"], saved["blocked_min_fp64"], saved["blocked_min_split"])
+    assert a.iterations == b.iterations
+    assert abs(a.energy - b.energy) <= 1e-9
+    assert np.max(np.abs(a.charges - b.charges)) <= 1e-8
+    assert np.max(np.abs(a.gradient - b.gradient)) <= 1e-8
+
+
+def test_schedule_choice_and_results():
+    reqs = W.served_stream(12, seed=5, nmax=400)
+    s = tuning.schedule(reqs, candidates=((2, 1), (4, 2)), pool_gib=2.0, max_slots=64)
+    assert (s["plain_workers"], s["iters_per_step"]) in ((2, 1), (4, 2))
+    assert len(s["span_s"]) == 2
+    out = {}
+    for w, i in ((2, 1), (4, 2)):
+        srv = X.Server(pool_gib=2.0, max_slots=64, plain_workers=w, iters_per_step=i)
+        out[w] = [srv.wait(srv.submit(r["numbers"], r["positions"], gradient=r["gradient"])) for r in reqs]
+        srv.close()
+    for r2, r4 in zip(out[2], out[4]):
+        assert abs(r2.energy - r4.energy) <= 1e-9

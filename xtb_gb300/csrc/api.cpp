@@ -19,6 +19,7 @@
 #include "../../include/xtb_gb300.h"
 #include "batch.h"
 #include "engine.h"
+#include "tune.h"
 #include "serve.h"
 #include "splitgemm.h"
 #include "host_model.h"
@@ -637,6 +638,43 @@ void xtbgb_fp64PeakDetail(double* out) {
         xg::fp64_peak_detail(out);
     } catch (const std::exception&) {
     }
+}
+
+int xtbgb_autotune(xtb_TEnvironment env, double* out, int nout) {
+    static const char* src = "xtbgb_autotune";
+    if (!check_env(env)) return 0;
+    if (xg::device_count() == 0) {
+        env->error("no CUDA device available for the GFN2 engine", src);
+        return 0;
+    }
+    try {
+        const xg::Tuned t = xg::autotune();
+        std::vector<double> v = {(double)t.sytrd_sym_min, (double)t.blocked_min_fp64, (double)t.blocked_min_split,
+                                 t.seconds, (double)(t.sytrd_rows.size() / 3)};
+        v.insert(v.end(), t.sytrd_rows.begin(), t.sytrd_rows.end());
+        v.push_back((double)(t.backtr_rows.size() / 4));
+        v.insert(v.end(), t.backtr_rows.begin(), t.backtr_rows.end());
+        const int m = std::min((int)v.size(), std::max(0, nout));
+        if (out) std::copy(v.begin(), v.begin() + m, out);
+        return m;
+    } catch (const std::exception& e) {
+        env->error(e.what(), src);
+        return 0;
+    }
+}
+
+void xtbgb_getTuning(xtb_TEnvironment env, double* out) {
+    if (!check_env(env) || !out) return;
+    const xg::Tuned t = xg::tuned();
+    out[0] = t.sytrd_sym_min;
+    out[1] = t.blocked_min_fp64;
+    out[2] = t.blocked_min_split;
+    out[3] = t.level;
+}
+
+void xtbgb_setTuning(xtb_TEnvironment env, int sytrd_sym_min, int blocked_min_fp64, int blocked_min_split) {
+    if (!check_env(env)) return;
+    xg::set_tuned(std::max(3, sytrd_sym_min), std::max(0, blocked_min_fp64), std::max(0, blocked_min_split));
 }
 
 void xtbgb_getIterations(xtb_TEnvironment env, xtb_TResults res, int* iterations, int* converged) {

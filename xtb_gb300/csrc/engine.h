@@ -4,6 +4,7 @@
 #include <vector>
 
 #include "host_model.h"
+#include "tune.h"
 
 namespace xg {
 
@@ -17,11 +18,10 @@ struct SPSettings {
     int precision = 0;
     int slices = 5;
     // AO count from which the back-transformation of the eigenvectors runs as compact-WY
-    // GEMMs instead of one warp per vector; -1 picks it by precision (measured on GB300 per
-    // single point: FP64 at (H2O)150, 900 AOs, warp form 41 ms vs 50 ms; at (H2O)300, 1800 AOs,
-    // 178 ms vs 165 ms; split precision 32 ms vs 34 ms and 149 ms vs 101 ms)
+    // GEMMs instead of one warp per vector; -1 takes the device's threshold for the precision
+    // (tune.h: measured by the autotuner, else the defaults measured once on GB300)
     int blocked_min = -1;
-    int blocked_threshold() const { return blocked_min >= 0 ? blocked_min : (precision == 1 ? 1000 : 1500); }
+    int blocked_threshold() const { return blocked_min >= 0 ? blocked_min : tuned_blocked_min(precision); }
     // CUDA stream priority of the single point's stream (lower is more urgent; clamped to the
     // device's range; 0 is the default priority)
     int stream_priority = 0;

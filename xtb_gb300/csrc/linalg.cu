@@ -15,6 +15,7 @@
 #include "linalg.h"
 #include "linalg_device.cuh"
 #include "splitgemm.h"
+#include "tune.h"
 
 namespace cg = cooperative_groups;
 
@@ -333,12 +334,342 @@ static void sytrd_launch(cudaStream_t st, int n, double* A, int lda, double* V, 
     ++launch_counter();
 }
 
+// ------------------------------------------------------------------ symmetric tridiagonalisation
+// Householder reduction A = Q T Q^T of a symmetric n x n matrix that keeps and updates only the
+// UPPER triangle: per column of the reduction every trailing element costs two FMAs for the
+// rank-2 update and two for the symmetric product (row part a x_j into (A x)_i, column part
+// a x_i into (A x)_j), 4/3 n^3 flops in all -- the algorithmic count of LAPACK's dsytrd -- where
+// a full-row pass costs 2 n^3.
+//
+// One cooperative launch, ONE grid barrier per column s (trailing size m = n - s - 1, local
+// indices 0..m-1 for global s + 1 + i):
+//   A  the trailing upper triangle in tiles of 16 rows x L columns (L = 32 or 64, chosen per
+//      column so that every warp gets a few tiles): each tile applies the pending update of
+//      column s-1 (A -= v w^T + w v^T), writes the elements back, and adds its row sums and
+//      column sums of A x into ax (FP64 atomics; x is the column's pivot row, not yet
+//      normalised).  Three ax buffers rotate: the one of column s+2 is cleared during column s,
+//      so the barrier of column s+1 orders the clearing before its first addition.
+//   C  after the barrier every block forms, from ax and a0 (row 0 of the trailing matrix, final
+//      up to column s-1): x.(A x) and x.a0, then beta, tau and the scale of the reflector
+//      v = (x - beta e0) / (x0 - beta), with |x[1:]|^2 from the previous column's pass; the
+//      product y = tau A v = tau scale (A x - beta a0) and w = y - (tau/2)(y.v) v elementwise;
+//      the next pivot row x' = a0[1:] - w[1:] - w0 v[1:] and its norm.
+// Normalising one column late lets the norm come from the explicitly formed pivot row.  Outputs
+// follow the row-by-row form (V row s = v_s on columns s+1.., tau, d, e).  The atomic sums make
+// the last bits of the results depend on the order in which tiles finish.
+constexpr int SYM_RB = 16;            // rows of a tile
+constexpr int SYM_MAXRT = 2;          // at most 32 * 2 columns per tile: a tile's 16 rows are
+                                      // loaded at once (the pass is bound by L2 latency otherwise)
+constexpr int SYM_NT = 256;
+
+__device__ __forceinline__ int sym_chunk_rt(int m, int nwarps) {
+    // tiles ~ m^2 / (2 * 16 * 32 rt): at least about four per warp before the tiles widen
+    const long long r = ((long long)m * m) / (4096LL * nwarps);
+    return (int)max(1LL, min((long long)SYM_MAXRT, r));
+}
+
+// task t of a step -> (row block I, chunk c); tasks are ordered by group a = I / q (q = L / 16
+// row blocks share the first chunk a), each row block of group a holding C - a chunks; gs[a] is
+// the first task of group a (gs[ngroups] = number of tasks)
+__device__ __forceinline__ void sym_task(int t, const int* gs, int ngroups, int C, int q, int& I, int& c) {
+    int lo = 0, hi = ngroups;   // gs[lo] <= t < gs[hi]
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (gs[mid] <= t) lo = mid;
+        else hi = mid;
+    }
+    const int off = t - gs[lo];
+    I = lo * q + off / (C - lo);
+    c = lo + off % (C - lo);
+}
+
+__global__ void __launch_bounds__(SYM_NT) k_sytrd_sym(int n, double* __restrict__ A, int lda,
+                                                      double* __restrict__ V, double* __restrict__ tau,
+                                                      double* __restrict__ d, double* __restrict__ e,
+                                                      double* __restrict__ ws) {
+    extern __shared__ double sm[];
+    double* xb[2] = {sm, sm + n};         // pivot row of the current / next column (unnormalised)
+    double* vps = sm + 2 * (size_t)n;     // pending update of the previous column: v, w (scratch
+    double* wps = vps + n;                // for A x and a0 between the tile pass and its rewrite)
+    double* red = wps + n;                // [2][8] block reductions
+    double* scal = red + 16;              // [16] scalars of the column
+    int* gs = reinterpret_cast<int*>(scal + 16);   // [n / 32 + 2] first task of each tile group
+    cg::grid_group grid = cg::this_grid();
+    const int G = gridDim.x;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int nwarps = G * (SYM_NT / 32);
+    const int gw = wid * G + blockIdx.x;   // consecutive tiles on consecutive SMs
+    const bool lead = blockIdx.x == 0;
+    auto axbuf = [&](int s) { return ws + (size_t)(s % 3) * n; };
+    // sum over the block of (a, b), every thread gets both
+    auto block_sum2 = [&](double a, double b, double& ra, double& rb) {
+        a = warp_sum(a);
+        b = warp_sum(b);
+        __syncthreads();
+        if (lane == 0) {
+            red[wid] = a;
+            red[8 + wid] = b;
+        }
+        __syncthreads();
+        double t0 = 0.0, t1 = 0.0, u0 = 0.0, u1 = 0.0;
+#pragma unroll
+        for (int w8 = 0; w8 < 8; w8 += 2) {
+            t0 += red[w8];
+            t1 += red[w8 + 1];
+            u0 += red[8 + w8];
+            u1 += red[9 + w8];
+        }
+        ra = t0 + t1;
+        rb = u0 + u1;
+    };
+
+    // prologue: pivot row of column 0, its norm, the first two ax buffers cleared
+    {
+        double nx2 = 0.0;
+        for (int i = threadIdx.x; i < n - 1; i += SYM_NT) {
+            const double v = A[i + 1];
+            xb[0][i] = v;
+            if (i >= 1) nx2 = fma(v, v, nx2);
+        }
+        double dummy;
+        block_sum2(nx2, 0.0, scal[8], dummy);
+        const int per = (n + G - 1) / G;
+        for (int i = blockIdx.x * per + threadIdx.x; i < min(n, (blockIdx.x + 1) * per); i += SYM_NT) {
+            axbuf(0)[i] = 0.0;
+            axbuf(1)[i] = 0.0;
+        }
+        if (lead && threadIdx.x == 0) d[0] = A[0];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) scal[9] = scal[8];
+    grid.sync();
+    bool pend = false;
+    int cur = 0;
+    for (int s = 0; s < n - 2; ++s) {
+        const int m = n - s - 1, b = s + 1;
+        const double* x = xb[cur];
+        double* xn = xb[cur ^ 1];
+        double* A22 = A + (size_t)b * lda + b;
+        double* ax = axbuf(s);
+        const int rt = sym_chunk_rt(m, nwarps);
+        const int L = 32 * rt, q = L / SYM_RB;
+        const int nrb = (m + SYM_RB - 1) / SYM_RB, C = (m + L - 1) / L;
+        // ---- tiles
+        const int ngroups = (nrb + q - 1) / q;
+        if (threadIdx.x == 0) {
+            int acc = 0;
+            for (int a = 0; a < ngroups; ++a) {
+                gs[a] = acc;
+                acc += min(q, nrb - a * q) * (C - a);
+            }
+            gs[ngroups] = acc;
+        }
+        __syncthreads();
+        const int ntask = gs[ngroups];
+        for (int t = gw; t < ntask; t += nwarps) {
+            int I, c;
+            sym_task(t, gs, ngroups, C, q, I, c);
+            const int i0 = I * SYM_RB;
+            double xj[SYM_MAXRT], vpj[SYM_MAXRT], wpj[SYM_MAXRT], cacc[SYM_MAXRT];
+            int jt[SYM_MAXRT];
+#pragma unroll
+            for (int u = 0; u < SYM_MAXRT; ++u) {
+                const int j = c * L + lane + 32 * u;
+                jt[u] = (u < rt && j < m) ? j : -1;
+                const int jj = jt[u] >= 0 ? j : 0;
+                xj[u] = x[jj];
+                vpj[u] = pend ? vps[jj + 1] : 0.0;
+                wpj[u] = pend ? wps[jj + 1] : 0.0;
+                cacc[u] = 0.0;
+            }
+            double rs[SYM_RB];
+            // the whole tile is loaded before any arithmetic: 16 rows x rt values per lane in flight
+            double at[SYM_RB][SYM_MAXRT];
+#pragma unroll
+            for (int rr = 0; rr < SYM_RB; ++rr)
+#pragma unroll
+                for (int u = 0; u < SYM_MAXRT; ++u) {
+                    const int i = i0 + rr, j = jt[u];
+                    at[rr][u] = (j >= i && i < m) ? A22[(size_t)i * lda + j] : 0.0;
+                }
+#pragma unroll
+            for (int rr = 0; rr < SYM_RB; ++rr) {
+                const int i = i0 + rr;
+                double s0 = 0.0;
+                if (i < m) {
+                    const double xi = x[i];
+                    const double vpi = pend ? vps[i + 1] : 0.0, wpi = pend ? wps[i + 1] : 0.0;
+                    double* arow = A22 + (size_t)i * lda;
+#pragma unroll
+                    for (int u = 0; u < SYM_MAXRT; ++u) {
+                        const int j = jt[u];
+                        if (j >= i) {
+                            double a = at[rr][u];
+                            if (pend) {
+                                a = fma(-vpi, wpj[u], a);
+                                a = fma(-wpi, vpj[u], a);
+                                arow[j] = a;
+                            }
+                            s0 = fma(a, xj[u], s0);
+                            if (j > i) cacc[u] = fma(a, xi, cacc[u]);
+                        }
+                    }
+                }
+                rs[rr] = s0;
+            }
+            // row sums over the 32 lanes: reduce-scatter, lane pair (2k, 2k+1) ends with row
+            // 8 b4 + 4 b3 + 2 b2 + b1 (b = lane bits)
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                const bool hi = lane & 16;
+                const double send = hi ? rs[k] : rs[k + 8];
+                rs[k] = (hi ? rs[k + 8] : rs[k]) + __shfl_xor_sync(0xffffffffu, send, 16);
+            }
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const bool hi = lane & 8;
+                const double send = hi ? rs[k] : rs[k + 4];
+                rs[k] = (hi ? rs[k + 4] : rs[k]) + __shfl_xor_sync(0xffffffffu, send, 8);
+            }
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                const bool hi = lane & 4;
+                const double send = hi ? rs[k] : rs[k + 2];
+                rs[k] = (hi ? rs[k + 2] : rs[k]) + __shfl_xor_sync(0xffffffffu, send, 4);
+            }
+            {
+                const bool hi = lane & 2;
+                const double send = hi ? rs[0] : rs[1];
+                rs[0] = (hi ? rs[1] : rs[0]) + __shfl_xor_sync(0xffffffffu, send, 2);
+            }
+            rs[0] += __shfl_xor_sync(0xffffffffu, rs[0], 1);
+            const int row = 8 * ((lane >> 4) & 1) + 4 * ((lane >> 3) & 1) + 2 * ((lane >> 2) & 1) + ((lane >> 1) & 1);
+            if (!(lane & 1) && i0 + row < m) atomicAdd(&ax[i0 + row], rs[0]);
+#pragma unroll
+            for (int u = 0; u < SYM_MAXRT; ++u)
+                if (jt[u] > i0) atomicAdd(&ax[jt[u]], cacc[u]);
+        }
+        grid.sync();
+        // ---- the column's reflector and update vectors, in every block
+        double sxa = 0.0, sx0 = 0.0;
+        for (int j = threadIdx.x; j < m; j += SYM_NT) {
+            const double a = ax[j], a0 = A22[j], xv = x[j];
+            vps[j] = a;   // the pending vectors are dead after the tile pass
+            wps[j] = a0;
+            sxa = fma(xv, a, sxa);
+            sx0 = fma(xv, a0, sx0);
+        }
+        double txa, tx0;
+        block_sum2(sxa, sx0, txa, tx0);
+        if (threadIdx.x == 0) {
+            const double alpha = x[0], ax0 = vps[0], a00 = wps[0], t0 = scal[9];
+            double beta, tk, sc, yv;
+            if (t0 == 0.0) {
+                tk = 0.0;
+                beta = alpha;
+                sc = 0.0;
+                yv = 0.0;
+            } else {
+                beta = -copysign(sqrt(alpha * alpha + t0), alpha);
+                tk = (beta - alpha) / beta;
+                sc = 1.0 / (alpha - beta);
+                // y.v = tau sc^2 (x - beta e0).(A x - beta a0)
+                yv = tk * sc * sc * (txa - beta * tx0 - beta * ax0 + beta * beta * a00);
+            }
+            scal[0] = beta;
+            scal[1] = tk;
+            scal[2] = sc;
+            scal[3] = 0.5 * tk * yv;                            // h
+            scal[4] = tk * sc * (ax0 - beta * a00) - scal[3];   // w0 (v0 = 1)
+            if (lead) {
+                tau[s] = tk;
+                e[s] = beta;
+                d[s + 1] = a00 - 2.0 * scal[4];
+            }
+        }
+        __syncthreads();
+        double nx2 = 0.0;
+        {
+            const double beta = scal[0], tk = scal[1], sc = scal[2], h = scal[3], w0 = scal[4];
+            const double f = tk * sc;
+            for (int j = threadIdx.x; j < m; j += SYM_NT) {
+                const double a = vps[j], a0 = wps[j];
+                const double v = (j == 0) ? 1.0 : sc * x[j];
+                const double w = f * (a - beta * a0) - h * v;
+                vps[j] = v;
+                wps[j] = w;
+                if (j >= 1) {
+                    const double xv = a0 - w - w0 * v;
+                    xn[j - 1] = xv;
+                    if (j >= 2) nx2 = fma(xv, xv, nx2);
+                }
+                if (lead) V[(size_t)s * n + b + j] = v;
+            }
+            if (lead)
+                for (int j = threadIdx.x; j <= s; j += SYM_NT) V[(size_t)s * n + j] = 0.0;
+            // clear this block's slice of the ax buffer of column s + 2
+            const int per = (m + G - 1) / G;
+            double* ax2 = axbuf(s + 2);
+            for (int j = blockIdx.x * per + threadIdx.x; j < min(m, (blockIdx.x + 1) * per); j += SYM_NT) ax2[j] = 0.0;
+        }
+        double tn, dummy;
+        block_sum2(nx2, 0.0, tn, dummy);
+        if (threadIdx.x == 0) scal[9] = tn;   // |x'[1:]|^2 of the next column
+        __syncthreads();
+        pend = true;
+        cur ^= 1;
+    }
+    if (lead && threadIdx.x == 0) {
+        // rows n-2 and n-1: the last pivot row is e[n-2]; the last diagonal still lacks the
+        // update of column n-3 (v, w of length 2 in vps, wps)
+        e[n - 2] = xb[cur][0];
+        d[n - 1] = A[(size_t)(n - 1) * lda + n - 1] - 2.0 * vps[1] * wps[1];
+        tau[n - 2] = 0.0;
+        tau[n - 1] = 0.0;
+        e[n - 1] = 0.0;
+    }
+    if (lead)
+        for (int i = threadIdx.x; i < 2 * n; i += SYM_NT) V[(size_t)(n - 2) * n + i] = 0.0;
+}
+
+static size_t sytrd_sym_smem(int n) {
+    return (4 * (size_t)n + 32) * sizeof(double) + ((size_t)n / 32 + 2) * sizeof(int);
+}
+
+static void sytrd_sym_launch(cudaStream_t st, int n, double* A, int lda, double* V, double* tau, double* d, double* e,
+                             double* ws) {
+    int dev = 0, nsm = 0, maxblk = 0;
+    XG_CUDA(cudaGetDevice(&dev));
+    XG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    const size_t smem = sytrd_sym_smem(n);
+    allow_max_dynamic_smem((const void*)k_sytrd_sym);
+    XG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxblk, k_sytrd_sym, SYM_NT, smem));
+    if (maxblk < 1) throw CudaError("sytrd: kernel does not fit on an SM");
+    const int blocks = std::min(nsm, SYTRD_SLOTS);
+    void* args[] = {&n, &A, &lda, &V, &tau, &d, &e, &ws};
+    XG_CUDA(cudaLaunchCooperativeKernel((void*)k_sytrd_sym, blocks, SYM_NT, args, smem, st));
+    ++launch_counter();
+}
+
 void sytrd(cudaStream_t st, int n, double* A, int lda, double* V, double* tau, double* d, double* e, double* p) {
+    sytrd_form(st, n, A, lda, V, tau, d, e, p, -1);
+}
+
+void sytrd_form(cudaStream_t st, int n, double* A, int lda, double* V, double* tau, double* d, double* e, double* p,
+                int form) {
     const size_t smem = (size_t)(4 * n + 72) * sizeof(double);
     if (n <= 2) {
         // trivial: copy diagonal / off-diagonal
         k_sytrd<256><<<1, 256, smem, st>>>(n, A, lda, V, tau, d, e, p);
         XG_LAUNCH_CHECK();
+        return;
+    }
+    // the upper-triangle form (its three A x buffers live after the row form's 2n + 2 SYTRD_SLOTS
+    // doubles of p)
+    const bool sym_fits = n >= 3 && sytrd_sym_smem(n) <= 220 * 1024;
+    if (form < 0) form = n >= tuned_sytrd_sym_min() ? 1 : 0;
+    if (form == 1 && sym_fits) {
+        sytrd_sym_launch(st, n, A, lda, V, tau, d, e, p + 2 * (size_t)n + 2 * SYTRD_SLOTS);
         return;
     }
     // More warps per block only for the largest matrices (measured: 1024 threads gain 7% at

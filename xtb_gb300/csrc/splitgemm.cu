@@ -13,10 +13,13 @@
 //
 // The products run as mma.sync.m16n8k16 (BF16 in, FP32 accumulate) from shared memory;
 // S(S+1)/2 tensor-core products replace one FP64 product.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 
 #include <algorithm>
 #include <cstdint>
+#include <mutex>
 
 #include "linalg.h"
 #include "splitgemm.h"
@@ -255,6 +258,303 @@ __global__ void __launch_bounds__(256) k_split_mma(int M, int N, int Kp, const _
             }
 }
 
+// ------------------------------------------------------------------ tcgen05 form
+// The same digit products on the 5th-generation tensor cores: tcgen05.mma (M = 128, N = 64,
+// K = 16, BF16 in, FP32 accumulate) with the accumulators in tensor memory (TMEM) and the digit
+// planes staged by TMA (cp.async.bulk.tensor, one 3-D box = all S planes of a 32-long K slice,
+// 64-byte swizzle) through a TC_STAGES-deep mbarrier pipeline.  Warp roles: warp 0 issues the
+// TMA loads, one thread of warp 1 issues the MMAs (warp 1 also owns the TMEM allocation),
+// warps 2..5 run the epilogue, one TMEM lane (= one output row) per thread.
+//
+// Exactness: digits are integers with |d| <= 256 (first) and <= 128 (later), so over a K chunk
+// of 256 the level-0 sum (at most 256 * 2^16) and the level-1 sum (at most 2 * 256 * 2^15)
+// are integers of at most 2^24 -- exact in FP32.  These two levels are reset every chunk and
+// folded by the epilogue into 64-bit integer accumulators (F2I and integer adds, no FP64
+// work: the FP64 pipe would otherwise bound the product), while the TMEM holds the next chunk's
+// sums (two buffers).  Levels 2 .. S-1 carry at most 2^-16 of the result; they accumulate over
+// the whole K in FP32 (rounding below 2^-40 of the result) and are added once at the end.
+constexpr int TC_BM = 128, TC_BN = 64, TC_BK = 32, TC_KC = 256;
+constexpr int TC_THREADS = 192;
+constexpr unsigned TC_SPIN = 1u << 25;   // iteration limit of every mbarrier wait
+
+template <int S>
+struct TcCfg {
+    static constexpr int A_BYTES = S * TC_BM * TC_BK * 2;   // one stage of A: [S][128][32] bf16
+    static constexpr int B_BYTES = S * TC_BN * TC_BK * 2;   // one stage of B: [S][64][32] bf16
+    static constexpr int STAGE = A_BYTES + B_BYTES;         // a multiple of 1024
+    static constexpr int STAGES = (3 * STAGE <= 200 * 1024) ? 3 : 2;
+    static constexpr int NB = (4 + (S - 2)) * TC_BN <= 512 ? 2 : 1;   // level-0/1 buffers in TMEM
+    static constexpr int SMEM = STAGES * STAGE + 1024 /* alignment */ + 256 /* barriers */;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// wait for the phase `parity` of an mbarrier; false after TC_SPIN polls or when another role
+// raised the abort flag
+__device__ __forceinline__ bool tc_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag) {
+    for (unsigned it = 0; it < TC_SPIN; ++it) {
+        uint32_t ok;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(ok)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (ok) return true;
+        if ((it & 255u) == 255u && *abort_flag) return false;
+    }
+    return false;
+}
+
+// K-major operand in shared memory, 64-byte swizzle: rows of 64 bytes (32 bf16), groups of 8
+// rows 512 bytes apart (SBO); the leading offset is unused for this layout
+__device__ __forceinline__ uint64_t tc_desc(uint32_t saddr) {
+    uint64_t d = (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)1 << 16;             // LBO (ignored)
+    d |= (uint64_t)(512 >> 4) << 32;    // SBO
+    d |= (uint64_t)1 << 46;             // descriptor version of this architecture
+    d |= (uint64_t)4 << 61;             // SWIZZLE_64B
+    return d;
+}
+
+// instruction descriptor, kind::f16: FP32 accumulator, BF16 A and B, both K-major, M x N
+__host__ __device__ constexpr uint32_t tc_idesc(int M, int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, float* v) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+    for (int k = 0; k < 16; ++k) v[k] = __uint_as_float(r[k]);
+}
+
+template <int S>
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    k_split_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int M, int N,
+               int Kp, const double* __restrict__ sA, const double* __restrict__ sB, double alpha, double beta,
+               double* __restrict__ C, int ldc, const int* __restrict__ dN, int kchunk, double* __restrict__ P,
+               int* __restrict__ err) {
+    using Cfg = TcCfg<S>;
+    extern __shared__ unsigned char tc_raw[];
+    unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(tc_raw) + 1023) & ~uintptr_t(1023));
+    uint64_t* bars = reinterpret_cast<uint64_t*>(base + Cfg::STAGES * Cfg::STAGE);
+    uint64_t* full = bars;                        // [STAGES]: TMA landed
+    uint64_t* empty = bars + Cfg::STAGES;         // [STAGES]: MMAs done reading
+    uint64_t* cfull = bars + 2 * Cfg::STAGES;     // [NB]: a chunk's level-0/1 sums complete
+    uint64_t* cempty = cfull + 2;                 // [NB]: the epilogue has read them
+    uint64_t* done = cempty + 2;                  // every MMA complete
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+    int* abort_flag = reinterpret_cast<int*>(tmem_slot + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int i0 = blockIdx.y * TC_BM, j0 = blockIdx.x * TC_BN;
+    const int Nl = dN ? min(N, *dN) : N;
+    if (j0 >= Nl) return;
+    const int kb = P ? (int)blockIdx.z * kchunk : 0;
+    const int ke = P ? min(Kp, kb + kchunk) : Kp;
+    const int nstage = (ke - kb) / TC_BK;
+    const int nchunk = (ke - kb + TC_KC - 1) / TC_KC;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < Cfg::STAGES; ++s) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&full[s])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&empty[s])));
+        }
+        for (int b = 0; b < 2; ++b) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&cfull[b])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 4;\n" ::"r"(smem_u32(&cempty[b])));
+        }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(done)));
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;\n" ::"r"(smem_u32(tmem_slot)));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+    volatile int* abort_v = abort_flag;
+
+    if (warp == 0) {
+        // ---- TMA producer
+        if (lane == 0) {
+            int issued = 0;
+            for (int ks = 0; ks < nstage; ++ks) {
+                const int s = ks % Cfg::STAGES;
+                if (ks >= Cfg::STAGES && !tc_wait(smem_u32(&empty[s]), ((ks / Cfg::STAGES) - 1) & 1, abort_v)) {
+                    *abort_v = 1;
+                    break;
+                }
+                unsigned char* sa = base + s * Cfg::STAGE;
+                unsigned char* sb = sa + Cfg::A_BYTES;
+                const uint32_t fb = smem_u32(&full[s]);
+                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(fb), "r"(Cfg::STAGE)
+                             : "memory");
+                const int kx = kb + ks * TC_BK;
+                asm volatile(
+                    "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, "
+                    "%3, %4}], [%5];\n" ::"r"(smem_u32(sa)),
+                    "l"(reinterpret_cast<uint64_t>(&tmA)), "r"(kx), "r"(i0), "r"(0), "r"(fb)
+                    : "memory");
+                asm volatile(
+                    "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, "
+                    "%3, %4}], [%5];\n" ::"r"(smem_u32(sb)),
+                    "l"(reinterpret_cast<uint64_t>(&tmB)), "r"(kx), "r"(j0), "r"(0), "r"(fb)
+                    : "memory");
+                ++issued;
+            }
+            // on an abort, the copies in flight still land: wait for them (bounded) before leaving
+            if (*abort_v)
+                for (int ks = max(0, issued - Cfg::STAGES); ks < issued; ++ks) {
+                    volatile int never = 0;
+                    tc_wait(smem_u32(&full[ks % Cfg::STAGES]), (ks / Cfg::STAGES) & 1, &never);
+                }
+        }
+    } else if (warp == 1) {
+        // ---- MMA issuer
+        if (lane == 0) {
+            constexpr uint32_t idesc = tc_idesc(TC_BM, TC_BN);
+            const uint32_t low0 = tmem + Cfg::NB * 2 * TC_BN;   // levels 2.. S-1
+            for (int ks = 0; ks < nstage; ++ks) {
+                const int s = ks % Cfg::STAGES;
+                const int c = (ks * TC_BK) / TC_KC, buf = c % Cfg::NB;
+                const bool cfirst = (ks * TC_BK) % TC_KC == 0;
+                const bool clast = ((ks + 1) * TC_BK) % TC_KC == 0 || ks + 1 == nstage;
+                if (cfirst && c >= Cfg::NB && !tc_wait(smem_u32(&cempty[buf]), ((c / Cfg::NB) - 1) & 1, abort_v)) {
+                    *abort_v = 1;
+                    break;
+                }
+                if (!tc_wait(smem_u32(&full[s]), (ks / Cfg::STAGES) & 1, abort_v)) {
+                    *abort_v = 1;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                const uint32_t sa = smem_u32(base + s * Cfg::STAGE);
+                const uint32_t sb = sa + Cfg::A_BYTES;
+#pragma unroll
+                for (int kk = 0; kk < TC_BK / 16; ++kk) {
+                    uint32_t started = 0;   // bit l: level l has had its first product of this k-step
+#pragma unroll
+                    for (int p = 0; p < S; ++p)
+#pragma unroll
+                        for (int q = 0; q < S - p; ++q) {
+                            const int l = p + q;
+                            const uint32_t d = l <= 1 ? tmem + buf * 2 * TC_BN + l * TC_BN : low0 + (l - 2) * TC_BN;
+                            // the first product of a level overwrites: levels 0/1 at the start of
+                            // their chunk, levels >= 2 at the very start
+                            const bool fresh = !(started >> l & 1u) && kk == 0 && (l <= 1 ? cfirst : ks == 0);
+                            started |= 1u << l;
+                            const uint64_t ad = tc_desc(sa + p * (TC_BM * TC_BK * 2) + kk * 32);
+                            const uint64_t bd = tc_desc(sb + q * (TC_BN * TC_BK * 2) + kk * 32);
+                            const uint32_t acc = fresh ? 0u : 1u;
+                            asm volatile(
+                                "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                                " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+                                "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+                        }
+                }
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                                 smem_u32(&empty[s]))
+                             : "memory");
+                if (clast)
+                    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                                     smem_u32(&cfull[buf]))
+                                 : "memory");
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                             smem_u32(done))
+                         : "memory");
+            if (*abort_v) {   // the MMAs issued so far must finish before the TMEM is freed
+                volatile int never = 0;
+                tc_wait(smem_u32(done), 0, &never);
+            }
+        }
+    } else {
+        // ---- epilogue: TMEM lane (32 (warp % 4) + lane) = output row
+        const int quarter = warp & 3;
+        const uint32_t lrow = (uint32_t)(32 * quarter) << 16;
+        const int i = i0 + 32 * quarter + lane;
+        long long ex[TC_BN];
+#pragma unroll
+        for (int j = 0; j < TC_BN; ++j) ex[j] = 0;
+        bool ok = true;
+        for (int c = 0; c < nchunk && ok; ++c) {
+            const int buf = c % Cfg::NB;
+            if (!tc_wait(smem_u32(&cfull[buf]), (c / Cfg::NB) & 1, abort_v)) {
+                *abort_v = 1;
+                ok = false;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+#pragma unroll
+            for (int cb = 0; cb < TC_BN / 16; ++cb) {
+                float l0[16], l1[16];
+                tc_ld16(tmem + lrow + buf * 2 * TC_BN + cb * 16, l0);
+                tc_ld16(tmem + lrow + buf * 2 * TC_BN + TC_BN + cb * 16, l1);
+#pragma unroll
+                for (int k = 0; k < 16; ++k)
+                    ex[cb * 16 + k] += 256LL * (long long)__float2int_rn(l0[k]) + (long long)__float2int_rn(l1[k]);
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+            __syncwarp();
+            if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(&cempty[buf])) : "memory");
+        }
+        if (ok && !tc_wait(smem_u32(done), 0, abort_v)) {
+            *abort_v = 1;
+            ok = false;
+        }
+        if (ok) {
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            const uint32_t low0 = tmem + lrow + Cfg::NB * 2 * TC_BN;
+            const double ra = (i < M) ? alpha * sA[i] : 0.0;
+#pragma unroll
+            for (int cb = 0; cb < TC_BN / 16; ++cb) {
+                double lo[16];
+#pragma unroll
+                for (int k = 0; k < 16; ++k) lo[k] = 0.0;
+#pragma unroll
+                for (int l = S - 1; l >= 2; --l) {
+                    float v[16];
+                    tc_ld16(low0 + (l - 2) * TC_BN + cb * 16, v);
+#pragma unroll
+                    for (int k = 0; k < 16; ++k) lo[k] = lo[k] * 0x1p-8 + (double)v[k];
+                }
+#pragma unroll
+                for (int k = 0; k < 16; ++k) {
+                    const int j = j0 + cb * 16 + k;
+                    if (i >= M || j >= Nl) continue;
+                    // sum of levels in units of level 0: exact part / 256 + lower levels / 65536
+                    const double sum = (double)ex[cb * 16 + k] * 0x1p-8 + lo[k] * 0x1p-16;
+                    double r = ra * sB[j] * (sum * 0x1p-16);
+                    if (P) {
+                        P[((size_t)blockIdx.z * M + i) * N + j] = r;
+                        continue;
+                    }
+                    if (beta != 0.0) r += beta * C[(size_t)i * ldc + j];
+                    C[(size_t)i * ldc + j] = r;
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    if (threadIdx.x == 0 && *abort_v) atomicExch(err, 1);
+    if (warp == 1) {
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;\n" ::"r"(tmem));
+    }
+}
+
 }  // namespace
 
 // Split K for products with few output tiles (the skinny products of the blocked
@@ -262,14 +562,45 @@ __global__ void __launch_bounds__(256) k_split_mma(int M, int N, int Kp, const _
 // SMs idle.  Partials need at most SG_KS x min(M N, SG_SPLIT_ELEMS) doubles.
 constexpr int SG_KS = 8;
 constexpr long SG_SPLIT_TILES = 304;
-constexpr size_t SG_SPLIT_ELEMS = (size_t)SG_SPLIT_TILES * SG_BM * SG_BN;
+constexpr size_t SG_SPLIT_ELEMS = (size_t)SG_SPLIT_TILES * TC_BM * TC_BN;
 
 static int split_k_slices(int M, int N, int Kp) {
-    const long tiles = (long)((M + SG_BM - 1) / SG_BM) * ((N + SG_BN - 1) / SG_BN);
+    const long tiles = (long)((M + TC_BM - 1) / TC_BM) * ((N + TC_BN - 1) / TC_BN);
     if (tiles >= SG_SPLIT_TILES) return 1;
-    const int by_chunks = Kp / (2 * SG_KC);   // at least two exact chunks per slice
-    const int want = (int)std::min<long>(SG_KS, std::max<long>(1, (2 * SG_SPLIT_TILES / 2) / tiles));
+    const int by_chunks = Kp / (2 * TC_KC);   // at least two exact chunks per slice
+    const int want = (int)std::min<long>(SG_KS, std::max<long>(1, SG_SPLIT_TILES / tiles));
     return std::max(1, std::min(want, by_chunks));
+}
+
+// cuTensorMapEncodeTiled from the driver (through the runtime, so nothing links libcuda)
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    });
+    if (!fn) throw CudaError("split_gemm: cuTensorMapEncodeTiled is not available");
+    return fn;
+}
+
+// 3-D map of S digit planes [S][rows][Kp] (bf16), boxes of 32 (K) x box_rows x S, 64-byte swizzle
+static CUtensorMap plane_map(const __nv_bfloat16* planes, int rows, int Kp, int S, int box_rows) {
+    CUtensorMap m;
+    const cuuint64_t dims[3] = {(cuuint64_t)Kp, (cuuint64_t)rows, (cuuint64_t)S};
+    const cuuint64_t strides[2] = {(cuuint64_t)Kp * 2, (cuuint64_t)rows * (cuuint64_t)Kp * 2};
+    const cuuint32_t box[3] = {(cuuint32_t)TC_BK, (cuuint32_t)box_rows, (cuuint32_t)S};
+    const cuuint32_t es[3] = {1, 1, 1};
+    const CUresult r = tensor_map_encoder()(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3,
+                                            const_cast<__nv_bfloat16*>(planes), dims, strides, box, es,
+                                            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+                                            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) throw CudaError("split_gemm: tensor map encoding failed");
+    return m;
 }
 
 // C[i][j] = sum_z P[z][i][j] (in slice order) + beta C[i][j], j < N (and < *dN)
@@ -289,7 +620,12 @@ size_t split_gemm_workspace(int M, int N, int K, int slices) {
     const size_t Kp = (size_t)((K + SG_KT - 1) / SG_KT) * SG_KT;
     const size_t bf = (size_t)slices * ((size_t)M + N) * Kp * sizeof(__nv_bfloat16);
     const size_t split = (size_t)SG_KS * std::min((size_t)M * N, SG_SPLIT_ELEMS);
-    return (bf + 255) / 256 * 256 + 2 * ((size_t)M + N) * sizeof(double) + split * sizeof(double) + 512;
+    return (bf + 255) / 256 * 256 + 2 * ((size_t)M + N) * sizeof(double) + split * sizeof(double) + 768;
+}
+
+// the tensor-core kernel's error flag: the last word of the workspace
+static int* split_error_flag(void* work, int M, int N, int K, int slices) {
+    return reinterpret_cast<int*>(static_cast<char*>(work) + split_gemm_workspace(M, N, K, slices) - sizeof(int));
 }
 
 // Digits and scales of the rows of op(X) (R rows, K long): along memory rows when !trans,
@@ -323,23 +659,28 @@ static void split_gemm_s(cudaStream_t st, bool ta, bool tb, int M, int N, int K,
     unsigned long long* mB = mA + M;
     split_operand<S>(st, M, K, Kp, A, lda, ta, dK, As, sA, mA);
     split_operand<S>(st, N, K, Kp, B, ldb, !tb, dK, Bs, sB, mB);
-    const size_t smem = (size_t)2 * S * SG_BM * SG_LD * sizeof(__nv_bfloat16);
-    if (smem > 48 * 1024) allow_max_dynamic_smem((const void*)k_split_mma<S>);
+    const CUtensorMap tmA = plane_map(As, M, Kp, S, TC_BM);
+    const CUtensorMap tmB = plane_map(Bs, N, Kp, S, TC_BN);
+    int* err = split_error_flag(work, M, N, K, S);
+    const int smem = TcCfg<S>::SMEM;
+    allow_max_dynamic_smem((const void*)k_split_tc<S>);
     const int ks = split_k_slices(M, N, Kp);
     if (ks > 1) {
-        const int kchunk = ((Kp / ks + SG_KC - 1) / SG_KC) * SG_KC;
+        const int kchunk = ((Kp / ks + TC_KC - 1) / TC_KC) * TC_KC;
         const int kz = (Kp + kchunk - 1) / kchunk;
         double* P = reinterpret_cast<double*>(
             (reinterpret_cast<uintptr_t>(mB + N) + 255) / 256 * 256);   // after the scales and maxima
-        dim3 grid(ceil_div(N, SG_BN), ceil_div(M, SG_BM), kz);
-        k_split_mma<S><<<grid, 256, smem, st>>>(M, N, Kp, As, Bs, sA, sB, alpha, beta, C, ldc, dN, kchunk, P);
+        dim3 grid(ceil_div(N, TC_BN), ceil_div(M, TC_BM), kz);
+        k_split_tc<S><<<grid, TC_THREADS, smem, st>>>(tmA, tmB, M, N, Kp, sA, sB, alpha, beta, C, ldc, dN, kchunk,
+                                                      P, err);
         XG_LAUNCH_CHECK();
         k_split_reduce<<<ceil_div((long)M * N, 256), 256, 0, st>>>(M, N, kz, P, beta, C, ldc, dN);
         XG_LAUNCH_CHECK();
         return;
     }
-    dim3 grid(ceil_div(N, SG_BN), ceil_div(M, SG_BM));
-    k_split_mma<S><<<grid, 256, smem, st>>>(M, N, Kp, As, Bs, sA, sB, alpha, beta, C, ldc, dN, Kp, nullptr);
+    dim3 grid(ceil_div(N, TC_BN), ceil_div(M, TC_BM));
+    k_split_tc<S><<<grid, TC_THREADS, smem, st>>>(tmA, tmB, M, N, Kp, sA, sB, alpha, beta, C, ldc, dN, Kp, nullptr,
+                                                  err);
     XG_LAUNCH_CHECK();
 }
 
@@ -417,6 +758,8 @@ void split_gemm_check(int M, int N, int K, int slices, unsigned seed, int exp_ra
     k_abs<<<ceil_div((long)na, 256), 256, 0, st>>>(na, A, Aa);
     k_abs<<<ceil_div((long)nb, 256), 256, 0, st>>>(nb, B, Ba);
     XG_LAUNCH_CHECK();
+    int* err = split_error_flag(work, M, N, K, slices);
+    XG_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
     dgemm(st, false, false, M, N, K, 1.0, Aa, K, Ba, N, 0.0, Cb, N);
     cudaEvent_t e0, e1, e2;
     XG_CUDA(cudaEventCreate(&e0));
@@ -432,8 +775,16 @@ void split_gemm_check(int M, int N, int K, int slices, unsigned seed, int exp_ra
     k_errmax<<<1, 256, 0, st>>>(nc, Cs, Cr, Cb, res);
     XG_LAUNCH_CHECK();
     double h[2];
+    int herr = 0;
     XG_CUDA(cudaMemcpyAsync(h, res, sizeof(h), cudaMemcpyDeviceToHost, st));
+    XG_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st));
     XG_CUDA(cudaStreamSynchronize(st));
+    if (herr) {
+        cudaFreeAsync(buf, st);
+        cudaStreamSynchronize(st);
+        cudaStreamDestroy(st);
+        throw CudaError("split_gemm: a pipeline wait of the tensor-core kernel timed out");
+    }
     float ms_s = 0.0f, ms_d = 0.0f;
     XG_CUDA(cudaEventElapsedTime(&ms_s, e0, e1));
     XG_CUDA(cudaEventElapsedTime(&ms_d, e1, e2));

@@ -1,0 +1,39 @@
+// Per-device choices between kernel forms, measured by the engine's own autotuner.
+//
+// Two decisions of the single point depend on the matrix size and on the device: which
+// tridiagonalisation runs (the row-by-row cooperative form, whose per-column vector work is
+// cheap for small matrices, or the upper-triangle form with 4/3 n^3 flops), and from which size
+// the back-transformation of the eigenvectors runs as compact-WY GEMMs instead of one warp per
+// vector (separately for FP64 and split-precision products).  Until `autotune` has run on a
+// device the defaults below (measured once on GB300) apply; afterwards the engine uses the
+// device's measured crossovers.
+#pragma once
+#include <vector>
+
+namespace xg {
+
+struct Tuned {
+    int sytrd_sym_min = 1 << 30;    // AOs from which the upper-triangle tridiagonalisation runs
+                                    // (never by default: on GB300 the row form measured faster up
+                                    // to 1024 AOs, its per-column latency being lower)
+    int blocked_min_fp64 = 1500;    // AOs from which the compact-WY back-transformation runs
+    int blocked_min_split = 1000;   // the same with split-precision products
+    int level = 0;                  // 0: defaults, 1: measured on this device
+    double seconds = 0.0;           // time the measurement took
+    // measurements: (n, row form ms, upper-triangle form ms) and
+    // (n, warp form ms, blocked FP64 ms, blocked split ms)
+    std::vector<double> sytrd_rows, backtr_rows;
+};
+
+// the current device's choices
+Tuned tuned();
+// measure the crossovers on the current device (once; later calls return the kept choices)
+Tuned autotune();
+// replace the current device's choices (level 1; for tests that pin a form)
+void set_tuned(int sytrd_sym_min, int blocked_min_fp64, int blocked_min_split);
+// back-transformation threshold for a precision (0 FP64, 1 split)
+int tuned_blocked_min(int precision);
+// tridiagonalisation threshold
+int tuned_sytrd_sym_min();
+
+}  // namespace xg
