@@ -60,6 +60,24 @@ extern void xtbgb_setBlockedBacktransform(xtb_TEnvironment env, xtb_TCalculator 
  * no device is present. */
 extern double xtbgb_fp64PeakTflops(void);
 
+/* Restart file of the reference (xtbrestart, src/restart.f90): a Fortran unformatted
+ * sequential file holding the shell charges and, for GFN2, the atomic dipole and quadrupole
+ * moments of the last single point on `res`.  xtbgb_writeRestart writes it (0 on error, reported
+ * on env).  xtbgb_readRestart loads it into `res`, so that the next xtb_singlepoint on `res`
+ * starts from it (the reference's warm start); it returns 1 when the file matched the molecule,
+ * 0 otherwise, with the reference's warnings on env (a missing file is silently 0). */
+extern int xtbgb_writeRestart(xtb_TEnvironment env, xtb_TMolecule mol, xtb_TResults res, const char* filename);
+extern int xtbgb_readRestart(xtb_TEnvironment env, xtb_TMolecule mol, xtb_TResults res, const char* filename);
+
+/* External point charges with explicit hardness values (bohr, e; hardness in Eh).  The
+ * reference's C API (xtb_setExternalCharges) takes each charge's hardness from an element
+ * number; its Fortran calculator also accepts the hardness directly (calc%pcem%gam, used with
+ * 999 for bare point charges in test/unit/test_gfn2.f90:500-520), which this call exposes.
+ * Replaces earlier external charges on the calculator; errors as xtb_setExternalCharges. */
+extern void xtbgb_setExternalChargesHardness(xtb_TEnvironment env, xtb_TCalculator calc, int n,
+                                             const double* charges, const double* positions,
+                                             const double* hardness);
+
 /* Autotuner (no counterpart in the reference).  Two choices of the single point depend on the
  * matrix size and the device: the form of the tridiagonalisation (row by row, or the
  * upper-triangle form with 4/3 n^3 flops) and the form of the eigenvector back-transformation

@@ -864,11 +864,40 @@ class Result:
     pass
 
 
+def pc_potential(basis, xyz, pc_q, pc_xyz, pc_gam):
+    """Shell potential of external point charges, jpot_pcem_gfn2 (src/embedding.f90:225-256):
+    V_sh = sum_k q_k / sqrt(r^2 + 1/x^2), x = (eta_sh + gam_k) / 2."""
+    P = get_params()
+    eta = P.shellHardnessSh[basis.sh_ish, basis.Z[basis.sh_atom] - 1]
+    d = xyz[basis.sh_atom][:, None, :] - pc_xyz[None, :, :]
+    r2 = np.sum(d * d, axis=2)
+    x = 0.5 * (eta[:, None] + pc_gam[None, :])
+    return np.sum(pc_q[None, :] / np.sqrt(r2 + 1.0 / x ** 2), axis=1)
+
+
+def pc_gradient(basis, xyz, qsh, pc_q, pc_xyz, pc_gam):
+    """pcem_grad_gfn2 (src/embedding.f90:329-365): gradient on the atoms and on the charges."""
+    P = get_params()
+    eta = P.shellHardnessSh[basis.sh_ish, basis.Z[basis.sh_atom] - 1]
+    dr = xyz[basis.sh_atom][:, None, :] - pc_xyz[None, :, :]          # [shell, pc, 3]
+    r2 = np.sum(dr * dr, axis=2)
+    rr = 1.0 / (0.5 * (eta[:, None] + pc_gam[None, :])) ** 2
+    yy = qsh[:, None] * pc_q[None, :] * (r2 + rr) ** -1.5
+    g = np.zeros((basis.nat, 3))
+    np.add.at(g, basis.sh_atom, -np.sum(dr * yy[..., None], axis=1))
+    gpc = np.sum(dr * yy[..., None], axis=0)
+    return g, gpc
+
+
 def singlepoint(Z, xyz, charge=0.0, uhf=0, etemp=300.0, accuracy=1.0, maxiter=250,
-                guess="eeq", q_init=None, qsh_init=None, dipm_init=None, qp_init=None, verbose=False):
+                guess="eeq", q_init=None, qsh_init=None, dipm_init=None, qp_init=None, verbose=False,
+                pc_charges=None, pc_positions=None, pc_gam=None):
     """GFN2-xTB energy, charges and gradient for a molecule (Bohr in, Eh and Eh/bohr out).
 
-    Follows scf, src/scf_module.F90:74-920, and scc, src/scc_core.f90:255-640.
+    Follows scf, src/scf_module.F90:74-920, and scc, src/scc_core.f90:255-640.  External point
+    charges (pc_charges[k], pc_positions[k, 3] in Bohr, pc_gam[k] hardness) add the shell
+    potential of jpot_pcem_gfn2 to every iteration's shift (src/scc_core.f90:438), their energy
+    (electro_pcem, src/embedding.f90:261-280) and gradient (src/embedding.f90:329-365).
     """
     Z = np.asarray(Z, dtype=np.int64)
     xyz = np.asarray(xyz, dtype=np.float64).reshape(-1, 3)
@@ -918,6 +947,14 @@ def singlepoint(Z, xyz, charge=0.0, uhf=0, etemp=300.0, accuracy=1.0, maxiter=25
     gab3, gab5 = aes_gab(xyz, radcn)
     J = coulomb_matrix(basis, xyz)
     gam3 = Pr.thirdOrderShell[basis.sh_ish, Z[basis.sh_atom] - 1]
+    pcem = pc_charges is not None and len(pc_charges) > 0
+    if pcem:
+        pc_q = np.asarray(pc_charges, dtype=float)
+        pc_x = np.asarray(pc_positions, dtype=float).reshape(-1, 3)
+        pc_g = np.asarray(pc_gam, dtype=float)
+        vpc = pc_potential(basis, xyz, pc_q, pc_x, pc_g)
+    else:
+        vpc = np.zeros(nsh)
 
     # SCC, src/scc_core.f90:406-640
     U = sla.cholesky(S, lower=False)
@@ -933,7 +970,7 @@ def singlepoint(Z, xyz, charge=0.0, uhf=0, etemp=300.0, accuracy=1.0, maxiter=25
     iters = 0
     for it in range(1, maxiter + 1):
         iters = it
-        shift = J @ qsh + gam3 * qsh ** 2
+        shift = vpc + J @ qsh + gam3 * qsh ** 2
         vs, vd, vq = setvsdq(Z, xyz, q, dipm, qp, gab3, gab5, shifted=True)
         atshift = scd4.potential(q)
         shift = shift + atshift[basis.sh_atom]
@@ -976,6 +1013,8 @@ def singlepoint(Z, xyz, charge=0.0, uhf=0, etemp=300.0, accuracy=1.0, maxiter=25
         eel += eaes + epol
         ed = scd4.energy(q)
         eel += ed
+        epcem = float(qsh @ vpc)
+        eel += epcem
         eel += ga + gb
         econv = abs(eel - eold) < scfconv
         dq = np.concatenate([qsh, dipm.ravel(), qp.ravel()]) - q_in
@@ -1008,6 +1047,10 @@ def singlepoint(Z, xyz, charge=0.0, uhf=0, etemp=300.0, accuracy=1.0, maxiter=25
     e2, embd, gd4 = d4_gradient(d4m, Z, xyz, q)
     grad += gd4
     grad += coulomb_grad(basis, xyz, qsh)
+    pcgrad = None
+    if pcem:
+        gpc_atoms, pcgrad = pc_gradient(basis, xyz, qsh, pc_q, pc_x, pc_g)
+        grad += gpc_atoms
 
     # dipole moment (calc_dipole, src/dipole.f90:94-128) and Wiberg-Mayer bond orders
     # (get_wiberg, src/scc_core.f90:1208-1245) from the last density
@@ -1038,6 +1081,7 @@ def singlepoint(Z, xyz, charge=0.0, uhf=0, etemp=300.0, accuracy=1.0, maxiter=25
     r.e_axc = epol
     r.e_disp = ed + embd
     r.gradient = grad
+    r.pcgrad = pcgrad
     r.gnorm = np.sqrt(np.sum(grad ** 2))
     r.q = q
     r.qsh = qsh

@@ -7,7 +7,12 @@ values the reference asserts, with the tolerance it asserts them at:
 * ``scc``   test_gfn2.f90:48-170   water, zero-charge guess, energy parts, charges, multipoles
 * ``api``   test_gfn2.f90:172-235  propyne C3H4, EEQ guess, energy, gap, gradient
 * ``pcem``  test_gfn2.f90:383-457  (H2O)4 cluster without point charges, energy, gap, gradient
+* ``pcem_charges``, ``pcem_point``  test_gfn2.f90:459-520  (H2O)2 in the field of the other two
+            waters as six external charges, with GFN2 hardnesses and with gamma = 999 (bare point
+            charges): energy, gap, gradient, point-charge gradient
 * ``capi``  c_api_example.c:38-112 propyne through the C ABI: energy, q[5], dipole, wbo
+* ``capi_pc`` c_api_example.c:298-410 the same dimer through xtb_setExternalCharges: energy,
+            gradient and point-charge gradient
 
 Usage: python tests/golden/make_golden.py [reference_root]
 """
@@ -76,6 +81,22 @@ def main():
         maxiter = int(re.search(r"maxiter\s*=\s*(\d+)", blk).group(1))
         cases[key] = {"numbers": at, "positions": xyz, "checks": cs, "maxiter": maxiter,
                       "guess": "zero" if key == "scc" else "eeq"}
+        if key == "pcem":
+            # the second half: molecule = first two waters, the other two as external charges
+            full = sub(src, name)
+            rest = full[full.index("! reset"):]
+            q = array(full, r"real\(wp\),parameter :: q\(nat2\)")
+            gam = array(full, r"real\(wp\),parameter :: gam\(nat2\)")
+            nat2 = len(at) // 2
+            parts = rest.split("! reset")
+            for pkey, part, g in (("pcem_charges", parts[1], gam), ("pcem_point", parts[2], [999.0] * nat2)):
+                pcs = []
+                for c in checks(part):
+                    c["thr"] = thr["thr"]
+                    pcs.append(c)
+                cases[pkey] = {"numbers": at[:nat2], "positions": xyz[:3 * nat2], "pc_charges": q,
+                               "pc_positions": xyz[3 * nat2:], "pc_gam": g, "checks": pcs,
+                               "maxiter": maxiter, "guess": "eeq"}
     capi = open(os.path.join(REF, "test/api/c_api_example.c")).read()
     first = capi[capi.index("testFirst"):capi.index("testSecond")]
     m = re.search(r"double const coord\[[^\]]*\]\s*=\s*\{(.*?)\};", first, re.S)
@@ -94,6 +115,25 @@ def main():
     hk.append({"expr": f"hess[{9 * natsq - 1}]", "value": fnum(m.group(1)), "thr": fnum(m.group(2))})
     cases["capi_hessian"] = {"numbers": at, "positions": coord, "checks": hk, "maxiter": 250, "guess": "eeq",
                              "step": 0.005}
+    # testSecond: the water dimer with six external charges through xtb_setExternalCharges
+    second = capi[capi.index("int testSecond"):]
+    second = second[:second.index("error:")]
+
+    def carr(name):
+        m = re.search(r"\b" + name + r"\[[^\]]*\]\s*=\s*\{(.*?)\};", second, re.S)
+        return [fnum(t) for t in re.findall(NUM, m.group(1))]
+
+    pck = []
+    for m in re.finditer(r"check\((\w+\[[^\]]+\]|\w+),\s*(" + NUM + r"),\s*(" + NUM + r")", second):
+        expr = m.group(1)
+        mi = re.fullmatch(r"(\w+)\[(\d+) \+ (\d+) \* 3\]", expr)
+        if mi:
+            expr = f"{mi.group(1)}[{int(mi.group(2)) + 3 * int(mi.group(3))}]"
+        pck.append({"expr": expr, "value": fnum(m.group(2)), "thr": fnum(m.group(3))})
+    cases["capi_pc"] = {"numbers": [int(v) for v in carr("attyp")], "positions": carr("coord"),
+                        "pc_charges": carr("pc"), "pc_positions": carr("pccoord"),
+                        "pc_numbers": [int(v) for v in carr("numbers")], "checks": pck, "maxiter": 250,
+                        "guess": "eeq"}
     # mindless01-10 (test_gfn2.f90:667-742, geometries from test/unit/molstock.f90): energy,
     # gradient norm and HOMO-LUMO gap at 1e-8 after a default single point from the EEQ guess
     blk = sub(src, "test_gfn2_mindless_basic")

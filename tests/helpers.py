@@ -44,6 +44,14 @@ def evaluate(expr, r):
         return r.emo[r.ihomo - 1]
     if expr == "wfn%focc(wfn%ihomo)":
         return r.focc[r.ihomo - 1]
+    if expr == "norm2(calc%pcem%grd)":
+        return float(np.linalg.norm(r.pcgrad))
+    m = re.fullmatch(r"calc%pcem%grd\((\d),(\d+)\)", expr)
+    if m:
+        return r.pcgrad[int(m.group(2)) - 1, int(m.group(1)) - 1]
+    m = re.fullmatch(r"(grad|pcgrad)\[(\d+)\]", expr)
+    if m:
+        return (r.gradient if m.group(1) == "grad" else r.pcgrad).ravel()[int(m.group(2))]
     m = re.fullmatch(r"(q|dipole)\[(\d+)\]", expr)
     if m:
         return getattr(r, m.group(1))[int(m.group(2))]

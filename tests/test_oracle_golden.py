@@ -71,3 +71,20 @@ def test_oracle_mindless_molecules():
         assert abs(r.energy - m["energy"]) <= m["thr"], m["name"]
         assert abs(np.linalg.norm(r.gradient) - m["gnorm"]) <= m["thr"], m["name"]
         assert abs(r.hl_gap - m["hl_gap"]) <= m["thr"], m["name"]
+
+
+@pytest.mark.parametrize("key", ["pcem_charges", "pcem_point", "capi_pc"])
+def test_oracle_external_point_charges(key):
+    """test_gfn2.f90:459-520 (water dimer in the field of six charges, GFN2 hardnesses and
+    gamma = 999) and c_api_example.c:298-410 (the same through xtb_setExternalCharges, which
+    takes each charge's hardness from its element): energy, gradient, point-charge gradient."""
+    from oracle.params import get_params
+    case = CASES[key]
+    Z, xyz = case_geometry(case)
+    gam = case.get("pc_gam") or [get_params().chemicalHardness[z - 1] for z in case["pc_numbers"]]
+    r = gfn2.singlepoint(Z, xyz, maxiter=case["maxiter"], pc_charges=case["pc_charges"],
+                         pc_positions=case["pc_positions"], pc_gam=gam)
+    assert r.converged
+    for c in case["checks"]:
+        got = evaluate(c["expr"], r)
+        assert abs(got - c["value"]) <= c["thr"], (c["expr"], got, c["value"], c["thr"])

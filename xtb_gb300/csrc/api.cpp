@@ -262,10 +262,67 @@ void xtb_setSolvent(xtb_TEnvironment env, xtb_TCalculator, char*, int*, double*,
     unsupported(env, "Implicit solvation", "xtb_api_setSolvent");
 }
 void xtb_releaseSolvent(xtb_TEnvironment, xtb_TCalculator) {}
-void xtb_setExternalCharges(xtb_TEnvironment env, xtb_TCalculator, int*, int*, double*, double*) {
-    unsupported(env, "External point charges", "xtb_api_setExternalCharges");
+namespace {
+// external point charges on a loaded calculator (setExternalCharges_api,
+// src/api/calculator.f90:482-537); gam null: the hardness of each charge's element
+void set_external_charges(xtb_TEnvironment env, xtb_TCalculator calc, int npc, const int* numbers,
+                          const double* charges, const double* positions, const double* gam, const char* src) {
+    if (npc <= 0) {
+        env->error("Negative number of point charges provided", src);
+        return;
+    }
+    if (!calc) {
+        env->error("Singlepoint calculator is not allocated", src);
+        return;
+    }
+    if (!calc->loaded) {
+        env->error("No calculator loaded to add external potential", src);
+        return;
+    }
+    if (!charges || !positions || (!gam && !numbers)) {
+        env->error("External charges, positions or numbers are missing", src);
+        return;
+    }
+    std::vector<double> q(charges, charges + npc), x(positions, positions + 3 * (size_t)npc), g(npc);
+    for (int k = 0; k < npc; ++k) {
+        if (gam) {
+            g[k] = gam[k];
+        } else {
+            if (numbers[k] < 1 || numbers[k] > kMaxElem) {
+                env->error("Invalid element for an external charge: " + std::to_string(numbers[k]), src);
+                return;
+            }
+            g[k] = xg::chemical_hardness(numbers[k]);
+        }
+        if (!(g[k] > 0.0) || !std::isfinite(q[k]) || !std::isfinite(x[3 * k]) || !std::isfinite(x[3 * k + 1]) ||
+            !std::isfinite(x[3 * k + 2])) {
+            env->error("External charge " + std::to_string(k + 1) + " has an invalid charge, position or hardness",
+                       src);
+            return;
+        }
+    }
+    calc->set.pc_q = std::move(q);
+    calc->set.pc_xyz = std::move(x);
+    calc->set.pc_gam = std::move(g);
 }
-void xtb_releaseExternalCharges(xtb_TEnvironment, xtb_TCalculator) {}
+}  // namespace
+
+void xtb_setExternalCharges(xtb_TEnvironment env, xtb_TCalculator calc, int* n, int* numbers, double* charges,
+                            double* positions) {
+    if (!check_env(env)) return;
+    set_external_charges(env, calc, n ? *n : 0, numbers, charges, positions, nullptr, "xtb_api_setExternalCharges");
+}
+
+void xtb_releaseExternalCharges(xtb_TEnvironment env, xtb_TCalculator calc) {
+    if (!check_env(env)) return;
+    if (!calc) {
+        env->error("Singlepoint calculator is not allocated", "xtb_api_releaseExternalCharges");
+        return;
+    }
+    calc->set.pc_q.clear();
+    calc->set.pc_xyz.clear();
+    calc->set.pc_gam.clear();
+}
 
 void xtb_setAccuracy(xtb_TEnvironment env, xtb_TCalculator calc, double accuracy) {
     const char* src = "xtb_api_setAccuracy";
@@ -521,8 +578,11 @@ void xtb_getPCGradient(xtb_TEnvironment env, xtb_TResults res, double* grad) {
         env->error("Results object is not allocated", "xtb_api_getPCGradient");
         return;
     }
-    (void)grad;
-    env->error("External charge gradients are not available in results", "xtb_api_getPCGradient");
+    if (!res->has || res->sp.pcgrad.empty()) {
+        env->error("External charge gradients are not available in results", "xtb_api_getPCGradient");
+        return;
+    }
+    if (grad) std::copy(res->sp.pcgrad.begin(), res->sp.pcgrad.end(), grad);
 }
 
 void xtb_getVirial(xtb_TEnvironment env, xtb_TResults res, double* virial) {
@@ -638,6 +698,127 @@ void xtbgb_fp64PeakDetail(double* out) {
         xg::fp64_peak_detail(out);
     } catch (const std::exception&) {
     }
+}
+
+namespace {
+// records of a Fortran unformatted sequential file: a 4-byte length before and after each
+// record (the layout gfortran writes)
+bool put_record(FILE* f, const void* p, size_t bytes) {
+    const int32_t len = (int32_t)bytes;
+    return fwrite(&len, 4, 1, f) == 1 && (bytes == 0 || fwrite(p, 1, bytes, f) == bytes) && fwrite(&len, 4, 1, f) == 1;
+}
+
+bool get_record(FILE* f, std::vector<char>& buf) {
+    int32_t a = 0, b = 0;
+    if (fread(&a, 4, 1, f) != 1 || a < 0) return false;
+    buf.resize((size_t)a);
+    if (a > 0 && fread(buf.data(), 1, (size_t)a, f) != (size_t)a) return false;
+    return fread(&b, 4, 1, f) == 1 && a == b;
+}
+}  // namespace
+
+// Restart file of the reference (writeRestart / readRestart, src/restart.f90:33-86, 182-200):
+// a record of six 64-bit integers (method twice, atoms, shells, electrons, unpaired electrons),
+// the shell charges, then for GFN2 the atomic dipoles (3, atoms) and quadrupoles (6, atoms).
+int xtbgb_writeRestart(xtb_TEnvironment env, xtb_TMolecule mol, xtb_TResults res, const char* filename) {
+    static const char* src = "xtbgb_writeRestart";
+    if (!check_env(env)) return 0;
+    if (!mol || !res || !filename) {
+        env->error("Molecule, results or file name missing", src);
+        return 0;
+    }
+    xg::HostMol hm;
+    const std::string err = xg::build_host_mol(mol->nat, mol->Z.data(), mol->xyz.data(), mol->charge, mol->uhf, hm);
+    if (!err.empty()) {
+        env->error(err, src);
+        return 0;
+    }
+    const xg::Wavefunction& w = res->wfn;
+    if (!w.valid() || w.nat != hm.nat || w.nsh != hm.nsh) {
+        env->error("Results hold no wavefunction of this molecule", src);
+        return 0;
+    }
+    FILE* f = fopen(filename, "wb");
+    if (!f) {
+        env->error(std::string("Could not open '") + filename + "' for writing", src);
+        return 0;
+    }
+    const int64_t head[6] = {2, 2, hm.nat, hm.nsh, hm.nel, hm.nel_a - hm.nel_b};
+    const bool ok = put_record(f, head, sizeof(head)) && put_record(f, w.qsh.data(), w.qsh.size() * 8) &&
+                    put_record(f, w.dipm.data(), w.dipm.size() * 8) && put_record(f, w.qp.data(), w.qp.size() * 8);
+    fclose(f);
+    if (!ok) {
+        env->error(std::string("Could not write '") + filename + "'", src);
+        return 0;
+    }
+    return 1;
+}
+
+int xtbgb_readRestart(xtb_TEnvironment env, xtb_TMolecule mol, xtb_TResults res, const char* filename) {
+    static const char* src = "restart_readRestart";
+    if (!check_env(env)) return 0;
+    if (!mol || !res || !filename) {
+        env->error("Molecule, results or file name missing", src);
+        return 0;
+    }
+    xg::HostMol hm;
+    const std::string err = xg::build_host_mol(mol->nat, mol->Z.data(), mol->xyz.data(), mol->charge, mol->uhf, hm);
+    if (!err.empty()) {
+        env->error(err, src);
+        return 0;
+    }
+    FILE* f = fopen(filename, "rb");
+    if (!f) return 0;   // no restart file: the reference goes on silently
+    std::vector<char> rec;
+    int64_t head[6] = {0, 0, 0, 0, 0, 0};
+    if (!get_record(f, rec) || rec.size() != sizeof(head)) {
+        fclose(f);
+        env->warning("Dimension missmatch in restart file.", src);
+        return 0;
+    }
+    std::memcpy(head, rec.data(), sizeof(head));
+    if (head[0] != 2) env->warning("Version number missmatch in restart file.", src);
+    if (head[4] != hm.nel) env->warning("Number of electron missmatch in restart file.", src);
+    if (head[5] != hm.nel_a - hm.nel_b) env->warning("Multiplicity missmatch in restart file.", src);
+    if (head[2] != hm.nat || head[3] != hm.nsh) {
+        fclose(f);
+        env->warning("Dimension missmatch in restart file.", src);
+        return 0;
+    }
+    xg::Wavefunction w;
+    w.nat = hm.nat;
+    w.nao = hm.nao;
+    w.nsh = hm.nsh;
+    w.qsh.assign(hm.nsh, 0.0);
+    w.dipm.assign(3 * (size_t)hm.nat, 0.0);
+    w.qp.assign(6 * (size_t)hm.nat, 0.0);
+    bool ok = get_record(f, rec) && rec.size() == w.qsh.size() * 8;
+    if (ok) std::memcpy(w.qsh.data(), rec.data(), rec.size());
+    if (ok && head[0] > 1) {   // GFN2 files carry the cumulative atomic multipoles
+        ok = get_record(f, rec) && rec.size() == w.dipm.size() * 8;
+        if (ok) std::memcpy(w.dipm.data(), rec.data(), rec.size());
+        ok = ok && get_record(f, rec) && rec.size() == w.qp.size() * 8;
+        if (ok) std::memcpy(w.qp.data(), rec.data(), rec.size());
+    }
+    fclose(f);
+    if (!ok) {
+        env->warning("Dimension missmatch in restart file.", src);
+        return 0;
+    }
+    w.q.assign(hm.nat, 0.0);
+    for (int s = 0; s < hm.nsh; ++s) w.q[hm.sh_atom[s]] += w.qsh[s];
+    res->wfn = std::move(w);
+    return 1;
+}
+
+void xtbgb_setExternalChargesHardness(xtb_TEnvironment env, xtb_TCalculator calc, int n, const double* charges,
+                                      const double* positions, const double* hardness) {
+    if (!check_env(env)) return;
+    if (!hardness) {
+        env->error("Hardness values are missing", "xtbgb_setExternalChargesHardness");
+        return;
+    }
+    set_external_charges(env, calc, n, nullptr, charges, positions, hardness, "xtbgb_setExternalChargesHardness");
 }
 
 int xtbgb_autotune(xtb_TEnvironment env, double* out, int nout) {

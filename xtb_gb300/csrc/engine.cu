@@ -55,17 +55,91 @@ __global__ void k_scale_energy_weights(int n, const double* __restrict__ focc, c
     if (i < n) fe[i] = focc[i] * emo[i] * EVTOAU;
 }
 
+// ---- external point charges (GFN2 forms of src/embedding.f90)
+// shell potential of the charges, jpot_pcem_gfn2 (:225-256): V_s = sum_k q_k / sqrt(r^2 + 1/x^2),
+// x = (eta_s + gam_k) / 2; one warp per shell
+__global__ void k_pc_potential(DevMol m, int npc, const double* __restrict__ pcq, const double* __restrict__ pcx,
+                               const double* __restrict__ pcg, double* __restrict__ vpc) {
+    const int s = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (s >= m.nsh) return;
+    const int a = m.sh_atom[s];
+    const double eta = m.sh_eta[s];
+    double acc = 0.0;
+    for (int k = lane; k < npc; k += 32) {
+        const double dx = pcx[3 * k] - m.xyz[3 * a], dy = pcx[3 * k + 1] - m.xyz[3 * a + 1],
+                     dz = pcx[3 * k + 2] - m.xyz[3 * a + 2];
+        const double x = 0.5 * (eta + pcg[k]);
+        acc += pcq[k] / sqrt(dx * dx + dy * dy + dz * dz + 1.0 / (x * x));
+    }
+    acc = warp_sum(acc);
+    if (lane == 0) vpc[s] = acc;
+}
+
+__global__ void k_add_vec(int n, const double* __restrict__ a, double* __restrict__ b) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) b[i] += a[i];
+}
+
+// gradient of sum_s qsh_s V_s, pcem_grad_gfn2 (:329-365): with dr = R_atom - R_k and
+// y = qsh_s q_k (r^2 + 1/x^2)^(-3/2), the atom gains -dr y and the charge +dr y.  One warp per
+// atom (its shells against all charges) and one warp per charge (against all shells): no atomics.
+__global__ void k_pc_grad_atoms(DevMol m, int npc, const double* __restrict__ pcq, const double* __restrict__ pcx,
+                                const double* __restrict__ pcg, const double* __restrict__ qsh,
+                                double* __restrict__ grad) {
+    const int a = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (a >= m.nat) return;
+    double g[3] = {0.0, 0.0, 0.0};
+    for (int s = m.at_sh0[a]; s < m.at_sh0[a] + m.at_nsh[a]; ++s)
+        for (int k = lane; k < npc; k += 32) {
+            const double dr[3] = {m.xyz[3 * a] - pcx[3 * k], m.xyz[3 * a + 1] - pcx[3 * k + 1],
+                                  m.xyz[3 * a + 2] - pcx[3 * k + 2]};
+            const double x = 0.5 * (m.sh_eta[s] + pcg[k]);
+            const double t = dr[0] * dr[0] + dr[1] * dr[1] + dr[2] * dr[2] + 1.0 / (x * x);
+            const double y = qsh[s] * pcq[k] / (t * sqrt(t));
+            for (int c = 0; c < 3; ++c) g[c] -= dr[c] * y;
+        }
+    for (int c = 0; c < 3; ++c) {
+        const double v = warp_sum(g[c]);
+        if (lane == 0) grad[3 * a + c] += v;
+    }
+}
+
+__global__ void k_pc_grad_charges(DevMol m, int npc, const double* __restrict__ pcq, const double* __restrict__ pcx,
+                                  const double* __restrict__ pcg, const double* __restrict__ qsh,
+                                  double* __restrict__ gpc) {
+    const int k = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (k >= npc) return;
+    double g[3] = {0.0, 0.0, 0.0};
+    for (int s = lane; s < m.nsh; s += 32) {
+        const int a = m.sh_atom[s];
+        const double dr[3] = {m.xyz[3 * a] - pcx[3 * k], m.xyz[3 * a + 1] - pcx[3 * k + 1],
+                              m.xyz[3 * a + 2] - pcx[3 * k + 2]};
+        const double x = 0.5 * (m.sh_eta[s] + pcg[k]);
+        const double t = dr[0] * dr[0] + dr[1] * dr[1] + dr[2] * dr[2] + 1.0 / (x * x);
+        const double y = qsh[s] * pcq[k] / (t * sqrt(t));
+        for (int c = 0; c < 3; ++c) g[c] += dr[c] * y;
+    }
+    for (int c = 0; c < 3; ++c) {
+        const double v = warp_sum(g[c]);
+        if (lane == 0) gpc[3 * k + c] = v;
+    }
+}
+
 // SCC energy from the current populations (electro + aniso_electro + edisp_scc + entropy;
-// src/scc_core.f90:686-722, src/aespot.F90:566-664, src/disp/dftd4.F90:821-864)
-// out: [0] eel, [1] es, [2] eaes, [3] epol, [4] ed, [5] entropy term
+// src/scc_core.f90:686-722, src/aespot.F90:566-664, src/disp/dftd4.F90:821-864), and the shells'
+// energy in the field of external charges (electro_pcem, src/embedding.f90:261-280; vpc may be null)
+// out: [0] eel, [1] es, [2] eaes, [3] epol, [4] ed, [5] entropy term, [6] external charges
 __global__ void k_scc_energy(int nsh, int nat, const double* __restrict__ qsh, const double* __restrict__ Jq,
                              const double* __restrict__ gam3, const double* __restrict__ eh0,
                              const double* __restrict__ eaes, const double* __restrict__ ed4,
-                             const double* __restrict__ fermi_scal, double* __restrict__ out) {
+                             const double* __restrict__ fermi_scal, const double* __restrict__ vpc,
+                             double* __restrict__ out) {
     __shared__ double red[32];
-    double es = 0.0, h = 0.0, ea = 0.0, ep = 0.0, ed = 0.0;
-    for (int s = threadIdx.x; s < nsh; s += blockDim.x)
+    double es = 0.0, h = 0.0, ea = 0.0, ep = 0.0, ed = 0.0, epc = 0.0;
+    for (int s = threadIdx.x; s < nsh; s += blockDim.x) {
         es += 0.5 * qsh[s] * Jq[s] + gam3[s] * qsh[s] * qsh[s] * qsh[s] / 3.0;
+        if (vpc) epc += qsh[s] * vpc[s];
+    }
     for (int a = threadIdx.x; a < nat; a += blockDim.x) {
         h += eh0[a];
         ea += eaes[a];
@@ -77,14 +151,16 @@ __global__ void k_scc_energy(int nsh, int nat, const double* __restrict__ qsh, c
     ea = block_sum(ea, red);
     ep = block_sum(ep, red);
     ed = block_sum(ed, red);
+    epc = block_sum(epc, red);
     if (threadIdx.x == 0) {
         const double ts = fermi_scal[0];
-        out[0] = es + h * EVTOAU + ea + ep + ed + ts;
+        out[0] = es + h * EVTOAU + ea + ep + ed + epc + ts;
         out[1] = es;
         out[2] = ea;
         out[3] = ep;
         out[4] = ed;
         out[5] = ts;
+        out[6] = epc;
     }
 }
 
@@ -277,6 +353,8 @@ void run_singlepoint(const HostMol& hm, const SPSettings& set, Wavefunction& wfn
         *zeta, *dzeta, *Wz, *zv, *zr, *zdcn, *zrdcn, *vat, *ed4, *eh0, *eaes, *erep, *e2, *e3, *grad, *dhdcn, *tmp2,
         *rows, *emo, *focc, *focca, *foccb, *fe, *tri_d, *tri_e, *tri_e2, *tri_tau, *tri_p, *bounds, *fscal, *escal, *rms, *dip, *qin,
         *qout, *dq;
+    double *pcq = nullptr, *pcx = nullptr, *pcg = nullptr, *vpc = nullptr, *pcgrad = nullptr;
+    const int npc = (int)set.pc_q.size();
     double* ormw;
     char* sgw = nullptr;
     unsigned char* piv;
@@ -331,6 +409,11 @@ void run_singlepoint(const HostMol& hm, const SPSettings& set, Wavefunction& wfn
     m.ao_sh = upload(ar, st, hm.ao_sh);
     m.ao_at = upload(ar, st, hm.ao_at);
     d_zval = upload(ar, st, hm.zval);
+    if (npc > 0) {
+        pcq = upload(ar, st, set.pc_q);
+        pcx = upload(ar, st, set.pc_xyz);
+        pcg = upload(ar, st, set.pc_gam);
+    }
 
     // ---- device buffers
     S = ar.take<double>(nn);
@@ -411,6 +494,10 @@ void run_singlepoint(const HostMol& hm, const SPSettings& set, Wavefunction& wfn
     qout = ar.take<double>(nbr);
     dq = ar.take<double>(nbr);
     info = ar.take<int>(8);
+    if (npc > 0) {
+        vpc = ar.take<double>(nsh);
+        pcgrad = ar.take<double>(3 * (size_t)npc);
+    }
     bs.nbr = nbr;
     bs.maxit = maxit;
     bs.df = ar.take<double>((size_t)maxit * nbr);
@@ -498,6 +585,10 @@ void run_singlepoint(const HostMol& hm, const SPSettings& set, Wavefunction& wfn
         if (hinfo != 0) throw std::runtime_error("overlap matrix is not positive definite (Cholesky failed)");
     }
 
+    if (npc > 0) {   // shell potential of the external charges, fixed for the single point
+        k_pc_potential<<<ceil_div((long)nsh * 32, 128), 128, 0, st>>>(m, npc, pcq, pcx, pcg, vpc);
+        XG_LAUNCH_CHECK();
+    }
     // ---- SCC iterations
     double eel = 0.0, eold = 0.0;
     bool lastdiag = false, converged = false;
@@ -508,6 +599,10 @@ void run_singlepoint(const HostMol& hm, const SPSettings& set, Wavefunction& wfn
         tm.mark(PH_HBUILD);
         d4_scc(st, m, gw, q, zeta, dzeta, Wz, vat, ed4);
         shell_shift(st, m, J, qsh, vat, shift, Jq);
+        if (npc > 0) {   // the external charges' field enters every iteration's shift
+            k_add_vec<<<ceil_div(nsh, 256), 256, 0, st>>>(nsh, vpc, shift);
+            XG_LAUNCH_CHECK();
+        }
         aes_potential(st, m, q, dipm, qp, gab3, gab5, true, vs, vd, vq);
         build_hu(st, m, th, H0, S, D, Q, shift, vs, vd, vq, H);
         // standard form A = X^T H X (X = U^-1 upper triangular) as B + B^T with B = X^T (Hu X):
@@ -549,12 +644,12 @@ void run_singlepoint(const HostMol& hm, const SPSettings& set, Wavefunction& wfn
         shell_shift(st, m, J, qsh, nullptr, T1, Jq);    // Jq for the electrostatic energy
         aes_energy(st, m, q, dipm, qp, gab3, gab5, eaes);
         d4_scc(st, m, gw, q, zeta, dzeta, Wz, vat, ed4);
-        k_scc_energy<<<1, 512, 0, st>>>(nsh, nat, qsh, Jq, m.sh_gam3, eh0, eaes, ed4, fscal, escal);
+        k_scc_energy<<<1, 512, 0, st>>>(nsh, nat, qsh, Jq, m.sh_gam3, eh0, eaes, ed4, fscal, vpc, escal);
         XG_LAUNCH_CHECK();
         broyden_pack(st, m, qsh, dipm, qp, qout);
         broyden_step(st, bs, it, 0.4, qin, qout, dq, rms, nat);
         broyden_unpack(st, m, qin, qsh, dipm, qp, q);
-        XG_CUDA(cudaMemcpyAsync(hsc, escal, 6 * sizeof(double), cudaMemcpyDeviceToHost, st));
+        XG_CUDA(cudaMemcpyAsync(hsc, escal, 7 * sizeof(double), cudaMemcpyDeviceToHost, st));
         double hrms[2];
         XG_CUDA(cudaMemcpyAsync(hrms, rms, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
         XG_CUDA(cudaStreamSynchronize(st));
@@ -602,6 +697,11 @@ void run_singlepoint(const HostMol& hm, const SPSettings& set, Wavefunction& wfn
     d4_grad(st, m, cn_tmp, q, gw, dgw, zv, zr, zdcn, zrdcn, c6, dc6, c6z, dc6z, e2, e3, tmp2, grad, iscr);
     cn_chain(st, m, 1, tmp2, grad);
     coulomb_grad(st, m, qsh, grad);
+    if (npc > 0) {
+        k_pc_grad_atoms<<<ceil_div((long)nat * 32, 128), 128, 0, st>>>(m, npc, pcq, pcx, pcg, qsh, grad);
+        k_pc_grad_charges<<<ceil_div((long)npc * 32, 128), 128, 0, st>>>(m, npc, pcq, pcx, pcg, qsh, pcgrad);
+        XG_LAUNCH_CHECK();
+    }
     k_dipole<<<1, 256, 0, st>>>(nat, nao, m.xyz, d_zval, rows, dip);
     XG_LAUNCH_CHECK();
     const bool closed = hm.nel_a == hm.nel_b;
@@ -637,6 +737,10 @@ void run_singlepoint(const HostMol& hm, const SPSettings& set, Wavefunction& wfn
     wfn.q.resize(nat); wfn.qsh.resize(nsh); wfn.dipm.resize(3 * nat); wfn.qp.resize(6 * nat);
     wfn.emo.resize(nao); wfn.focc.resize(nao);
     XG_CUDA(cudaMemcpyAsync(hs2, escal + 8, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    res.pcgrad.assign(3 * (size_t)npc, 0.0);
+    if (npc > 0)
+        XG_CUDA(cudaMemcpyAsync(res.pcgrad.data(), pcgrad, 3 * (size_t)npc * sizeof(double), cudaMemcpyDeviceToHost,
+                                st));
     XG_CUDA(cudaMemcpyAsync(res.gradient.data(), grad, 3 * nat * sizeof(double), cudaMemcpyDeviceToHost, st));
     XG_CUDA(cudaMemcpyAsync(res.dipole.data(), dip, 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
     XG_CUDA(cudaMemcpyAsync(wfn.q.data(), q, nat * sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -666,6 +770,7 @@ void run_singlepoint(const HostMol& hm, const SPSettings& set, Wavefunction& wfn
         XG_CUDA(cudaEventElapsedTime(&t, tm.pool[total_ev], tm.pool[total_end]));
         res.phase_ms[PH_TOTAL] = t;
     }
+    res.e_pc = hsc[6];
     res.e_rep = hs2[0];
     res.e_atm = hs2[1];
     res.energy = eel + hs2[0] + hs2[1];

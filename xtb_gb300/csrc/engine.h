@@ -25,6 +25,9 @@ struct SPSettings {
     // CUDA stream priority of the single point's stream (lower is more urgent; clamped to the
     // device's range; 0 is the default priority)
     int stream_priority = 0;
+    // external point charges (xtb_setExternalCharges): charge, position [k][3] (Bohr) and
+    // hardness of charge k; empty for none
+    std::vector<double> pc_q, pc_xyz, pc_gam;
 };
 
 // Wavefunction kept between calls on the same results object (res%chk of the reference).
@@ -49,6 +52,8 @@ struct SPResult {
     // energy parts (Eh)
     double e_elec = 0, e_rep = 0, e_es = 0, e_aes = 0, e_axc = 0, e_disp = 0, e_atm = 0;
     double gnorm = 0.0;
+    double e_pc = 0.0;                          // energy of the shells in the external charges' field
+    std::vector<double> pcgrad;                 // [npc][3] gradient on the external charges
     // device time per phase (ms), measured with CUDA events on the engine stream
     std::vector<double> phase_ms;
     // bytes copied host->device and device->host by this single point

@@ -101,6 +101,8 @@ void trap_weights(double* w) {
 
 }  // namespace
 
+double chemical_hardness(int Z) { return (Z >= 1 && Z <= 86) ? k_chemicalHardness[Z - 1] : 0.0; }
+
 std::string build_host_mol(int nat, const int* Zin, const double* xyzin, double charge, int uhf, HostMol& hm) {
     hm = HostMol();
     if (nat <= 0) return "molecule has no atoms";

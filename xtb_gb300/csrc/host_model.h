@@ -33,6 +33,9 @@ struct HostMol {
 
 // Returns an empty string on success, else an error message (unsupported element, ...).
 std::string build_host_mol(int nat, const int* Z, const double* xyz, double charge, int uhf, HostMol& hm);
+// GFN2-xTB chemical hardness of element Z (1..86; 0 outside), the hardness an external point
+// charge of that element takes (setExternalCharges_api, src/api/calculator.f90:482-537)
+double chemical_hardness(int Z);
 // iniqshell (src/scc_core.f90:1475-1506): shell charges from atomic charges
 void ini_qshell(const HostMol& hm, const double* q, double* qsh);
 

@@ -456,13 +456,15 @@ __global__ void __launch_bounds__(SYM_NT) k_sytrd_sym(int n, double* __restrict_
         const int nrb = (m + SYM_RB - 1) / SYM_RB, C = (m + L - 1) / L;
         // ---- tiles
         const int ngroups = (nrb + q - 1) / q;
-        if (threadIdx.x == 0) {
-            int acc = 0;
-            for (int a = 0; a < ngroups; ++a) {
-                gs[a] = acc;
-                acc += min(q, nrb - a * q) * (C - a);
+        {
+            // first task of group a: full groups hold q (C - a') tasks each, the last one may be short
+            const int afull = nrb / q;
+            for (int a = threadIdx.x; a <= ngroups; a += SYM_NT) {
+                const int k = min(a, afull);
+                int v = q * (k * C - k * (k - 1) / 2);
+                if (a > afull) v += (nrb - afull * q) * (C - afull);
+                gs[a] = v;
             }
-            gs[ngroups] = acc;
         }
         __syncthreads();
         const int ntask = gs[ngroups];
@@ -571,8 +573,8 @@ __global__ void __launch_bounds__(SYM_NT) k_sytrd_sym(int n, double* __restrict_
                 yv = 0.0;
             } else {
                 beta = -copysign(sqrt(alpha * alpha + t0), alpha);
-                tk = (beta - alpha) / beta;
-                sc = 1.0 / (alpha - beta);
+                tk = (beta - alpha) * rcp_fast(beta);
+                sc = rcp_fast(alpha - beta);
                 // y.v = tau sc^2 (x - beta e0).(A x - beta a0)
                 yv = tk * sc * sc * (txa - beta * tx0 - beta * ax0 + beta * beta * a00);
             }
@@ -603,11 +605,12 @@ __global__ void __launch_bounds__(SYM_NT) k_sytrd_sym(int n, double* __restrict_
                     xn[j - 1] = xv;
                     if (j >= 2) nx2 = fma(xv, xv, nx2);
                 }
-                if (lead) V[(size_t)s * n + b + j] = v;
             }
-            if (lead)
-                for (int j = threadIdx.x; j <= s; j += SYM_NT) V[(size_t)s * n + j] = 0.0;
-            // clear this block's slice of the ax buffer of column s + 2
+            // this block's slices: row s of V (zeros left of column s + 1) and the ax buffer of
+            // column s + 2
+            const int pv = (n + G - 1) / G;
+            for (int c = blockIdx.x * pv + threadIdx.x; c < min(n, (blockIdx.x + 1) * pv); c += SYM_NT)
+                V[(size_t)s * n + c] = c < b ? 0.0 : (c == b ? 1.0 : sc * x[c - b]);
             const int per = (m + G - 1) / G;
             double* ax2 = axbuf(s + 2);
             for (int j = blockIdx.x * per + threadIdx.x; j < min(m, (blockIdx.x + 1) * per); j += SYM_NT) ax2[j] = 0.0;

@@ -4,14 +4,13 @@
 // every row of op(A) (column of op(B)) is scaled by a power of two s_i (t_j) so that
 // |x| < 1, and cut into S digits of 8 bits, x / s = sum_{p=1..S} d_p 2^(-8p) with integer
 // d_p in [-256, 256] -- exactly representable in BF16.  A digit product d_p e_q is exact in
-// FP32 (16 bits), and the tensor cores' FP32 sums of such products over a K chunk of 128
-// stay below 2^24, so they are exact too.  Products are grouped by level p + q <= S + 1
-// (the lower levels carry less than 2^(-8S) of the result and are dropped), each level is
-// summed exactly over a chunk, and the chunks are recombined in FP64 with the weights
-// 2^(-8(p+q)).  The only errors are the truncation to S digits and the FP64 additions:
-// with S = 5 the relative error per product term is about 2^-40.
+// FP32 (16 bits).  Products are grouped by level p + q (levels beyond S - 1 carry less than
+// 2^(-8S) of the result and are dropped); the two leading levels are summed exactly over K
+// chunks and recombined as integers, the others in FP32 (see the kernel), and the result is
+// scaled back in FP64 with the weights 2^(-8(p+q)).  The errors are the truncation to S digits
+// and the FP32 sums of the lower levels: with S = 5 about 2^-40 relative per product term.
 //
-// The products run as mma.sync.m16n8k16 (BF16 in, FP32 accumulate) from shared memory;
+// The products run on the tcgen05 tensor cores (BF16 in, FP32 accumulate in tensor memory);
 // S(S+1)/2 tensor-core products replace one FP64 product.
 #include <cuda.h>
 #include <cudaTypedefs.h>
@@ -28,10 +27,7 @@ namespace xg {
 
 namespace {
 
-constexpr int SG_BM = 64, SG_BN = 64;   // output tile per block (8 warps, each 32 x 16)
-constexpr int SG_KT = 32;               // K per shared-memory stage
-constexpr int SG_KC = 128;              // K per exact FP32 chunk
-constexpr int SG_LD = 40;               // shared row stride in bf16 (80 bytes: conflict-free fragments)
+constexpr int SG_KT = 32;               // K is padded to a multiple of this (one pipeline stage)
 
 // Digits of row r of X (element k = trans ? X[k*ldx + r] : X[r*ldx + k]), k < K (and k < *dK),
 // zero beyond; out[p][r][k] for k < Kp.  One warp per row.
@@ -131,133 +127,6 @@ __global__ void __launch_bounds__(256) k_col_digits(int R, int K, int Kp, const 
 
 namespace {
 
-__device__ __forceinline__ void mma_bf16(float* c, const uint32_t* a, const uint32_t* b) {
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-        "{%0,%1,%2,%3};\n"
-        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
-}
-
-// One 64 x 64 output tile per block of 8 warps (warp tile 32 x 16: 2 x 2 mma tiles).
-// As: S planes of M x Kp digits (rows of op(A)), Bs: S planes of N x Kp digits (columns of op(B)).
-// Dynamic shared memory: 2 * S * 64 * SG_LD bf16.
-template <int S>
-__global__ void __launch_bounds__(256) k_split_mma(int M, int N, int Kp, const __nv_bfloat16* __restrict__ As,
-                                                   const __nv_bfloat16* __restrict__ Bs, const double* __restrict__ sA,
-                                                   const double* __restrict__ sB, double alpha, double beta,
-                                                   double* __restrict__ C, int ldc, const int* __restrict__ dN,
-                                                   int kchunk, double* __restrict__ P) {
-    extern __shared__ __align__(16) unsigned char sg_raw[];
-    __nv_bfloat16* smA = reinterpret_cast<__nv_bfloat16*>(sg_raw);
-    __nv_bfloat16* smB = smA + S * SG_BM * SG_LD;
-    const int i0 = blockIdx.y * SG_BM, j0 = blockIdx.x * SG_BN;
-    const int Nl = dN ? min(N, *dN) : N;
-    if (j0 >= Nl) return;
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, t = lane & 3;
-    const int wm = warp >> 2, wn = warp & 3;   // warp rows wm*32.., cols wn*16..
-    const size_t planeA = (size_t)M * Kp, planeB = (size_t)N * Kp;
-    float acc[S][2][2][4];
-    double acc64[2][2][4];
-    float low[2][2][4];
-#pragma unroll
-    for (int mt = 0; mt < 2; ++mt)
-#pragma unroll
-        for (int nt = 0; nt < 2; ++nt)
-#pragma unroll
-            for (int v = 0; v < 4; ++v) {
-                acc64[mt][nt][v] = 0.0;
-                low[mt][nt][v] = 0.0f;
-#pragma unroll
-                for (int L = 0; L < S; ++L) acc[L][mt][nt][v] = 0.0f;
-            }
-    const int srow = tid >> 2, scol = (tid & 3) * 8;   // staging: one 16-byte chunk per thread per plane
-    // split K (P != nullptr): slice blockIdx.z covers [z kchunk, (z+1) kchunk), a whole number of
-    // exact chunks, and leaves alpha sA sB (its sum) in P[z][i][j] for k_split_reduce
-    const int kb = P ? (int)blockIdx.z * kchunk : 0;
-    const int ke = P ? min(Kp, kb + kchunk) : Kp;
-    for (int k0 = kb; k0 < ke; k0 += SG_KT) {
-#pragma unroll
-        for (int p = 0; p < S; ++p) {
-            const int gi = i0 + srow, gj = j0 + srow;
-            uint4 va = make_uint4(0u, 0u, 0u, 0u), vb = make_uint4(0u, 0u, 0u, 0u);
-            if (gi < M) va = *reinterpret_cast<const uint4*>(As + p * planeA + (size_t)gi * Kp + k0 + scol);
-            if (gj < N) vb = *reinterpret_cast<const uint4*>(Bs + p * planeB + (size_t)gj * Kp + k0 + scol);
-            *reinterpret_cast<uint4*>(smA + (p * SG_BM + srow) * SG_LD + scol) = va;
-            *reinterpret_cast<uint4*>(smB + (p * SG_BN + srow) * SG_LD + scol) = vb;
-        }
-        __syncthreads();
-#pragma unroll
-        for (int kk = 0; kk < SG_KT; kk += 16) {
-#pragma unroll
-            for (int p = 0; p < S; ++p) {
-                uint32_t a[2][4];
-#pragma unroll
-                for (int mt = 0; mt < 2; ++mt) {
-                    const __nv_bfloat16* base = smA + (p * SG_BM + wm * 32 + mt * 16 + g) * SG_LD + kk + 2 * t;
-                    a[mt][0] = *reinterpret_cast<const uint32_t*>(base);
-                    a[mt][1] = *reinterpret_cast<const uint32_t*>(base + 8 * SG_LD);
-                    a[mt][2] = *reinterpret_cast<const uint32_t*>(base + 8);
-                    a[mt][3] = *reinterpret_cast<const uint32_t*>(base + 8 * SG_LD + 8);
-                }
-#pragma unroll
-                for (int q = 0; q < S - p; ++q) {
-                    uint32_t b[2][2];
-#pragma unroll
-                    for (int nt = 0; nt < 2; ++nt) {
-                        const __nv_bfloat16* base = smB + (q * SG_BN + wn * 16 + nt * 8 + g) * SG_LD + kk + 2 * t;
-                        b[nt][0] = *reinterpret_cast<const uint32_t*>(base);
-                        b[nt][1] = *reinterpret_cast<const uint32_t*>(base + 8);
-                    }
-#pragma unroll
-                    for (int mt = 0; mt < 2; ++mt)
-#pragma unroll
-                        for (int nt = 0; nt < 2; ++nt) mma_bf16(acc[p + q][mt][nt], a[mt], b[nt]);
-                }
-            }
-        }
-        __syncthreads();
-        if ((k0 + SG_KT) % SG_KC == 0 || k0 + SG_KT >= ke) {
-            // levels 0..2 (exact FP32 chunk sums) into FP64; lower levels into an FP32 sum at the
-            // scale of level 3, whose rounding is below 2^-48 of the result
-#pragma unroll
-            for (int mt = 0; mt < 2; ++mt)
-#pragma unroll
-                for (int nt = 0; nt < 2; ++nt)
-#pragma unroll
-                    for (int v = 0; v < 4; ++v) {
-                        acc64[mt][nt][v] += (double)acc[0][mt][nt][v] +
-                                            ((double)acc[1][mt][nt][v] + (double)acc[2][mt][nt][v] * 0x1p-8) * 0x1p-8;
-                        float lo = 0.0f;
-#pragma unroll
-                        for (int L = S - 1; L >= 3; --L) lo = lo * 0x1p-8f + acc[L][mt][nt][v];
-                        low[mt][nt][v] += lo;
-#pragma unroll
-                        for (int L = 0; L < S; ++L) acc[L][mt][nt][v] = 0.0f;
-                    }
-        }
-    }
-    // C = alpha sA sB 2^-16 (sum of levels) + beta C
-#pragma unroll
-    for (int mt = 0; mt < 2; ++mt)
-#pragma unroll
-        for (int nt = 0; nt < 2; ++nt)
-#pragma unroll
-            for (int v = 0; v < 4; ++v) {
-                const int i = i0 + wm * 32 + mt * 16 + g + ((v & 2) ? 8 : 0);
-                const int j = j0 + wn * 16 + nt * 8 + 2 * t + (v & 1);
-                if (i >= M || j >= Nl) continue;
-                const double sum = acc64[mt][nt][v] + (double)low[mt][nt][v] * 0x1p-24;
-                double r = alpha * sA[i] * sB[j] * (sum * 0x1p-16);
-                if (P) {
-                    P[((size_t)blockIdx.z * M + i) * N + j] = r;
-                    continue;
-                }
-                if (beta != 0.0) r += beta * C[(size_t)i * ldc + j];
-                C[(size_t)i * ldc + j] = r;
-            }
-}
-
 // ------------------------------------------------------------------ tcgen05 form
 // The same digit products on the 5th-generation tensor cores: tcgen05.mma (M = 128, N = 64,
 // K = 16, BF16 in, FP32 accumulate) with the accumulators in tensor memory (TMEM) and the digit
@@ -275,6 +144,7 @@ __global__ void __launch_bounds__(256) k_split_mma(int M, int N, int Kp, const _
 // the whole K in FP32 (rounding below 2^-40 of the result) and are added once at the end.
 constexpr int TC_BM = 128, TC_BN = 64, TC_BK = 32, TC_KC = 256;
 constexpr int TC_THREADS = 192;
+constexpr int TC_GROUP = 8;              // row tiles per group of the tile order
 constexpr unsigned TC_SPIN = 1u << 25;   // iteration limit of every mbarrier wait
 
 template <int S>
@@ -354,7 +224,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     int* abort_flag = reinterpret_cast<int*>(tmem_slot + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int i0 = blockIdx.y * TC_BM, j0 = blockIdx.x * TC_BN;
+    // grouped tile order: TC_GROUP row tiles share each column tile in turn, so that the A and
+    // B tiles of the CTAs in flight together stay in L2
+    int tm, tn;
+    {
+        const int npm = (M + TC_BM - 1) / TC_BM, npn = (N + TC_BN - 1) / TC_BN;
+        const int pid = blockIdx.x, group = TC_GROUP * npn;
+        const int first = (pid / group) * TC_GROUP, gsz = min(npm - first, TC_GROUP);
+        tm = first + (pid % group) % gsz;
+        tn = (pid % group) / gsz;
+    }
+    const int i0 = tm * TC_BM, j0 = tn * TC_BN;
     const int Nl = dN ? min(N, *dN) : N;
     if (j0 >= Nl) return;
     const int kb = P ? (int)blockIdx.z * kchunk : 0;
@@ -670,7 +550,7 @@ static void split_gemm_s(cudaStream_t st, bool ta, bool tb, int M, int N, int K,
         const int kz = (Kp + kchunk - 1) / kchunk;
         double* P = reinterpret_cast<double*>(
             (reinterpret_cast<uintptr_t>(mB + N) + 255) / 256 * 256);   // after the scales and maxima
-        dim3 grid(ceil_div(N, TC_BN), ceil_div(M, TC_BM), kz);
+        dim3 grid(ceil_div(N, TC_BN) * ceil_div(M, TC_BM), 1, kz);
         k_split_tc<S><<<grid, TC_THREADS, smem, st>>>(tmA, tmB, M, N, Kp, sA, sB, alpha, beta, C, ldc, dN, kchunk,
                                                       P, err);
         XG_LAUNCH_CHECK();
@@ -678,7 +558,7 @@ static void split_gemm_s(cudaStream_t st, bool ta, bool tb, int M, int N, int K,
         XG_LAUNCH_CHECK();
         return;
     }
-    dim3 grid(ceil_div(N, TC_BN), ceil_div(M, TC_BM));
+    dim3 grid(ceil_div(N, TC_BN) * ceil_div(M, TC_BM));
     k_split_tc<S><<<grid, TC_THREADS, smem, st>>>(tmA, tmB, M, N, Kp, sA, sB, alpha, beta, C, ldc, dN, Kp, nullptr,
                                                   err);
     XG_LAUNCH_CHECK();

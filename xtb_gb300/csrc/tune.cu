@@ -100,7 +100,7 @@ Tuned autotune() {
     XG_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
     XG_CUDA(cudaEventCreate(&e0));
     XG_CUDA(cudaEventCreate(&e1));
-    const int nmax = 2400;
+    const int nmax = 3072;
     const size_t nn = (size_t)nmax * nmax;
     const size_t split_ws = (split_gemm_workspace(nmax, nmax, nmax, 5) + 255) / 256 * 256;
     const size_t doubles = 4 * nn + 3 * (size_t)nmax + sytrd_workspace(nmax) + ormtr_workspace(nmax) + 64;
@@ -119,7 +119,7 @@ Tuned autotune() {
     int* ncol = reinterpret_cast<int*>(ormw + ormtr_workspace(nmax));
     try {
         // 1. tridiagonalisation: row form against the upper-triangle form
-        const std::vector<int> tsz = {192, 256, 384, 512, 768, 1024, 1536, 2048};
+        const std::vector<int> tsz = {192, 256, 384, 512, 768, 1024, 1536, 2048, 2560, 3072};
         std::vector<bool> sym_wins;
         for (int n : tsz) {
             k_tune_sym<<<ceil_div((long)n * n, 256), 256, 0, st>>>(n, 17u + n, A0);

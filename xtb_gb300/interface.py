@@ -70,6 +70,8 @@ def load_library(path=LIBPATH):
         "xtb_getVirial": (None, [vp, vp, dp]),
         "xtb_getSolvationEnergy": (None, [vp, vp, dp]),
         "xtb_getPCGradient": (None, [vp, vp, dp]),
+        "xtb_setExternalCharges": (None, [vp, vp, ip, ip, dp, dp]),
+        "xtb_releaseExternalCharges": (None, [vp, vp]),
         "xtbgb_deviceCount": (C.c_int, []),
         "xtbgb_getIterations": (None, [vp, vp, ip, ip]),
         "xtbgb_getEnergyParts": (None, [vp, vp, dp]),
@@ -83,6 +85,9 @@ def load_library(path=LIBPATH):
         "xtbgb_fp64PeakTflops": (C.c_double, []),
         "xtbgb_fp64PeakDetail": (None, [C.POINTER(C.c_double)]),
         "xtbgb_autotune": (C.c_int, [vp, dp, C.c_int]),
+        "xtbgb_setExternalChargesHardness": (None, [vp, vp, C.c_int, dp, dp, dp]),
+        "xtbgb_writeRestart": (C.c_int, [vp, vp, vp, C.c_char_p]),
+        "xtbgb_readRestart": (C.c_int, [vp, vp, vp, C.c_char_p]),
         "xtbgb_getTuning": (None, [vp, dp]),
         "xtbgb_setTuning": (None, [vp, C.c_int, C.c_int, C.c_int]),
         "xtbgb_fp64LatencyCycles": (None, [dp]),
@@ -168,6 +173,40 @@ class Calculator:
         self.env.check()
         self.res = C.c_void_p(self.lib.xtb_newResults())
 
+    def set_external_charges(self, charges, positions, numbers=None, hardness=None):
+        """External point charges (e, bohr): xtb_setExternalCharges with element numbers (the
+        charges take those elements' hardness), or xtbgb_setExternalChargesHardness with explicit
+        hardness values."""
+        q = np.ascontiguousarray(charges, dtype=np.float64)
+        x = np.ascontiguousarray(positions, dtype=np.float64).reshape(-1, 3)
+        n = len(q)
+        if hardness is not None:
+            g = np.ascontiguousarray(hardness, dtype=np.float64)
+            self.lib.xtbgb_setExternalChargesHardness(self.env.h, self.calc, n, _dptr(q), _dptr(x), _dptr(g))
+        else:
+            z = np.ascontiguousarray(numbers, dtype=np.int32)
+            nn = C.c_int(n)
+            self.lib.xtb_setExternalCharges(self.env.h, self.calc, C.byref(nn), z.ctypes.data_as(C.POINTER(C.c_int)),
+                                            _dptr(q), _dptr(x))
+        self.env.check()
+        self.npc = n
+
+    def write_restart(self, path):
+        """Write the last single point's wavefunction as an xtbrestart file (xtbgb_writeRestart)."""
+        ok = self.lib.xtbgb_writeRestart(self.env.h, self.mol, self.res, str(path).encode())
+        self.env.check()
+        return bool(ok)
+
+    def read_restart(self, path):
+        """Load an xtbrestart file; the next singlepoint(fresh=False) starts from it. Returns
+        whether the file matched the molecule (warnings stay on the environment)."""
+        return bool(self.lib.xtbgb_readRestart(self.env.h, self.mol, self.res, str(path).encode()))
+
+    def release_external_charges(self):
+        self.lib.xtb_releaseExternalCharges(self.env.h, self.calc)
+        self.env.check()
+        self.npc = 0
+
     def update(self, positions):
         self.positions = np.ascontiguousarray(positions, dtype=np.float64).reshape(-1, 3)
         self.lib.xtb_updateMolecule(self.env.h, self.mol, _dptr(self.positions), None)
@@ -243,6 +282,10 @@ class Results:
         self.gnorm = float(np.sqrt(np.sum(self.gradient ** 2)))
         self.phase_ms = np.zeros(len(PHASES))
         lib.xtbgb_getPhaseTimes(env.h, res, _dptr(self.phase_ms))
+        self.pcgrad = None
+        if getattr(calc, "npc", 0):
+            self.pcgrad = np.zeros((calc.npc, 3))
+            lib.xtb_getPCGradient(env.h, res, _dptr(self.pcgrad))
         tb = (C.c_longlong * 3)()
         lib.xtbgb_getTransferBytes(env.h, res, tb)
         self.h2d_bytes, self.d2h_bytes, self.launches = int(tb[0]), int(tb[1]), int(tb[2])
