@@ -891,13 +891,17 @@ def pc_gradient(basis, xyz, qsh, pc_q, pc_xyz, pc_gam):
 
 def singlepoint(Z, xyz, charge=0.0, uhf=0, etemp=300.0, accuracy=1.0, maxiter=250,
                 guess="eeq", q_init=None, qsh_init=None, dipm_init=None, qp_init=None, verbose=False,
-                pc_charges=None, pc_positions=None, pc_gam=None):
+                pc_charges=None, pc_positions=None, pc_gam=None, solvation=None):
     """GFN2-xTB energy, charges and gradient for a molecule (Bohr in, Eh and Eh/bohr out).
 
     Follows scf, src/scf_module.F90:74-920, and scc, src/scc_core.f90:255-640.  External point
     charges (pc_charges[k], pc_positions[k, 3] in Bohr, pc_gam[k] hardness) add the shell
     potential of jpot_pcem_gfn2 to every iteration's shift (src/scc_core.f90:438), their energy
     (electro_pcem, src/embedding.f90:261-280) and gradient (src/embedding.f90:329-365).
+    An implicit solvent (`solvation`, an oracle.solvation.Solvation of this molecule) is updated
+    for the geometry once (src/scf_module.F90:298-321), adds B q to the atomic potential of every
+    iteration (src/scc_core.f90:444-448) and its energy to the electronic energy
+    (src/scc_core.f90:544-548), and its gradient after convergence (src/scf_module.F90:761-776).
     """
     Z = np.asarray(Z, dtype=np.int64)
     xyz = np.asarray(xyz, dtype=np.float64).reshape(-1, 3)
@@ -956,6 +960,9 @@ def singlepoint(Z, xyz, charge=0.0, uhf=0, etemp=300.0, accuracy=1.0, maxiter=25
     else:
         vpc = np.zeros(nsh)
 
+    if solvation is not None:
+        solvation.update(xyz)
+
     # SCC, src/scc_core.f90:406-640
     U = sla.cholesky(S, lower=False)
     nbr = nsh + 9 * n
@@ -973,6 +980,8 @@ def singlepoint(Z, xyz, charge=0.0, uhf=0, etemp=300.0, accuracy=1.0, maxiter=25
         shift = vpc + J @ qsh + gam3 * qsh ** 2
         vs, vd, vq = setvsdq(Z, xyz, q, dipm, qp, gab3, gab5, shifted=True)
         atshift = scd4.potential(q)
+        if solvation is not None:
+            atshift = atshift + solvation.shift(q)
         shift = shift + atshift[basis.sh_atom]
         # buildIsoAnisotropicH1, src/scc_core.f90:154-251 (eV)
         dum = S * AUTOEV * 0.5
@@ -1015,6 +1024,8 @@ def singlepoint(Z, xyz, charge=0.0, uhf=0, etemp=300.0, accuracy=1.0, maxiter=25
         eel += ed
         epcem = float(qsh @ vpc)
         eel += epcem
+        if solvation is not None:
+            eel += solvation.energy(q)
         eel += ga + gb
         econv = abs(eel - eold) < scfconv
         dq = np.concatenate([qsh, dipm.ravel(), qp.ravel()]) - q_in
@@ -1051,6 +1062,10 @@ def singlepoint(Z, xyz, charge=0.0, uhf=0, etemp=300.0, accuracy=1.0, maxiter=25
     if pcem:
         gpc_atoms, pcgrad = pc_gradient(basis, xyz, qsh, pc_q, pc_x, pc_g)
         grad += gpc_atoms
+    esolv = None
+    if solvation is not None:
+        grad += solvation.gradient(q)
+        esolv = sum(solvation.energy_parts(q))
 
     # dipole moment (calc_dipole, src/dipole.f90:94-128) and Wiberg-Mayer bond orders
     # (get_wiberg, src/scc_core.f90:1208-1245) from the last density
@@ -1082,6 +1097,7 @@ def singlepoint(Z, xyz, charge=0.0, uhf=0, etemp=300.0, accuracy=1.0, maxiter=25
     r.e_disp = ed + embd
     r.gradient = grad
     r.pcgrad = pcgrad
+    r.e_solv = esolv
     r.gnorm = np.sqrt(np.sum(grad ** 2))
     r.q = q
     r.qsh = qsh

@@ -13,6 +13,13 @@ values the reference asserts, with the tolerance it asserts them at:
 * ``capi``  c_api_example.c:38-112 propyne through the C ABI: energy, q[5], dipole, wbo
 * ``capi_pc`` c_api_example.c:298-410 the same dimer through xtb_setExternalCharges: energy,
             gradient and point-charge gradient
+* ``gbsa``  test_gfn2.f90:237-308  11-atom molecule in water (GBSA, Still kernel): energy, gap,
+            gradient
+* ``salt``  test_gfn2.f90:310-381  8-atom molecule in CH2Cl2 with 1 mM salt (ion radius 1 A)
+* ``capi_gbsa``, ``capi_alpb`` c_api_example.c:114-163 propyne in water through xtb_setSolvent
+            ("gbsa", then "alpb"), each started from the previous result's wavefunction
+* ``mindless_solvation`` test_gfn2.f90:745-828 mindless01-10 in ten solvents, every second one
+            with the ALPB correction (Still kernel)
 
 Usage: python tests/golden/make_golden.py [reference_root]
 """
@@ -154,6 +161,50 @@ def main():
                      "positions": xyz, "energy": ref["ref_energies"][i - 1], "gnorm": ref["ref_gnorms"][i - 1],
                      "hl_gap": ref["ref_hlgaps"][i - 1], "thr": 1e-8})
     cases["mindless"] = mols
+    # implicit solvation
+    for key, name in (("gbsa", "test_gfn2gbsa_api"), ("salt", "test_gfn2salt_api")):
+        blk = sub(src, name)
+        at = [int(v) for v in array(blk, r"integer, parameter :: at\(nat\)")]
+        xyz = array(blk, r"real\(wp\),parameter :: xyz\(3,nat\)")
+        thr = fnum(re.search(r"real\(wp\),parameter :: thr\s*=\s*(" + NUM + r")_wp", blk).group(1))
+        cs = []
+        for c in checks(blk):
+            c["thr"] = thr if c["thr"] in (None, "thr") else fnum(c["thr"])
+            cs.append(c)
+        solvent = re.search(r'solvent\s*=\s*[\'"](\w+)[\'"]', blk).group(1)
+        add = blk[blk.index("call addSolvationModel"):]
+        add = add[:add.index("call calc%singlepoint")]
+        assert "alpb=.false." in add and "kernel=gbKernel%still" in add, add
+        case = {"numbers": at, "positions": xyz, "checks": cs,
+                "maxiter": int(re.search(r"maxiter\s*=\s*(\d+)", blk).group(1)), "guess": "eeq",
+                "solvent": solvent, "kernel": "still", "alpb": False}
+        if key == "salt":
+            m = re.search(r"ionRad=(" + NUM + r")_wp\*aatoau, ionStrength=(" + NUM + r")_wp", add)
+            case["ion_rad_angstrom"] = fnum(m.group(1))
+            case["ion_strength"] = fnum(m.group(2))
+        cases[key] = case
+    blk = sub(src, "test_gfn2_mindless_solvation")
+    ref = {}
+    for key in ("ref_energies", "ref_gnorms", "ref_hlgaps"):
+        m = re.search(key + r"\(10\)\s*=[\s&]*\[(.*?)\]", blk, re.S)
+        ref[key] = [fnum(t) for t in re.findall(NUM, m.group(1))]
+    m = re.search(r"solvents\(10\)\s*=\s*\[character\(len=20\)\s*::(.*?)\]", blk, re.S)
+    solvents = re.findall(r'"(\w+)"', m.group(1))
+    assert "alpb=mod(iMol, 2)==0, kernel=gbKernel%still" in blk
+    cases["mindless_solvation"] = [
+        {"name": mols[i]["name"], "numbers": mols[i]["numbers"], "positions": mols[i]["positions"],
+         "solvent": solvents[i], "kernel": "still", "alpb": (i + 1) % 2 == 0,
+         "energy": ref["ref_energies"][i], "gnorm": ref["ref_gnorms"][i], "hl_gap": ref["ref_hlgaps"][i],
+         "thr": 1e-8} for i in range(10)]
+    for key, start, stop, model in (("capi_gbsa", "// GBSA", "// ALPB", "gbsa"),
+                                    ("capi_alpb", "// ALPB", "// COSMO", "alpb")):
+        part = first[first.index(start):first.index(stop)]
+        assert f"NULL, NULL, NULL, {model});" in part
+        cks = [{"expr": m.group(1), "value": fnum(m.group(2)), "thr": fnum(m.group(3))}
+               for m in re.finditer(r"check\((\w+(?:\[\d+\])?),\s*(" + NUM + r"),\s*(" + NUM + r")", part)]
+        cases[key] = {"numbers": cases["capi"]["numbers"], "positions": cases["capi"]["positions"],
+                      "checks": cks, "maxiter": 30, "guess": "eeq", "solvent": "h2o", "model": model,
+                      "warm_start_from": "capi" if model == "gbsa" else "capi_gbsa"}
     json.dump(cases, open(OUT, "w"), indent=1)
     print("wrote", OUT)
 

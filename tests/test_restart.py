@@ -69,7 +69,7 @@ def test_restart_warm_start(tmp_path):
     assert a.write_restart(path)
     data = path.read_bytes()
     head = struct.unpack("<6q", data[4:52])
-    assert head[:4] == (2, 2, len(Z), 40) and head[5] == 0
+    assert head[:4] == (2, 2, len(Z), 80) and head[5] == 0     # 20 x (O: 2 shells, 2 H: 1 shell each)
     b = X.Calculator(Z, xyz)
     assert b.read_restart(path)
     rb = b.singlepoint(fresh=False)               # starts from the file's charges and moments
