@@ -15,9 +15,10 @@
  *    a NULL environment makes a call a silent no-op;
  *  - output arrays are caller-owned, getters copy into them.
  *
- * Only the GFN2-xTB Hamiltonian is implemented.  Entry points for other
- * methods and for solvation / external charges are exported and push an
- * "unsupported" error, as the reference does for unavailable features.
+ * Only the GFN2-xTB Hamiltonian is implemented, with external point charges
+ * and the GBSA / ALPB implicit solvents.  Entry points for the other methods
+ * and solvent models (GFN0/GFN1/GFN-FF, COSMO, CPCM-X) are exported and push
+ * an "unsupported" error, as the reference does for unavailable features.
  */
 #pragma once
 
@@ -90,9 +91,16 @@ extern XTB_API_ENTRY void XTB_API_CALL
 xtb_loadGFN1xTB(xtb_TEnvironment env, xtb_TMolecule mol, xtb_TCalculator calc, char* filename);
 extern XTB_API_ENTRY void XTB_API_CALL
 xtb_loadGFNFF(xtb_TEnvironment env, xtb_TMolecule mol, xtb_TCalculator calc, char* filename);
+/* implicit solvent on a loaded calculator: solvent name (the reference's aliases, "none"/"gas"/"vac"
+ * for none), solution state (NULL: 1 gsolv; 2 reference, 3 1 bar), temperature in K (NULL: 298.15),
+ * Lebedev grid points per atom (NULL: 230) and model (NULL or "gbsa": Still kernel with the GBSA
+ * parameters; "alpb": ALPB with the P16 kernel); "cosmo", "tmcosmo" and "cpcmx" push an error.
+ * Unknown solvents push "solvent: '<name>' is not parametrized" and "Could not add solvation model
+ * for '<name>'" [ref include/xtb.h:181-189] */
 extern XTB_API_ENTRY void XTB_API_CALL
 xtb_setSolvent(xtb_TEnvironment env, xtb_TCalculator calc, char* solvent, int* state, double* temp,
                int* grid, char* model);
+/* back to the gas phase [ref include/xtb.h:191-195] */
 extern XTB_API_ENTRY void XTB_API_CALL xtb_releaseSolvent(xtb_TEnvironment env, xtb_TCalculator calc);
 extern XTB_API_ENTRY void XTB_API_CALL
 xtb_setExternalCharges(xtb_TEnvironment env, xtb_TCalculator calc, int* n, int* numbers, double* charges,
@@ -131,12 +139,13 @@ extern XTB_API_ENTRY void XTB_API_CALL xtb_delResults(xtb_TResults* res);       
 extern XTB_API_ENTRY xtb_TResults XTB_API_CALL xtb_copyResults(xtb_TResults res);           /* [ref :268] */
 /* total energy in Hartree [ref include/xtb.h:272] */
 extern XTB_API_ENTRY void XTB_API_CALL xtb_getEnergy(xtb_TEnvironment env, xtb_TResults res, double* energy);
-/* gas phase only: pushes "not available" like a reference results object without solvation
- * [ref include/xtb.h:278] */
+/* pushes "Solvation energy is not available in results", as the reference does for every model but
+ * CPCM-X (the GBSA / ALPB parts are read with xtbgb_getSolvationEnergyParts) [ref include/xtb.h:278] */
 extern XTB_API_ENTRY void XTB_API_CALL xtb_getSolvationEnergy(xtb_TEnvironment env, xtb_TResults res, double* energy);
 /* gradient[natoms][3] in Hartree/Bohr [ref include/xtb.h:284] */
 extern XTB_API_ENTRY void XTB_API_CALL xtb_getGradient(xtb_TEnvironment env, xtb_TResults res, double* grad);
-/* no external charges: pushes "not available" [ref include/xtb.h:290] */
+/* gradient[npc][3] on the external charges of the last single point; without charges pushes
+ * "not available" [ref include/xtb.h:290] */
 extern XTB_API_ENTRY void XTB_API_CALL xtb_getPCGradient(xtb_TEnvironment env, xtb_TResults res, double* grad);
 /* virial[3][3] in Hartree: dE/d(strain) = sum_A R_A g_A^T of the molecule [ref include/xtb.h:296] */
 extern XTB_API_ENTRY void XTB_API_CALL xtb_getVirial(xtb_TEnvironment env, xtb_TResults res, double* virial);

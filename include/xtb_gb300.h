@@ -78,6 +78,28 @@ extern void xtbgb_setExternalChargesHardness(xtb_TEnvironment env, xtb_TCalculat
                                              const double* charges, const double* positions,
                                              const double* hardness);
 
+/* Implicit solvent of the last single point (an xtb_setSolvent calculator): parts[0..4] = free
+ * energy of solvation (contained in the total energy), its Born part (without the H-bond term),
+ * the H-bond correction, the surface term and the constant shift, all in Hartree at the final
+ * charges (getEnergyParts, src/solv/gbsa.f90:552-596; the reference keeps them in
+ * scc_results%g_solv / g_born / g_hb / g_sasa / g_shift, src/scf_module.F90:906-912, without a C
+ * getter: xtb_getSolvationEnergy serves only CPCM-X, include/xtb.h:276-280).  Returns 1 when the
+ * single point had a solvent, else 0 (parts then zero). */
+extern int xtbgb_getSolvationEnergyParts(xtb_TEnvironment env, xtb_TResults res, double* parts);
+
+/* Salt screening of the GBSA kernel (Debye-Hueckel; TSolvInput%ionStrength / %ionRad,
+ * src/solv/input.F90, src/solv/gbsa.f90:296-309, exercised by test/unit/test_gfn2.f90:310-381;
+ * the reference C API has no setter): ion strength in mol/L (0 switches it off) and ion radius
+ * in Bohr.  Kept across xtb_setSolvent calls on the calculator; needs the "gbsa" model. */
+extern void xtbgb_setSolventSalt(xtb_TEnvironment env, xtb_TCalculator calc, double ion_strength,
+                                 double ion_rad);
+
+/* Born kernel of the solvent set on the calculator: 0 Still (with the GBSA parameter sets), 1 P16
+ * (with the ALPB sets).  xtb_setSolvent ties the kernel to the model ("gbsa": Still, "alpb": P16);
+ * TSolvInput%kernel (src/solv/input.F90) decouples them, as test/unit/test_gfn2.f90:745-828 does
+ * with the ALPB correction on the Still kernel.  Call after xtb_setSolvent. */
+extern void xtbgb_setSolventKernel(xtb_TEnvironment env, xtb_TCalculator calc, int kernel);
+
 /* Autotuner (no counterpart in the reference).  Two choices of the single point depend on the
  * matrix size and the device: the form of the tridiagonalisation (row by row, or the
  * upper-triangle form with 4/3 n^3 flops) and the form of the eigenvector back-transformation

@@ -1,6 +1,6 @@
 /* Drop-in check: a plain C program driving libxtb_gb300.so exactly like the
- * reference's C API example drives libxtb (propyne, GFN2-xTB, 300 K, 30 iterations)
- * and asserting the reference's published values. */
+ * reference's C API example drives libxtb (propyne, GFN2-xTB, 300 K, 30 iterations; then in
+ * implicit water with GBSA and ALPB) and asserting the reference's published values. */
 #include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -61,6 +61,36 @@ int main(void) {
     ok &= check(dipole[2], -0.298279305689518, 1.0e-6, "dipole");
     ok &= check(wbo[9], 2.89823984265213, 1.0e-8, "bond order");
     ok &= check(grad[3 * 0 + 2], -0.74649908147372E-03, 1.0e-9, "gradient");
+    /* implicit water, GBSA then ALPB, each started from the previous result (c_api_example.c:114-163) */
+    {
+        char solvent[] = "h2o", gbsa[] = "gbsa", alpb[] = "alpb", bogus[] = "unobtainium";
+        xtb_setSolvent(env, calc, solvent, NULL, NULL, NULL, gbsa);
+        xtb_singlepoint(env, mol, calc, res);
+        xtb_getEnergy(env, res, &energy);
+        xtb_getCharges(env, res, q);
+        xtb_getDipole(env, res, dipole);
+        xtb_getBondOrders(env, res, wbo);
+        if (xtb_checkEnvironment(env)) return 9;
+        ok &= check(energy, -8.38393864716134, 1.0e-9, "GBSA energy");
+        ok &= check(q[5], 0.06090868805034, 1.0e-8, "GBSA charge");
+        ok &= check(dipole[2], -0.35455233974705, 1.0e-6, "GBSA dipole");
+        ok &= check(wbo[9], 2.89453979224265, 1.0e-8, "GBSA bond order");
+        xtb_releaseSolvent(env, calc);
+        xtb_setSolvent(env, calc, solvent, NULL, NULL, NULL, alpb);
+        xtb_singlepoint(env, mol, calc, res);
+        xtb_getEnergy(env, res, &energy);
+        xtb_getCharges(env, res, q);
+        xtb_getDipole(env, res, dipole);
+        xtb_getBondOrders(env, res, wbo);
+        if (xtb_checkEnvironment(env)) return 10;
+        ok &= check(energy, -8.384076843892, 1.0e-9, "ALPB energy");
+        ok &= check(q[5], 0.0644849340, 1.0e-8, "ALPB charge");
+        ok &= check(dipole[2], -0.3641866008, 1.0e-6, "ALPB dipole");
+        ok &= check(wbo[9], 2.8932146955, 1.0e-8, "ALPB bond order");
+        xtb_releaseSolvent(env, calc);
+        xtb_setSolvent(env, calc, bogus, NULL, NULL, NULL, gbsa);   /* not parametrized: an error */
+        if (!xtb_checkEnvironment(env)) return 11;
+    }
     xtb_delResults(&res);
     xtb_delCalculator(&calc);
     xtb_delMolecule(&mol);

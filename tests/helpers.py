@@ -54,8 +54,11 @@ def evaluate(expr, r):
         return (r.gradient if m.group(1) == "grad" else r.pcgrad).ravel()[int(m.group(2))]
     m = re.fullmatch(r"(q|dipole)\[(\d+)\]", expr)
     if m:
-        return getattr(r, m.group(1))[int(m.group(2))]
+        name = m.group(1)
+        vals = getattr(r, name) if hasattr(r, name) else r.charges     # engine results name them charges
+        return vals[int(m.group(2))]
     m = re.fullmatch(r"wbo\[(\d+)\]", expr)
     if m:
-        return r.wbo.ravel()[int(m.group(1))]
+        wbo = r.wbo if hasattr(r, "wbo") else r.bond_orders
+        return wbo.ravel()[int(m.group(1))]
     raise KeyError(expr)

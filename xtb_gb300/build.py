@@ -15,7 +15,7 @@ CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libxtb_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["api.cpp", "host_model.cpp", "engine.cu", "gfn2_kernels.cu", "integrals.cu", "linalg.cu", "noalloc.cu", "batch.cu", "batch_integrals.cu", "batch_runner.cpp", "serve.cpp", "splitgemm.cu", "tune.cu"]
+SOURCES = ["api.cpp", "host_model.cpp", "engine.cu", "gfn2_kernels.cu", "integrals.cu", "linalg.cu", "noalloc.cu", "batch.cu", "batch_integrals.cu", "batch_runner.cpp", "serve.cpp", "splitgemm.cu", "tune.cu", "solvation.cu"]
 
 
 def nvcc():

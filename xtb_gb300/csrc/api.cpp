@@ -258,10 +258,46 @@ void xtb_loadGFN1xTB(xtb_TEnvironment env, xtb_TMolecule, xtb_TCalculator, char*
 void xtb_loadGFNFF(xtb_TEnvironment env, xtb_TMolecule, xtb_TCalculator, char*) {
     unsupported(env, "GFN-FF", "xtb_api_loadGFNFF");
 }
-void xtb_setSolvent(xtb_TEnvironment env, xtb_TCalculator, char*, int*, double*, int*, char*) {
-    unsupported(env, "Implicit solvation", "xtb_api_setSolvent");
+// implicit solvent (setSolvent_api, src/api/calculator.f90:341-439): state, temperature, grid and
+// model are optional (NULL: gsolv, 298.15 K, 230 points, "gbsa")
+void xtb_setSolvent(xtb_TEnvironment env, xtb_TCalculator calc, char* solvent, int* state, double* temperature,
+                    int* grid, char* model) {
+    static const char* src = "xtb_api_setSolvent";
+    if (!check_env(env)) return;
+    if (!calc) {
+        env->error("Singlepoint calculator is not allocated", src);
+        return;
+    }
+    if (!calc->loaded) {
+        env->error("No calculator loaded to add solvation model", src);
+        return;
+    }
+    if (!solvent) {
+        env->error("Solvent name is missing", src);
+        return;
+    }
+    xg::SolventSpec spec;
+    const std::string err = xg::make_solvent_spec(solvent, model ? model : "gbsa", state ? *state : 1,
+                                                  temperature ? *temperature : 298.15, grid ? *grid : 230, spec);
+    if (!err.empty()) {
+        env->error(err, err == "Unknown solvation model" ? src : "solv_model_loadInternalParam");
+        if (err != "Unknown solvation model")
+            env->error(std::string("Could not add solvation model for '") + solvent + "'", src);
+        return;
+    }
+    spec.ion_strength = calc->set.solv.ion_strength;   // salt set through xtbgb_setSolventSalt is kept
+    spec.ion_rad = calc->set.solv.ion_rad;
+    calc->set.solv = spec;
 }
-void xtb_releaseSolvent(xtb_TEnvironment, xtb_TCalculator) {}
+
+void xtb_releaseSolvent(xtb_TEnvironment env, xtb_TCalculator calc) {
+    if (!check_env(env)) return;
+    if (!calc) {
+        env->error("Singlepoint calculator is not allocated", "xtb_api_setRelease");
+        return;
+    }
+    calc->set.solv = xg::SolventSpec();
+}
 namespace {
 // external point charges on a loaded calculator (setExternalCharges_api,
 // src/api/calculator.f90:482-537); gam null: the hardness of each charge's element
@@ -492,7 +528,25 @@ void xtb_hessian(xtb_TEnvironment env, xtb_TMolecule mol, xtb_TCalculator calc, 
         set.etemp = calc->set.etemp;
         set.maxiter = calc->set.maxiter;
         xg::BatchResults br;
-        xg::run_batch(mols, set, std::vector<int>(mols.size(), 1), br, &guesses);
+        if (calc->set.solv.on || !calc->set.pc_q.empty()) {
+            // an implicit solvent or external charges: the displaced points run on the plain
+            // engine, which carries both (the batched engine is gas phase only)
+            const size_t nm = mols.size();
+            br.status.assign(nm, xg::BST_OK);
+            br.gradient.assign(3 * (size_t)n * nm, 0.0);
+            br.dipole.assign(3 * nm, 0.0);
+            for (size_t k = 0; k < nm; ++k) {
+                xg::Wavefunction w = *chk0;
+                xg::SPResult r;
+                bool failed = false;
+                xg::run_singlepoint(mols[k], calc->set, w, r, false, failed);
+                if (failed) br.status[k] = xg::BST_NOT_CONVERGED;
+                std::copy(r.gradient.begin(), r.gradient.end(), br.gradient.begin() + 3 * (size_t)n * k);
+                std::copy(r.dipole.begin(), r.dipole.end(), br.dipole.begin() + 3 * k);
+            }
+        } else {
+            xg::run_batch(mols, set, std::vector<int>(mols.size(), 1), br, &guesses);
+        }
         const int N3 = 3 * n;
         std::vector<double> H((size_t)N3 * N3, 0.0);
         int bad = 0;
@@ -869,6 +923,65 @@ void xtbgb_getEnergyParts(xtb_TEnvironment env, xtb_TResults res, double* parts)
     const auto& s = res->sp;
     const double v[8] = {s.e_elec, s.e_rep, s.e_es, s.e_aes, s.e_axc, s.e_disp, s.e_atm, s.hl_gap};
     std::copy(v, v + 8, parts);
+}
+
+int xtbgb_getSolvationEnergyParts(xtb_TEnvironment env, xtb_TResults res, double* parts) {
+    if (!res_ready(env, res, "xtbgb_getSolvationEnergyParts", "Solvation energy") || !parts) return 0;
+    const auto& s = res->sp;
+    const double v[5] = {s.g_solv, s.g_born, s.g_hb, s.g_sasa, s.g_shift};
+    std::copy(v, v + 5, parts);
+    return s.solvated ? 1 : 0;
+}
+
+void xtbgb_setSolventKernel(xtb_TEnvironment env, xtb_TCalculator calc, int kernel) {
+    static const char* src = "xtbgb_setSolventKernel";
+    if (!check_env(env)) return;
+    if (!calc) {
+        env->error("Singlepoint calculator is not allocated", src);
+        return;
+    }
+    const xg::SolventSpec& cur = calc->set.solv;
+    if (!cur.on) {
+        env->error("No solvation model set", src);
+        return;
+    }
+    if (kernel != 0 && kernel != 1) {
+        env->error("Unknown Born kernel (0 Still, 1 P16)", src);
+        return;
+    }
+    if (kernel == 1 && cur.ion_strength > 0.0) {
+        env->error("Salt screening needs the GBSA (Still) kernel", src);
+        return;
+    }
+    xg::SolventSpec spec;
+    const std::string err = xg::make_solvent_spec(cur.solvent, cur.alpb ? "alpb" : "gbsa", cur.state, cur.temperature,
+                                                  cur.nang, spec, kernel);
+    if (!err.empty()) {
+        env->error(err, src);
+        return;
+    }
+    spec.ion_strength = cur.ion_strength;
+    spec.ion_rad = cur.ion_rad;
+    calc->set.solv = spec;
+}
+
+void xtbgb_setSolventSalt(xtb_TEnvironment env, xtb_TCalculator calc, double ion_strength, double ion_rad) {
+    static const char* src = "xtbgb_setSolventSalt";
+    if (!check_env(env)) return;
+    if (!calc) {
+        env->error("Singlepoint calculator is not allocated", src);
+        return;
+    }
+    if (!(ion_strength >= 0.0) || !(ion_rad >= 0.0) || !std::isfinite(ion_strength) || !std::isfinite(ion_rad)) {
+        env->error("Ion strength and ion radius must be finite and not negative", src);
+        return;
+    }
+    if (calc->set.solv.on && calc->set.solv.kernel != 0 && ion_strength > 0.0) {
+        env->error("Salt screening needs the GBSA (Still) kernel", src);
+        return;
+    }
+    calc->set.solv.ion_strength = ion_strength;
+    calc->set.solv.ion_rad = ion_rad;
 }
 
 void xtbgb_getPhaseTimes(xtb_TEnvironment env, xtb_TResults res, double* ms) {

@@ -128,12 +128,13 @@ __global__ void k_pc_grad_charges(DevMol m, int npc, const double* __restrict__ 
 // SCC energy from the current populations (electro + aniso_electro + edisp_scc + entropy;
 // src/scc_core.f90:686-722, src/aespot.F90:566-664, src/disp/dftd4.F90:821-864), and the shells'
 // energy in the field of external charges (electro_pcem, src/embedding.f90:261-280; vpc may be null)
-// out: [0] eel, [1] es, [2] eaes, [3] epol, [4] ed, [5] entropy term, [6] external charges
+// and the implicit solvent's energy (esolv[0] from solv_energy; null without a solvent)
+// out: [0] eel, [1] es, [2] eaes, [3] epol, [4] ed, [5] entropy term, [6] external charges, [7] solvent
 __global__ void k_scc_energy(int nsh, int nat, const double* __restrict__ qsh, const double* __restrict__ Jq,
                              const double* __restrict__ gam3, const double* __restrict__ eh0,
                              const double* __restrict__ eaes, const double* __restrict__ ed4,
                              const double* __restrict__ fermi_scal, const double* __restrict__ vpc,
-                             double* __restrict__ out) {
+                             const double* __restrict__ esolv, double* __restrict__ out) {
     __shared__ double red[32];
     double es = 0.0, h = 0.0, ea = 0.0, ep = 0.0, ed = 0.0, epc = 0.0;
     for (int s = threadIdx.x; s < nsh; s += blockDim.x) {
@@ -154,7 +155,9 @@ __global__ void k_scc_energy(int nsh, int nat, const double* __restrict__ qsh, c
     epc = block_sum(epc, red);
     if (threadIdx.x == 0) {
         const double ts = fermi_scal[0];
-        out[0] = es + h * EVTOAU + ea + ep + ed + epc + ts;
+        const double gsolv = esolv ? esolv[0] : 0.0;
+        out[0] = es + h * EVTOAU + ea + ep + ed + epc + gsolv + ts;
+        out[7] = gsolv;
         out[1] = es;
         out[2] = ea;
         out[3] = ep;
@@ -355,6 +358,11 @@ void run_singlepoint(const HostMol& hm, const SPSettings& set, Wavefunction& wfn
         *qout, *dq;
     double *pcq = nullptr, *pcx = nullptr, *pcg = nullptr, *vpc = nullptr, *pcgrad = nullptr;
     const int npc = (int)set.pc_q.size();
+    // implicit solvent: host model of this molecule, device state carved below
+    const bool solv = set.solv.on;
+    SolvHost sh;
+    SolvDev sd;
+    if (solv) build_solv_host(set.solv, nat, hm.Z.data(), hm.xyz.data(), sh);
     double* ormw;
     char* sgw = nullptr;
     unsigned char* piv;
@@ -413,6 +421,35 @@ void run_singlepoint(const HostMol& hm, const SPSettings& set, Wavefunction& wfn
         pcq = upload(ar, st, set.pc_q);
         pcx = upload(ar, st, set.pc_xyz);
         pcg = upload(ar, st, set.pc_gam);
+    }
+    if (solv) {
+        sd.nat = nat; sd.npt = sh.npt; sd.kernel = sh.kernel;
+        sd.alpb = sh.alpb; sd.lhb = sh.lhb; sd.lsalt = sh.lsalt;
+        sd.keps = sh.keps; sd.alpbet = sh.alpbet; sd.c1 = sh.c1; sd.gshift = sh.gshift; sd.eps = sh.eps;
+        sd.kappa = sh.kappa; sd.ion_rad = sh.ion_rad;
+        sd.vdwr = upload(ar, st, sh.vdwr);
+        sd.rho = upload(ar, st, sh.rho);
+        sd.svdw = upload(ar, st, sh.svdw);
+        sd.vdwsa = upload(ar, st, sh.vdwsa);
+        sd.wrp = upload(ar, st, sh.wrp);
+        sd.gamsasa = upload(ar, st, sh.gamsasa);
+        sd.hbmag = upload(ar, st, sh.hbmag);
+        sd.grid = upload(ar, st, sh.grid);
+        sd.nb_off = upload(ar, st, sh.nb_off);
+        sd.nb = upload(ar, st, sh.nb);
+        sd.brad = ar.take<double>(nat);
+        sd.dbrad = ar.take<double>(nat);
+        sd.sasa = ar.take<double>(nat);
+        sd.hbw = ar.take<double>(nat);
+        sd.ionscr = ar.take<double>(nat);
+        sd.discr = ar.take<double>(nat);
+        sd.bq = ar.take<double>(nat);
+        sd.grddb = ar.take<double>(nat);
+        sd.wsur = ar.take<double>(nat);
+        sd.sasap = ar.take<double>((size_t)nat * sh.npt);
+        sd.B = ar.take<double>(aa);
+        sd.aux = ar.take<double>(16);
+        sd.esolv = ar.take<double>(8);
     }
 
     // ---- device buffers
@@ -585,6 +622,7 @@ void run_singlepoint(const HostMol& hm, const SPSettings& set, Wavefunction& wfn
         if (hinfo != 0) throw std::runtime_error("overlap matrix is not positive definite (Cholesky failed)");
     }
 
+    if (solv) solv_update(st, sd, m.xyz);   // Born radii, surface, Born matrix (src/scf_module.F90:298-321)
     if (npc > 0) {   // shell potential of the external charges, fixed for the single point
         k_pc_potential<<<ceil_div((long)nsh * 32, 128), 128, 0, st>>>(m, npc, pcq, pcx, pcg, vpc);
         XG_LAUNCH_CHECK();
@@ -598,6 +636,7 @@ void run_singlepoint(const HostMol& hm, const SPSettings& set, Wavefunction& wfn
         iter = it;
         tm.mark(PH_HBUILD);
         d4_scc(st, m, gw, q, zeta, dzeta, Wz, vat, ed4);
+        if (solv) solv_shift(st, sd, q, vat);          // atomic potential B q (src/scc_core.f90:444-448)
         shell_shift(st, m, J, qsh, vat, shift, Jq);
         if (npc > 0) {   // the external charges' field enters every iteration's shift
             k_add_vec<<<ceil_div(nsh, 256), 256, 0, st>>>(nsh, vpc, shift);
@@ -644,12 +683,14 @@ void run_singlepoint(const HostMol& hm, const SPSettings& set, Wavefunction& wfn
         shell_shift(st, m, J, qsh, nullptr, T1, Jq);    // Jq for the electrostatic energy
         aes_energy(st, m, q, dipm, qp, gab3, gab5, eaes);
         d4_scc(st, m, gw, q, zeta, dzeta, Wz, vat, ed4);
-        k_scc_energy<<<1, 512, 0, st>>>(nsh, nat, qsh, Jq, m.sh_gam3, eh0, eaes, ed4, fscal, vpc, escal);
+        if (solv) solv_energy(st, sd, q);               // src/scc_core.f90:544-548
+        k_scc_energy<<<1, 512, 0, st>>>(nsh, nat, qsh, Jq, m.sh_gam3, eh0, eaes, ed4, fscal, vpc,
+                                        solv ? sd.esolv : nullptr, escal);
         XG_LAUNCH_CHECK();
         broyden_pack(st, m, qsh, dipm, qp, qout);
         broyden_step(st, bs, it, 0.4, qin, qout, dq, rms, nat);
         broyden_unpack(st, m, qin, qsh, dipm, qp, q);
-        XG_CUDA(cudaMemcpyAsync(hsc, escal, 7 * sizeof(double), cudaMemcpyDeviceToHost, st));
+        XG_CUDA(cudaMemcpyAsync(hsc, escal, 8 * sizeof(double), cudaMemcpyDeviceToHost, st));
         double hrms[2];
         XG_CUDA(cudaMemcpyAsync(hrms, rms, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
         XG_CUDA(cudaStreamSynchronize(st));
@@ -701,6 +742,13 @@ void run_singlepoint(const HostMol& hm, const SPSettings& set, Wavefunction& wfn
         k_pc_grad_atoms<<<ceil_div((long)nat * 32, 128), 128, 0, st>>>(m, npc, pcq, pcx, pcg, qsh, grad);
         k_pc_grad_charges<<<ceil_div((long)npc * 32, 128), 128, 0, st>>>(m, npc, pcq, pcx, pcg, qsh, pcgrad);
         XG_LAUNCH_CHECK();
+    }
+    double hsolv[4] = {0, 0, 0, 0};
+    if (solv) {   // gradient and energy parts at the final charges (src/scf_module.F90:761-776)
+        solv_gradient(st, sd, m.xyz, q, grad);
+        solv_energy(st, sd, q);
+        XG_CUDA(cudaMemcpyAsync(hsolv, sd.esolv, 4 * sizeof(double), cudaMemcpyDeviceToHost, st));
+        d2h += 4 * sizeof(double);
     }
     k_dipole<<<1, 256, 0, st>>>(nat, nao, m.xyz, d_zval, rows, dip);
     XG_LAUNCH_CHECK();
@@ -771,6 +819,12 @@ void run_singlepoint(const HostMol& hm, const SPSettings& set, Wavefunction& wfn
         res.phase_ms[PH_TOTAL] = t;
     }
     res.e_pc = hsc[6];
+    res.solvated = solv;
+    res.g_solv = hsolv[0];
+    res.g_hb = hsolv[1];
+    res.g_sasa = hsolv[2];
+    res.g_shift = hsolv[3];
+    res.g_born = hsolv[0] - hsolv[1] - hsolv[2] - hsolv[3];
     res.e_rep = hs2[0];
     res.e_atm = hs2[1];
     res.energy = eel + hs2[0] + hs2[1];

@@ -4,6 +4,7 @@
 #include <vector>
 
 #include "host_model.h"
+#include "solvation.h"
 #include "tune.h"
 
 namespace xg {
@@ -28,6 +29,8 @@ struct SPSettings {
     // external point charges (xtb_setExternalCharges): charge, position [k][3] (Bohr) and
     // hardness of charge k; empty for none
     std::vector<double> pc_q, pc_xyz, pc_gam;
+    // implicit solvent (xtb_setSolvent); solv.on == false for the gas phase
+    SolventSpec solv;
 };
 
 // Wavefunction kept between calls on the same results object (res%chk of the reference).
@@ -54,6 +57,10 @@ struct SPResult {
     double gnorm = 0.0;
     double e_pc = 0.0;                          // energy of the shells in the external charges' field
     std::vector<double> pcgrad;                 // [npc][3] gradient on the external charges
+    // implicit solvent: free energy of solvation (in the electronic energy) and its parts at the
+    // final charges (getEnergyParts, src/solv/gbsa.f90:552-596)
+    bool solvated = false;
+    double g_solv = 0.0, g_born = 0.0, g_hb = 0.0, g_sasa = 0.0, g_shift = 0.0;
     // device time per phase (ms), measured with CUDA events on the engine stream
     std::vector<double> phase_ms;
     // bytes copied host->device and device->host by this single point

@@ -72,6 +72,11 @@ def load_library(path=LIBPATH):
         "xtb_getPCGradient": (None, [vp, vp, dp]),
         "xtb_setExternalCharges": (None, [vp, vp, ip, ip, dp, dp]),
         "xtb_releaseExternalCharges": (None, [vp, vp]),
+        "xtb_setSolvent": (None, [vp, vp, C.c_char_p, ip, dp, ip, C.c_char_p]),
+        "xtb_releaseSolvent": (None, [vp, vp]),
+        "xtbgb_getSolvationEnergyParts": (C.c_int, [vp, vp, dp]),
+        "xtbgb_setSolventSalt": (None, [vp, vp, C.c_double, C.c_double]),
+        "xtbgb_setSolventKernel": (None, [vp, vp, C.c_int]),
         "xtbgb_deviceCount": (C.c_int, []),
         "xtbgb_getIterations": (None, [vp, vp, ip, ip]),
         "xtbgb_getEnergyParts": (None, [vp, vp, dp]),
@@ -191,6 +196,30 @@ class Calculator:
         self.env.check()
         self.npc = n
 
+    def set_solvent(self, solvent, model="gbsa", state=None, temperature=None, grid=None, ion_strength=None,
+                    ion_rad=None, kernel=None):
+        """Implicit solvent (xtb_setSolvent): model "gbsa" or "alpb"; state 1 gsolv, 2 reference,
+        3 1 bar; temperature in K; grid = Lebedev points per atom.  ion_strength (mol/L) and
+        ion_rad (Bohr) switch on salt screening of the GBSA kernel (xtbgb_setSolventSalt);
+        kernel "still" or "p16" replaces the model's Born kernel (xtbgb_setSolventKernel)."""
+        if ion_strength is not None:
+            self.lib.xtbgb_setSolventSalt(self.env.h, self.calc, float(ion_strength), float(ion_rad or 0.0))
+            self.env.check()
+        st = C.c_int(state) if state is not None else None
+        tp = C.c_double(temperature) if temperature is not None else None
+        gr = C.c_int(grid) if grid is not None else None
+        self.lib.xtb_setSolvent(self.env.h, self.calc, solvent.encode(), C.byref(st) if st is not None else None,
+                                C.byref(tp) if tp is not None else None, C.byref(gr) if gr is not None else None,
+                                model.encode() if model is not None else None)
+        self.env.check()
+        if kernel is not None:
+            self.lib.xtbgb_setSolventKernel(self.env.h, self.calc, {"still": 0, "p16": 1}[kernel])
+            self.env.check()
+
+    def release_solvent(self):
+        self.lib.xtb_releaseSolvent(self.env.h, self.calc)
+        self.env.check()
+
     def write_restart(self, path):
         """Write the last single point's wavefunction as an xtbrestart file (xtbgb_writeRestart)."""
         ok = self.lib.xtbgb_writeRestart(self.env.h, self.mol, self.res, str(path).encode())
@@ -282,6 +311,9 @@ class Results:
         self.gnorm = float(np.sqrt(np.sum(self.gradient ** 2)))
         self.phase_ms = np.zeros(len(PHASES))
         lib.xtbgb_getPhaseTimes(env.h, res, _dptr(self.phase_ms))
+        sp = np.zeros(5)
+        self.solvated = bool(lib.xtbgb_getSolvationEnergyParts(env.h, res, _dptr(sp)))
+        self.g_solv, self.g_born, self.g_hb, self.g_sasa, self.g_shift = sp
         self.pcgrad = None
         if getattr(calc, "npc", 0):
             self.pcgrad = np.zeros((calc.npc, 3))
