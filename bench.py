@@ -48,9 +48,20 @@ SERVED_METRIC = "single points/s + p99 latency, served vs plain GPU SCC, at |ΔE
 METRIC = "GFN2-xTB single points/s (energy + Mulliken charges + gradient on request)"
 PHASES = ("setup", "integrals", "cholesky", "hbuild", "stdform", "sytrd", "trieig", "backtransform", "density",
           "popmix", "gradient", "total")
-# DRAM bytes per matrix element of one k_sytrd launch, from the ncu capture of the (H2O)300
-# single point (26.43 MB read + 4.47 MB written for n = 1800); traffic grows as n^2.
+# DRAM bytes per matrix element of one tridiagonalisation launch; traffic grows as n^2.
+# Row form k_sytrd: ncu capture of the (H2O)300 single point (26.43 MB read + 4.47 MB written,
+# n = 1800).  Upper-triangle form k_sytrd_sym: ncu capture at n = 3072 (40.59 MB read +
+# 134.58 MB written).
 SYTRD_BYTES_PER_ELEM = (26.430976e6 + 4.467968e6) / 1800.0 ** 2
+SYTRD_SYM_BYTES_PER_ELEM = (40.590080e6 + 134.576640e6) / 3072.0 ** 2
+
+
+def sytrd_form(n):
+    """(kernel, DRAM bytes per launch, note) of the tridiagonalisation the engine runs at n AOs on
+    this device (the autotuner's crossover)."""
+    if n >= X.get_tuning()["sytrd_sym_min"]:
+        return "k_sytrd_sym", SYTRD_SYM_BYTES_PER_ELEM * float(n) ** 2, "traffic scaled as n^2 from the ncu capture at n = 3072"
+    return "k_sytrd", SYTRD_BYTES_PER_ELEM * float(n) ** 2, "traffic scaled as n^2 from the ncu capture at n = 1800"
 
 
 class ClockSampler:
@@ -388,13 +399,12 @@ def run_served(args, ws, rank):
                        "peak_resident": int(st1["peak_resident"])},
         "served_kernels": served_kernels,
         "autotune": tuned,
-        "roofline": {"bound": "fp64", "kernel": "k_sytrd", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
-                     "frac": ach / peak if peak else None,
-                     "traffic": SYTRD_BYTES_PER_ELEM * float(big.nao) ** 2, "traffic_unit": "bytes per launch",
+        "roofline": {"bound": "fp64", "kernel": sytrd_form(big.nao)[0], "achieved": ach, "peak": peak,
+                     "unit": "TFLOP/s", "frac": ach / peak if peak else None,
+                     "traffic": sytrd_form(big.nao)[1], "traffic_unit": "bytes per launch",
                      "launch_ms": sy_ms, "nao": int(big.nao), "launches": int(big.iterations),
                      "note": "4/3 n^3 FP64 flops per launch / CUDA-event time per launch, largest request of the "
-                             "stream in the sequential plain pass (no concurrent work); traffic scaled as n^2 from "
-                             "the ncu capture at n = 1800",
+                             "stream in the sequential plain pass (no concurrent work); " + sytrd_form(big.nao)[2],
                      "peak_detail": peak_detail},
         # the whole run against the FP64 pipe: FP64-only algorithmic work of all requests (plain
         # engine: standard form n^3 + tridiagonal reduction 4/3 n^3 per SCC iteration, the counts
@@ -489,10 +499,10 @@ def run_plain(args, ws, rank):
         "parity": fixture_parity({"h2o300": "h2o_300_seed1"}.get(args.workload, ""), r),
         "phase_ms_per_step": {k: round(float(v), 3) for k, v in zip(PHASES, per_step)},
         "algorithmic_tflops_per_sp": sp_flops(nao, nocc, iters) / 1e12,
-        "roofline": {"bound": "fp64", "kernel": "k_sytrd", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
+        "roofline": {"bound": "fp64", "kernel": sytrd_form(nao)[0], "achieved": ach, "peak": peak, "unit": "TFLOP/s",
                      "frac": ach / peak if peak else None, "launch_ms": sy_ms,
-                     "traffic": SYTRD_BYTES_PER_ELEM * float(nao) ** 2, "traffic_unit": "bytes per launch",
-                     "note": "4/3 n^3 FP64 flops per launch / CUDA-event time per launch",
+                     "traffic": sytrd_form(nao)[1], "traffic_unit": "bytes per launch",
+                     "note": "4/3 n^3 FP64 flops per launch / CUDA-event time per launch; " + sytrd_form(nao)[2],
                      "peak_detail": peak_detail},
         "clocks": clk,
     }
@@ -571,9 +581,9 @@ def run_split(args, ws, rank):
                 "d2h_bytes_per_step": int(r.d2h_bytes)},
         "gpu_launches": int(launches),
         "phase_ms_per_step": {k: round(float(v), 3) for k, v in zip(PHASES, per)},
-        "roofline": {"bound": "fp64", "kernel": "k_sytrd", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
+        "roofline": {"bound": "fp64", "kernel": sytrd_form(n)[0], "achieved": ach, "peak": peak, "unit": "TFLOP/s",
                      "frac": ach / peak if peak else None, "launch_ms": sy,
-                     "traffic": SYTRD_BYTES_PER_ELEM * float(n) ** 2, "traffic_unit": "bytes per launch",
+                     "traffic": sytrd_form(n)[1], "traffic_unit": "bytes per launch",
                      "note": "the tridiagonalisation stays FP64 and dominates; split products are in "
                              "backtransform/density/gradient",
                      "peak_detail": peak_detail},
