@@ -3,7 +3,8 @@
 // C = alpha op(A) op(B) + beta C for FP64 operands, computed from fixed-point slices:
 // every row of op(A) (column of op(B)) is scaled by a power of two s_i (t_j) so that
 // |x| < 1, and cut into S digits of 8 bits, x / s = sum_{p=1..S} d_p 2^(-8p) with integer
-// d_p in [-256, 256] -- exactly representable in BF16.  A digit product d_p e_q is exact in
+// d_p in [-256, 256] -- exactly representable in BF16 (the cut rounds x / s 2^(8S) to a 64-bit
+// integer and takes its balanced base-256 digits with integer arithmetic).  A digit product d_p e_q is exact in
 // FP32 (16 bits).  Products are grouped by level p + q (levels beyond S - 1 carry less than
 // 2^(-8S) of the result and are dropped); the two leading levels are summed exactly over K
 // chunks and recombined as integers, the others in FP32 (see the kernel), and the result is
@@ -29,6 +30,33 @@ namespace {
 
 constexpr int SG_KT = 32;               // K is padded to a multiple of this (one pipeline stage)
 
+// 2^(8S - e) for scaling an element of a row with maximum magnitude in [2^(e-1), 2^e) to S
+// digits, or 0 when that power of two is not a normal double (rows of subnormal magnitude)
+template <int S>
+__device__ __forceinline__ double digit_scale(int e) {
+    const int sh = 8 * S - e;
+    return sh <= 1023 ? ldexp(1.0, sh) : 0.0;
+}
+
+// The S balanced base-256 digits of y = x 2^(8S - e), |x| < 2^e: v = round(y) as a 64-bit
+// integer (|v| <= 2^(8S) <= 2^56, and y itself is x with a shifted exponent), then the digits
+// from the least significant one, each in [-128, 127], the leading one taking the rest (in
+// [-256, 256]).  sum_p d_p 2^(8(S-1-p)) = v, so x 2^-e = sum_p d_p 2^(-8(p+1)) up to the rounding
+// of the last digit -- the representation the products need, with one FP64 multiply and one
+// conversion per element; the digit arithmetic is integer.
+template <int S>
+__device__ __forceinline__ void cut_digits(double x, double sc, int e, __nv_bfloat16 (&d)[S]) {
+    const double y = sc != 0.0 ? x * sc : ldexp(x, 8 * S - e);
+    long long v = __double2ll_rn(y);
+#pragma unroll
+    for (int p = S - 1; p > 0; --p) {
+        const long long t = ((v + 128) & 255) - 128;
+        d[p] = __float2bfloat16_rn((float)t);
+        v = (v - t) >> 8;
+    }
+    d[0] = __float2bfloat16_rn((float)v);
+}
+
 // Digits of row r of X (element k = trans ? X[k*ldx + r] : X[r*ldx + k]), k < K (and k < *dK),
 // zero beyond; out[p][r][k] for k < Kp.  One warp per row.
 template <int S>
@@ -47,15 +75,12 @@ __global__ void k_split_rows(int R, int K, int Kp, const double* __restrict__ X,
     }
     if (lane == 0) scale[r] = (mx > 0.0) ? ldexp(1.0, e) : 1.0;
     const size_t plane = (size_t)R * Kp;
+    const double sc = digit_scale<S>(e);
     for (int k = lane; k < Kp; k += 32) {
-        double x = (k < kmax && mx > 0.0) ? ldexp(at(k), -e) : 0.0;
+        __nv_bfloat16 d[S];
+        cut_digits<S>((k < kmax && mx > 0.0) ? at(k) : 0.0, sc, e, d);
 #pragma unroll
-        for (int p = 0; p < S; ++p) {
-            x *= 256.0;
-            const double d = rint(x);
-            x -= d;
-            out[p * plane + (size_t)r * Kp + k] = __double2bfloat16(d);
-        }
+        for (int p = 0; p < S; ++p) out[p * plane + (size_t)r * Kp + k] = d[p];
     }
 }
 
@@ -101,17 +126,14 @@ __global__ void __launch_bounds__(256) k_col_digits(int R, int K, int Kp, const 
     int e = 0;
     if (mx > 0.0) frexp(mx, &e);
     if (blockIdx.y == 0 && w == 0 && r < R) scale[r] = (mx > 0.0) ? ldexp(1.0, e) : 1.0;
+    const double sc = digit_scale<S>(e);
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
         const int kk = w + 8 * j, k = k0 + kk;
-        double x = (r < R && k < kmax && mx > 0.0) ? ldexp(X[(size_t)k * ldx + r], -e) : 0.0;
+        __nv_bfloat16 d[S];
+        cut_digits<S>((r < R && k < kmax && mx > 0.0) ? X[(size_t)k * ldx + r] : 0.0, sc, e, d);
 #pragma unroll
-        for (int p = 0; p < S; ++p) {
-            x *= 256.0;
-            const double d = rint(x);
-            x -= d;
-            dig[p][l][kk] = __double2bfloat16(d);
-        }
+        for (int p = 0; p < S; ++p) dig[p][l][kk] = d[p];
     }
     __syncthreads();
     const size_t plane = (size_t)R * Kp;
