@@ -720,65 +720,77 @@ __device__ inline void d_broyden(int nbr, int it, int maxit, double alpha, doubl
     const double inv = s_inv;
     for (int i = threadIdx.x; i < nbr; i += blockDim.x) dfr[i] *= inv;
     __syncthreads();
-    // a(i, r) for i <= r, c(i) = omega_i df_i . dq
+    // a(i, r) for i <= r, c(i) = omega_i df_i . dq: one warp per history row, warp sums only
     double* c = work;                      // [maxit]
     double* beta = work + maxit;           // [it1 x it1]
     double* binv = beta + (size_t)maxit * maxit;
-    for (int i = 0; i < it1; ++i) {
-        const double* dfi = df + (size_t)i * nbr;
-        double s1 = 0.0, s2 = 0.0;
-        for (int k = threadIdx.x; k < nbr; k += blockDim.x) {
-            s1 += dfi[k] * dfr[k];
-            s2 += dfi[k] * dq[k];
-        }
-        s1 = block_sum(s1, red);
-        s2 = block_sum(s2, red);
-        if (threadIdx.x == 0) {
-            amat[(size_t)i * maxit + r] = s1;
-            amat[(size_t)r * maxit + i] = s1;
-            c[i] = omega[i] * s2;
-        }
-    }
-    __syncthreads();
-    // beta = omega_i omega_j a_ij + omega0^2 delta_ij ; invert by Gauss-Jordan with partial pivoting
-    for (int t = threadIdx.x; t < it1 * it1; t += blockDim.x) {
-        const int i = t / it1, j = t % it1;
-        beta[t] = omega[i] * omega[j] * amat[(size_t)i * maxit + j] + (i == j ? omega0 * omega0 : 0.0);
-        binv[t] = (i == j) ? 1.0 : 0.0;
-    }
-    __syncthreads();
-    __shared__ int piv;
-    for (int k = 0; k < it1; ++k) {
-        if (threadIdx.x == 0) {
-            int p = k;
-            double best = fabs(beta[k * it1 + k]);
-            for (int i = k + 1; i < it1; ++i)
-                if (fabs(beta[i * it1 + k]) > best) { best = fabs(beta[i * it1 + k]); p = i; }
-            piv = p;
-        }
-        __syncthreads();
-        const int p = piv;
-        if (p != k)
-            for (int j = threadIdx.x; j < it1; j += blockDim.x) {
-                double t1 = beta[k * it1 + j]; beta[k * it1 + j] = beta[p * it1 + j]; beta[p * it1 + j] = t1;
-                double t2 = binv[k * it1 + j]; binv[k * it1 + j] = binv[p * it1 + j]; binv[p * it1 + j] = t2;
+    {
+        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+        for (int i = wid; i < it1; i += nw) {
+            const double* dfi = df + (size_t)i * nbr;
+            double s1 = 0.0, s2 = 0.0;
+            for (int k = lane; k < nbr; k += 32) {
+                s1 += dfi[k] * dfr[k];
+                s2 += dfi[k] * dq[k];
             }
-        __syncthreads();
-        const double pk = beta[k * it1 + k];
-        for (int j = threadIdx.x; j < it1; j += blockDim.x) { beta[k * it1 + j] /= pk; binv[k * it1 + j] /= pk; }
-        __syncthreads();
-        for (int t = threadIdx.x; t < it1 * it1; t += blockDim.x) {
-            const int i = t / it1, j = t % it1;
-            if (i == k) continue;
-            const double f = beta[i * it1 + k];
-            if (j != k) beta[t] -= f * beta[k * it1 + j];
-            binv[t] -= f * binv[k * it1 + j];
+            s1 = warp_sum(s1);
+            s2 = warp_sum(s2);
+            if (lane == 0) {
+                amat[(size_t)i * maxit + r] = s1;
+                amat[(size_t)r * maxit + i] = s1;
+                c[i] = omega[i] * s2;
+            }
         }
-        __syncthreads();
-        for (int i = threadIdx.x; i < it1; i += blockDim.x)
-            if (i != k) beta[i * it1 + k] = 0.0;
-        __syncthreads();
     }
+    __syncthreads();
+    // beta = omega_i omega_j a_ij + omega0^2 delta_ij, inverted by Gauss-Jordan with partial
+    // pivoting; the history is short, so one warp does it with warp barriers only
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+        for (int t = lane; t < it1 * it1; t += 32) {
+            const int i = t / it1, j = t % it1;
+            beta[t] = omega[i] * omega[j] * amat[(size_t)i * maxit + j] + (i == j ? omega0 * omega0 : 0.0);
+            binv[t] = (i == j) ? 1.0 : 0.0;
+        }
+        __syncwarp();
+        for (int k = 0; k < it1; ++k) {
+            // pivot: the row of largest magnitude in column k (first one on ties)
+            int p = k;
+            double best = -1.0;
+            for (int i = k + lane; i < it1; i += 32) {
+                const double v = fabs(beta[i * it1 + k]);
+                if (v > best) { best = v; p = i; }
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+                const int op = __shfl_xor_sync(0xffffffffu, p, o);
+                if (ob > best || (ob == best && op < p)) { best = ob; p = op; }
+            }
+            if (p != k)
+                for (int j = lane; j < it1; j += 32) {
+                    double t1 = beta[k * it1 + j]; beta[k * it1 + j] = beta[p * it1 + j]; beta[p * it1 + j] = t1;
+                    double t2 = binv[k * it1 + j]; binv[k * it1 + j] = binv[p * it1 + j]; binv[p * it1 + j] = t2;
+                }
+            __syncwarp();
+            const double pk = beta[k * it1 + k];
+            __syncwarp();
+            for (int j = lane; j < it1; j += 32) { beta[k * it1 + j] /= pk; binv[k * it1 + j] /= pk; }
+            __syncwarp();
+            for (int t = lane; t < it1 * it1; t += 32) {
+                const int i = t / it1, j = t % it1;
+                if (i == k) continue;
+                const double f = beta[i * it1 + k];
+                if (j != k) beta[t] -= f * beta[k * it1 + j];
+                binv[t] -= f * binv[k * it1 + j];
+            }
+            __syncwarp();
+            for (int i = lane; i < it1; i += 32)
+                if (i != k) beta[i * it1 + k] = 0.0;
+            __syncwarp();
+        }
+    }
+    __syncthreads();
     // gamma_j = sum_i c_i binv_ij ; store omega_j * gamma_j in work tail
     double* og = binv + (size_t)maxit * maxit;
     for (int j = threadIdx.x; j < it1; j += blockDim.x) {

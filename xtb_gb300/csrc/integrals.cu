@@ -2,6 +2,7 @@
 //
 // Split from the other GFN2 kernels so that the heavily unrolled per-(l_i, l_j)
 // templates compile in their own translation unit.
+#include <algorithm>
 #include <cmath>
 
 #include "gfn2_kernels.h"
@@ -20,6 +21,35 @@ __global__ void k_sdqh0(DevMol m, const double* __restrict__ se, double intcut, 
 }
 
 
+// one warp per shell pair (classes with many Cartesian component pairs)
+constexpr int WI_WARPS = 4;
+constexpr int WI_MAX_BLOCKS = 4096;
+
+template <int LI, int LJ>
+__global__ void __launch_bounds__(32 * WI_WARPS) k_sdqh0_w(DevMol m, const double* __restrict__ se, double intcut,
+                                                          long npairs, double* __restrict__ S, double* __restrict__ D,
+                                                          double* __restrict__ Q, double* __restrict__ H0) {
+    __shared__ double sm[WI_WARPS][WarpInt<LI, LJ>::SMEM];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (long t = (long)blockIdx.x * WI_WARPS + w; t < npairs; t += (long)gridDim.x * WI_WARPS)
+        d_sdqh0_warp<LI, LJ>(m, se, intcut, S, D, Q, H0, t, lane, sm[w]);
+}
+
+template <int LI, int LJ>
+__global__ void __launch_bounds__(32 * WI_WARPS) k_grad_sdqh0_w(DevMol m, const double* __restrict__ se, double intcut,
+                                                               long npairs, const double* __restrict__ P,
+                                                               const double* __restrict__ Pew,
+                                                               const double* __restrict__ shift,
+                                                               const double* __restrict__ vs,
+                                                               const double* __restrict__ vd,
+                                                               const double* __restrict__ vq, double* __restrict__ grad,
+                                                               double* __restrict__ dhdcn) {
+    __shared__ double sm[WI_WARPS][WarpInt<LI, LJ>::SMEM];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (long t = (long)blockIdx.x * WI_WARPS + w; t < npairs; t += (long)gridDim.x * WI_WARPS)
+        d_grad_sdqh0_warp<LI, LJ>(m, se, intcut, P, Pew, shift, vs, vd, vq, grad, dhdcn, t, lane, sm[w]);
+}
+
 void build_sdqh0(cudaStream_t st, const DevMol& m, const double* se, Thresholds th, double* S, double* D, double* Q,
                  double* H0) {
     const size_t nn = (size_t)m.nao * m.nao;
@@ -29,17 +59,19 @@ void build_sdqh0(cudaStream_t st, const DevMol& m, const double* se, Thresholds 
     XG_CUDA(cudaMemsetAsync(Q, 0, 6 * nn * sizeof(double), st));
     const long np = (long)m.nsh * (m.nsh + 1) / 2;
     const int nb = ceil_div(np, 128);
+    const int nw = (int)std::min<long>(WI_MAX_BLOCKS, ceil_div(np, WI_WARPS));
+    // s-s and p-s pairs: one thread per pair; the others: one warp per pair
     k_sdqh0<0, 0><<<nb, 128, 0, st>>>(m, se, th.intcut, np, S, D, Q, H0);
     XG_LAUNCH_CHECK();
     k_sdqh0<1, 0><<<nb, 128, 0, st>>>(m, se, th.intcut, np, S, D, Q, H0);
     XG_LAUNCH_CHECK();
-    k_sdqh0<1, 1><<<nb, 128, 0, st>>>(m, se, th.intcut, np, S, D, Q, H0);
+    k_sdqh0_w<1, 1><<<nw, 32 * WI_WARPS, 0, st>>>(m, se, th.intcut, np, S, D, Q, H0);
     XG_LAUNCH_CHECK();
-    k_sdqh0<2, 0><<<nb, 128, 0, st>>>(m, se, th.intcut, np, S, D, Q, H0);
+    k_sdqh0_w<2, 0><<<nw, 32 * WI_WARPS, 0, st>>>(m, se, th.intcut, np, S, D, Q, H0);
     XG_LAUNCH_CHECK();
-    k_sdqh0<2, 1><<<nb, 128, 0, st>>>(m, se, th.intcut, np, S, D, Q, H0);
+    k_sdqh0_w<2, 1><<<nw, 32 * WI_WARPS, 0, st>>>(m, se, th.intcut, np, S, D, Q, H0);
     XG_LAUNCH_CHECK();
-    k_sdqh0<2, 2><<<nb, 128, 0, st>>>(m, se, th.intcut, np, S, D, Q, H0);
+    k_sdqh0_w<2, 2><<<nw, 32 * WI_WARPS, 0, st>>>(m, se, th.intcut, np, S, D, Q, H0);
     XG_LAUNCH_CHECK();
 }
 
@@ -61,17 +93,18 @@ void grad_sdqh0(cudaStream_t st, const DevMol& m, Thresholds th, const double* s
                 double* dhdcn) {
     const long np = (long)m.nsh * (m.nsh + 1) / 2;
     const int nb = ceil_div(np, 128);
+    const int nw = (int)std::min<long>(WI_MAX_BLOCKS, ceil_div(np, WI_WARPS));
     k_grad_sdqh0<0, 0><<<nb, 128, 0, st>>>(m, se, th.intcut, np, P, Pew, shift, vs, vd, vq, grad, dhdcn);
     XG_LAUNCH_CHECK();
     k_grad_sdqh0<1, 0><<<nb, 128, 0, st>>>(m, se, th.intcut, np, P, Pew, shift, vs, vd, vq, grad, dhdcn);
     XG_LAUNCH_CHECK();
-    k_grad_sdqh0<1, 1><<<nb, 128, 0, st>>>(m, se, th.intcut, np, P, Pew, shift, vs, vd, vq, grad, dhdcn);
+    k_grad_sdqh0_w<1, 1><<<nw, 32 * WI_WARPS, 0, st>>>(m, se, th.intcut, np, P, Pew, shift, vs, vd, vq, grad, dhdcn);
     XG_LAUNCH_CHECK();
-    k_grad_sdqh0<2, 0><<<nb, 128, 0, st>>>(m, se, th.intcut, np, P, Pew, shift, vs, vd, vq, grad, dhdcn);
+    k_grad_sdqh0_w<2, 0><<<nw, 32 * WI_WARPS, 0, st>>>(m, se, th.intcut, np, P, Pew, shift, vs, vd, vq, grad, dhdcn);
     XG_LAUNCH_CHECK();
-    k_grad_sdqh0<2, 1><<<nb, 128, 0, st>>>(m, se, th.intcut, np, P, Pew, shift, vs, vd, vq, grad, dhdcn);
+    k_grad_sdqh0_w<2, 1><<<nw, 32 * WI_WARPS, 0, st>>>(m, se, th.intcut, np, P, Pew, shift, vs, vd, vq, grad, dhdcn);
     XG_LAUNCH_CHECK();
-    k_grad_sdqh0<2, 2><<<nb, 128, 0, st>>>(m, se, th.intcut, np, P, Pew, shift, vs, vd, vq, grad, dhdcn);
+    k_grad_sdqh0_w<2, 2><<<nw, 32 * WI_WARPS, 0, st>>>(m, se, th.intcut, np, P, Pew, shift, vs, vd, vq, grad, dhdcn);
     XG_LAUNCH_CHECK();
 }
 

@@ -396,4 +396,336 @@ __device__ inline void d_grad_sdqh0(DevMol m, const double* __restrict__ se, dou
     atomicAdd(&dhdcn[jat], dcn * (-m.sh_kcn[jsh]));
 }
 
+
+// ================================================================== one warp per shell pair
+// The same integrals and gradient contraction with a warp per shell pair, for the classes whose
+// per-thread form would hold hundreds of doubles (p-p, d-s, d-p, d-d).  Per primitive pair the
+// lanes share the 1D moment integrals through the warp's shared-memory slice, and each lane owns
+// one or two Cartesian component pairs (a, b) with their contraction weights in registers.
+
+// shared-memory doubles one warp needs for class (LI, LJ): the gradient's 1D integrals about
+// two centres (powers up to LI + 1), or the integrals' 1D table plus the Cartesian results
+template <int LI, int LJ>
+struct WarpInt {
+    static constexpr int NV = 3 * 3 * (LI + 1) * (LJ + 1);       // [x][e][i][j]
+    static constexpr int NRES = Cart<LI>::n * Cart<LJ>::n * 10;  // [a*NCJ + b][k]
+    static constexpr int NG = 2 * 3 * 3 * (LI + 2) * (LJ + 1);   // [o][x][e][i][j]
+    static constexpr int SMEM = (NV + NRES > NG ? NV + NRES : NG);
+};
+
+// one entry (i, j) of mom1d: s_e = int (x-A)^i (x-B)^j (x-C)^e exp(-g (x-P)^2) dx / sqrt(pi/g)
+template <int MT>
+__device__ __forceinline__ void mom1d_entry(double PA, double PB, double PC, double g, int i, int j, double& s0,
+                                            double& s1, double& s2) {
+    double t[MT];
+    const double h = 0.5 / g;
+    t[0] = 1.0;
+    t[1] = 0.0;
+#pragma unroll
+    for (int k = 2; k < MT; ++k) t[k] = (k - 1) * h * t[k - 2];
+    const int binom[4][4] = {{1, 0, 0, 0}, {1, 1, 0, 0}, {1, 2, 1, 0}, {1, 3, 3, 1}};
+    double pa[4], pb[4];
+    pa[0] = pb[0] = 1.0;
+#pragma unroll
+    for (int k = 1; k < 4; ++k) {
+        pa[k] = pa[k - 1] * PA;
+        pb[k] = pb[k - 1] * PB;
+    }
+    s0 = s1 = s2 = 0.0;
+    for (int a = 0; a <= i; ++a)
+        for (int b = 0; b <= j; ++b) {
+            const double c = binom[i][a] * binom[j][b] * pa[i - a] * pb[j - b];
+            const int mm = a + b;
+            s0 += c * t[mm];
+            s1 += c * (t[mm + 1] + PC * t[mm]);
+            s2 += c * (t[mm + 2] + 2.0 * PC * t[mm + 1] + PC * PC * t[mm]);
+        }
+}
+
+template <int LI, int LJ>
+__device__ inline void d_sdqh0_warp(const DevMol& m, const double* __restrict__ se, double intcut, double* __restrict__ S,
+                                    double* __restrict__ D, double* __restrict__ Q, double* __restrict__ H0, long t,
+                                    int lane, double* __restrict__ sm) {
+    int ish, jsh;
+    if (!canonical_pair<LI, LJ>(m, t, ish, jsh)) return;
+    constexpr int NCI = Cart<LI>::n, NCJ = Cart<LJ>::n, NSI = Sph<LI>::n, NSJ = Sph<LJ>::n;
+    constexpr int NAB = NCI * NCJ, LJ1 = LJ + 1, SZ = (LI + 1) * (LJ + 1);
+    static_assert(NAB <= 64, "at most two component pairs per lane");
+    const int iat = m.sh_atom[ish], jat = m.sh_atom[jsh];
+    const bool same = iat == jat;
+    const double A[3] = {m.xyz[3 * iat], m.xyz[3 * iat + 1], m.xyz[3 * iat + 2]};
+    const double B[3] = {m.xyz[3 * jat], m.xyz[3 * jat + 1], m.xyz[3 * jat + 2]};
+    const double r2 = sqi(A[0] - B[0]) + sqi(A[1] - B[1]) + sqi(A[2] - B[2]);
+    const size_t nao = m.nao, nn = nao * nao;
+    const int ai0 = m.sh_ao[ish], aj0 = m.sh_ao[jsh];
+    if (same && ish == jsh && lane < NSI) {
+        S[(ai0 + lane) * nao + ai0 + lane] = 1.0;
+        H0[(ai0 + lane) * nao + ai0 + lane] = se[ish];
+    }
+    if (r2 > 2000.0) return;
+    double* v = sm;                              // [x][e][i][j]
+    double* res = sm + WarpInt<LI, LJ>::NV;      // [ab][k]
+    double acc[2][10];
+    int ab_x[2][3], ab_y[2][3];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int ab = lane + 32 * h;
+#pragma unroll
+        for (int k = 0; k < 10; ++k) acc[h][k] = 0.0;
+        int ix = 0, iy = 0, iz = 0, jx = 0, jy = 0, jz = 0;
+        if (ab < NAB) {
+            cart_pow(LI, ab / NCJ, ix, iy, iz);
+            cart_pow(LJ, ab % NCJ, jx, jy, jz);
+        }
+        ab_x[h][0] = ix; ab_x[h][1] = iy; ab_x[h][2] = iz;
+        ab_y[h][0] = jx; ab_y[h][1] = jy; ab_y[h][2] = jz;
+    }
+    const double sqrtpi = 1.7724538509055160273;
+    const int npi = m.sh_nprim[ish], npj = m.sh_nprim[jsh];
+    for (int p = 0; p < npi; ++p) {
+        const double ai = m.sh_alpha[ish * MAXPRIM + p], ci = m.sh_coef[ish * MAXPRIM + p];
+        for (int q = 0; q < npj; ++q) {
+            const double aj = m.sh_alpha[jsh * MAXPRIM + q], cj = m.sh_coef[jsh * MAXPRIM + q];
+            double est = r2 * ai * aj;
+            if (est > intcut * (ai + aj)) continue;
+            const double g = ai + aj, ab = 1.0 / g;
+            est *= ab;
+            const double sab = sqrtpi * sqrt(ab);
+            const double cc = exp(-est) * (sab * sab * sab) * ci * cj;
+            __syncwarp();
+            for (int u = lane; u < 3 * SZ; u += 32) {
+                const int x = u / SZ, i = (u % SZ) / LJ1, j = u % LJ1;
+                const double P = (ai * A[x] + aj * B[x]) * ab;
+                double s0, s1, s2;
+                mom1d_entry<LI + LJ + 3>(P - A[x], P - B[x], P, g, i, j, s0, s1, s2);
+                v[(x * 3 + 0) * SZ + i * LJ1 + j] = s0;
+                v[(x * 3 + 1) * SZ + i * LJ1 + j] = s1;
+                v[(x * 3 + 2) * SZ + i * LJ1 + j] = s2;
+            }
+            __syncwarp();
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                if (lane + 32 * h >= NAB) continue;
+                const int* pi = ab_x[h];
+                const int* pj = ab_y[h];
+#pragma unroll
+                for (int k = 0; k < 10; ++k)
+                    acc[h][k] += cc * v[(0 * 3 + c_mom[k][0]) * SZ + pi[0] * LJ1 + pj[0]] *
+                                 v[(1 * 3 + c_mom[k][1]) * SZ + pi[1] * LJ1 + pj[1]] *
+                                 v[(2 * 3 + c_mom[k][2]) * SZ + pi[2] * LJ1 + pj[2]];
+            }
+        }
+    }
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+        if (lane + 32 * h < NAB)
+#pragma unroll
+            for (int k = 0; k < 10; ++k) res[(lane + 32 * h) * 10 + k] = acc[h][k];
+    __syncwarp();
+    const double hfac = same ? 0.0 : h0_factor(m, se, ish, jsh, sqrt(r2));
+    for (int su = lane; su < NSI * NSJ; su += 32) {
+        const int s = su / NSJ, u = su % NSJ;
+        double val[10];
+#pragma unroll
+        for (int k = 0; k < 10; ++k) val[k] = 0.0;
+        for (int a = 0; a < NCI; ++a) {
+            const double ta = tr(LI, s, a);
+            if (ta == 0.0) continue;
+            for (int b = 0; b < NCJ; ++b) {
+                const double w = ta * tr(LJ, u, b);
+                if (w == 0.0) continue;
+#pragma unroll
+                for (int k = 0; k < 10; ++k) val[k] += w * res[(a * NCJ + b) * 10 + k];
+            }
+        }
+        const size_t ia = ai0 + s, ja = aj0 + u;
+        if (!same) {
+            S[ia * nao + ja] = val[0];
+            S[ja * nao + ia] = val[0];
+            H0[ia * nao + ja] = hfac * val[0];
+            H0[ja * nao + ia] = hfac * val[0];
+        }
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            D[k * nn + ia * nao + ja] = val[1 + k];
+            D[k * nn + ja * nao + ia] = val[1 + k];
+        }
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            Q[k * nn + ia * nao + ja] = val[4 + k];
+            Q[k * nn + ja * nao + ia] = val[4 + k];
+        }
+    }
+    __syncwarp();
+}
+
+template <int LI, int LJ>
+__device__ inline void d_grad_sdqh0_warp(const DevMol& m, const double* __restrict__ se, double intcut,
+                                         const double* __restrict__ P, const double* __restrict__ Pew,
+                                         const double* __restrict__ shift, const double* __restrict__ vs,
+                                         const double* __restrict__ vd, const double* __restrict__ vq,
+                                         double* __restrict__ grad, double* __restrict__ dhdcn, long t, int lane,
+                                         double* __restrict__ sm) {
+    int ish, jsh;
+    if (!canonical_pair<LI, LJ>(m, t, ish, jsh)) return;
+    const int iat = m.sh_atom[ish], jat = m.sh_atom[jsh];
+    if (iat == jat) return;
+    constexpr int NCI = Cart<LI>::n, NCJ = Cart<LJ>::n, NSI = Sph<LI>::n, NSJ = Sph<LJ>::n;
+    constexpr int NAB = NCI * NCJ, MI1 = LI + 2, LJ1 = LJ + 1, SZ = MI1 * LJ1;
+    const double A[3] = {m.xyz[3 * iat], m.xyz[3 * iat + 1], m.xyz[3 * iat + 2]};
+    const double B[3] = {m.xyz[3 * jat], m.xyz[3 * jat + 1], m.xyz[3 * jat + 2]};
+    const double rij[3] = {A[0] - B[0], A[1] - B[1], A[2] - B[2]};
+    const double rab2 = sqi(rij[0]) + sqi(rij[1]) + sqi(rij[2]);
+    if (rab2 > 1600.0) return;
+    const size_t nao = m.nao;
+    const int ai0 = m.sh_ao[ish], aj0 = m.sh_ao[jsh];
+    const double rab = sqrt(rab2);
+    const double rr = m.arad[iat] + m.arad[jat];
+    const double t14 = sqrt(rab / rr);
+    const double k1 = m.sh_poly[ish] * 0.01, k2 = m.sh_poly[jsh] * 0.01;
+    const double t15 = k1 * t14, t23 = k2 * t14;
+    const double shpoly = (1.0 + t15) * (1.0 + k2 * t14);
+    const double dsp = (t15 * (1.0 + t23) + (1.0 + t15) * k2 * t14) * 0.5 / rab2;
+    const double hnov = h0_factor(m, se, ish, jsh, rab) * EVTOAU;
+    const double hav0 = 0.5 * (se[ish] + se[jsh]);
+    const double vsum = vs[iat] + vs[jat];
+    const double esum = shift[ish] + shift[jsh];
+    // contraction weights of this lane's component pairs (same meaning as in d_grad_sdqh0)
+    double w[2][20];
+    int pi_[2][3], pj_[2][3];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int ab = lane + 32 * h;
+#pragma unroll
+        for (int k = 0; k < 20; ++k) w[h][k] = 0.0;
+        int a = 0, b = 0;
+        if (ab < NAB) {
+            a = ab / NCJ;
+            b = ab % NCJ;
+        }
+        cart_pow(LI, a, pi_[h][0], pi_[h][1], pi_[h][2]);
+        cart_pow(LJ, b, pj_[h][0], pj_[h][1], pj_[h][2]);
+        if (ab >= NAB) continue;
+        for (int s = 0; s < NSI; ++s) {
+            const double fa = tr(LI, s, a);
+            if (fa == 0.0) continue;
+            for (int u = 0; u < NSJ; ++u) {
+                const double f = fa * tr(LJ, u, b);
+                if (f == 0.0) continue;
+                const size_t ia = ai0 + s, ja = aj0 + u;
+                const double p = P[ja * nao + ia];
+                const double hp = hnov * p;
+                w[h][0] += f * (2.0 * hp - 2.0 * Pew[ja * nao + ia] - p * esum + p * vsum);
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    w[h][1 + k] += f * p * vd[3 * iat + k];
+                    w[h][4 + k] += f * p * vd[3 * jat + k];
+                }
+#pragma unroll
+                for (int k = 0; k < 6; ++k) {
+                    w[h][7 + k] += f * p * vq[6 * iat + k];
+                    w[h][13 + k] += f * p * vq[6 * jat + k];
+                }
+                w[h][19] += f * hp;
+            }
+        }
+    }
+    double gx[3] = {0.0, 0.0, 0.0};
+    double sHPS = 0.0;
+    const double sqrtpi = 1.7724538509055160273;
+    const int npi = m.sh_nprim[ish], npj = m.sh_nprim[jsh];
+    for (int p = 0; p < npi; ++p) {
+        const double ai = m.sh_alpha[ish * MAXPRIM + p], ci = m.sh_coef[ish * MAXPRIM + p];
+        for (int q = 0; q < npj; ++q) {
+            const double aj = m.sh_alpha[jsh * MAXPRIM + q], cj = m.sh_coef[jsh * MAXPRIM + q];
+            double est = ai * aj * rab2;
+            if (est > intcut * (ai + aj)) continue;
+            const double g = ai + aj, ab = 1.0 / g;
+            est *= ab;
+            const double sab = sqrtpi * sqrt(ab);
+            const double cc = exp(-est) * (sab * sab * sab) * ci * cj;
+            __syncwarp();
+            // 1D integrals about B (o = 0) and about A (o = 1): sm[((o*3 + x)*3 + e)*SZ + i*LJ1 + j]
+            for (int u = lane; u < 6 * SZ; u += 32) {
+                const int o = u / (3 * SZ), x = (u / SZ) % 3, i = (u % SZ) / LJ1, j = u % LJ1;
+                const double Pp = (ai * A[x] + aj * B[x]) * ab;
+                double s0, s1, s2;
+                mom1d_entry<LI + LJ + 4>(Pp - A[x], Pp - B[x], o == 0 ? Pp - B[x] : Pp - A[x], g, i, j, s0, s1, s2);
+                double* dst = sm + ((o * 3 + x) * 3) * SZ + i * LJ1 + j;
+                dst[0] = s0;
+                dst[SZ] = s1;
+                dst[2 * SZ] = s2;
+            }
+            __syncwarp();
+            auto vB = [&](int x, int e, int i, int j) { return sm[((0 * 3 + x) * 3 + e) * SZ + i * LJ1 + j]; };
+            auto vA = [&](int x, int e, int i, int j) { return sm[((1 * 3 + x) * 3 + e) * SZ + i * LJ1 + j]; };
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                if (lane + 32 * h >= NAB) continue;
+                const int* pi = pi_[h];
+                const int* pj = pj_[h];
+                const double* wt = w[h];
+                sHPS += cc * wt[19] * vB(0, 0, pi[0], pj[0]) * vB(1, 0, pi[1], pj[1]) * vB(2, 0, pi[2], pj[2]);
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    auto dB = [&](int e) {
+                        double r = 2.0 * ai * vB(c, e, pi[c] + 1, pj[c]);
+                        if (pi[c] > 0) r -= pi[c] * vB(c, e, pi[c] - 1, pj[c]);
+                        return r;
+                    };
+                    auto dA = [&](int e) {
+                        double r = 2.0 * ai * vA(c, e, pi[c] + 1, pj[c]);
+                        if (pi[c] > 0) r -= pi[c] * vA(c, e, pi[c] - 1, pj[c]);
+                        return r;
+                    };
+                    double acc = 0.0;
+#pragma unroll
+                    for (int k = 0; k < 10; ++k) {
+                        double fb = 1.0, fa = 1.0;
+#pragma unroll
+                        for (int x = 0; x < 3; ++x) {
+                            const int e = c_mom[k][x];
+                            if (x == c) {
+                                fb *= dB(e);
+                                fa *= dA(e);
+                            } else {
+                                fb *= vB(x, e, pi[x], pj[x]);
+                                fa *= vA(x, e, pi[x], pj[x]);
+                            }
+                        }
+                        const int ec = c_mom[k][c];
+                        if (ec > 0) {
+                            double lo = 1.0;
+#pragma unroll
+                            for (int x = 0; x < 3; ++x) lo *= vA(x, c_mom[k][x] - (x == c ? 1 : 0), pi[x], pj[x]);
+                            fa -= ec * lo;
+                        }
+                        if (k == 0) acc += wt[0] * fb;
+                        else if (k < 4) acc += wt[k] * fa + wt[3 + k] * fb;
+                        else acc += wt[3 + k] * fa + wt[9 + k] * fb;
+                    }
+                    gx[c] += cc * acc;
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) gx[c] = warp_sum(gx[c]);
+    sHPS = warp_sum(sHPS);
+    __syncwarp();
+    if (lane == 0) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) gx[c] += 2.0 * sHPS * dsp * rij[c] / shpoly;
+        const double dcn = sHPS / hav0;
+        atomicAdd(&grad[3 * iat + 0], gx[0]);
+        atomicAdd(&grad[3 * iat + 1], gx[1]);
+        atomicAdd(&grad[3 * iat + 2], gx[2]);
+        atomicAdd(&grad[3 * jat + 0], -gx[0]);
+        atomicAdd(&grad[3 * jat + 1], -gx[1]);
+        atomicAdd(&grad[3 * jat + 2], -gx[2]);
+        atomicAdd(&dhdcn[iat], dcn * (-m.sh_kcn[ish]));
+        atomicAdd(&dhdcn[jat], dcn * (-m.sh_kcn[jsh]));
+    }
+}
+
 }  // namespace xg
