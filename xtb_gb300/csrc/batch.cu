@@ -69,6 +69,8 @@ void layout_mol(Carver& cv, const HostMol& hm, BatchMol& b, const std::vector<do
     m.sh_poly = cv.upload(hm.sh_poly); m.sh_eta = cv.upload(hm.sh_eta); m.sh_gam3 = cv.upload(hm.sh_gam3);
     m.sh_zsh = cv.upload(hm.sh_zsh);
     m.ao_sh = cv.upload(hm.ao_sh); m.ao_at = cv.upload(hm.ao_at);
+    m.sh_byl = cv.upload(hm.sh_byl);
+    for (int l = 0; l < 4; ++l) m.l_off[l] = hm.l_off[l];
     b.zval = cv.upload(hm.zval);
     b.guess = guess ? cv.upload(*guess) : nullptr;
 

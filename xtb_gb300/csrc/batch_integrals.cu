@@ -23,8 +23,7 @@ __global__ void __launch_bounds__(BI_THREADS) k_batch_sdqh0(BatchMol* __restrict
     if (mi >= nmol) return;
     BatchMol* b = mols + mi;
     if (b->stage != BS_SETUP) return;
-    const int nsh = b->m.nsh;
-    const long np = (long)nsh * (nsh + 1) / 2;
+    const long np = class_pairs<LI, LJ>(b->m);
     for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < np; t += (long)gridDim.x * blockDim.x)
         d_sdqh0<LI, LJ>(b->m, b->se, intcut, np, b->S, b->D, b->Q, b->H0, t);
 }
@@ -36,8 +35,7 @@ __global__ void __launch_bounds__(BI_THREADS) k_batch_grad_sdqh0(BatchMol* __res
     if (mi >= nmol) return;
     BatchMol* b = mols + mi;
     if (b->stage != BS_GRAD || !b->want_grad) return;
-    const int nsh = b->m.nsh;
-    const long np = (long)nsh * (nsh + 1) / 2;
+    const long np = class_pairs<LI, LJ>(b->m);
     for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < np; t += (long)gridDim.x * blockDim.x)
         d_grad_sdqh0<LI, LJ>(b->m, b->se, intcut, np, b->P, b->W, b->shift, b->vs, b->vd, b->vq, b->grad, b->dhdcn,
                              t);
@@ -53,7 +51,7 @@ __global__ void __launch_bounds__(BI_THREADS) k_batch_sdqh0_w(BatchMol* __restri
     BatchMol* b = mols + mi;
     if (b->stage != BS_SETUP) return;
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const long np = (long)b->m.nsh * (b->m.nsh + 1) / 2;
+    const long np = class_pairs<LI, LJ>(b->m);
     for (long t = (long)blockIdx.x * NW + w; t < np; t += (long)gridDim.x * NW)
         d_sdqh0_warp<LI, LJ>(b->m, b->se, intcut, b->S, b->D, b->Q, b->H0, t, lane, sm[w]);
 }
@@ -68,7 +66,7 @@ __global__ void __launch_bounds__(BI_THREADS) k_batch_grad_sdqh0_w(BatchMol* __r
     BatchMol* b = mols + mi;
     if (b->stage != BS_GRAD || !b->want_grad) return;
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const long np = (long)b->m.nsh * (b->m.nsh + 1) / 2;
+    const long np = class_pairs<LI, LJ>(b->m);
     for (long t = (long)blockIdx.x * NW + w; t < np; t += (long)gridDim.x * NW)
         d_grad_sdqh0_warp<LI, LJ>(b->m, b->se, intcut, b->P, b->W, b->shift, b->vs, b->vd, b->vq, b->grad, b->dhdcn, t,
                                   lane, sm[w]);

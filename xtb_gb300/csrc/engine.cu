@@ -414,6 +414,8 @@ void run_singlepoint(const HostMol& hm, const SPSettings& set, Wavefunction& wfn
     m.sh_eta = upload(ar, st, hm.sh_eta);
     m.sh_gam3 = upload(ar, st, hm.sh_gam3);
     m.sh_zsh = upload(ar, st, hm.sh_zsh);
+    m.sh_byl = upload(ar, st, hm.sh_byl);
+    for (int l = 0; l < 4; ++l) m.l_off[l] = hm.l_off[l];
     m.ao_sh = upload(ar, st, hm.ao_sh);
     m.ao_at = upload(ar, st, hm.ao_at);
     d_zval = upload(ar, st, hm.zval);
@@ -653,7 +655,7 @@ void run_singlepoint(const HostMol& hm, const SPSettings& set, Wavefunction& wfn
         dgemm(st, true, false, nao, nao, nao, 1.0, X, nao, T1, nao, 0.0, A, nao, GF_A_LOWER | GF_B_UPPER);
         sym_add(st, nao, A, nao);
         tm.mark(PH_SYTRD);
-        sytrd(st, nao, A, nao, V, tri_tau, tri_d, tri_e, tri_p);
+        sytrd_form(st, nao, A, nao, V, tri_tau, tri_d, tri_e, tri_p, -1, split ? set.slices : 0, sgw);
         // eigenvalues, occupations, then eigenvectors of the occupied orbitals only
         tm.mark(PH_TRIEIG);
         tridiag_eigvals(st, nao, tri_d, tri_e, tri_e2, bounds, emo);

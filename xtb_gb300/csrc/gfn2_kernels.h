@@ -42,6 +42,9 @@ struct DevMol {
     const double* sh_eta = nullptr, *sh_gam3 = nullptr, *sh_zsh = nullptr;
     // AOs
     const int* ao_sh = nullptr, *ao_at = nullptr;
+    // shells grouped by angular momentum: group l is sh_byl[l_off[l] .. l_off[l + 1])
+    const int* sh_byl = nullptr;
+    int l_off[4] = {0, 0, 0, 0};
 };
 
 struct Thresholds {

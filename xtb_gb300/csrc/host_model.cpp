@@ -214,6 +214,13 @@ std::string build_host_mol(int nat, const int* Zin, const double* xyzin, double 
     }
     hm.nsh = (int)hm.sh_atom.size();
     hm.nao = ao;
+    hm.sh_byl.clear();
+    for (int l = 0; l < 3; ++l) {
+        hm.l_off[l] = (int)hm.sh_byl.size();
+        for (int s = 0; s < hm.nsh; ++s)
+            if (hm.sh_l[s] == l) hm.sh_byl.push_back(s);
+    }
+    hm.l_off[3] = (int)hm.sh_byl.size();
     if (hm.nel < 0) return "negative number of electrons";
     if (hm.nel > 2 * hm.nao) return "Not enough basis functions for filling orbitals";
     {

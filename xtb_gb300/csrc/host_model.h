@@ -29,6 +29,10 @@ struct HostMol {
     std::vector<double> sh_alpha, sh_coef, sh_zeta, sh_se0, sh_kcn, sh_poly, sh_eta, sh_gam3, sh_zsh, sh_refocc;
     // AOs
     std::vector<int> ao_sh, ao_at;
+    // shells grouped by angular momentum (increasing index within a group): group l is
+    // sh_byl[l_off[l] .. l_off[l + 1])
+    std::vector<int> sh_byl;
+    int l_off[4] = {0, 0, 0, 0};
 };
 
 // Returns an empty string on success, else an error message (unsupported element, ...).

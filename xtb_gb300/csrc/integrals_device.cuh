@@ -108,14 +108,28 @@ __device__ __forceinline__ void tri_index(long t, int& a, int& b) {
 }
 
 
-// shell pair in canonical order (l_i >= l_j); returns false if the pair is not of type (LI, LJ)
+// shell pairs of class (LI, LJ), LI >= LJ: all pairs of an LI shell with an LJ shell, for LI == LJ
+// the pairs with ish >= jsh (diagonal included)
+template <int LI, int LJ>
+__host__ __device__ __forceinline__ long class_pairs(const DevMol& m) {
+    const long ni = m.l_off[LI + 1] - m.l_off[LI], nj = m.l_off[LJ + 1] - m.l_off[LJ];
+    return LI == LJ ? ni * (ni + 1) / 2 : ni * nj;
+}
+
+// pair t (< class_pairs) of class (LI, LJ) in canonical order (the LI shell first)
 template <int LI, int LJ>
 __device__ __forceinline__ bool canonical_pair(const DevMol& m, long t, int& ish, int& jsh) {
-    int a, b;
-    tri_index(t, a, b);
-    const int la = m.sh_l[a], lb = m.sh_l[b];
-    if (la >= lb) { ish = a; jsh = b; } else { ish = b; jsh = a; }
-    return m.sh_l[ish] == LI && m.sh_l[jsh] == LJ;
+    if (LI == LJ) {
+        int a, b;
+        tri_index(t, a, b);
+        ish = m.sh_byl[m.l_off[LI] + a];
+        jsh = m.sh_byl[m.l_off[LI] + b];
+    } else {
+        const long nj = m.l_off[LJ + 1] - m.l_off[LJ];
+        ish = m.sh_byl[m.l_off[LI] + (int)(t / nj)];
+        jsh = m.sh_byl[m.l_off[LJ] + (int)(t % nj)];
+    }
+    return true;
 }
 
 
