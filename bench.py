@@ -60,10 +60,7 @@ def sytrd_form(n):
     """(kernel, DRAM bytes per launch, note) of the tridiagonalisation the engine runs at n AOs on
     this device (the autotuner's crossover)."""
     from xtb_gb300 import interface as X
-    tu = X.get_tuning()
-    if n >= tu["sytrd_blocked_min"]:
-        return "k_sytrd_panel", None, "blocked form: per column one trailing product, rank-2 updates as GEMMs per panel"
-    if n >= tu["sytrd_sym_min"]:
+    if n >= X.get_tuning()["sytrd_sym_min"]:
         return "k_sytrd_sym", SYTRD_SYM_BYTES_PER_ELEM * float(n) ** 2, "traffic scaled as n^2 from the ncu capture at n = 3072"
     return "k_sytrd", SYTRD_BYTES_PER_ELEM * float(n) ** 2, "traffic scaled as n^2 from the ncu capture at n = 1800"
 

@@ -101,26 +101,22 @@ extern void xtbgb_setSolventSalt(xtb_TEnvironment env, xtb_TCalculator calc, dou
 extern void xtbgb_setSolventKernel(xtb_TEnvironment env, xtb_TCalculator calc, int kernel);
 
 /* Autotuner (no counterpart in the reference).  Two choices of the single point depend on the
- * matrix size and the device: the form of the tridiagonalisation (row by row; the upper-triangle
- * form with 4/3 n^3 flops; or the blocked form, panels of 32 columns whose rank-2 updates reach
- * the trailing matrix as GEMMs) and the form of the eigenvector back-transformation (one warp per
- * vector, or compact-WY GEMMs; FP64 and split precision apart).  xtbgb_autotune times the forms
- * on synthetic matrices of the current device (a few seconds, once per device and process; later
- * calls return the kept choices) and the engine uses the measured crossovers from then on.
- * out[nout] receives: [0] AOs from which the upper-triangle tridiagonalisation runs, [1] AOs from
- * which the blocked back-transformation runs in FP64, [2] the same in split precision, [3]
- * seconds taken, [4] R, then R rows (n, row form ms, upper-triangle form ms, blocked form ms),
- * then R2, then R2 rows (n, warp form ms, blocked FP64 ms, blocked split ms), then the AOs from
- * which the blocked tridiagonalisation runs.  Returns the number of values written (0 on error,
- * reported on env). */
+ * matrix size and the device: the form of the tridiagonalisation (row by row, or the
+ * upper-triangle form with 4/3 n^3 flops) and the form of the eigenvector back-transformation
+ * (one warp per vector, or compact-WY GEMMs; FP64 and split precision apart).  xtbgb_autotune
+ * times both forms of each on synthetic matrices of the current device (a few seconds, once per
+ * device and process; later calls return the kept choices) and the engine uses the measured
+ * crossovers from then on.  out[nout] receives: [0] AOs from which the upper-triangle
+ * tridiagonalisation runs, [1] AOs from which the blocked back-transformation runs in FP64,
+ * [2] the same in split precision, [3] seconds taken, [4] R, then R rows (n, row form ms,
+ * upper-triangle form ms), then R2, then R2 rows (n, warp form ms, blocked FP64 ms, blocked
+ * split ms).  Returns the number of values written (0 on error, reported on env). */
 extern int xtbgb_autotune(xtb_TEnvironment env, double* out, int nout);
-/* The current device's choices: out[0..2] as above, out[3] 1 when measured, 0 for defaults,
- * out[4] AOs from which the blocked tridiagonalisation runs (out holds 5 values). */
+/* The current device's choices: out[0..2] as above, out[3] 1 when measured, 0 for defaults. */
 extern void xtbgb_getTuning(xtb_TEnvironment env, double* out);
 /* Pin the current device's choices (sizes in AOs; for tests and for callers with their own
  * measurements). */
-extern void xtbgb_setTuning(xtb_TEnvironment env, int sytrd_sym_min, int blocked_min_fp64, int blocked_min_split,
-                            int sytrd_blocked_min);
+extern void xtbgb_setTuning(xtb_TEnvironment env, int sytrd_sym_min, int blocked_min_fp64, int blocked_min_split);
 
 /* The three figures behind xtbgb_fp64PeakTflops, measured anew (TFLOP/s): out[0] FMA chains with
  * uniform operands, out[1] GEMM-style accumulator chains, out[2] FP64 GEMM C = A B at 4096^3. */

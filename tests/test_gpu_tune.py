@@ -20,11 +20,11 @@ def test_kernel_forms_measured_and_kept():
     assert t["seconds"] > 0.0
     assert len(t["sytrd_ms"]) >= 5 and len(t["backtransform_ms"]) >= 4
     for row in t["sytrd_ms"]:
-        assert row["row_form"] > 0.0 and row["upper_triangle_form"] > 0.0 and row["blocked_form"] > 0.0
+        assert row["row_form"] > 0.0 and row["upper_triangle_form"] > 0.0
     g = X.get_tuning()
     assert g["measured"]
-    assert (g["sytrd_sym_min"], g["sytrd_blocked_min"], g["blocked_min_fp64"], g["blocked_min_split"]) == \
-        (t["sytrd_sym_min"], t["sytrd_blocked_min"], t["blocked_min_fp64"], t["blocked_min_split"])
+    assert (g["sytrd_sym_min"], g["blocked_min_fp64"], g["blocked_min_split"]) == \
+        (t["sytrd_sym_min"], t["blocked_min_fp64"], t["blocked_min_split"])
     assert tuning.kernel_forms()["seconds"] == t["seconds"]      # kept, not measured again
 
 
@@ -32,22 +32,17 @@ def test_kernel_forms_measured_and_kept():
 def test_results_do_not_depend_on_the_forms(precision):
     Z, xyz = W.water_cluster(110, seed=3)             # 660 AOs
     saved = X.get_tuning()
-    runs = []
     try:
-        for forms in ((3, 0, 0, 1 << 30),              # upper-triangle form, blocked back-transformation
-                      (1 << 30, 1 << 30, 1 << 30, 1 << 30),   # row form, one warp per vector
-                      (1 << 30, 0, 0, 3)):             # blocked tridiagonalisation
-            X.set_tuning(*forms)
-            runs.append(X.Calculator(Z, xyz, keep_orbitals=False, precision=precision).singlepoint())
+        X.set_tuning(3, 0, 0)                          # upper-triangle form, blocked back-transformation
+        a = X.Calculator(Z, xyz, keep_orbitals=False, precision=precision).singlepoint()
+        X.set_tuning(1 << 30, 1 << 30, 1 << 30)        # row form, one warp per vector
+        b = X.Calculator(Z, xyz, keep_orbitals=False, precision=precision).singlepoint()
     finally:
-        X.set_tuning(saved["sytrd_sym_min"], saved["blocked_min_fp64"], saved["blocked_min_split"],
-                     saved["sytrd_blocked_min"])
-    a = runs[0]
-    for b in runs[1:]:
-        assert a.iterations == b.iterations
-        assert abs(a.energy - b.energy) <= 1e-9
-        assert np.max(np.abs(a.charges - b.charges)) <= 1e-8
-        assert np.max(np.abs(a.gradient - b.gradient)) <= 1e-8
+        X.set_tuning(saved["sytrd_sym_min"], saved["blocked_min_fp64"], saved["blocked_min_split"])
+    assert a.iterations == b.iterations
+    assert abs(a.energy - b.energy) <= 1e-9
+    assert np.max(np.abs(a.charges - b.charges)) <= 1e-8
+    assert np.max(np.abs(a.gradient - b.gradient)) <= 1e-8
 
 
 def test_schedule_choice_and_results():
@@ -62,26 +57,3 @@ def test_schedule_choice_and_results():
         srv.close()
     for r2, r4 in zip(out[2], out[4]):
         assert abs(r2.energy - r4.energy) <= 1e-9
-
-
-def test_blocked_tridiagonalisation_on_every_panel_shape():
-    """The blocked form against the row form on molecules whose AO counts give one partial panel
-    (6, 22 AOs), whole panels and a partial last one (alkanes and water clusters up to ~400 AOs),
-    in FP64 and split precision."""
-    mols = [W.water_cluster(1, seed=1), W.alkane(3, 0.02, seed=2), W.water_cluster(11, seed=5),
-            W.alkane(21, 0.02, seed=3), W.water_cluster(67, seed=7)]
-    saved = X.get_tuning()
-    try:
-        for Z, xyz in mols:
-            for precision in ("fp64", "split"):
-                res = []
-                for forms in ((1 << 30, 1 << 30, 1 << 30, 1 << 30), (1 << 30, 1 << 30, 1 << 30, 3)):
-                    X.set_tuning(*forms)
-                    res.append(X.Calculator(Z, xyz, keep_orbitals=False, precision=precision).singlepoint())
-                a, b = res
-                assert a.iterations == b.iterations
-                assert abs(a.energy - b.energy) <= 1e-9, (len(Z), precision)
-                assert np.max(np.abs(a.gradient - b.gradient)) <= 1e-8
-    finally:
-        X.set_tuning(saved["sytrd_sym_min"], saved["blocked_min_fp64"], saved["blocked_min_split"],
-                     saved["sytrd_blocked_min"])

@@ -885,11 +885,10 @@ int xtbgb_autotune(xtb_TEnvironment env, double* out, int nout) {
     try {
         const xg::Tuned t = xg::autotune();
         std::vector<double> v = {(double)t.sytrd_sym_min, (double)t.blocked_min_fp64, (double)t.blocked_min_split,
-                                 t.seconds, (double)(t.sytrd_rows.size() / 4)};
+                                 t.seconds, (double)(t.sytrd_rows.size() / 3)};
         v.insert(v.end(), t.sytrd_rows.begin(), t.sytrd_rows.end());
         v.push_back((double)(t.backtr_rows.size() / 4));
         v.insert(v.end(), t.backtr_rows.begin(), t.backtr_rows.end());
-        v.push_back((double)t.sytrd_blocked_min);
         const int m = std::min((int)v.size(), std::max(0, nout));
         if (out) std::copy(v.begin(), v.begin() + m, out);
         return m;
@@ -906,14 +905,11 @@ void xtbgb_getTuning(xtb_TEnvironment env, double* out) {
     out[1] = t.blocked_min_fp64;
     out[2] = t.blocked_min_split;
     out[3] = t.level;
-    out[4] = t.sytrd_blocked_min;
 }
 
-void xtbgb_setTuning(xtb_TEnvironment env, int sytrd_sym_min, int blocked_min_fp64, int blocked_min_split,
-                     int sytrd_blocked_min) {
+void xtbgb_setTuning(xtb_TEnvironment env, int sytrd_sym_min, int blocked_min_fp64, int blocked_min_split) {
     if (!check_env(env)) return;
-    xg::set_tuned(std::max(3, sytrd_sym_min), std::max(0, blocked_min_fp64), std::max(0, blocked_min_split),
-                  std::max(3, sytrd_blocked_min));
+    xg::set_tuned(std::max(3, sytrd_sym_min), std::max(0, blocked_min_fp64), std::max(0, blocked_min_split));
 }
 
 void xtbgb_getIterations(xtb_TEnvironment env, xtb_TResults res, int* iterations, int* converged) {

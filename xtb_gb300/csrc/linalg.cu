@@ -654,281 +654,12 @@ static void sytrd_sym_launch(cudaStream_t st, int n, double* A, int lda, double*
     ++launch_counter();
 }
 
-// ------------------------------------------------------------------ blocked tridiagonalisation
-// The reduction in panels of PNL_NB columns (LAPACK's dsytrd / dlatrd scheme, restated for one
-// cooperative grid).  Within a panel the trailing matrix is not touched: the pivot row of column
-// s and the product y = A22 v see the panel's earlier reflectors through their vectors
-// (Vp, Wp: A_s = A - sum_k (v_k w_k^T + w_k v_k^T)), so per column the FP64 work is one
-// matrix-vector product over the trailing rows; the panel's rank-2 updates then reach the
-// trailing matrix as one product of K = 2 x columns (a GEMM: FP64, or split precision on the
-// tensor cores).  Two grid barriers per column: after the pivot row (its norm), and after y.
-//
-// Ownership: within a panel, index j of [s0, n) belongs to block (j - s0) / per for the pivot
-// row, the update vector and the panel vectors, so a block reads back only what it wrote itself
-// between barriers; the rows of the product go to all warps cyclically.  The scalars of index
-// s + 1 that every block needs (the newest w at the next pivot) are formed redundantly in every
-// block from the same inputs in the same order.
-constexpr int PNL_NB = 32;             // columns per panel
-constexpr int PNL_NT = 512;            // threads per block
-constexpr int PNL_SLOT = 2 * PNL_NB + 2;
-
-__global__ void __launch_bounds__(PNL_NT, 1) k_sytrd_panel(int n, int s0, int s1, const double* __restrict__ A, int lda,
-                                                        double* __restrict__ V, double* __restrict__ tau,
-                                                        double* __restrict__ d, double* __restrict__ e,
-                                                        double* __restrict__ PA, double* __restrict__ PB,
-                                                        double* __restrict__ ws) {
-    extern __shared__ double sm[];
-    double* vs = sm;                          // v over [b, n)
-    double* wtv = vs + n;                     // [PNL_NB] w_k . v
-    double* vtv = wtv + PNL_NB;               // [PNL_NB] v_k . v
-    double* vsc = vtv + PNL_NB;               // [PNL_NB] V_k[s]: the panel vectors at the pivot index
-    double* wsc = vsc + PNL_NB;               // [PNL_NB] W_k[s]
-    double* red = wsc + PNL_NB;               // [PNL_NT / 32] block reductions
-    double* scal = red + PNL_NT / 32;         // [8]
-    cg::grid_group grid = cg::this_grid();
-    const int G = gridDim.x, g = blockIdx.x;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    constexpr int NW = PNL_NT / 32;
-    const int cnt = s1 - s0;                  // columns of this panel
-    // panel rows: PA = [V_p; W_p], PB = [W_p; V_p] (rows of length n), so that the trailing update
-    // is one product PA^T PB
-    auto Vp = [&](int k) { return PA + (size_t)k * n; };
-    auto Wp = [&](int k) { return PA + (size_t)(cnt + k) * n; };
-    double* xb = ws;                          // pivot row (global, index j)
-    double* yb = ws + n;                      // A22 v (global, index j)
-    double* slots = ws + 2 * (size_t)n;       // [G][PNL_SLOT]
-    const int per = (n - s0 + G - 1) / G;
-    const int lo = s0 + g * per, hi = min(n, lo + per);
-    auto block_sum = [&](double v) {
-        v = warp_sum(v);
-        __syncthreads();
-        if (lane == 0) red[wid] = v;
-        __syncthreads();
-        double t = 0.0;
-        for (int k = 0; k < NW; ++k) t += red[k];
-        return t;
-    };
-    // the rows of V left of the panel's partition are zero: each block clears a share of [0, s0)
-    {
-        const int p0 = (s0 + G - 1) / G;
-        for (int s = s0; s < s1; ++s)
-            for (int j = g * p0 + threadIdx.x; j < min(s0, (g + 1) * p0); j += PNL_NT) V[(size_t)s * n + j] = 0.0;
-    }
-    // scalars at the first pivot: nothing of this panel applies yet
-    if (threadIdx.x < PNL_NB) {
-        vsc[threadIdx.x] = 0.0;
-        wsc[threadIdx.x] = 0.0;
-    }
-    __syncthreads();
-    for (int s = s0; s < s1; ++s) {
-        const int c = s - s0, b = s + 1, m = n - b;
-        // ---- phase 1: this block's slice of the pivot row, with the panel's earlier updates (one
-        // warp per element, the panel columns over the lanes)
-        double nx = 0.0;
-        for (int j = max(lo, b) + wid; j < hi; j += NW) {
-            double acc = 0.0;
-            for (int k = lane; k < c; k += 32) acc += vsc[k] * Wp(k)[j] + wsc[k] * Vp(k)[j];
-            acc = warp_sum(acc);
-            const double x = A[(size_t)s * lda + j] - acc;
-            if (lane == 0) {
-                xb[j] = x;
-                if (j > b) nx = fma(x, x, nx);
-            }
-        }
-        nx = block_sum(nx);
-        if (threadIdx.x == 0) slots[(size_t)g * PNL_SLOT] = nx;
-        if (g == 0 && threadIdx.x == 0) {
-            double dd = A[(size_t)s * lda + s];
-            for (int k = 0; k < c; ++k) dd -= 2.0 * vsc[k] * wsc[k];
-            d[s] = dd;
-        }
-        grid.sync();
-        // ---- phase 2: reflector (every block), y = A22 v over all warps, partial dots
-        if (wid == 0) {
-            double t0 = 0.0;
-            for (int q = lane; q < G; q += 32) t0 += slots[(size_t)q * PNL_SLOT];
-            t0 = warp_sum(t0);
-            const double alpha = xb[b];
-            double beta, tk, sc;
-            if (t0 == 0.0) {
-                beta = alpha;
-                tk = 0.0;
-                sc = 0.0;
-            } else {
-                beta = -copysign(sqrt(alpha * alpha + t0), alpha);
-                tk = (beta - alpha) / beta;
-                sc = 1.0 / (alpha - beta);
-            }
-            if (lane == 0) {
-                scal[0] = beta;
-                scal[1] = tk;
-                scal[2] = sc;
-            }
-        }
-        __syncthreads();
-        const double beta = scal[0], tk = scal[1], sc = scal[2];
-        for (int j = threadIdx.x; j < m; j += PNL_NT) vs[j] = j == 0 ? 1.0 : sc * xb[b + j];
-        __syncthreads();
-        double yv = 0.0;
-        for (int r = g + G * wid; r < m; r += G * NW) {
-            const double* row = A + (size_t)(b + r) * lda + b;
-            double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
-            int j = lane;
-            for (; j + 96 < m; j += 128) {
-                a0 = fma(row[j], vs[j], a0);
-                a1 = fma(row[j + 32], vs[j + 32], a1);
-                a2 = fma(row[j + 64], vs[j + 64], a2);
-                a3 = fma(row[j + 96], vs[j + 96], a3);
-            }
-            for (; j < m; j += 32) a0 = fma(row[j], vs[j], a0);
-            const double y = warp_sum((a0 + a1) + (a2 + a3));
-            if (lane == 0) yb[b + r] = y;
-            yv = fma(y, vs[r], yv);           // lanes hold the same y: lane 0's share counts below
-        }
-        // partial dots of the panel vectors with v over this block's slice
-        double pw[2] = {0.0, 0.0};
-        {
-            // (w_k . v, v_k . v) for k < c: warp k takes k
-            for (int k = wid; k < c; k += NW) {
-                double sw = 0.0, sv = 0.0;
-                for (int j = max(lo, b) + lane; j < hi; j += 32) {
-                    const double v = vs[j - b];
-                    sw = fma(Wp(k)[j], v, sw);
-                    sv = fma(Vp(k)[j], v, sv);
-                }
-                sw = warp_sum(sw);
-                sv = warp_sum(sv);
-                if (lane == 0) {
-                    slots[(size_t)g * PNL_SLOT + 2 + 2 * k] = sw;
-                    slots[(size_t)g * PNL_SLOT + 3 + 2 * k] = sv;
-                }
-            }
-            (void)pw;
-        }
-        yv = block_sum(lane == 0 ? yv : 0.0);
-        if (threadIdx.x == 0) slots[(size_t)g * PNL_SLOT + 1] = yv;
-        grid.sync();
-        // ---- phase 3: dots (every block, fixed order), w over this block's slice
-        // sums over the blocks' slots: one warp per value, the blocks over the lanes
-        for (int f = wid; f < 2 * c + 1; f += NW) {
-            double t = 0.0;
-            for (int q = lane; q < G; q += 32) t += slots[(size_t)q * PNL_SLOT + 1 + f];
-            t = warp_sum(t);
-            if (lane == 0) {
-                if (f == 0) scal[3] = t;
-                else if (f & 1) wtv[(f - 1) >> 1] = t;
-                else vtv[(f - 2) >> 1] = t;
-            }
-        }
-        __syncthreads();
-        // the panel's correction of y at index j: sum_k V_k[j] (w_k . v) + W_k[j] (v_k . v)
-        auto ycorr = [&](int j) {
-            double acc = 0.0;
-            for (int k = lane; k < c; k += 32) acc += Vp(k)[j] * wtv[k] + Wp(k)[j] * vtv[k];
-            return warp_sum(acc);
-        };
-        if (wid == 0) {
-            double ytv = 0.0;
-            for (int k = lane; k < c; k += 32) ytv += wtv[k] * vtv[k];
-            ytv = scal[3] - 2.0 * warp_sum(ytv);
-            const double hh = 0.5 * tk * tk * ytv;
-            // w at the next pivot index b (v_b = 1), the same in every block
-            const double wb = tk * (yb[b] - ycorr(b)) - hh;
-            if (lane == 0) {
-                scal[4] = hh;
-                scal[5] = wb;
-                if (g == 0) {
-                    tau[s] = tk;
-                    e[s] = beta;
-                }
-            }
-        }
-        __syncthreads();
-        const double hh = scal[4];
-        for (int j = max(lo, b) + wid; j < hi; j += NW) {
-            const double corr = ycorr(j);
-            if (lane == 0) {
-                const double v = vs[j - b];
-                const double w = tk * (yb[j] - corr) - hh * v;
-                Vp(c)[j] = v;
-                Wp(c)[j] = w;
-                PB[(size_t)c * n + j] = w;            // PB = [W_p; V_p]
-                PB[(size_t)(cnt + c) * n + j] = v;
-            }
-        }
-        // this block's slice of V row s: 0 left of b, v from b on
-        for (int j = lo + threadIdx.x; j < hi; j += PNL_NT) V[(size_t)s * n + j] = j < b ? 0.0 : vs[j - b];
-        // scalars of the next pivot index b for every block: V_k[b] and W_k[b] (k <= c)
-        __syncthreads();
-        if (threadIdx.x <= c) {
-            const int k = threadIdx.x;
-            vsc[k] = k == c ? 1.0 : Vp(k)[b];
-            wsc[k] = k == c ? scal[5] : Wp(k)[b];
-        }
-        __syncthreads();
-    }
-}
-
-// the last 2 x 2 block after the final trailing update, and the unused tails
-__global__ void k_sytrd_tail(int n, const double* __restrict__ A, int lda, double* __restrict__ V,
-                             double* __restrict__ tau, double* __restrict__ d, double* __restrict__ e) {
-    for (int i = threadIdx.x; i < 2 * n; i += blockDim.x) V[(size_t)(n - 2) * n + i] = 0.0;
-    if (threadIdx.x == 0) {
-        d[n - 2] = A[(size_t)(n - 2) * lda + n - 2];
-        d[n - 1] = A[(size_t)(n - 1) * lda + n - 1];
-        e[n - 2] = A[(size_t)(n - 2) * lda + n - 1];
-        e[n - 1] = 0.0;
-        tau[n - 2] = 0.0;
-        tau[n - 1] = 0.0;
-    }
-}
-
-size_t sytrd_blocked_workspace(int n) {
-    return 2 * (size_t)n + (size_t)SYTRD_SLOTS * PNL_SLOT + 4 * (size_t)PNL_NB * n;
-}
-
-static size_t sytrd_panel_smem(int n) { return ((size_t)n + 4 * PNL_NB + PNL_NT / 32 + 8) * sizeof(double); }
-
-bool sytrd_blocked_fits(int n) { return n >= 3 && sytrd_panel_smem(n) <= 200 * 1024; }
-
-void sytrd_blocked(cudaStream_t st, int n, double* A, int lda, double* V, double* tau, double* d, double* e,
-                   double* ws, int slices, void* split_work) {
-    int dev = 0, nsm = 0, maxblk = 0;
-    XG_CUDA(cudaGetDevice(&dev));
-    XG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    const size_t smem = sytrd_panel_smem(n);
-    allow_max_dynamic_smem((const void*)k_sytrd_panel);
-    XG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxblk, k_sytrd_panel, PNL_NT, smem));
-    if (maxblk < 1) throw CudaError("sytrd: panel kernel does not fit on an SM");
-    const int blocks = std::min(nsm, SYTRD_SLOTS);
-    double* PA = ws + 2 * (size_t)n + (size_t)SYTRD_SLOTS * PNL_SLOT;
-    double* PB = PA + 2 * (size_t)PNL_NB * n;
-    for (int s0 = 0; s0 < n - 2; s0 += PNL_NB) {
-        int s1 = std::min(s0 + PNL_NB, n - 2);
-        void* args[] = {&n, &s0, &s1, &A, &lda, &V, &tau, &d, &e, &PA, &PB, &ws};
-        XG_CUDA(cudaLaunchCooperativeKernel((void*)k_sytrd_panel, blocks, PNL_NT, args, smem, st));
-        ++launch_counter();
-        // trailing update A[t:, t:] -= PA[:, t:]^T PB[:, t:] (K = 2 x columns)
-        const int t = s1, mt = n - t, K = 2 * (s1 - s0);
-        if (mt <= 0) continue;
-        double* C = A + (size_t)t * lda + t;
-        if (slices > 0) {
-            split_gemm(st, true, false, mt, mt, K, -1.0, PA + t, n, PB + t, n, 1.0, C, lda, slices, split_work);
-        } else {
-            dgemm(st, true, false, mt, mt, K, -1.0, PA + t, n, PB + t, n, 1.0, C, lda, GF_SYM);
-            mirror_lower(st, mt, C, lda);
-        }
-    }
-    k_sytrd_tail<<<1, 256, 0, st>>>(n, A, lda, V, tau, d, e);
-    XG_LAUNCH_CHECK();
-}
-
 void sytrd(cudaStream_t st, int n, double* A, int lda, double* V, double* tau, double* d, double* e, double* p) {
     sytrd_form(st, n, A, lda, V, tau, d, e, p, -1);
 }
 
 void sytrd_form(cudaStream_t st, int n, double* A, int lda, double* V, double* tau, double* d, double* e, double* p,
-                int form, int slices, void* split_work) {
+                int form) {
     const size_t smem = (size_t)(4 * n + 72) * sizeof(double);
     if (n <= 2) {
         // trivial: copy diagonal / off-diagonal
@@ -939,12 +670,7 @@ void sytrd_form(cudaStream_t st, int n, double* A, int lda, double* V, double* t
     // the upper-triangle form (its three A x buffers live after the row form's 2n + 2 SYTRD_SLOTS
     // doubles of p)
     const bool sym_fits = n >= 3 && sytrd_sym_smem(n) <= 220 * 1024;
-    if (form < 0) form = n >= tuned_sytrd_blocked_min() ? 2 : (n >= tuned_sytrd_sym_min() ? 1 : 0);
-    if (form == 2 && sytrd_blocked_fits(n)) {
-        sytrd_blocked(st, n, A, lda, V, tau, d, e, p, slices, split_work);
-        return;
-    }
-    if (form == 2) form = 1;
+    if (form < 0) form = n >= tuned_sytrd_sym_min() ? 1 : 0;
     if (form == 1 && sym_fits) {
         sytrd_sym_launch(st, n, A, lda, V, tau, d, e, p + 2 * (size_t)n + 2 * SYTRD_SLOTS);
         return;

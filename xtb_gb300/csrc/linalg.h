@@ -25,22 +25,13 @@ void trinv_upper(cudaStream_t st, int n, const double* U, int ldu, double* X, in
 // p: sytrd_workspace(n) doubles of device scratch.
 constexpr int SYTRD_SLOTS = 256;   // most blocks of the cooperative tridiagonalisation
 // the upper-triangle form (4/3 n^3 flops) keeps three A x buffers (3n doubles) after the row
-// form's 2n + 2 SYTRD_SLOTS; the blocked form needs sytrd_blocked_workspace(n)
-size_t sytrd_blocked_workspace(int n);
-inline size_t sytrd_workspace(int n) {
-    return std::max(5 * (size_t)n + 2 * (size_t)SYTRD_SLOTS, sytrd_blocked_workspace(n));
-}
+// form's 2n + 2 SYTRD_SLOTS
+inline size_t sytrd_workspace(int n) { return 5 * (size_t)n + 2 * (size_t)SYTRD_SLOTS; }
 void sytrd(cudaStream_t st, int n, double* A, int lda, double* V, double* tau, double* d, double* e, double* p);
-// the same with the form chosen: 0 the row-by-row form, 1 the upper-triangle form, 2 the blocked
-// form (panels of 32 columns, trailing updates as GEMMs: split precision with `slices` > 0 and
-// split_work of split_gemm_workspace(n, n, n, slices) bytes, else FP64), each when its shared
-// memory fits; -1 by the device's measured thresholds (tune.h)
+// the same with the form chosen: 0 the row-by-row form, 1 the upper-triangle form (when its
+// shared memory fits), -1 by the device's measured threshold (tune.h)
 void sytrd_form(cudaStream_t st, int n, double* A, int lda, double* V, double* tau, double* d, double* e, double* p,
-                int form, int slices = 0, void* split_work = nullptr);
-// the blocked form alone (A must be full symmetric; it is overwritten)
-bool sytrd_blocked_fits(int n);
-void sytrd_blocked(cudaStream_t st, int n, double* A, int lda, double* V, double* tau, double* d, double* e,
-                   double* ws, int slices, void* split_work);
+                int form);
 // eigenvalues of the tridiagonal (d, e): w[n] ascending; e2: n, bounds: 4
 void tridiag_eigvals(cudaStream_t st, int n, const double* d, const double* e, double* e2, double* bounds, double* w);
 // eigenvectors j < *ncol (all if ncol is null): Y[i*n+j] = component i of vector j.

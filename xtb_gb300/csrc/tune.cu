@@ -78,16 +78,10 @@ int tuned_sytrd_sym_min() {
     return g_tuned[current_device()].sytrd_sym_min;
 }
 
-int tuned_sytrd_blocked_min() {
-    std::lock_guard<std::mutex> lk(g_tune_mu);
-    return g_tuned[current_device()].sytrd_blocked_min;
-}
-
-void set_tuned(int sytrd_sym_min, int blocked_min_fp64, int blocked_min_split, int sytrd_blocked_min) {
+void set_tuned(int sytrd_sym_min, int blocked_min_fp64, int blocked_min_split) {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     Tuned& t = g_tuned[current_device()];
     t.sytrd_sym_min = sytrd_sym_min;
-    t.sytrd_blocked_min = sytrd_blocked_min;
     t.blocked_min_fp64 = blocked_min_fp64;
     t.blocked_min_split = blocked_min_split;
     t.level = std::max(t.level, 1);
@@ -124,25 +118,23 @@ Tuned autotune() {
     double* ormw = p + sytrd_workspace(nmax);
     int* ncol = reinterpret_cast<int*>(ormw + ormtr_workspace(nmax));
     try {
-        // 1. tridiagonalisation: row form, upper-triangle form and blocked form (FP64 updates)
+        // 1. tridiagonalisation: row form against the upper-triangle form
         const std::vector<int> tsz = {192, 256, 384, 512, 768, 1024, 1536, 2048, 2560, 3072};
-        std::vector<bool> sym_wins, blk_wins;
+        std::vector<bool> sym_wins;
         for (int n : tsz) {
             k_tune_sym<<<ceil_div((long)n * n, 256), 256, 0, st>>>(n, 17u + n, A0);
             XG_LAUNCH_CHECK();
-            double ms[3];
-            for (int form = 0; form < 3; ++form)
+            double ms[2];
+            for (int form = 0; form < 2; ++form)
                 ms[form] = best_ms(st, e0, e1, 3, [&] {
                     XG_CUDA(cudaMemcpyAsync(A, A0, sizeof(double) * n * n, cudaMemcpyDeviceToDevice, st));
                     sytrd_form(st, n, A, n, V, tau, d, e, p, form);
                 });
-            // the copy is inside the timing of every form alike
-            t.sytrd_rows.insert(t.sytrd_rows.end(), {(double)n, ms[0], ms[1], ms[2]});
+            // the copy is inside the timing of both forms alike
+            t.sytrd_rows.insert(t.sytrd_rows.end(), {(double)n, ms[0], ms[1]});
             sym_wins.push_back(ms[1] < ms[0]);
-            blk_wins.push_back(ms[2] < std::min(ms[0], ms[1]));
         }
         t.sytrd_sym_min = crossover(tsz, sym_wins);
-        t.sytrd_blocked_min = crossover(tsz, blk_wins);
         // 2. back-transformation of n / 2 vectors: one warp per vector against compact-WY GEMMs
         const std::vector<int> bsz = {600, 900, 1200, 1500, 1800, 2400};
         std::vector<bool> fp64_wins, split_wins;

@@ -16,13 +16,11 @@ struct Tuned {
     int sytrd_sym_min = 1 << 30;    // AOs from which the upper-triangle tridiagonalisation runs
                                     // (never by default: on GB300 the row form measured faster up
                                     // to 1024 AOs, its per-column latency being lower)
-    int sytrd_blocked_min = 1 << 30;// AOs from which the blocked tridiagonalisation (panels +
-                                    // GEMM trailing updates) runs
     int blocked_min_fp64 = 1500;    // AOs from which the compact-WY back-transformation runs
     int blocked_min_split = 1000;   // the same with split-precision products
     int level = 0;                  // 0: defaults, 1: measured on this device
     double seconds = 0.0;           // time the measurement took
-    // measurements: (n, row form ms, upper-triangle form ms, blocked form ms) and
+    // measurements: (n, row form ms, upper-triangle form ms) and
     // (n, warp form ms, blocked FP64 ms, blocked split ms)
     std::vector<double> sytrd_rows, backtr_rows;
 };
@@ -32,11 +30,10 @@ Tuned tuned();
 // measure the crossovers on the current device (once; later calls return the kept choices)
 Tuned autotune();
 // replace the current device's choices (level 1; for tests that pin a form)
-void set_tuned(int sytrd_sym_min, int blocked_min_fp64, int blocked_min_split, int sytrd_blocked_min = 1 << 30);
+void set_tuned(int sytrd_sym_min, int blocked_min_fp64, int blocked_min_split);
 // back-transformation threshold for a precision (0 FP64, 1 split)
 int tuned_blocked_min(int precision);
-// tridiagonalisation thresholds
+// tridiagonalisation threshold
 int tuned_sytrd_sym_min();
-int tuned_sytrd_blocked_min();
 
 }  // namespace xg

@@ -94,7 +94,7 @@ def load_library(path=LIBPATH):
         "xtbgb_writeRestart": (C.c_int, [vp, vp, vp, C.c_char_p]),
         "xtbgb_readRestart": (C.c_int, [vp, vp, vp, C.c_char_p]),
         "xtbgb_getTuning": (None, [vp, dp]),
-        "xtbgb_setTuning": (None, [vp, C.c_int, C.c_int, C.c_int, C.c_int]),
+        "xtbgb_setTuning": (None, [vp, C.c_int, C.c_int, C.c_int]),
         "xtbgb_fp64LatencyCycles": (None, [dp]),
         "xtbgb_reciprocalCheck": (C.c_int, [dp]),
         "xtbgb_splitGemmCheck": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, dp]),
@@ -512,13 +512,12 @@ def autotune():
     env.check()
     v = out[:m]
     r1 = int(v[4])
-    rows1 = v[5:5 + 4 * r1].reshape(r1, 4)
-    r2 = int(v[5 + 4 * r1])
-    rows2 = v[6 + 4 * r1:6 + 4 * r1 + 4 * r2].reshape(r2, 4)
-    return {"sytrd_sym_min": int(v[0]), "sytrd_blocked_min": int(v[6 + 4 * r1 + 4 * r2]),
-            "blocked_min_fp64": int(v[1]), "blocked_min_split": int(v[2]), "seconds": float(v[3]),
-            "sytrd_ms": [{"n": int(a), "row_form": float(b), "upper_triangle_form": float(c), "blocked_form": float(d)}
-                         for a, b, c, d in rows1],
+    rows1 = v[5:5 + 3 * r1].reshape(r1, 3)
+    r2 = int(v[5 + 3 * r1])
+    rows2 = v[6 + 3 * r1:6 + 3 * r1 + 4 * r2].reshape(r2, 4)
+    return {"sytrd_sym_min": int(v[0]), "blocked_min_fp64": int(v[1]), "blocked_min_split": int(v[2]),
+            "seconds": float(v[3]),
+            "sytrd_ms": [{"n": int(a), "row_form": b, "upper_triangle_form": c} for a, b, c in rows1],
             "backtransform_ms": [{"n": int(a), "warp_form": b, "blocked_fp64": c, "blocked_split": d}
                                  for a, b, c, d in rows2]}
 
@@ -526,15 +525,14 @@ def autotune():
 def get_tuning():
     lib = load_library()
     env = Environment(0)
-    out = np.zeros(5)
+    out = np.zeros(4)
     lib.xtbgb_getTuning(env.h, _dptr(out))
     return {"sytrd_sym_min": int(out[0]), "blocked_min_fp64": int(out[1]), "blocked_min_split": int(out[2]),
-            "measured": bool(out[3]), "sytrd_blocked_min": int(out[4])}
+            "measured": bool(out[3])}
 
 
-def set_tuning(sytrd_sym_min, blocked_min_fp64, blocked_min_split, sytrd_blocked_min=1 << 30):
+def set_tuning(sytrd_sym_min, blocked_min_fp64, blocked_min_split):
     lib = load_library()
     env = Environment(0)
-    lib.xtbgb_setTuning(env.h, int(sytrd_sym_min), int(blocked_min_fp64), int(blocked_min_split),
-                        int(sytrd_blocked_min))
+    lib.xtbgb_setTuning(env.h, int(sytrd_sym_min), int(blocked_min_fp64), int(blocked_min_split))
     env.check()
