@@ -268,13 +268,15 @@ def autotune_served(args, reqs):
     from xtb_gb300 import tuning
     forms = tuning.kernel_forms()
     out = {"kernel_forms": forms}
-    if args.workers is None or args.iters_per_step is None:
+    if args.workers is None or args.iters_per_step is None or args.pool_max_nao is None:
         sched = tuning.schedule(reqs, pool_gib=args.pool_gib, precision=args.served_precision, slices=args.slices)
         out["schedule"] = sched
         if args.workers is None:
             args.workers = sched["plain_workers"]
         if args.iters_per_step is None:
             args.iters_per_step = sched["iters_per_step"]
+        if args.pool_max_nao is None:
+            args.pool_max_nao = sched["pool_max_nao"]
     return out
 
 
@@ -286,7 +288,8 @@ def run_served(args, ws, rank):
     metric, wdesc = workload_spec(args)
     tuned = autotune_served(args, reqs)
     srv = X.Server(pool_gib=args.pool_gib, max_slots=1024, plain_workers=args.workers,
-                   iters_per_step=args.iters_per_step, precision=args.served_precision, slices=args.slices)
+                   iters_per_step=args.iters_per_step, precision=args.served_precision, slices=args.slices,
+                   pool_max_nao=args.pool_max_nao)
     for _ in range(args.warmup):
         served_pass(srv, reqs, args.rate)
     st0 = srv.stats()
@@ -380,6 +383,7 @@ def run_served(args, ws, rank):
                    "served_precision": (f"split products ({args.slices} bf16 digits) on the plain-engine workers"
                                         if args.served_precision == "split" else "fp64"),
                    "pool_gib": args.pool_gib, "plain_workers": args.workers, "iters_per_step": args.iters_per_step,
+                   "pool_max_nao": args.pool_max_nao,
                    "parallelism": f"replicas x{ws}",
                    "l2": "large requests hold n^2 matrices far above L2 (129 MB); no flush"},
         "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
@@ -751,6 +755,8 @@ def main():
     ap.add_argument("--iters-per-step", type=int, default=None,
                     help="served: SCC iterations per pool step (default: autotuned)")
     ap.add_argument("--pool-gib", type=float, default=24.0, help="served: HBM budget of the resident pool")
+    ap.add_argument("--pool-max-nao", type=int, default=None,
+                    help="served: largest molecule (AOs) of the resident pool (default: autotuned)")
     ap.add_argument("--cpu-batch-sample", type=int, default=512,
                     help="batch4096: molecules of the set the CPU restatement runs")
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -25,6 +25,7 @@ FIXTURES = {
     "h2o_30_seed1": lambda: W.water_cluster(30, seed=1),
     "c50h102_seed3": lambda: W.alkane(50, 0.02, seed=3),
     "h2o_300_seed1": lambda: W.water_cluster(300, seed=1),
+    "c200h402_seed1": lambda: W.alkane(200, 0.02, seed=1),
 }
 
 

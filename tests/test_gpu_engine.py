@@ -86,7 +86,7 @@ def test_water_clusters_match_oracle(m):
     assert_parity(gpu(Z, xyz), gfn2.singlepoint(Z, xyz))
 
 
-@pytest.mark.parametrize("name", ["c10h22_seed1", "h2o_30_seed1", "c50h102_seed3", "h2o_300_seed1"])
+@pytest.mark.parametrize("name", ["c10h22_seed1", "h2o_30_seed1", "c50h102_seed3", "h2o_300_seed1", "c200h402_seed1"])
 def test_workload_fixtures(name):
     path = os.path.join(GOLD, f"{name}.npz")
     if not os.path.exists(path):

@@ -45,3 +45,22 @@ def test_split_rejects_bad_slice_count():
     Z, xyz = W.alkane(2, 0.02, seed=1)
     with pytest.raises(X.XTBException, match="4..7"):
         X.Calculator(Z, xyz, precision="split", slices=3)
+
+
+def test_split_at_the_tensor_core_sizes_matches_the_oracle_fixture():
+    """C200H402 (602 atoms, 1202 AOs): from 1000 AOs the split mode also takes the blocked
+    back-transformation on the tensor cores.  Against the committed oracle fixture at the
+    spec tolerances, and against the FP64 mode of the engine (reported bound 1e-8 Eh)."""
+    import os
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "c200h402_seed1.npz")
+    if not os.path.exists(path):
+        pytest.skip("fixture c200h402_seed1 not generated")
+    fx = np.load(path)
+    Z, xyz = fx["numbers"], fx["positions"]
+    f, s = both(Z, xyz)
+    assert abs(s.energy - fx["energy"]) <= TOL_E
+    assert np.max(np.abs(s.charges - fx["charges"])) <= TOL_Q
+    assert np.max(np.abs(s.gradient - fx["gradient"])) <= TOL_G
+    assert abs(s.iterations - int(fx["iterations"])) <= TOL_ITER
+    assert abs(s.energy - f.energy) <= 1e-8
+    assert np.max(np.abs(s.gradient - f.gradient)) <= 1e-7

@@ -46,14 +46,19 @@ def test_results_do_not_depend_on_the_forms(precision):
 
 
 def test_schedule_choice_and_results():
+    """The schedule tuner picks one of its candidates, and the results do not depend on the
+    schedule: worker count, pool step, and which molecules the pool takes (here up to 400 AOs
+    or only up to 64, the rest on the plain engine)."""
     reqs = W.served_stream(12, seed=5, nmax=400)
-    s = tuning.schedule(reqs, candidates=((2, 1), (4, 2)), pool_gib=2.0, max_slots=64)
-    assert (s["plain_workers"], s["iters_per_step"]) in ((2, 1), (4, 2))
+    cands = ((2, 1, 512), (4, 2, 64))
+    s = tuning.schedule(reqs, candidates=cands, pool_gib=2.0, max_slots=64)
+    assert (s["plain_workers"], s["iters_per_step"], s["pool_max_nao"]) in cands
     assert len(s["span_s"]) == 2
     out = {}
-    for w, i in ((2, 1), (4, 2)):
-        srv = X.Server(pool_gib=2.0, max_slots=64, plain_workers=w, iters_per_step=i)
+    for w, i, p in cands:
+        srv = X.Server(pool_gib=2.0, max_slots=64, plain_workers=w, iters_per_step=i, pool_max_nao=p)
         out[w] = [srv.wait(srv.submit(r["numbers"], r["positions"], gradient=r["gradient"])) for r in reqs]
         srv.close()
+    assert sum(x.engine for x in out[4]) > sum(x.engine for x in out[2])    # more on the plain engine
     for r2, r4 in zip(out[2], out[4]):
         assert abs(r2.energy - r4.energy) <= 1e-9

@@ -1200,12 +1200,13 @@ struct _xtbgb_TServer {
 
 xtbgb_TServer xtbgb_newServer(xtb_TEnvironment env, double pool_gib, int max_slots, int plain_workers,
                               int iters_per_step, double accuracy, double etemp, int maxiter) {
-    return xtbgb_newServerEx(env, pool_gib, max_slots, plain_workers, iters_per_step, accuracy, etemp, maxiter, 0, 5);
+    return xtbgb_newServerEx(env, pool_gib, max_slots, plain_workers, iters_per_step, accuracy, etemp, maxiter, 0, 5,
+                             0);
 }
 
 xtbgb_TServer xtbgb_newServerEx(xtb_TEnvironment env, double pool_gib, int max_slots, int plain_workers,
                                 int iters_per_step, double accuracy, double etemp, int maxiter, int split,
-                                int slices) {
+                                int slices, int pool_max_nao) {
     static const char* src = "xtbgb_newServer";
     if (!check_env(env)) return nullptr;
     xg::ServeConfig cfg;
@@ -1222,6 +1223,7 @@ xtbgb_TServer xtbgb_newServerEx(xtb_TEnvironment env, double pool_gib, int max_s
     }
     cfg.precision = split ? 1 : 0;
     cfg.slices = slices;
+    cfg.pool_max_nao = pool_max_nao > 0 ? std::min(pool_max_nao, xg::BATCH_MAX_NAO) : xg::BATCH_MAX_NAO;
     auto* s = new _xtbgb_TServer();
     try {
         s->srv = std::make_unique<xg::Server>(cfg);

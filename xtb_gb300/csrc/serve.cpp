@@ -49,7 +49,7 @@ long long Server::submit(int nat, const int* Z, const double* xyz, double charge
         r->id = next_id_++;
         r->t_submit = now();
         const long long id = r->id;
-        if (r->hm.nao <= BATCH_MAX_NAO) small_q_.push_back(std::move(r));
+        if (r->hm.nao <= cfg_.pool_max_nao) small_q_.push_back(std::move(r));
         else large_q_.push_back(std::move(r));
         ++inflight_;
         cv_work_.notify_all();

@@ -5,9 +5,10 @@ Two levels:
 * ``kernel_forms()``: the size crossovers between the two forms of the tridiagonalisation and
   of the eigenvector back-transformation, measured by the library itself
   (``xtbgb_autotune``); the engine uses them from then on.
-* ``schedule(requests)``: the request loop's schedule -- plain-engine workers and SCC
-  iterations per pool step -- measured on the caller's own request stream: one pass of the
-  stream per candidate on a fresh server, the shortest device span wins.
+* ``schedule(requests)``: the request loop's schedule -- plain-engine workers, SCC iterations
+  per pool step and the largest molecule the resident pool takes -- measured on the caller's
+  own request stream: one pass of the stream per candidate on a fresh server, the shortest
+  device span wins.
 
 Both keep their choices in this process (per device and, for the schedule, per stream), so a
 second call returns at once.
@@ -16,7 +17,8 @@ import numpy as np
 
 from . import interface as X
 
-CANDIDATES = ((4, 1), (6, 1), (8, 1), (6, 2))
+# (plain workers, SCC iterations per pool step, largest molecule of the pool in AOs)
+CANDIDATES = ((4, 1, 512), (6, 1, 512), (8, 1, 512), (6, 2, 512), (6, 1, 384), (6, 1, 256), (8, 1, 256))
 _schedules = {}
 
 
@@ -32,21 +34,22 @@ def _stream_key(requests):
 
 
 def schedule(requests, candidates=CANDIDATES, pool_gib=24.0, precision="split", slices=5, max_slots=1024):
-    """Best (plain_workers, iters_per_step) for `requests` (dicts with numbers, positions,
-    gradient), with the span of each candidate's pass in seconds."""
+    """Best (plain_workers, iters_per_step, pool_max_nao) for `requests` (dicts with numbers,
+    positions, gradient), with the span of each candidate's pass in seconds."""
     key = (_stream_key(requests), tuple(candidates), precision, slices)
     if key in _schedules:
         return _schedules[key]
     spans = {}
-    for workers, iters in candidates:
+    for workers, iters, pmax in candidates:
         srv = X.Server(pool_gib=pool_gib, max_slots=max_slots, plain_workers=workers, iters_per_step=iters,
-                       precision=precision, slices=slices)
+                       precision=precision, slices=slices, pool_max_nao=pmax)
         ids = [srv.submit(r["numbers"], r["positions"], gradient=r["gradient"]) for r in requests]
         res = [srv.wait(i, check=False) for i in ids]
         srv.close()
-        spans[(workers, iters)] = max(x.t_done for x in res) - min(x.t_start for x in res)
+        spans[(workers, iters, pmax)] = max(x.t_done for x in res) - min(x.t_start for x in res)
     best = min(spans, key=spans.get)
-    out = {"plain_workers": best[0], "iters_per_step": best[1],
-           "span_s": {f"workers {w}, iterations per step {i}": s for (w, i), s in spans.items()}}
+    out = {"plain_workers": best[0], "iters_per_step": best[1], "pool_max_nao": best[2],
+           "span_s": {f"workers {w}, iterations per step {i}, pool up to {p} AOs": s
+                      for (w, i, p), s in spans.items()}}
     _schedules[key] = out
     return out
