@@ -18,7 +18,8 @@ import numpy as np
 from . import interface as X
 
 # (plain workers, SCC iterations per pool step, largest molecule of the pool in AOs)
-CANDIDATES = ((4, 1, 512), (6, 1, 512), (8, 1, 512), (6, 2, 512), (6, 1, 384), (6, 1, 256), (8, 1, 256))
+CANDIDATES = ((4, 1, 512), (6, 1, 512), (8, 1, 512), (6, 2, 512), (6, 1, 384), (6, 1, 256), (8, 1, 256),
+              (6, 1, 192), (8, 1, 128))
 _schedules = {}
 
 
