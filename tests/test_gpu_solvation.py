@@ -129,3 +129,35 @@ def test_solvated_hessian_matches_oracle():
     Ho, dgo = gfn2.hessian(Z, xyz, solvation=S.Solvation(Z, "water", "alpb"))
     assert np.max(np.abs(H - Ho)) <= 1e-6
     assert np.max(np.abs(dg - dgo)) <= 1e-6
+
+
+@pytest.mark.parametrize("Z,xyz", [([10], [[0.0, 0.0, 0.0]]), ([1, 1], [[0.0, 0.0, 0.0], [0.0, 0.0, 1.4]])])
+def test_smallest_solutes(Z, xyz):
+    """A single atom (empty neighbour lists, one Born radius) and H2 in implicit water."""
+    Z, xyz = np.array(Z), np.array(xyz, dtype=float)
+    for model in ("gbsa", "alpb"):
+        c = X.Calculator(Z, xyz)
+        c.set_solvent("water", model)
+        r = c.singlepoint()
+        o = gfn2.singlepoint(Z, xyz, solvation=S.Solvation(Z, "water", model))
+        assert abs(r.energy - o.energy) < 1e-9, model
+        assert np.max(np.abs(r.gradient - o.gradient)) < 1e-9, model
+        assert abs(r.g_solv - o.e_solv) < 1e-10, model
+
+
+def test_solvent_with_external_charges():
+    """Point charges and an implicit solvent together (the reference adds both to the same SCC):
+    the water dimer of the reference's point-charge test in ALPB water."""
+    from oracle.params import get_params
+    case = CASES["capi_pc"]
+    Z, xyz = case_geometry(case)
+    gam = [get_params().chemicalHardness[z - 1] for z in case["pc_numbers"]]
+    c = X.Calculator(Z, xyz)
+    c.set_external_charges(case["pc_charges"], case["pc_positions"], numbers=case["pc_numbers"])
+    c.set_solvent("water", "alpb")
+    r = c.singlepoint()
+    o = gfn2.singlepoint(Z, xyz, pc_charges=case["pc_charges"], pc_positions=case["pc_positions"], pc_gam=gam,
+                         solvation=S.Solvation(Z, "water", "alpb"))
+    assert abs(r.energy - o.energy) < 1e-9
+    assert np.max(np.abs(r.gradient - o.gradient)) < 1e-9
+    assert np.max(np.abs(r.pcgrad - o.pcgrad)) < 1e-9
