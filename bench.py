@@ -268,7 +268,7 @@ def autotune_served(args, reqs):
     from xtb_gb300 import tuning
     forms = tuning.kernel_forms()
     out = {"kernel_forms": forms}
-    if args.workers is None or args.iters_per_step is None or args.pool_max_nao is None:
+    if args.workers is None or args.iters_per_step is None or args.pool_max_nao is None or args.coop_blocks is None:
         sched = tuning.schedule(reqs, pool_gib=args.pool_gib, precision=args.served_precision, slices=args.slices)
         out["schedule"] = sched
         if args.workers is None:
@@ -277,6 +277,8 @@ def autotune_served(args, reqs):
             args.iters_per_step = sched["iters_per_step"]
         if args.pool_max_nao is None:
             args.pool_max_nao = sched["pool_max_nao"]
+        if args.coop_blocks is None:
+            args.coop_blocks = sched["coop_blocks"]
     return out
 
 
@@ -289,7 +291,7 @@ def run_served(args, ws, rank):
     tuned = autotune_served(args, reqs)
     srv = X.Server(pool_gib=args.pool_gib, max_slots=1024, plain_workers=args.workers,
                    iters_per_step=args.iters_per_step, precision=args.served_precision, slices=args.slices,
-                   pool_max_nao=args.pool_max_nao)
+                   pool_max_nao=args.pool_max_nao, coop_blocks=args.coop_blocks)
     for _ in range(args.warmup):
         served_pass(srv, reqs, args.rate)
     st0 = srv.stats()
@@ -383,7 +385,7 @@ def run_served(args, ws, rank):
                    "served_precision": (f"split products ({args.slices} bf16 digits) on the plain-engine workers"
                                         if args.served_precision == "split" else "fp64"),
                    "pool_gib": args.pool_gib, "plain_workers": args.workers, "iters_per_step": args.iters_per_step,
-                   "pool_max_nao": args.pool_max_nao,
+                   "pool_max_nao": args.pool_max_nao, "coop_blocks": args.coop_blocks,
                    "parallelism": f"replicas x{ws}",
                    "l2": "large requests hold n^2 matrices far above L2 (129 MB); no flush"},
         "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
@@ -757,6 +759,9 @@ def main():
     ap.add_argument("--pool-gib", type=float, default=24.0, help="served: HBM budget of the resident pool")
     ap.add_argument("--pool-max-nao", type=int, default=None,
                     help="served: largest molecule (AOs) of the resident pool (default: autotuned)")
+    ap.add_argument("--coop-blocks", type=int, default=None,
+                    help="served: most blocks of a worker's cooperative tridiagonalisation, 0 = all SMs "
+                         "(default: autotuned)")
     ap.add_argument("--cpu-batch-sample", type=int, default=512,
                     help="batch4096: molecules of the set the CPU restatement runs")
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -187,10 +187,12 @@ extern xtbgb_TServer xtbgb_newServer(xtb_TEnvironment env, double pool_gib, int 
                                      int iters_per_step, double accuracy, double etemp, int maxiter);
 /* As xtbgb_newServer; split = 1 runs the plain-engine workers with split-precision products
  * (xtbgb_setPrecision semantics, `slices` digits); pool_max_nao (1..512, <= 0 for 512) is the
- * largest molecule in AOs the resident pool takes, larger ones go to the plain-engine workers. */
+ * largest molecule in AOs the resident pool takes, larger ones go to the plain-engine workers;
+ * coop_blocks > 0 caps the blocks of a worker's cooperative tridiagonalisation (0: one per SM),
+ * so that the workers' single points can share the SMs. */
 extern xtbgb_TServer xtbgb_newServerEx(xtb_TEnvironment env, double pool_gib, int max_slots, int plain_workers,
                                        int iters_per_step, double accuracy, double etemp, int maxiter, int split,
-                                       int slices, int pool_max_nao);
+                                       int slices, int pool_max_nao, int coop_blocks);
 /* Finishes all submitted work, then frees the server. */
 extern void xtbgb_delServer(xtbgb_TServer* server);
 /* Queue one GFN2-xTB single point (positions [natoms][3] Bohr); returns the request id, or

@@ -47,18 +47,39 @@ def test_results_do_not_depend_on_the_forms(precision):
 
 def test_schedule_choice_and_results():
     """The schedule tuner picks one of its candidates, and the results do not depend on the
-    schedule: worker count, pool step, and which molecules the pool takes (here up to 400 AOs
-    or only up to 64, the rest on the plain engine)."""
+    schedule: worker count, pool step, which molecules the pool takes (here up to 400 AOs or only
+    up to 64, the rest on the plain engine) and the cap of the workers' cooperative grids."""
     reqs = W.served_stream(12, seed=5, nmax=400)
-    cands = ((2, 1, 512), (4, 2, 64))
+    cands = ((2, 1, 512, 0), (4, 2, 64, 24))
     s = tuning.schedule(reqs, candidates=cands, pool_gib=2.0, max_slots=64)
-    assert (s["plain_workers"], s["iters_per_step"], s["pool_max_nao"]) in cands
+    assert (s["plain_workers"], s["iters_per_step"], s["pool_max_nao"], s["coop_blocks"]) in cands
     assert len(s["span_s"]) == 2
     out = {}
-    for w, i, p in cands:
-        srv = X.Server(pool_gib=2.0, max_slots=64, plain_workers=w, iters_per_step=i, pool_max_nao=p)
+    for w, i, p, cb in cands:
+        srv = X.Server(pool_gib=2.0, max_slots=64, plain_workers=w, iters_per_step=i, pool_max_nao=p, coop_blocks=cb)
         out[w] = [srv.wait(srv.submit(r["numbers"], r["positions"], gradient=r["gradient"])) for r in reqs]
         srv.close()
     assert sum(x.engine for x in out[4]) > sum(x.engine for x in out[2])    # more on the plain engine
     for r2, r4 in zip(out[2], out[4]):
         assert abs(r2.energy - r4.energy) <= 1e-9
+
+
+def test_capped_cooperative_tridiagonalisation():
+    """Both tridiagonalisation forms with a capped grid (16 and 40 blocks) give the single point
+    of the full grid: the request loop with every molecule on the workers against the plain
+    calculator."""
+    reqs = W.served_stream(6, seed=9, nmin=40, nmax=300)
+    saved = X.get_tuning()
+    try:
+        for sym in (1 << 30, 3):                           # row form, upper-triangle form
+            X.set_tuning(sym, saved["blocked_min_fp64"], saved["blocked_min_split"])
+            ref = [X.Calculator(r["numbers"], r["positions"], keep_orbitals=False).singlepoint() for r in reqs]
+            for cap in (16, 40):
+                srv = X.Server(pool_gib=1.0, max_slots=8, plain_workers=2, pool_max_nao=1, coop_blocks=cap)
+                out = [srv.wait(srv.submit(r["numbers"], r["positions"], gradient=r["gradient"])) for r in reqs]
+                srv.close()
+                for a, b in zip(out, ref):
+                    assert a.engine == 1
+                    assert abs(a.energy - b.energy) <= 1e-9, (sym, cap)
+    finally:
+        X.set_tuning(saved["sytrd_sym_min"], saved["blocked_min_fp64"], saved["blocked_min_split"])

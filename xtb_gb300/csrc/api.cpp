@@ -1201,12 +1201,12 @@ struct _xtbgb_TServer {
 xtbgb_TServer xtbgb_newServer(xtb_TEnvironment env, double pool_gib, int max_slots, int plain_workers,
                               int iters_per_step, double accuracy, double etemp, int maxiter) {
     return xtbgb_newServerEx(env, pool_gib, max_slots, plain_workers, iters_per_step, accuracy, etemp, maxiter, 0, 5,
-                             0);
+                             0, 0);
 }
 
 xtbgb_TServer xtbgb_newServerEx(xtb_TEnvironment env, double pool_gib, int max_slots, int plain_workers,
                                 int iters_per_step, double accuracy, double etemp, int maxiter, int split,
-                                int slices, int pool_max_nao) {
+                                int slices, int pool_max_nao, int coop_blocks) {
     static const char* src = "xtbgb_newServer";
     if (!check_env(env)) return nullptr;
     xg::ServeConfig cfg;
@@ -1224,6 +1224,7 @@ xtbgb_TServer xtbgb_newServerEx(xtb_TEnvironment env, double pool_gib, int max_s
     cfg.precision = split ? 1 : 0;
     cfg.slices = slices;
     cfg.pool_max_nao = pool_max_nao > 0 ? std::min(pool_max_nao, xg::BATCH_MAX_NAO) : xg::BATCH_MAX_NAO;
+    cfg.coop_blocks = std::max(0, coop_blocks);
     auto* s = new _xtbgb_TServer();
     try {
         s->srv = std::make_unique<xg::Server>(cfg);

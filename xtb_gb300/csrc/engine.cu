@@ -655,7 +655,7 @@ void run_singlepoint(const HostMol& hm, const SPSettings& set, Wavefunction& wfn
         dgemm(st, true, false, nao, nao, nao, 1.0, X, nao, T1, nao, 0.0, A, nao, GF_A_LOWER | GF_B_UPPER);
         sym_add(st, nao, A, nao);
         tm.mark(PH_SYTRD);
-        sytrd(st, nao, A, nao, V, tri_tau, tri_d, tri_e, tri_p);
+        sytrd_form(st, nao, A, nao, V, tri_tau, tri_d, tri_e, tri_p, -1, set.max_coop_blocks);
         // eigenvalues, occupations, then eigenvectors of the occupied orbitals only
         tm.mark(PH_TRIEIG);
         tridiag_eigvals(st, nao, tri_d, tri_e, tri_e2, bounds, emo);

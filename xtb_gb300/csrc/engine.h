@@ -26,6 +26,9 @@ struct SPSettings {
     // CUDA stream priority of the single point's stream (lower is more urgent; clamped to the
     // device's range; 0 is the default priority)
     int stream_priority = 0;
+    // most blocks of the cooperative tridiagonalisation (0: one per SM); a cap lets concurrent
+    // single points share the GPU instead of waiting for all SMs
+    int max_coop_blocks = 0;
     // external point charges (xtb_setExternalCharges): charge, position [k][3] (Bohr) and
     // hardness of charge k; empty for none
     std::vector<double> pc_q, pc_xyz, pc_gam;

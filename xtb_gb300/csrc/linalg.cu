@@ -320,7 +320,7 @@ __global__ void __launch_bounds__(NT) k_sytrd(int n, double* __restrict__ A, int
 
 template <int NT>
 static void sytrd_launch(cudaStream_t st, int n, double* A, int lda, double* V, double* tau, double* d, double* e,
-                         double* p, size_t smem) {
+                         double* p, size_t smem, int max_blocks) {
     int dev = 0, nsm = 0, maxblk = 0;
     XG_CUDA(cudaGetDevice(&dev));
     XG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
@@ -329,6 +329,7 @@ static void sytrd_launch(cudaStream_t st, int n, double* A, int lda, double* V, 
     if (maxblk < 1) throw CudaError("sytrd: kernel does not fit on an SM");
     int blocks = std::min(std::min(nsm * maxblk, nsm), std::max(1, ceil_div(n, NT / 32)));
     blocks = std::min(blocks, SYTRD_SLOTS);
+    if (max_blocks > 0) blocks = std::min(blocks, max_blocks);
     void* args[] = {&n, &A, &lda, &V, &tau, &d, &e, &p};
     XG_CUDA(cudaLaunchCooperativeKernel((void*)k_sytrd<NT>, blocks, NT, args, smem, st));
     ++launch_counter();
@@ -640,7 +641,7 @@ static size_t sytrd_sym_smem(int n) {
 }
 
 static void sytrd_sym_launch(cudaStream_t st, int n, double* A, int lda, double* V, double* tau, double* d, double* e,
-                             double* ws) {
+                             double* ws, int max_blocks) {
     int dev = 0, nsm = 0, maxblk = 0;
     XG_CUDA(cudaGetDevice(&dev));
     XG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
@@ -648,7 +649,8 @@ static void sytrd_sym_launch(cudaStream_t st, int n, double* A, int lda, double*
     allow_max_dynamic_smem((const void*)k_sytrd_sym);
     XG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxblk, k_sytrd_sym, SYM_NT, smem));
     if (maxblk < 1) throw CudaError("sytrd: kernel does not fit on an SM");
-    const int blocks = std::min(nsm, SYTRD_SLOTS);
+    int blocks = std::min(nsm, SYTRD_SLOTS);
+    if (max_blocks > 0) blocks = std::min(blocks, max_blocks);
     void* args[] = {&n, &A, &lda, &V, &tau, &d, &e, &ws};
     XG_CUDA(cudaLaunchCooperativeKernel((void*)k_sytrd_sym, blocks, SYM_NT, args, smem, st));
     ++launch_counter();
@@ -659,7 +661,7 @@ void sytrd(cudaStream_t st, int n, double* A, int lda, double* V, double* tau, d
 }
 
 void sytrd_form(cudaStream_t st, int n, double* A, int lda, double* V, double* tau, double* d, double* e, double* p,
-                int form) {
+                int form, int max_blocks) {
     const size_t smem = (size_t)(4 * n + 72) * sizeof(double);
     if (n <= 2) {
         // trivial: copy diagonal / off-diagonal
@@ -672,14 +674,14 @@ void sytrd_form(cudaStream_t st, int n, double* A, int lda, double* V, double* t
     const bool sym_fits = n >= 3 && sytrd_sym_smem(n) <= 220 * 1024;
     if (form < 0) form = n >= tuned_sytrd_sym_min() ? 1 : 0;
     if (form == 1 && sym_fits) {
-        sytrd_sym_launch(st, n, A, lda, V, tau, d, e, p + 2 * (size_t)n + 2 * SYTRD_SLOTS);
+        sytrd_sym_launch(st, n, A, lda, V, tau, d, e, p + 2 * (size_t)n + 2 * SYTRD_SLOTS, max_blocks);
         return;
     }
     // More warps per block only for the largest matrices (measured: 1024 threads gain 7% at
     // n = 6000, 512 threads lose 19% at n = 1800 and 47% at n = 1202); at most one block per
     // SM, because every block repeats the O(n) per-column vector work.
-    if (n >= 4000) sytrd_launch<1024>(st, n, A, lda, V, tau, d, e, p, smem);
-    else sytrd_launch<256>(st, n, A, lda, V, tau, d, e, p, smem);
+    if (n >= 4000) sytrd_launch<1024>(st, n, A, lda, V, tau, d, e, p, smem, max_blocks);
+    else sytrd_launch<256>(st, n, A, lda, V, tau, d, e, p, smem, max_blocks);
 }
 
 // ------------------------------------------------------------------ bisection

@@ -30,8 +30,9 @@ inline size_t sytrd_workspace(int n) { return 5 * (size_t)n + 2 * (size_t)SYTRD_
 void sytrd(cudaStream_t st, int n, double* A, int lda, double* V, double* tau, double* d, double* e, double* p);
 // the same with the form chosen: 0 the row-by-row form, 1 the upper-triangle form (when its
 // shared memory fits), -1 by the device's measured threshold (tune.h)
+// max_blocks > 0 caps the cooperative grid (so that concurrent single points can share the SMs)
 void sytrd_form(cudaStream_t st, int n, double* A, int lda, double* V, double* tau, double* d, double* e, double* p,
-                int form);
+                int form, int max_blocks = 0);
 // eigenvalues of the tridiagonal (d, e): w[n] ascending; e2: n, bounds: 4
 void tridiag_eigvals(cudaStream_t st, int n, const double* d, const double* e, double* e2, double* bounds, double* w);
 // eigenvectors j < *ncol (all if ncol is null): Y[i*n+j] = component i of vector j.

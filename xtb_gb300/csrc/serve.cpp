@@ -285,6 +285,7 @@ void Server::plain_loop() {
             ps.maxiter = cfg_.set.maxiter;
             ps.precision = cfg_.precision;
             ps.slices = cfg_.slices;
+            ps.max_coop_blocks = cfg_.coop_blocks;
             int least = 0, greatest = 0;
             XG_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
             ps.stream_priority = std::min(least, greatest + rank);

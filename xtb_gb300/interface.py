@@ -112,7 +112,7 @@ def load_library(path=LIBPATH):
         "xtbgb_batchNao": (None, [vp, vp, ip]),
         "xtbgb_newServer": (vp, [vp, C.c_double, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int]),
         "xtbgb_newServerEx": (vp, [vp, C.c_double, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int,
-                                   C.c_int, C.c_int, C.c_int]),
+                                   C.c_int, C.c_int, C.c_int, C.c_int]),
         "xtbgb_delServer": (None, [C.POINTER(vp)]),
         "xtbgb_serverSubmit": (C.c_longlong, [vp, vp, C.c_int, ip, dp, C.c_double, C.c_int, C.c_int]),
         "xtbgb_serverWait": (C.c_int, [vp, vp, C.c_longlong, C.c_double, dp, dp, dp, dp]),
@@ -416,14 +416,14 @@ class Server:
     """
 
     def __init__(self, pool_gib=16.0, max_slots=1024, plain_workers=6, iters_per_step=1, accuracy=1.0,
-                 etemp=300.0, maxiter=250, precision="fp64", slices=5, pool_max_nao=512):
+                 etemp=300.0, maxiter=250, precision="fp64", slices=5, pool_max_nao=512, coop_blocks=0):
         import threading
         self.lib = load_library()
         self._tls = threading.local()
         env = self._env()
         self.h = C.c_void_p(self.lib.xtbgb_newServerEx(env.h, pool_gib, max_slots, plain_workers, iters_per_step,
                                                        accuracy, etemp, maxiter, 1 if precision == "split" else 0,
-                                                       slices, int(pool_max_nao)))
+                                                       slices, int(pool_max_nao), int(coop_blocks)))
         env.check()
         self._natoms = {}
 

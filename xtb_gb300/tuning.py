@@ -17,9 +17,11 @@ import numpy as np
 
 from . import interface as X
 
-# (plain workers, SCC iterations per pool step, largest molecule of the pool in AOs)
-CANDIDATES = ((4, 1, 512), (6, 1, 512), (8, 1, 512), (6, 2, 512), (6, 1, 384), (6, 1, 256), (8, 1, 256),
-              (6, 1, 192), (8, 1, 128))
+# (plain workers, SCC iterations per pool step, largest molecule of the pool in AOs, most blocks
+# of a worker's cooperative tridiagonalisation: 0 = one per SM)
+CANDIDATES = ((4, 1, 512, 0), (6, 1, 512, 0), (8, 1, 512, 0), (6, 2, 512, 0), (6, 1, 384, 0), (6, 1, 256, 0),
+              (8, 1, 256, 0), (6, 1, 192, 0), (8, 1, 128, 0), (6, 1, 256, 96), (6, 1, 256, 76), (6, 1, 256, 52),
+              (8, 1, 192, 76), (8, 1, 192, 52), (8, 1, 192, 38))
 _schedules = {}
 
 
@@ -35,22 +37,22 @@ def _stream_key(requests):
 
 
 def schedule(requests, candidates=CANDIDATES, pool_gib=24.0, precision="split", slices=5, max_slots=1024):
-    """Best (plain_workers, iters_per_step, pool_max_nao) for `requests` (dicts with numbers,
-    positions, gradient), with the span of each candidate's pass in seconds."""
+    """Best (plain_workers, iters_per_step, pool_max_nao, coop_blocks) for `requests` (dicts with
+    numbers, positions, gradient), with the span of each candidate's pass in seconds."""
     key = (_stream_key(requests), tuple(candidates), precision, slices)
     if key in _schedules:
         return _schedules[key]
     spans = {}
-    for workers, iters, pmax in candidates:
+    for workers, iters, pmax, coop in candidates:
         srv = X.Server(pool_gib=pool_gib, max_slots=max_slots, plain_workers=workers, iters_per_step=iters,
-                       precision=precision, slices=slices, pool_max_nao=pmax)
+                       precision=precision, slices=slices, pool_max_nao=pmax, coop_blocks=coop)
         ids = [srv.submit(r["numbers"], r["positions"], gradient=r["gradient"]) for r in requests]
         res = [srv.wait(i, check=False) for i in ids]
         srv.close()
-        spans[(workers, iters, pmax)] = max(x.t_done for x in res) - min(x.t_start for x in res)
+        spans[(workers, iters, pmax, coop)] = max(x.t_done for x in res) - min(x.t_start for x in res)
     best = min(spans, key=spans.get)
-    out = {"plain_workers": best[0], "iters_per_step": best[1], "pool_max_nao": best[2],
-           "span_s": {f"workers {w}, iterations per step {i}, pool up to {p} AOs": s
-                      for (w, i, p), s in spans.items()}}
+    out = {"plain_workers": best[0], "iters_per_step": best[1], "pool_max_nao": best[2], "coop_blocks": best[3],
+           "span_s": {f"workers {w}, iterations per step {i}, pool up to {p} AOs, cooperative blocks "
+                      f"{c if c else 'all'}": s for (w, i, p, c), s in spans.items()}}
     _schedules[key] = out
     return out
