@@ -463,6 +463,7 @@ def run_plain(args, ws, rank):
     metric, desc = workload_spec(args)
     Z, xyz = PLAIN_WORKLOADS[args.workload][1](W)
     lib = X.load_library()
+    X.autotune()          # the device's kernel forms, as the served run and the engine use them
     calc = X.Calculator(Z, xyz, keep_orbitals=False)
     for _ in range(args.warmup):
         r = calc.singlepoint()
@@ -528,6 +529,7 @@ def run_split(args, ws, rank):
     metric, desc = workload_spec(args)
     Z, xyz = SPLIT_WORKLOADS[args.workload][1](W)
     lib = X.load_library()
+    X.autotune()          # the device's kernel forms, as the served run and the engine use them
     cs = X.Calculator(Z, xyz, keep_orbitals=False, precision="split", slices=args.slices)
     for _ in range(args.warmup):
         r = cs.singlepoint()
