@@ -342,292 +342,381 @@ static void sytrd_launch(cudaStream_t st, int n, double* A, int lda, double* V, 
 // a x_i into (A x)_j), 4/3 n^3 flops in all -- the algorithmic count of LAPACK's dsytrd -- where
 // a full-row pass costs 2 n^3.
 //
-// One cooperative launch, ONE grid barrier per column s (trailing size m = n - s - 1, local
-// indices 0..m-1 for global s + 1 + i):
-//   A  the trailing upper triangle in tiles of 16 rows x L columns (L = 32 or 64, chosen per
-//      column so that every warp gets a few tiles): each tile applies the pending update of
-//      column s-1 (A -= v w^T + w v^T), writes the elements back, and adds its row sums and
-//      column sums of A x into ax (FP64 atomics; x is the column's pivot row, not yet
-//      normalised).  Three ax buffers rotate: the one of column s+2 is cleared during column s,
-//      so the barrier of column s+1 orders the clearing before its first addition.
-//   C  after the barrier every block forms, from ax and a0 (row 0 of the trailing matrix, final
-//      up to column s-1): x.(A x) and x.a0, then beta, tau and the scale of the reflector
-//      v = (x - beta e0) / (x0 - beta), with |x[1:]|^2 from the previous column's pass; the
-//      product y = tau A v = tau scale (A x - beta a0) and w = y - (tau/2)(y.v) v elementwise;
-//      the next pivot row x' = a0[1:] - w[1:] - w0 v[1:] and its norm.
-// Normalising one column late lets the norm come from the explicitly formed pivot row.  Outputs
-// follow the row-by-row form (V row s = v_s on columns s+1.., tau, d, e).  The atomic sums make
-// the last bits of the results depend on the order in which tiles finish.
+// One cooperative launch of P x Q blocks and ONE grid barrier per column s (pivot row s, trailing
+// rows and columns g = s+1 .. n-1, all indices global):
+//   tile pass  the trailing upper triangle in tiles of 16 rows x 32 RT columns, tile (I, c) owned
+//      by block (I mod P, c mod Q) -- on the rows of odd cycles I / P by block (I mod P,
+//      2 rL + 1 - c mod Q), rL the class of the last chunk -- for the whole reduction (a block
+//      with fewer tiles than warps
+//      splits them into row parts): each tile applies the pending update of column s-1
+//      (A -= v w^T + w v^T), writes the elements back, and adds its row sums and column sums of
+//      A x into ax (FP64 atomics; x is the column's pivot row, not yet normalised) and its share
+//      of x^T A x into the column's scalar (3 FMAs per tile from the reduced sums).  Three ax
+//      buffers rotate: the one of column s+2 is cleared during column s.
+//   vector phase  after the barrier one warp forms the column's scalars from five numbers
+//      (x^T A x, |x[1:]|^2, x_0 = pivot element, (A x)_0 = x . a0 by symmetry, a00): beta,
+//      tau, the reflector's scale, w0 (FP64 issue is scarce: the chain is not repeated in every
+//      warp) while the other threads have the operands of their first entries in flight; then
+//      each block forms v, w and the next pivot row x' = a0[1:] - w[1:] - w0 v[1:] ONLY on its
+//      own rows (row blocks I = p mod P) and columns (its two chunk classes), about m / P + 2 m / Q
+//      of the m entries, which is all its next tile pass reads.  Each entry has one owner block
+//      that writes V and adds x'^2 into the next column's |x[1:]|^2.
 constexpr int SYM_RB = 16;            // rows of a tile
-constexpr int SYM_MAXRT = 2;          // at most 32 * 2 columns per tile: a tile's 16 rows are
-                                      // loaded at once (the pass is bound by L2 latency otherwise)
 constexpr int SYM_NT = 256;
+constexpr int SYM_PF = 2;             // vector-phase entries per thread loaded with the column's scalars
+static_assert(SYM_NT == 256, "the block reduction of the tile pass sums 8 x 32 shares");
 
-__device__ __forceinline__ int sym_chunk_rt(int m, int nwarps) {
-    // tiles ~ m^2 / (2 * 16 * 32 rt): at least about four per warp before the tiles widen
-    const long long r = ((long long)m * m) / (4096LL * nwarps);
-    return (int)max(1LL, min((long long)SYM_MAXRT, r));
+// One task of the tile pass: rows r0 .. r0 + RPT - 1 of a tile, columns jt (-1 past the end).
+// A block with fewer tiles than warps splits its tiles into row parts (RPT = 16 / parts), so
+// that the FP64 work of a column with few tiles spreads over the block's four schedulers.
+template <int RT, int RPT>
+__device__ __forceinline__ void sym_load(double (&at)[SYM_RB][RT], const double* A, int lda, int g0, int r0,
+                                         const int (&jt)[RT]) {
+#pragma unroll
+    for (int rr = 0; rr < RPT; ++rr)
+#pragma unroll
+        for (int u = 0; u < RT; ++u) {
+            const int i = r0 + rr, j = jt[u];
+            at[rr][u] = (j >= i && i >= g0) ? A[(size_t)i * lda + j] : 0.0;
+        }
 }
 
-// task t of a step -> (row block I, chunk c); tasks are ordered by group a = I / q (q = L / 16
-// row blocks share the first chunk a), each row block of group a holding C - a chunks; gs[a] is
-// the first task of group a (gs[ngroups] = number of tasks)
-__device__ __forceinline__ void sym_task(int t, const int* gs, int ngroups, int C, int q, int& I, int& c) {
-    int lo = 0, hi = ngroups;   // gs[lo] <= t < gs[hi]
-    while (hi - lo > 1) {
-        const int mid = (lo + hi) >> 1;
-        if (gs[mid] <= t) lo = mid;
-        else hi = mid;
+template <int RT, int RPT>
+__device__ __forceinline__ void sym_compute(const double (&at)[SYM_RB][RT], double* A, int lda, int n, int g0, int r0,
+                                            const int (&jt)[RT], const double* X, const double* Vp,
+                                            const double* Wp, bool pend, double* ax, double& txa, int lane) {
+    double xj[RT], vpj[RT], wpj[RT], cacc[RT];
+#pragma unroll
+    for (int u = 0; u < RT; ++u) {
+        const int jj = jt[u] >= 0 ? jt[u] : 0;
+        xj[u] = X[jj];
+        vpj[u] = pend ? Vp[jj] : 0.0;
+        wpj[u] = pend ? Wp[jj] : 0.0;
+        cacc[u] = 0.0;
     }
-    const int off = t - gs[lo];
-    I = lo * q + off / (C - lo);
-    c = lo + off % (C - lo);
+    double rs[RPT];
+#pragma unroll
+    for (int rr = 0; rr < RPT; ++rr) {
+        const int i = r0 + rr;
+        double s0 = 0.0;
+        if (i >= g0 && i < n) {
+            const double xi = X[i];
+            const double vpi = pend ? Vp[i] : 0.0, wpi = pend ? Wp[i] : 0.0;
+            double* arow = A + (size_t)i * lda;
+#pragma unroll
+            for (int u = 0; u < RT; ++u) {
+                const int j = jt[u];
+                if (j >= i) {
+                    double a = at[rr][u];
+                    if (pend) {
+                        a = fma(-vpi, wpj[u], a);
+                        a = fma(-wpi, vpj[u], a);
+                        arow[j] = a;
+                    }
+                    s0 = fma(a, xj[u], s0);
+                    if (j > i) cacc[u] = fma(a, xi, cacc[u]);
+                }
+            }
+        }
+        rs[rr] = s0;
+    }
+    // row sums over the 32 lanes: reduce-scatter over the high lane bits (each level halves the
+    // rows a lane holds), then full sums over the rest; `row` collects the kept halves
+    int row = 0;
+#pragma unroll
+    for (int cnt = RPT, off = 16; cnt > 1; cnt >>= 1, off >>= 1) {
+        const bool hi = lane & off;
+#pragma unroll
+        for (int k = 0; k < cnt / 2; ++k) {
+            const double send = hi ? rs[k] : rs[k + cnt / 2];
+            rs[k] = (hi ? rs[k + cnt / 2] : rs[k]) + __shfl_xor_sync(0xffffffffu, send, off);
+        }
+        if (hi) row += cnt / 2;
+    }
+    constexpr int LV = RPT >= 16 ? 4 : RPT >= 8 ? 3 : RPT >= 4 ? 2 : RPT >= 2 ? 1 : 0;
+#pragma unroll
+    for (int off = 16 >> LV; off > 0; off >>= 1) rs[0] += __shfl_xor_sync(0xffffffffu, rs[0], off);
+    const int ir = r0 + row;
+    if ((lane & (32 / RPT - 1)) == 0 && ir >= g0 && ir < n) {
+        atomicAdd(&ax[ir], rs[0]);
+        txa = fma(X[ir], rs[0], txa);
+    }
+    const int ifirst = max(r0, g0);
+#pragma unroll
+    for (int u = 0; u < RT; ++u)
+        if (jt[u] > ifirst) {
+            atomicAdd(&ax[jt[u]], cacc[u]);
+            txa = fma(xj[u], cacc[u], txa);
+        }
 }
 
-__global__ void __launch_bounds__(SYM_NT) k_sytrd_sym(int n, double* __restrict__ A, int lda,
+template <int RT>
+__global__ void __launch_bounds__(SYM_NT) k_sytrd_sym(int n, int P, int Q, double* __restrict__ A, int lda,
                                                       double* __restrict__ V, double* __restrict__ tau,
                                                       double* __restrict__ d, double* __restrict__ e,
                                                       double* __restrict__ ws) {
+    constexpr int CW = 32 * RT;       // columns of a tile
     extern __shared__ double sm[];
-    double* xb[2] = {sm, sm + n};         // pivot row of the current / next column (unnormalised)
-    double* vps = sm + 2 * (size_t)n;     // pending update of the previous column: v, w (scratch
-    double* wps = vps + n;                // for A x and a0 between the tile pass and its rewrite)
-    double* red = wps + n;                // [2][8] block reductions
-    double* scal = red + 16;              // [16] scalars of the column
-    int* gs = reinterpret_cast<int*>(scal + 16);   // [n / 32 + 2] first task of each tile group
+    double* X = sm;                   // pivot row x of the current column (this block's entries)
+    double* Vp = X + n;               // v and w of the previous column (the pending update)
+    double* Wp = Vp + n;
+    double* r1 = Wp + n;              // [SYM_NT] per-thread shares of x^T A x
+    double* r2 = r1 + SYM_NT;         // [SYM_NT] per-thread shares of |x[1:]|^2
+    double* scal = r2 + SYM_NT;       // [8] the column's scalars
+    int* pre = reinterpret_cast<int*>(scal + 8);   // [R + 1] tiles before each of this block's row blocks
     cg::grid_group grid = cg::this_grid();
     const int G = gridDim.x;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int nwarps = G * (SYM_NT / 32);
-    const int gw = wid * G + blockIdx.x;   // consecutive tiles on consecutive SMs
+    const int p = blockIdx.x % P, q = blockIdx.x / P;
     const bool lead = blockIdx.x == 0;
-    auto axbuf = [&](int s) { return ws + (size_t)(s % 3) * n; };
-    // sum over the block of (a, b), every thread gets both
-    auto block_sum2 = [&](double a, double b, double& ra, double& rb) {
-        a = warp_sum(a);
-        b = warp_sum(b);
-        __syncthreads();
-        if (lane == 0) {
-            red[wid] = a;
-            red[8 + wid] = b;
+    const int nrb = (n + SYM_RB - 1) / SYM_RB, nch = (n + CW - 1) / CW;
+    const int R = nrb > p ? (nrb - p + P - 1) / P : 0;        // row blocks I = p + P a, a < R
+    // column classes: chunks c = q mod Q on the rows of even cycles I / P, c = q2 mod Q on the
+    // others.  Every row ends at the last chunk, so the classes just left of its class rL get one
+    // tile more on most rows; q2 mirrors q about rL (the class at distance d from the last chunk
+    // pairs with the one at distance Q - 1 - d), which evens the blocks' counts out
+    const int rL = (nch - 1) % Q;
+    const int q2 = ((2 * rL + 1 - q) % Q + Q) % Q;
+    const int NC = nch > q ? (nch - q + Q - 1) / Q : 0;                       // chunks q + Q b, b < NC
+    const int NC2 = (q2 != q && nch > q2) ? (nch - q2 + Q - 1) / Q : 0;       // chunks q2 + Q b
+    double* axb = ws;                                          // [3][n] A x of columns s mod 3
+    double* s_alpha = ws + 3 * (size_t)n;                      // [n] x_0 of column s
+    double* s_txa = s_alpha + n;                               // [n] x^T A x of column s
+    double* s_nx2 = s_txa + n;                                 // [n] |x[1:]|^2 of column s
+    // first chunk of this block at or right of the diagonal of row block I
+    auto cfirst = [&](int I) {
+        const int lo = (SYM_RB * I) / CW;
+        const int cls = ((I / P) & 1) ? q2 : q;
+        return lo + ((cls - lo) % Q + Q) % Q;
+    };
+    auto own = [&](int g) {
+        const int I = g / SYM_RB;
+        return (I % P) == p && ((I / P) % Q) == q;
+    };
+    // this block's entries at or after g0: its rows (row blocks I = p mod P), then its columns
+    // (chunks of its two classes) that are not rows; -1 for a skipped slot
+    int ea0 = 0, eb0 = 0, eb2 = 0, enr = 0, enc = 0, enc2 = 0;
+    auto entries = [&](int g0) {
+        const int Ia = g0 / SYM_RB;
+        ea0 = Ia <= p ? 0 : (Ia - p + P - 1) / P;
+        enr = max(0, R - ea0) * SYM_RB;
+        const int Cb = g0 / CW;
+        eb0 = Cb <= q ? 0 : (Cb - q + Q - 1) / Q;
+        enc = max(0, NC - eb0) * CW;
+        eb2 = Cb <= q2 ? 0 : (Cb - q2 + Q - 1) / Q;
+        enc2 = max(0, NC2 - eb2) * CW;
+        return enr + enc + enc2;
+    };
+    auto entry_at = [&](int g0, int t) {
+        int g;
+        if (t < enr) {
+            g = SYM_RB * (p + P * (ea0 + t / SYM_RB)) + (t % SYM_RB);
+        } else if (t < enr + enc) {
+            t -= enr;
+            g = CW * (q + Q * (eb0 + t / CW)) + (t % CW);
+            if ((g / SYM_RB) % P == p) return -1;
+        } else {
+            t -= enr + enc;
+            g = CW * (q2 + Q * (eb2 + t / CW)) + (t % CW);
+            if ((g / SYM_RB) % P == p) return -1;
         }
-        __syncthreads();
-        double t0 = 0.0, t1 = 0.0, u0 = 0.0, u1 = 0.0;
+        return (g >= g0 && g < n) ? g : -1;
+    };
+    // the tile pass of column s: tiles from pre[ta0] on, split into `parts` row parts
+    int ta0 = 0, tbase = 0, ntask = 0, parts = 1;
+    auto column_tasks = [&](int s) {
+        const int Ia = (s + 1) / SYM_RB;
+        ta0 = Ia <= p ? 0 : min(R, (Ia - p + P - 1) / P);
+        tbase = pre[ta0];
+        const int ntile = pre[R] - tbase;
+        parts = ntile >= 8 ? 1 : ntile >= 4 ? 2 : ntile >= 2 ? 4 : 8;
+        ntask = ntile * parts;
+    };
+    auto decode = [&](int t, int& r0, int (&jt)[RT]) {
+        const int T = tbase + t / parts, part = t % parts;
+        int lo = ta0, hi = R;   // pre[lo] <= T < pre[hi]
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (pre[mid] <= T) lo = mid;
+            else hi = mid;
+        }
+        const int I = p + P * lo;
+        const int c = cfirst(I) + (T - pre[lo]) * Q;
+        r0 = SYM_RB * I + part * (SYM_RB / parts);
 #pragma unroll
-        for (int w8 = 0; w8 < 8; w8 += 2) {
-            t0 += red[w8];
-            t1 += red[w8 + 1];
-            u0 += red[8 + w8];
-            u1 += red[9 + w8];
+        for (int u = 0; u < RT; ++u) {
+            const int j = c * CW + lane + 32 * u;
+            jt[u] = j < n ? j : -1;
         }
-        ra = t0 + t1;
-        rb = u0 + u1;
     };
 
-    // prologue: pivot row of column 0, its norm, the first two ax buffers cleared
-    {
-        double nx2 = 0.0;
-        for (int i = threadIdx.x; i < n - 1; i += SYM_NT) {
-            const double v = A[i + 1];
-            xb[0][i] = v;
-            if (i >= 1) nx2 = fma(v, v, nx2);
-        }
-        double dummy;
-        block_sum2(nx2, 0.0, scal[8], dummy);
-        const int per = (n + G - 1) / G;
-        for (int i = blockIdx.x * per + threadIdx.x; i < min(n, (blockIdx.x + 1) * per); i += SYM_NT) {
-            axbuf(0)[i] = 0.0;
-            axbuf(1)[i] = 0.0;
-        }
-        if (lead && threadIdx.x == 0) d[0] = A[0];
+    // prologue 1: the tile table, the scalar arrays and the first two ax buffers cleared
+    for (int a = threadIdx.x; a < R; a += SYM_NT) {
+        const int cf = cfirst(p + P * a);
+        pre[a + 1] = cf < nch ? (nch - 1 - cf) / Q + 1 : 0;
     }
     __syncthreads();
-    if (threadIdx.x == 0) scal[9] = scal[8];
+    if (threadIdx.x == 0) {
+        pre[0] = 0;
+        for (int a = 0; a < R; ++a) pre[a + 1] += pre[a];
+    }
+    for (size_t i = (size_t)blockIdx.x * SYM_NT + threadIdx.x; i < 6 * (size_t)n; i += (size_t)G * SYM_NT)
+        if (i < 2 * (size_t)n || i >= 3 * (size_t)n) ws[i] = 0.0;
     grid.sync();
+    // prologue 2: pivot row of column 0 on this block's entries, its norm
+    double nx2p = 0.0;
+    {
+        const int ne = entries(1);
+        for (int t = threadIdx.x; t < ne; t += SYM_NT) {
+            const int g = entry_at(1, t);
+            if (g < 0) continue;
+            const double v = A[g];
+            X[g] = v;
+            if (g >= 2 && own(g)) nx2p = fma(v, v, nx2p);
+        }
+    }
+    if (lead && threadIdx.x == 0) {
+        d[0] = A[0];
+        s_alpha[0] = A[1];
+    }
+    __syncthreads();
     bool pend = false;
-    int cur = 0;
+    double at[SYM_RB][RT];
     for (int s = 0; s < n - 2; ++s) {
-        const int m = n - s - 1, b = s + 1;
-        const double* x = xb[cur];
-        double* xn = xb[cur ^ 1];
-        double* A22 = A + (size_t)b * lda + b;
-        double* ax = axbuf(s);
-        const int rt = sym_chunk_rt(m, nwarps);
-        const int L = 32 * rt, q = L / SYM_RB;
-        const int nrb = (m + SYM_RB - 1) / SYM_RB, C = (m + L - 1) / L;
-        // ---- tiles
-        const int ngroups = (nrb + q - 1) / q;
-        {
-            // first task of group a: full groups hold q (C - a') tasks each, the last one may be short
-            const int afull = nrb / q;
-            for (int a = threadIdx.x; a <= ngroups; a += SYM_NT) {
-                const int k = min(a, afull);
-                int v = q * (k * C - k * (k - 1) / 2);
-                if (a > afull) v += (nrb - afull * q) * (C - afull);
-                gs[a] = v;
+        const int g0 = s + 1;
+        double* ax = axb + (size_t)(s % 3) * n;
+        // ---- tile pass
+        column_tasks(s);
+        double txa = 0.0;
+        for (int t = wid; t < ntask; t += SYM_NT / 32) {
+            int r0, jt[RT];
+            decode(t, r0, jt);
+            switch (parts) {
+                case 1:
+                    sym_load<RT, 16>(at, A, lda, g0, r0, jt);
+                    sym_compute<RT, 16>(at, A, lda, n, g0, r0, jt, X, Vp, Wp, pend, ax, txa, lane);
+                    break;
+                case 2:
+                    sym_load<RT, 8>(at, A, lda, g0, r0, jt);
+                    sym_compute<RT, 8>(at, A, lda, n, g0, r0, jt, X, Vp, Wp, pend, ax, txa, lane);
+                    break;
+                case 4:
+                    sym_load<RT, 4>(at, A, lda, g0, r0, jt);
+                    sym_compute<RT, 4>(at, A, lda, n, g0, r0, jt, X, Vp, Wp, pend, ax, txa, lane);
+                    break;
+                default:
+                    sym_load<RT, 2>(at, A, lda, g0, r0, jt);
+                    sym_compute<RT, 2>(at, A, lda, n, g0, r0, jt, X, Vp, Wp, pend, ax, txa, lane);
+                    break;
             }
         }
+        // this block's shares of x^T A x and (from the previous vector phase) |x[1:]|^2, summed by
+        // two warps on two schedulers
+        r1[threadIdx.x] = txa;
+        r2[threadIdx.x] = nx2p;
         __syncthreads();
-        const int ntask = gs[ngroups];
-        for (int t = gw; t < ntask; t += nwarps) {
-            int I, c;
-            sym_task(t, gs, ngroups, C, q, I, c);
-            const int i0 = I * SYM_RB;
-            double xj[SYM_MAXRT], vpj[SYM_MAXRT], wpj[SYM_MAXRT], cacc[SYM_MAXRT];
-            int jt[SYM_MAXRT];
-#pragma unroll
-            for (int u = 0; u < SYM_MAXRT; ++u) {
-                const int j = c * L + lane + 32 * u;
-                jt[u] = (u < rt && j < m) ? j : -1;
-                const int jj = jt[u] >= 0 ? j : 0;
-                xj[u] = x[jj];
-                vpj[u] = pend ? vps[jj + 1] : 0.0;
-                wpj[u] = pend ? wps[jj + 1] : 0.0;
-                cacc[u] = 0.0;
-            }
-            double rs[SYM_RB];
-            // the whole tile is loaded before any arithmetic: 16 rows x rt values per lane in flight
-            double at[SYM_RB][SYM_MAXRT];
-#pragma unroll
-            for (int rr = 0; rr < SYM_RB; ++rr)
-#pragma unroll
-                for (int u = 0; u < SYM_MAXRT; ++u) {
-                    const int i = i0 + rr, j = jt[u];
-                    at[rr][u] = (j >= i && i < m) ? A22[(size_t)i * lda + j] : 0.0;
-                }
-#pragma unroll
-            for (int rr = 0; rr < SYM_RB; ++rr) {
-                const int i = i0 + rr;
-                double s0 = 0.0;
-                if (i < m) {
-                    const double xi = x[i];
-                    const double vpi = pend ? vps[i + 1] : 0.0, wpi = pend ? wps[i + 1] : 0.0;
-                    double* arow = A22 + (size_t)i * lda;
-#pragma unroll
-                    for (int u = 0; u < SYM_MAXRT; ++u) {
-                        const int j = jt[u];
-                        if (j >= i) {
-                            double a = at[rr][u];
-                            if (pend) {
-                                a = fma(-vpi, wpj[u], a);
-                                a = fma(-wpi, vpj[u], a);
-                                arow[j] = a;
-                            }
-                            s0 = fma(a, xj[u], s0);
-                            if (j > i) cacc[u] = fma(a, xi, cacc[u]);
-                        }
-                    }
-                }
-                rs[rr] = s0;
-            }
-            // row sums over the 32 lanes: reduce-scatter, lane pair (2k, 2k+1) ends with row
-            // 8 b4 + 4 b3 + 2 b2 + b1 (b = lane bits)
-#pragma unroll
-            for (int k = 0; k < 8; ++k) {
-                const bool hi = lane & 16;
-                const double send = hi ? rs[k] : rs[k + 8];
-                rs[k] = (hi ? rs[k + 8] : rs[k]) + __shfl_xor_sync(0xffffffffu, send, 16);
-            }
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const bool hi = lane & 8;
-                const double send = hi ? rs[k] : rs[k + 4];
-                rs[k] = (hi ? rs[k + 4] : rs[k]) + __shfl_xor_sync(0xffffffffu, send, 8);
-            }
-#pragma unroll
-            for (int k = 0; k < 2; ++k) {
-                const bool hi = lane & 4;
-                const double send = hi ? rs[k] : rs[k + 2];
-                rs[k] = (hi ? rs[k + 2] : rs[k]) + __shfl_xor_sync(0xffffffffu, send, 4);
-            }
-            {
-                const bool hi = lane & 2;
-                const double send = hi ? rs[0] : rs[1];
-                rs[0] = (hi ? rs[1] : rs[0]) + __shfl_xor_sync(0xffffffffu, send, 2);
-            }
-            rs[0] += __shfl_xor_sync(0xffffffffu, rs[0], 1);
-            const int row = 8 * ((lane >> 4) & 1) + 4 * ((lane >> 3) & 1) + 2 * ((lane >> 2) & 1) + ((lane >> 1) & 1);
-            if (!(lane & 1) && i0 + row < m) atomicAdd(&ax[i0 + row], rs[0]);
-#pragma unroll
-            for (int u = 0; u < SYM_MAXRT; ++u)
-                if (jt[u] > i0) atomicAdd(&ax[jt[u]], cacc[u]);
+        if (wid < 2) {
+            const double* r = wid ? r2 : r1;
+            double v = ((r[lane] + r[lane + 32]) + (r[lane + 64] + r[lane + 96])) +
+                       ((r[lane + 128] + r[lane + 160]) + (r[lane + 192] + r[lane + 224]));
+            v = warp_sum(v);
+            if (lane == 0) atomicAdd(wid ? &s_nx2[s] : &s_txa[s], v);
         }
         grid.sync();
-        // ---- the column's reflector and update vectors, in every block
-        double sxa = 0.0, sx0 = 0.0;
-        for (int j = threadIdx.x; j < m; j += SYM_NT) {
-            const double a = ax[j], a0 = A22[j], xv = x[j];
-            vps[j] = a;   // the pending vectors are dead after the tile pass
-            wps[j] = a0;
-            sxa = fma(xv, a, sxa);
-            sx0 = fma(xv, a0, sx0);
+        // ---- the operands of this thread's first entries (they do not wait for the scalars)
+        const double* a0row = A + (size_t)g0 * lda;
+        const int ne = entries(g0);
+        int gp[SYM_PF];
+        double pa[SYM_PF], pa0[SYM_PF];
+#pragma unroll
+        for (int k = 0; k < SYM_PF; ++k) {
+            const int t = threadIdx.x + k * SYM_NT;
+            gp[k] = t < ne ? entry_at(g0, t) : -1;
+            pa[k] = gp[k] >= 0 ? ax[gp[k]] : 0.0;
+            pa0[k] = gp[k] >= 0 ? a0row[gp[k]] : 0.0;
         }
-        double txa, tx0;
-        block_sum2(sxa, sx0, txa, tx0);
-        if (threadIdx.x == 0) {
-            const double alpha = x[0], ax0 = vps[0], a00 = wps[0], t0 = scal[9];
-            double beta, tk, sc, yv;
+        // ---- the column's scalars (one warp: FP64 issue is scarce) while the others clear
+        if (wid == 0) {
+            const double alpha = s_alpha[s], t0 = s_nx2[s], txs = s_txa[s];
+            const double ax0 = ax[g0], a00 = a0row[g0];
+            double beta, tk, sc, h, w0;
             if (t0 == 0.0) {
                 tk = 0.0;
                 beta = alpha;
                 sc = 0.0;
-                yv = 0.0;
+                h = 0.0;
+                w0 = 0.0;
             } else {
-                beta = -copysign(sqrt(alpha * alpha + t0), alpha);
+                beta = -copysign(sqrt(fma(alpha, alpha, t0)), alpha);
                 tk = (beta - alpha) * rcp_fast(beta);
                 sc = rcp_fast(alpha - beta);
-                // y.v = tau sc^2 (x - beta e0).(A x - beta a0)
-                yv = tk * sc * sc * (txa - beta * tx0 - beta * ax0 + beta * beta * a00);
+                // y.v = tau sc^2 (x - beta e0).(A x - beta a0), x . a0 = (A x)_0
+                const double yv = tk * sc * sc * (txs - 2.0 * beta * ax0 + beta * beta * a00);
+                h = 0.5 * tk * yv;
+                w0 = tk * sc * (ax0 - beta * a00) - h;   // v0 = 1
             }
-            scal[0] = beta;
-            scal[1] = tk;
-            scal[2] = sc;
-            scal[3] = 0.5 * tk * yv;                            // h
-            scal[4] = tk * sc * (ax0 - beta * a00) - scal[3];   // w0 (v0 = 1)
-            if (lead) {
-                tau[s] = tk;
-                e[s] = beta;
-                d[s + 1] = a00 - 2.0 * scal[4];
-            }
-        }
-        __syncthreads();
-        double nx2 = 0.0;
-        {
-            const double beta = scal[0], tk = scal[1], sc = scal[2], h = scal[3], w0 = scal[4];
-            const double f = tk * sc;
-            for (int j = threadIdx.x; j < m; j += SYM_NT) {
-                const double a = vps[j], a0 = wps[j];
-                const double v = (j == 0) ? 1.0 : sc * x[j];
-                const double w = f * (a - beta * a0) - h * v;
-                vps[j] = v;
-                wps[j] = w;
-                if (j >= 1) {
-                    const double xv = a0 - w - w0 * v;
-                    xn[j - 1] = xv;
-                    if (j >= 2) nx2 = fma(xv, xv, nx2);
+            if (lane == 0) {
+                scal[0] = beta;
+                scal[1] = sc;
+                scal[2] = h;
+                scal[3] = w0;
+                scal[4] = tk * sc;
+                if (lead) {
+                    tau[s] = tk;
+                    e[s] = beta;
+                    d[s + 1] = a00 - 2.0 * w0;
                 }
             }
-            // this block's slices: row s of V (zeros left of column s + 1) and the ax buffer of
-            // column s + 2
-            const int pv = (n + G - 1) / G;
-            for (int c = blockIdx.x * pv + threadIdx.x; c < min(n, (blockIdx.x + 1) * pv); c += SYM_NT)
-                V[(size_t)s * n + c] = c < b ? 0.0 : (c == b ? 1.0 : sc * x[c - b]);
-            const int per = (m + G - 1) / G;
-            double* ax2 = axbuf(s + 2);
-            for (int j = blockIdx.x * per + threadIdx.x; j < min(m, (blockIdx.x + 1) * per); j += SYM_NT) ax2[j] = 0.0;
+        } else {
+            // this block's slices: zeros of row s of V left of column s + 1, the ax buffer of column s + 2
+            const int tid = threadIdx.x - 32, nt = SYM_NT - 32;
+            const int pv = (g0 + G - 1) / G;
+            for (int c = blockIdx.x * pv + tid; c < min(g0, (blockIdx.x + 1) * pv); c += nt)
+                V[(size_t)s * n + c] = 0.0;
+            double* ax2 = axb + (size_t)((s + 2) % 3) * n;
+            const int per = (n + G - 1) / G;
+            for (int j = blockIdx.x * per + tid; j < min(n, (blockIdx.x + 1) * per); j += nt) ax2[j] = 0.0;
         }
-        double tn, dummy;
-        block_sum2(nx2, 0.0, tn, dummy);
-        if (threadIdx.x == 0) scal[9] = tn;   // |x'[1:]|^2 of the next column
+        __syncthreads();
+        // ---- this block's entries of v, w and the next pivot row x'
+        const double beta = scal[0], sc = scal[1], h = scal[2], w0 = scal[3], f = scal[4];
+        nx2p = 0.0;
+        auto entry = [&](int g, double a, double a0) {
+            const double v = (g == g0) ? 1.0 : sc * X[g];
+            const double w = f * (a - beta * a0) - h * v;
+            Vp[g] = v;
+            Wp[g] = w;
+            const bool ow = own(g);
+            if (ow) V[(size_t)s * n + g] = v;
+            if (g > g0) {
+                const double xn = a0 - w - w0 * v;
+                X[g] = xn;
+                if (ow) {
+                    if (g == g0 + 1) {
+                        s_alpha[s + 1] = xn;
+                        if (g == n - 1) {
+                            // column n-3: the last pivot row is e[n-2]; the last diagonal takes
+                            // this column's update
+                            e[n - 2] = xn;
+                            d[n - 1] = A[(size_t)(n - 1) * lda + n - 1] - 2.0 * v * w;
+                        }
+                    } else {
+                        nx2p = fma(xn, xn, nx2p);
+                    }
+                }
+            }
+        };
+#pragma unroll
+        for (int k = 0; k < SYM_PF; ++k)
+            if (gp[k] >= 0) entry(gp[k], pa[k], pa0[k]);
+        for (int t = threadIdx.x + SYM_PF * SYM_NT; t < ne; t += SYM_NT) {
+            const int g = entry_at(g0, t);
+            if (g >= 0) entry(g, ax[g], a0row[g]);
+        }
         __syncthreads();
         pend = true;
-        cur ^= 1;
     }
     if (lead && threadIdx.x == 0) {
-        // rows n-2 and n-1: the last pivot row is e[n-2]; the last diagonal still lacks the
-        // update of column n-3 (v, w of length 2 in vps, wps)
-        e[n - 2] = xb[cur][0];
-        d[n - 1] = A[(size_t)(n - 1) * lda + n - 1] - 2.0 * vps[1] * wps[1];
         tau[n - 2] = 0.0;
         tau[n - 1] = 0.0;
         e[n - 1] = 0.0;
@@ -637,7 +726,25 @@ __global__ void __launch_bounds__(SYM_NT) k_sytrd_sym(int n, double* __restrict_
 }
 
 static size_t sytrd_sym_smem(int n) {
-    return (4 * (size_t)n + 32) * sizeof(double) + ((size_t)n / 32 + 2) * sizeof(int);
+    return (3 * (size_t)n + 2 * SYM_NT + 8) * sizeof(double) + ((size_t)n / SYM_RB + 2) * sizeof(int);
+}
+
+// P x Q blocks for at most G: a near-square factorisation keeps each block's share of the
+// vector phase small (m / P + 2 m / Q entries); up to a tenth of the blocks may stay idle for it
+static void sym_grid(int G, int& P, int& Q) {
+    double best = 1e30;
+    P = 1;
+    Q = std::max(1, G);
+    for (int g = G; g >= std::max(1, G - G / 10); --g)
+        for (int a = 1; a * a <= g; ++a) {
+            if (g % a) continue;
+            const double cost = 1.0 / a + 2.0 / (g / a) + 2.0 * (G - g) / G;
+            if (cost < best) {
+                best = cost;
+                P = a;
+                Q = g / a;
+            }
+        }
 }
 
 static void sytrd_sym_launch(cudaStream_t st, int n, double* A, int lda, double* V, double* tau, double* d, double* e,
@@ -646,13 +753,18 @@ static void sytrd_sym_launch(cudaStream_t st, int n, double* A, int lda, double*
     XG_CUDA(cudaGetDevice(&dev));
     XG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     const size_t smem = sytrd_sym_smem(n);
-    allow_max_dynamic_smem((const void*)k_sytrd_sym);
-    XG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxblk, k_sytrd_sym, SYM_NT, smem));
+    const bool wide = n >= 4096;
+    const void* fn = wide ? (const void*)k_sytrd_sym<2> : (const void*)k_sytrd_sym<1>;
+    allow_max_dynamic_smem(fn);
+    XG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxblk, fn, SYM_NT, smem));
     if (maxblk < 1) throw CudaError("sytrd: kernel does not fit on an SM");
-    int blocks = std::min(nsm, SYTRD_SLOTS);
-    if (max_blocks > 0) blocks = std::min(blocks, max_blocks);
-    void* args[] = {&n, &A, &lda, &V, &tau, &d, &e, &ws};
-    XG_CUDA(cudaLaunchCooperativeKernel((void*)k_sytrd_sym, blocks, SYM_NT, args, smem, st));
+    int G = std::min(nsm, SYTRD_SLOTS);
+    if (max_blocks > 0) G = std::min(G, max_blocks);
+    int P = 1, Q = 1;
+    sym_grid(G, P, Q);
+    const int blocks = P * Q;
+    void* args[] = {&n, &P, &Q, &A, &lda, &V, &tau, &d, &e, &ws};
+    XG_CUDA(cudaLaunchCooperativeKernel(fn, blocks, SYM_NT, args, smem, st));
     ++launch_counter();
 }
 
@@ -669,8 +781,8 @@ void sytrd_form(cudaStream_t st, int n, double* A, int lda, double* V, double* t
         XG_LAUNCH_CHECK();
         return;
     }
-    // the upper-triangle form (its three A x buffers live after the row form's 2n + 2 SYTRD_SLOTS
-    // doubles of p)
+    // the upper-triangle form (its three A x buffers and three per-column scalar arrays live after
+    // the row form's 2n + 2 SYTRD_SLOTS doubles of p)
     const bool sym_fits = n >= 3 && sytrd_sym_smem(n) <= 220 * 1024;
     if (form < 0) form = n >= tuned_sytrd_sym_min() ? 1 : 0;
     if (form == 1 && sym_fits) {

@@ -24,9 +24,9 @@ void trinv_upper(cudaStream_t st, int n, const double* U, int ldu, double* X, in
 // Householder tridiagonalisation of the symmetric n x n matrix A (one cooperative launch).
 // p: sytrd_workspace(n) doubles of device scratch.
 constexpr int SYTRD_SLOTS = 256;   // most blocks of the cooperative tridiagonalisation
-// the upper-triangle form (4/3 n^3 flops) keeps three A x buffers (3n doubles) after the row
-// form's 2n + 2 SYTRD_SLOTS
-inline size_t sytrd_workspace(int n) { return 5 * (size_t)n + 2 * (size_t)SYTRD_SLOTS; }
+// the upper-triangle form (4/3 n^3 flops) keeps three A x buffers and three per-column scalar
+// arrays (6n doubles) after the row form's 2n + 2 SYTRD_SLOTS
+inline size_t sytrd_workspace(int n) { return 8 * (size_t)n + 2 * (size_t)SYTRD_SLOTS; }
 void sytrd(cudaStream_t st, int n, double* A, int lda, double* V, double* tau, double* d, double* e, double* p);
 // the same with the form chosen: 0 the row-by-row form, 1 the upper-triangle form (when its
 // shared memory fits), -1 by the device's measured threshold (tune.h)

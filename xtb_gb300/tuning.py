@@ -7,8 +7,10 @@ Two levels:
   (``xtbgb_autotune``); the engine uses them from then on.
 * ``schedule(requests)``: the request loop's schedule -- plain-engine workers, SCC iterations
   per pool step and the largest molecule the resident pool takes -- measured on the caller's
-  own request stream: one pass of the stream per candidate on a fresh server, the shortest
-  device span wins.
+  own request stream: one pass of the stream per candidate on a fresh server; among the
+  candidates whose device span is within ``SPAN_TIE`` of the shortest, the lowest p99 latency
+  wins (the spans of the best candidates differ by less than the pass-to-pass spread, their
+  latencies by much more).
 
 Both keep their choices in this process (per device and, for the schedule, per stream), so a
 second call returns at once.
@@ -22,6 +24,7 @@ from . import interface as X
 CANDIDATES = ((4, 1, 512, 0), (6, 1, 512, 0), (8, 1, 512, 0), (6, 2, 512, 0), (6, 1, 384, 0), (6, 1, 256, 0),
               (8, 1, 256, 0), (6, 1, 192, 0), (8, 1, 128, 0), (6, 1, 256, 96), (6, 1, 256, 76), (6, 1, 256, 52),
               (8, 1, 192, 76), (8, 1, 192, 52), (8, 1, 192, 38))
+SPAN_TIE = 0.03
 _schedules = {}
 
 
@@ -38,11 +41,12 @@ def _stream_key(requests):
 
 def schedule(requests, candidates=CANDIDATES, pool_gib=24.0, precision="split", slices=5, max_slots=1024):
     """Best (plain_workers, iters_per_step, pool_max_nao, coop_blocks) for `requests` (dicts with
-    numbers, positions, gradient), with the span of each candidate's pass in seconds."""
+    numbers, positions, gradient), with the span and p99 latency of each candidate's pass in
+    seconds."""
     key = (_stream_key(requests), tuple(candidates), precision, slices)
     if key in _schedules:
         return _schedules[key]
-    spans = {}
+    spans, p99 = {}, {}
     for workers, iters, pmax, coop in candidates:
         srv = X.Server(pool_gib=pool_gib, max_slots=max_slots, plain_workers=workers, iters_per_step=iters,
                        precision=precision, slices=slices, pool_max_nao=pmax, coop_blocks=coop)
@@ -50,9 +54,13 @@ def schedule(requests, candidates=CANDIDATES, pool_gib=24.0, precision="split", 
         res = [srv.wait(i, check=False) for i in ids]
         srv.close()
         spans[(workers, iters, pmax, coop)] = max(x.t_done for x in res) - min(x.t_start for x in res)
-    best = min(spans, key=spans.get)
+        p99[(workers, iters, pmax, coop)] = float(np.percentile([x.latency for x in res], 99))
+    shortest = min(spans.values())
+    best = min((c for c in spans if spans[c] <= shortest * (1.0 + SPAN_TIE)), key=p99.get)
     out = {"plain_workers": best[0], "iters_per_step": best[1], "pool_max_nao": best[2], "coop_blocks": best[3],
            "span_s": {f"workers {w}, iterations per step {i}, pool up to {p} AOs, cooperative blocks "
-                      f"{c if c else 'all'}": s for (w, i, p, c), s in spans.items()}}
+                      f"{c if c else 'all'}": s for (w, i, p, c), s in spans.items()},
+           "p99_s": {f"workers {w}, iterations per step {i}, pool up to {p} AOs, cooperative blocks "
+                     f"{c if c else 'all'}": s for (w, i, p, c), s in p99.items()}}
     _schedules[key] = out
     return out
