@@ -360,8 +360,9 @@ def run_served(args, ws, rank):
     served_kernels = {
         "k_batch_scc": {"device_ms": round(pool_ms, 2), "tflops": (pool_flops / (pool_ms * 1e-3) / 1e12)
                         if pool_ms > 0 else None, "launches": int(d["steps"])},
-        "k_sytrd": {"device_ms": round(ssy_ms, 2), "tflops": (ssy_flops / (ssy_ms * 1e-3) / 1e12)
-                    if ssy_ms > 0 else None, "launches": int(sum(x.iterations for x in plain_res))},
+        "tridiagonalisation": {"kernels": sorted({sytrd_form(x.nao)[0] for x in plain_res}),
+                               "device_ms": round(ssy_ms, 2), "tflops": (ssy_flops / (ssy_ms * 1e-3) / 1e12)
+                               if ssy_ms > 0 else None, "launches": int(sum(x.iterations for x in plain_res))},
         "note": "CUDA-event times inside the served timed region, summed over concurrent requests "
                 "(they overlap, and include time queued behind other requests' kernels)",
     }

@@ -45,6 +45,25 @@ def test_results_do_not_depend_on_the_forms(precision):
     assert np.max(np.abs(a.gradient - b.gradient)) <= 1e-8
 
 
+def test_wide_tiles_match_the_row_form():
+    """From 4096 AOs the upper-triangle tridiagonalisation runs tiles of 16 x 64 (two columns per
+    lane): (H2O)683, 4098 AOs, in split mode, against the row form."""
+    Z, xyz = W.water_cluster(683, seed=5)
+    saved = X.get_tuning()
+    try:
+        X.set_tuning(3, saved["blocked_min_fp64"], saved["blocked_min_split"])
+        a = X.Calculator(Z, xyz, keep_orbitals=False, precision="split").singlepoint()
+        X.set_tuning(1 << 30, saved["blocked_min_fp64"], saved["blocked_min_split"])
+        b = X.Calculator(Z, xyz, keep_orbitals=False, precision="split").singlepoint()
+    finally:
+        X.set_tuning(saved["sytrd_sym_min"], saved["blocked_min_fp64"], saved["blocked_min_split"])
+    assert a.nao == 4098 and a.converged and b.converged
+    assert a.iterations == b.iterations
+    assert abs(a.energy - b.energy) <= 1e-8
+    assert np.max(np.abs(a.charges - b.charges)) <= 1e-7
+    assert np.max(np.abs(a.gradient - b.gradient)) <= 1e-7
+
+
 def test_schedule_choice_and_results():
     """The schedule tuner picks one of its candidates, and the results do not depend on the
     schedule: worker count, pool step, which molecules the pool takes (here up to 400 AOs or only
