@@ -763,8 +763,8 @@ def main():
     ap.add_argument("--pool-max-nao", type=int, default=None,
                     help="served: largest molecule (AOs) of the resident pool (default: autotuned)")
     ap.add_argument("--coop-blocks", type=int, default=None,
-                    help="served: most blocks of a worker's cooperative tridiagonalisation, 0 = all SMs "
-                         "(default: autotuned)")
+                    help="served: most blocks of a worker's cooperative tridiagonalisation, 0 = all SMs, "
+                         "-D = one per D AOs of the request (default: autotuned)")
     ap.add_argument("--cpu-batch-sample", type=int, default=512,
                     help="batch4096: molecules of the set the CPU restatement runs")
     ap.add_argument("--no-cpu-baseline", action="store_true")

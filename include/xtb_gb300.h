@@ -112,6 +112,11 @@ extern void xtbgb_setSolventKernel(xtb_TEnvironment env, xtb_TCalculator calc, i
  * upper-triangle form ms), then R2, then R2 rows (n, warp form ms, blocked FP64 ms, blocked
  * split ms).  Returns the number of values written (0 on error, reported on env). */
 extern int xtbgb_autotune(xtb_TEnvironment env, double* out, int nout);
+/* CUDA-event time in ms (best of reps, a device-to-device copy of the matrix included) of one
+ * tridiagonalisation of a random symmetric n x n matrix (3 <= n <= 8192) on the current device:
+ * form 0 the row form, 1 the upper-triangle form, -1 the tuned choice; max_blocks > 0 caps the
+ * cooperative grid.  Returns -1 on error (reported on env). */
+extern double xtbgb_sytrdMs(xtb_TEnvironment env, int n, int form, int max_blocks, int reps);
 /* The current device's choices: out[0..2] as above, out[3] 1 when measured, 0 for defaults. */
 extern void xtbgb_getTuning(xtb_TEnvironment env, double* out);
 /* Pin the current device's choices (sizes in AOs; for tests and for callers with their own
@@ -189,7 +194,8 @@ extern xtbgb_TServer xtbgb_newServer(xtb_TEnvironment env, double pool_gib, int 
  * (xtbgb_setPrecision semantics, `slices` digits); pool_max_nao (1..512, <= 0 for 512) is the
  * largest molecule in AOs the resident pool takes, larger ones go to the plain-engine workers;
  * coop_blocks > 0 caps the blocks of a worker's cooperative tridiagonalisation (0: one per SM),
- * so that the workers' single points can share the SMs. */
+ * so that the workers' single points can share the SMs; coop_blocks = -D caps it at one block per
+ * D AOs of the request (at least 8). */
 extern xtbgb_TServer xtbgb_newServerEx(xtb_TEnvironment env, double pool_gib, int max_slots, int plain_workers,
                                        int iters_per_step, double accuracy, double etemp, int maxiter, int split,
                                        int slices, int pool_max_nao, int coop_blocks);

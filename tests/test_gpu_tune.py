@@ -84,16 +84,16 @@ def test_schedule_choice_and_results():
 
 
 def test_capped_cooperative_tridiagonalisation():
-    """Both tridiagonalisation forms with a capped grid (16 and 40 blocks) give the single point
-    of the full grid: the request loop with every molecule on the workers against the plain
-    calculator."""
+    """Both tridiagonalisation forms with a capped grid (16 and 40 blocks, and one block per 20
+    AOs of the request) give the single point of the full grid: the request loop with every
+    molecule on the workers against the plain calculator."""
     reqs = W.served_stream(6, seed=9, nmin=40, nmax=300)
     saved = X.get_tuning()
     try:
         for sym in (1 << 30, 3):                           # row form, upper-triangle form
             X.set_tuning(sym, saved["blocked_min_fp64"], saved["blocked_min_split"])
             ref = [X.Calculator(r["numbers"], r["positions"], keep_orbitals=False).singlepoint() for r in reqs]
-            for cap in (16, 40):
+            for cap in (16, 40, -20):
                 srv = X.Server(pool_gib=1.0, max_slots=8, plain_workers=2, pool_max_nao=1, coop_blocks=cap)
                 out = [srv.wait(srv.submit(r["numbers"], r["positions"], gradient=r["gradient"])) for r in reqs]
                 srv.close()

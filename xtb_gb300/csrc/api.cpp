@@ -875,6 +875,25 @@ void xtbgb_setExternalChargesHardness(xtb_TEnvironment env, xtb_TCalculator calc
     set_external_charges(env, calc, n, nullptr, charges, positions, hardness, "xtbgb_setExternalChargesHardness");
 }
 
+double xtbgb_sytrdMs(xtb_TEnvironment env, int n, int form, int max_blocks, int reps) {
+    static const char* src = "xtbgb_sytrdMs";
+    if (!check_env(env)) return -1.0;
+    if (xg::device_count() == 0) {
+        env->error("no CUDA device available for the GFN2 engine", src);
+        return -1.0;
+    }
+    if (n < 3 || n > 8192 || form < -1 || form > 1) {
+        env->error("n must lie in 3..8192 and form in -1..1", src);
+        return -1.0;
+    }
+    try {
+        return xg::time_sytrd(n, form, max_blocks, reps);
+    } catch (const std::exception& e) {
+        env->error(e.what(), src);
+        return -1.0;
+    }
+}
+
 int xtbgb_autotune(xtb_TEnvironment env, double* out, int nout) {
     static const char* src = "xtbgb_autotune";
     if (!check_env(env)) return 0;
@@ -1224,7 +1243,7 @@ xtbgb_TServer xtbgb_newServerEx(xtb_TEnvironment env, double pool_gib, int max_s
     cfg.precision = split ? 1 : 0;
     cfg.slices = slices;
     cfg.pool_max_nao = pool_max_nao > 0 ? std::min(pool_max_nao, xg::BATCH_MAX_NAO) : xg::BATCH_MAX_NAO;
-    cfg.coop_blocks = std::max(0, coop_blocks);
+    cfg.coop_blocks = coop_blocks;
     auto* s = new _xtbgb_TServer();
     try {
         s->srv = std::make_unique<xg::Server>(cfg);

@@ -285,7 +285,11 @@ void Server::plain_loop() {
             ps.maxiter = cfg_.set.maxiter;
             ps.precision = cfg_.precision;
             ps.slices = cfg_.slices;
-            ps.max_coop_blocks = cfg_.coop_blocks;
+            // a cap proportional to the request's size: the per-column chain bounds a medium
+            // tridiagonalisation, so a few dozen blocks do it nearly as fast as every SM and leave
+            // the rest to the other requests
+            ps.max_coop_blocks = cfg_.coop_blocks >= 0 ? cfg_.coop_blocks
+                                                        : std::max(8, r->hm.nao / (-cfg_.coop_blocks));
             int least = 0, greatest = 0;
             XG_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
             ps.stream_priority = std::min(least, greatest + rank);

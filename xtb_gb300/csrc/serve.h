@@ -31,7 +31,8 @@ struct ServeConfig {
                                               // its SMs for that long; one measured best)
     int precision = 0, slices = 5;            // plain-engine workers: 1 = split-precision products
     int coop_blocks = 0;                      // plain-engine workers: most blocks of a cooperative
-                                              // tridiagonalisation (0: one per SM)
+                                              // tridiagonalisation (0: one per SM; -D: one per D
+                                              // AOs of the request, at least 8)
     int pool_max_nao = BATCH_MAX_NAO;         // largest molecule (AOs) admitted to the pool; larger
                                               // ones go to the plain-engine workers.  A pool step
                                               // holds its SMs for one SCC iteration of its largest

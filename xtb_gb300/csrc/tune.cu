@@ -87,6 +87,47 @@ void set_tuned(int sytrd_sym_min, int blocked_min_fp64, int blocked_min_split) {
     t.level = std::max(t.level, 1);
 }
 
+double time_sytrd(int n, int form, int max_blocks, int reps) {
+    if (n < 3 || n > 8192) throw std::runtime_error("time_sytrd: n must lie in 3..8192");
+    cudaStream_t st = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    XG_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    XG_CUDA(cudaEventCreate(&e0));
+    XG_CUDA(cudaEventCreate(&e1));
+    const size_t nn = (size_t)n * n;
+    const size_t doubles = 3 * nn + 3 * (size_t)n + sytrd_workspace(n);
+    double* A0 = nullptr;
+    double ms = 0.0;
+    XG_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&A0), doubles * sizeof(double), st));
+    try {
+        double* A = A0 + nn;
+        double* V = A + nn;
+        double* tau = V + nn;
+        double* d = tau + n;
+        double* e = d + n;
+        double* p = e + n;
+        k_tune_sym<<<ceil_div((long)n * n, 256), 256, 0, st>>>(n, 17u + n, A0);
+        XG_LAUNCH_CHECK();
+        ms = best_ms(st, e0, e1, std::max(1, reps), [&] {
+            XG_CUDA(cudaMemcpyAsync(A, A0, sizeof(double) * nn, cudaMemcpyDeviceToDevice, st));
+            sytrd_form(st, n, A, n, V, tau, d, e, p, form, max_blocks);
+        });
+    } catch (...) {
+        cudaFreeAsync(A0, st);
+        cudaStreamSynchronize(st);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        cudaStreamDestroy(st);
+        throw;
+    }
+    XG_CUDA(cudaFreeAsync(A0, st));
+    XG_CUDA(cudaStreamSynchronize(st));
+    XG_CUDA(cudaEventDestroy(e0));
+    XG_CUDA(cudaEventDestroy(e1));
+    XG_CUDA(cudaStreamDestroy(st));
+    return ms;
+}
+
 Tuned autotune() {
     const int dev = current_device();
     {

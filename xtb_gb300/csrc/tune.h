@@ -29,6 +29,10 @@ struct Tuned {
 Tuned tuned();
 // measure the crossovers on the current device (once; later calls return the kept choices)
 Tuned autotune();
+// CUDA-event time (ms, best of `reps`, the matrix copy included) of one tridiagonalisation of a
+// random symmetric n x n matrix: form 0 row form, 1 upper-triangle form, -1 the tuned choice;
+// max_blocks > 0 caps the cooperative grid
+double time_sytrd(int n, int form, int max_blocks, int reps);
 // replace the current device's choices (level 1; for tests that pin a form)
 void set_tuned(int sytrd_sym_min, int blocked_min_fp64, int blocked_min_split);
 // back-transformation threshold for a precision (0 FP64, 1 split)

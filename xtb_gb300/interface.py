@@ -90,6 +90,7 @@ def load_library(path=LIBPATH):
         "xtbgb_fp64PeakTflops": (C.c_double, []),
         "xtbgb_fp64PeakDetail": (None, [C.POINTER(C.c_double)]),
         "xtbgb_autotune": (C.c_int, [vp, dp, C.c_int]),
+        "xtbgb_sytrdMs": (C.c_double, [vp, C.c_int, C.c_int, C.c_int, C.c_int]),
         "xtbgb_setExternalChargesHardness": (None, [vp, vp, C.c_int, dp, dp, dp]),
         "xtbgb_writeRestart": (C.c_int, [vp, vp, vp, C.c_char_p]),
         "xtbgb_readRestart": (C.c_int, [vp, vp, vp, C.c_char_p]),
@@ -520,6 +521,17 @@ def autotune():
             "sytrd_ms": [{"n": int(a), "row_form": b, "upper_triangle_form": c} for a, b, c in rows1],
             "backtransform_ms": [{"n": int(a), "warp_form": b, "blocked_fp64": c, "blocked_split": d}
                                  for a, b, c, d in rows2]}
+
+
+def sytrd_ms(n, form=-1, max_blocks=0, reps=3):
+    """CUDA-event time (ms, best of reps) of one tridiagonalisation of a random symmetric n x n
+    matrix (xtbgb_sytrdMs): form 0 row form, 1 upper-triangle form, -1 the tuned choice;
+    max_blocks > 0 caps the cooperative grid."""
+    lib = load_library()
+    env = Environment(0)
+    ms = lib.xtbgb_sytrdMs(env.h, int(n), int(form), int(max_blocks), int(reps))
+    env.check()
+    return float(ms)
 
 
 def get_tuning():

@@ -20,10 +20,11 @@ import numpy as np
 from . import interface as X
 
 # (plain workers, SCC iterations per pool step, largest molecule of the pool in AOs, most blocks
-# of a worker's cooperative tridiagonalisation: 0 = one per SM)
-CANDIDATES = ((4, 1, 512, 0), (6, 1, 512, 0), (8, 1, 512, 0), (6, 2, 512, 0), (6, 1, 384, 0), (6, 1, 256, 0),
-              (8, 1, 256, 0), (6, 1, 192, 0), (8, 1, 128, 0), (6, 1, 256, 96), (6, 1, 256, 76), (6, 1, 256, 52),
-              (8, 1, 192, 76), (8, 1, 192, 52), (8, 1, 192, 38))
+# of a worker's cooperative tridiagonalisation: 0 = one per SM, -D = one per D AOs of the request)
+CANDIDATES = ((6, 1, 512, 0), (8, 1, 512, 0), (6, 1, 384, 0), (6, 1, 256, 0), (8, 1, 256, 0), (6, 1, 192, 0),
+              (6, 1, 256, 96), (6, 1, 256, 76), (8, 1, 192, 76), (6, 1, 256, -30), (8, 1, 256, -30),
+              (6, 1, 256, -25), (6, 1, 256, -20), (8, 1, 256, -20), (6, 1, 384, -20), (6, 1, 256, -15),
+              (8, 1, 256, -15), (6, 1, 256, -12))
 SPAN_TIE = 0.03
 _schedules = {}
 
@@ -37,6 +38,12 @@ def _stream_key(requests):
     sizes = tuple(len(r["numbers"]) for r in requests)
     first = float(np.asarray(requests[0]["positions"]).ravel()[0]) if requests else 0.0
     return sizes, first
+
+
+def _label(cand):
+    w, i, p, c = cand
+    blocks = "all" if c == 0 else (str(c) if c > 0 else f"one per {-c} AOs")
+    return f"workers {w}, iterations per step {i}, pool up to {p} AOs, cooperative blocks {blocks}"
 
 
 def schedule(requests, candidates=CANDIDATES, pool_gib=24.0, precision="split", slices=5, max_slots=1024):
@@ -58,9 +65,7 @@ def schedule(requests, candidates=CANDIDATES, pool_gib=24.0, precision="split", 
     shortest = min(spans.values())
     best = min((c for c in spans if spans[c] <= shortest * (1.0 + SPAN_TIE)), key=p99.get)
     out = {"plain_workers": best[0], "iters_per_step": best[1], "pool_max_nao": best[2], "coop_blocks": best[3],
-           "span_s": {f"workers {w}, iterations per step {i}, pool up to {p} AOs, cooperative blocks "
-                      f"{c if c else 'all'}": s for (w, i, p, c), s in spans.items()},
-           "p99_s": {f"workers {w}, iterations per step {i}, pool up to {p} AOs, cooperative blocks "
-                     f"{c if c else 'all'}": s for (w, i, p, c), s in p99.items()}}
+           "span_s": {_label(c): s for c, s in spans.items()},
+           "p99_s": {_label(c): s for c, s in p99.items()}}
     _schedules[key] = out
     return out
