@@ -12,6 +12,7 @@ import pytest
 
 from helpers import TOL_E, TOL_G, TOL_ITER, TOL_Q, case_geometry, evaluate, golden
 from oracle import gfn2
+from oracle.params import EVTOAU
 from xtb_gb300 import interface as X
 from xtb_gb300 import workloads as W
 
@@ -115,6 +116,23 @@ def test_full_size_invariants():
     em = calc.singlepoint().energy
     fd = (ep - em) / (2 * h)
     assert abs(fd - np.sum(r.gradient * d)) < 1e-6 * max(1.0, abs(fd))
+
+
+@pytest.mark.parametrize("etemp", [5000.0, 20000.0])
+def test_smearing_beyond_the_first_levels(etemp):
+    """Inside the SCC the engine bisects the lowest nocc + 32 levels first; at high electronic
+    temperature the occupations reach past them, the device gate bisects the rest and the
+    smearing runs again: the single point still matches the oracle, orbital energies included."""
+    Z, xyz = W.water_cluster(20, seed=2)
+    Z, xyz = np.asarray(Z), np.asarray(xyz)
+    r = X.Calculator(Z, xyz, etemp=etemp).singlepoint()
+    o = gfn2.singlepoint(Z, xyz, etemp=etemp)
+    assert r.converged and o.converged
+    assert abs(r.energy - o.energy) < TOL_E * 1e-2
+    assert np.max(np.abs(r.charges - o.q)) < TOL_Q * 1e-2
+    assert np.max(np.abs(r.gradient - o.gradient)) < TOL_G * 1e-3
+    assert abs(r.iterations - o.iterations) <= TOL_ITER
+    assert np.max(np.abs(r.emo - o.emo * EVTOAU)) < 1e-9     # Hartree against the oracle's eV
 
 
 def test_warm_start_and_determinism():

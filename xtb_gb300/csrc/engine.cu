@@ -658,8 +658,17 @@ void run_singlepoint(const HostMol& hm, const SPSettings& set, Wavefunction& wfn
         sytrd_form(st, nao, A, nao, V, tri_tau, tri_d, tri_e, tri_p, -1, set.max_coop_blocks);
         // eigenvalues, occupations, then eigenvectors of the occupied orbitals only
         tm.mark(PH_TRIEIG);
-        tridiag_eigvals(st, nao, tri_d, tri_e, tri_e2, bounds, emo);
+        // inside the SCC only the levels that can carry occupation are needed: the lowest
+        // nocc + max(32, n / 16), unless the smearing reaches further (then the rest follow, still
+        // on the device); the last diagonalisation computes all of them for the results
+        const bool all_levels = lastdiag || it == maxit;
+        const int klev = all_levels ? nao : std::min(nao, std::max(hm.nel_a, hm.nel_b) + std::max(32, nao / 16));
+        tridiag_eigvals(st, nao, tri_d, tri_e, tri_e2, bounds, emo, klev);
         fermi(st, nao, emo, hm.nel_a, hm.nel_b, set.etemp, focc, focca, foccb, fscal, info + 1);
+        if (klev < nao) {
+            tridiag_eigvals_rest(st, nao, tri_d, tri_e2, bounds, emo, klev, fscal, KB_AU * AUTOEV * set.etemp, info + 2);
+            fermi(st, nao, emo, hm.nel_a, hm.nel_b, set.etemp, focc, focca, foccb, fscal, info + 1, info + 2);
+        }
         tridiag_eigvecs(st, nao, tri_d, tri_e, bounds, emo, Y, iscr, piv, info + 1);
         tm.mark(PH_BACKTR);
         // Y[:, :kocc] = Q Y: compact-WY GEMMs pay off for large n, one warp per vector below

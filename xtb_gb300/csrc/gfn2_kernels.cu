@@ -293,12 +293,15 @@ void build_hu(cudaStream_t st, const DevMol& m, Thresholds th, const double* H0,
 
 __global__ void k_fermi(int n, const double* __restrict__ emo, int nel_a, int nel_b, double etemp,
                         double* __restrict__ focc, double* __restrict__ fa, double* __restrict__ fb,
-                        double* __restrict__ scal, int* __restrict__ kocc) { d_fermi(n, emo, nel_a, nel_b, etemp, focc, fa, fb, scal, kocc); }
+                        double* __restrict__ scal, int* __restrict__ kocc, const int* __restrict__ gate) {
+    if (gate && *gate == 0) return;
+    d_fermi(n, emo, nel_a, nel_b, etemp, focc, fa, fb, scal, kocc);
+}
 
 
 void fermi(cudaStream_t st, int n, const double* emo, int nel_a, int nel_b, double etemp, double* focc, double* fa,
-           double* fb, double* scal, int* kocc) {
-    k_fermi<<<1, 1024, 0, st>>>(n, emo, nel_a, nel_b, etemp, focc, fa, fb, scal, kocc);
+           double* fb, double* scal, int* kocc, const int* gate) {
+    k_fermi<<<1, 1024, 0, st>>>(n, emo, nel_a, nel_b, etemp, focc, fa, fb, scal, kocc, gate);
     XG_LAUNCH_CHECK();
 }
 

@@ -86,8 +86,9 @@ void build_hu(cudaStream_t st, const DevMol& m, Thresholds th, const double* H0,
               const double* Q, const double* shift, const double* vs, const double* vd, const double* vq, double* H);
 // Fermi smearing (one block): focc = fa + fb (alpha, beta occupations), scal = {entropy term, e_fermi_a, e_fermi_b}
 // kocc[0] = number of leading orbitals with non-zero occupation
+// (only when *gate != 0, if gate is given)
 void fermi(cudaStream_t st, int n, const double* emo, int nel_a, int nel_b, double etemp, double* focc, double* fa,
-           double* fb, double* scal, int* kocc);
+           double* fb, double* scal, int* kocc, const int* gate = nullptr);
 // scale columns: Cf[i][j] = C[i][j] * f[j]
 void scale_cols(cudaStream_t st, int n, const double* C, const double* f, double* Cf);
 // Mulliken + multipole row sums and per-atom/shell reduction

@@ -802,19 +802,44 @@ __global__ void k_tri_prep(int n, const double* __restrict__ d, const double* __
     d_tri_prep(n, d, e, e2, bounds);
 }
 
-// One warp per block handles 32 / BIS_G eigenvalues, so the eigenvalues spread over as many
-// SMs as possible (FP64 latency, not throughput, is the limit); d, e^2 and their FP32 copies
-// are staged in shared memory (dynamic, 2n doubles + 2n floats).
+// One warp per block handles 32 / G eigenvalues, so the eigenvalues spread over as many SMs as
+// possible; d, e^2 and their FP32 copies are staged in shared memory (dynamic, 2n doubles + 2n
+// floats).  A warp's time is its chain of multisection rounds, each a few Sturm counts of n
+// dependent FP64 steps, so the launch takes the largest group G whose warps still find a
+// scheduler each: a (G + 1)-fold bracket per round needs fewer rounds.
+// Eigenvalues j0 .. j1 - 1 (only when *gate != 0, if gate is given); w[j1 .. n) = BIS_ABOVE when
+// fill is set.
+constexpr double BIS_ABOVE = 1.0e300;
+template <int G>
 __global__ void __launch_bounds__(32) k_bisect(int n, const double* __restrict__ d, const double* __restrict__ e2,
-                                               const double* __restrict__ bounds, double* __restrict__ w) {
+                                               const double* __restrict__ bounds, double* __restrict__ w, int j0,
+                                               int j1, const int* __restrict__ gate, bool fill) {
+    if (gate && *gate == 0) return;   // the whole block (one warp) leaves together
+    const int jb = j0 + blockIdx.x * (32 / G);
+    const int j = jb + (int)(threadIdx.x / G);
+    if (jb >= j1) {                    // every group of this block lies above the range
+        if (fill && j < n && threadIdx.x % G == 0) w[j] = BIS_ABOVE;
+        return;
+    }
+    // all 32 lanes stay from here on: the staging is strided over them and the group shuffles
+    // name the full warp
     extern __shared__ double sde[];
     stage_tridiag(n, d, e2, sde);
     __syncthreads();
     const float* fsm = reinterpret_cast<const float*>(sde + 2 * n);
-    const int j = blockIdx.x * (32 / BIS_G) + (int)(threadIdx.x / BIS_G);
-    const bool valid = j < n;
-    const double v = d_bisect_group<false>(n, sde, sde + n, fsm, fsm + n, bounds, valid ? j : 0, valid);
-    if (valid && threadIdx.x % BIS_G == 0) w[j] = v;
+    const bool valid = j < j1;
+    const double v = d_bisect_group<false, G>(n, sde, sde + n, fsm, fsm + n, bounds, valid ? j : 0, valid);
+    if (threadIdx.x % G == 0) {
+        if (valid) w[j] = v;
+        else if (fill && j < n) w[j] = BIS_ABOVE;
+    }
+}
+
+// gate = 1 when the levels above the first k may carry occupation: the k-th lies less than
+// 60 kT above either Fermi level (the smearing gives exactly zero from 50 kT on)
+__global__ void k_levels_gate(int k, const double* __restrict__ w, const double* __restrict__ scal, double bkt,
+                              int* __restrict__ gate) {
+    gate[0] = (w[k - 1] - fmax(scal[1], scal[2]) < 60.0 * bkt) ? 1 : 0;
 }
 
 // ------------------------------------------------------------------ inverse iteration
@@ -837,16 +862,46 @@ __global__ void k_reorth(int n, const double* __restrict__ w, const double* __re
     d_reorth(n, w, bounds, ctol, Y, U1, U2, U3, ML, piv, nc, j, lane);
 }
 
-void tridiag_eigvals(cudaStream_t st, int n, const double* d, const double* e, double* e2, double* bounds,
-                     double* w) {
-    k_tri_prep<<<1, 256, 0, st>>>(n, d, e, e2, bounds);
-    XG_LAUNCH_CHECK();
+// eigenvalues j0 .. j1 - 1 (and the fill of w[j1 .. n)) with the group size for j1 - j0 of them
+static void bisect_launch(cudaStream_t st, int n, const double* d, const double* e2, const double* bounds, double* w,
+                          int j0, int j1, const int* gate, bool fill) {
     const size_t smem = 2 * (size_t)n * (sizeof(double) + sizeof(float));
     if (smem > 200 * 1024) throw CudaError("tridiag_eigvals: matrix too large for the shared-memory bisection");
-    if (smem > 48 * 1024)
-        allow_max_dynamic_smem((const void*)k_bisect);
-    k_bisect<<<ceil_div(n, 32 / BIS_G), 32, smem, st>>>(n, d, e2, bounds, w);
+    int dev = 0, nsm = 0;
+    XG_CUDA(cudaGetDevice(&dev));
+    XG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    // warps = count G / 32 up to one per scheduler (four per SM)
+    const int count = std::max(1, j1 - j0), slots = 4 * nsm;
+    int G = 4;
+    while (G < 32 && (long)count * (2 * G) <= 32L * slots) G *= 2;
+    const int span = fill ? n - j0 : j1 - j0;
+    auto go = [&](auto kern, int g) {
+        if (smem > 48 * 1024) allow_max_dynamic_smem((const void*)kern);
+        kern<<<ceil_div(span, 32 / g), 32, smem, st>>>(n, d, e2, bounds, w, j0, j1, gate, fill);
+    };
+    switch (G) {
+        case 4: go(k_bisect<4>, 4); break;
+        case 8: go(k_bisect<8>, 8); break;
+        case 16: go(k_bisect<16>, 16); break;
+        default: go(k_bisect<32>, 32); break;
+    }
     XG_LAUNCH_CHECK();
+}
+
+void tridiag_eigvals(cudaStream_t st, int n, const double* d, const double* e, double* e2, double* bounds,
+                     double* w, int k) {
+    k_tri_prep<<<1, 256, 0, st>>>(n, d, e, e2, bounds);
+    XG_LAUNCH_CHECK();
+    const int j1 = (k > 0 && k < n) ? k : n;
+    bisect_launch(st, n, d, e2, bounds, w, 0, j1, nullptr, j1 < n);
+}
+
+void tridiag_eigvals_rest(cudaStream_t st, int n, const double* d, const double* e2, const double* bounds, double* w,
+                          int k, const double* scal, double bkt, int* gate) {
+    if (k <= 0 || k >= n) return;
+    k_levels_gate<<<1, 1, 0, st>>>(k, w, scal, bkt, gate);
+    XG_LAUNCH_CHECK();
+    bisect_launch(st, n, d, e2, bounds, w, k, n, gate, false);
 }
 
 void tridiag_eigvecs(cudaStream_t st, int n, const double* d, const double* e, const double* bounds, const double* w,

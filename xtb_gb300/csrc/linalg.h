@@ -33,8 +33,16 @@ void sytrd(cudaStream_t st, int n, double* A, int lda, double* V, double* tau, d
 // max_blocks > 0 caps the cooperative grid (so that concurrent single points can share the SMs)
 void sytrd_form(cudaStream_t st, int n, double* A, int lda, double* V, double* tau, double* d, double* e, double* p,
                 int form, int max_blocks = 0);
-// eigenvalues of the tridiagonal (d, e): w[n] ascending; e2: n, bounds: 4
-void tridiag_eigvals(cudaStream_t st, int n, const double* d, const double* e, double* e2, double* bounds, double* w);
+// eigenvalues of the tridiagonal (d, e): w[n] ascending; e2: n, bounds: 4.  With 0 < k < n only
+// the lowest k (each is bisected on its own, so they equal those of the full call) and
+// w[k..n) = 1e300.
+void tridiag_eigvals(cudaStream_t st, int n, const double* d, const double* e, double* e2, double* bounds, double* w,
+                     int k = -1);
+// after tridiag_eigvals(..., k) and the Fermi smearing (scal = {entropy, e_fermi_a, e_fermi_b},
+// energies in the units of bkt): gate[0] = 1 and the levels k..n-1 bisected when the k-th level
+// lies less than 60 kT above a Fermi level, else gate[0] = 0 and nothing more
+void tridiag_eigvals_rest(cudaStream_t st, int n, const double* d, const double* e2, const double* bounds, double* w,
+                          int k, const double* scal, double bkt, int* gate);
 // eigenvectors j < *ncol (all if ncol is null): Y[i*n+j] = component i of vector j.
 // scratch: 4*n*n doubles, pivbuf: n*n bytes
 void tridiag_eigvecs(cudaStream_t st, int n, const double* d, const double* e, const double* bounds, const double* w,

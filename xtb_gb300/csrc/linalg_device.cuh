@@ -528,8 +528,8 @@ __device__ inline void d_tri_prep(int n, const double* __restrict__ d, const dou
 }
 
 // Eigenvalue j of T to an absolute accuracy of 2 eps ||T|| (the accuracy inverse iteration
-// needs) by multisection: the BIS_G lanes of a group evaluate Sturm counts at BIS_G interior
-// points of the bracket, which shrinks (BIS_G + 1)-fold per round.  The bracket is first
+// needs) by multisection: the G lanes of a group evaluate Sturm counts at G interior points of
+// the bracket, which shrinks (G + 1)-fold per round.  The bracket is first
 // narrowed with FP32 counts to about 1e-6 ||T||, widened by a margin far above the FP32
 // backward error, and verified with two FP64 counts (falling back to the Gershgorin bracket
 // if the check fails); FP64 rounds then finish it.  Must be called by all 32 lanes of a warp
@@ -542,12 +542,13 @@ constexpr int BIS_G = 4;
 // limit (the batched engine: +9% single points/s on the mixed set); on the plain engine's
 // large clusters (many near-degenerate levels) Newton often falls back to multisection, and the
 // latency-bound launch measured slower, so it is off there.
-template <bool NEWTON>
+template <bool NEWTON, int G = BIS_G>
 __device__ inline double d_bisect_group(int n, const double* sd, const double* se2, const float* fd, const float* fe2,
                                         const double* __restrict__ bounds, int j, bool valid) {
     const unsigned FULL = 0xffffffffu;
-    const int lane = threadIdx.x & 31, gl = lane % BIS_G, gbase = lane - gl;
-    const unsigned gmask = ((1u << BIS_G) - 1u) << gbase;
+    static_assert(G >= 2 && G <= 32 && (G & (G - 1)) == 0, "group of 2..32 lanes, a power of two");
+    const int lane = threadIdx.x & 31, gl = lane % G, gbase = lane - gl;
+    const unsigned gmask = (G == 32 ? 0xffffffffu : ((1u << G) - 1u)) << gbase;
     const double glo = bounds[0], ghi = bounds[1];
     const double tn = fmax(bounds[3], 1e-300);
     const double atol = 2.0 * 2.220446049250313e-16 * tn;
@@ -559,14 +560,14 @@ __device__ inline double d_bisect_group(int n, const double* sd, const double* s
     for (int r = 0; r < 48; ++r) {
         fact = fact && (fhi - flo > ftol);
         if (!__any_sync(FULL, fact)) break;
-        const float h = (fhi - flo) / (float)(BIS_G + 1);
+        const float h = (fhi - flo) / (float)(G + 1);
         const float x = flo + h * (float)(gl + 1);
         const int c = fact ? sturm_count32(n, fd, fe2, x, pivf) : 0;
         const unsigned bits = (__ballot_sync(FULL, fact && c > j) & gmask) >> gbase;
         if (fact) {
-            const int k = bits ? __ffs(bits) - 1 : BIS_G;
+            const int k = bits ? __ffs(bits) - 1 : G;
             const float nlo = (k == 0) ? flo : flo + h * (float)k;
-            const float nhi = (k == BIS_G) ? fhi : flo + h * (float)(k + 1);
+            const float nhi = (k == G) ? fhi : flo + h * (float)(k + 1);
             if (nlo == flo && nhi == fhi) fact = false;
             flo = nlo;
             fhi = nhi;
@@ -626,14 +627,14 @@ __device__ inline double d_bisect_group(int n, const double* sd, const double* s
     for (int r = 0; r < 80; ++r) {
         act = act && (hi - lo > atol);
         if (!__any_sync(FULL, act)) break;
-        const double h = (hi - lo) / (double)(BIS_G + 1);
+        const double h = (hi - lo) / (double)(G + 1);
         const double x = lo + h * (double)(gl + 1);
         const int c = act ? sturm_count(n, sd, se2, x) : 0;
         const unsigned bits = (__ballot_sync(FULL, act && c > j) & gmask) >> gbase;
         if (act) {
-            const int k = bits ? __ffs(bits) - 1 : BIS_G;
+            const int k = bits ? __ffs(bits) - 1 : G;
             const double nlo = (k == 0) ? lo : lo + h * (double)k;
-            const double nhi = (k == BIS_G) ? hi : lo + h * (double)(k + 1);
+            const double nhi = (k == G) ? hi : lo + h * (double)(k + 1);
             if (nlo == lo && nhi == hi) act = false;
             lo = nlo;
             hi = nhi;
