@@ -334,7 +334,8 @@ __device__ void scc_iteration(BatchMol* b, const DevThresh& th, double etemp, in
     WARP_FOR(j, kocc) d_reorth(nao, b->emo, b->bounds, 1.0e-7, b->Y, U1, U1 + nn, U1 + 2 * nn, U1 + 3 * nn, b->piv,
                                kocc, j, lane);
     __syncthreads();
-    WARP_FOR(j, kocc) d_ormtr(nao, b->V, b->tri_tau, b->Y, b->Zt, j, lane, sm + (size_t)(4 + wid) * nao);
+    // Z = Q Y: one occupied column per lane, 32 per warp
+    for (int g = wid; g * 32 < kocc; g += (int)(blockDim.x >> 5)) d_ormtr_cols(nao, b->V, b->tri_tau, b->Y, b->Zt, g * 32, kocc, lane);
     __syncthreads();
     // C = X Z, P = C f C^T
     cta_dgemm<false, true>(nao, nao, nao, 1.0, b->X, nao, b->Zt, nao, 0.0, b->C, nao, GF_A_UPPER, nullptr, b->kocc, sm);

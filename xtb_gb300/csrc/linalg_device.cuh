@@ -914,6 +914,38 @@ __device__ inline void d_ormtr(int n, const double* __restrict__ V, const double
     for (int i = lane; i < n; i += 32) Zt[(size_t)j * n + i] = y[i];
 }
 
+// Zt[j][:] = Q Y[:, j] for the columns j0 .. j0 + 31 below ncol, one column per lane of the
+// calling warp, Y (row-major, updated in place) read and written a row of 32 columns at a time
+// and each reflector broadcast from V.  A warp-wide FP64 instruction costs the same with one lane
+// active as with 32, so this form spends about n^2 of them on 32 columns where the one-warp-per-
+// column form spends n^2 / 32 + 7 n on each (its dot products end in a five-level shuffle sum).
+// Lanes past ncol read column j0 (valid) and store nothing.
+__device__ inline void d_ormtr_cols(int n, const double* __restrict__ V, const double* __restrict__ tau,
+                                    double* __restrict__ Y, double* __restrict__ Zt, int j0, int ncol, int lane) {
+    const int j = j0 + lane;
+    const bool ok = j < ncol;
+    double* yc = Y + (ok ? j : j0);
+    for (int k = n - 3; k >= 0; --k) {
+        const double t = tau[k];
+        if (t == 0.0) continue;
+        const double* vk = V + (size_t)k * n;
+        double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+        int i = k + 1;
+        for (; i + 3 < n; i += 4) {
+            s0 = fma(vk[i], yc[(size_t)i * n], s0);
+            s1 = fma(vk[i + 1], yc[(size_t)(i + 1) * n], s1);
+            s2 = fma(vk[i + 2], yc[(size_t)(i + 2) * n], s2);
+            s3 = fma(vk[i + 3], yc[(size_t)(i + 3) * n], s3);
+        }
+        for (; i < n; ++i) s0 = fma(vk[i], yc[(size_t)i * n], s0);
+        const double s = ((s0 + s1) + (s2 + s3)) * t;
+        if (ok)
+            for (i = k + 1; i < n; ++i) yc[(size_t)i * n] = fma(-s, vk[i], yc[(size_t)i * n]);
+    }
+    if (ok)
+        for (int i = 0; i < n; ++i) Zt[(size_t)j * n + i] = yc[(size_t)i * n];
+}
+
 
 
 // ------------------------------------------------------------------ one-block routines (batched engine)
