@@ -101,6 +101,21 @@ def test_energy_only_and_repeat(mixed):
 
 
 @pytest.mark.gpu
+def test_hot_smearing_matches_plain_engine():
+    """At 20000 K the occupations reach past the levels the batched SCC bisects first (nocc +
+    max(8, n / 8)): the block bisects the rest and smears again, and the batch still matches
+    the plain engine."""
+    mols = [W.water_cluster(m, seed=20 + m) for m in (3, 8)] + [W.alkane(6, 0.02, seed=4)]
+    r = X.Batch(mols).run(etemp=20000.0)
+    assert np.all(r.status == 0) and np.all(r.engine == 0)
+    for i, (Z, xyz) in enumerate(mols):
+        p = X.Calculator(Z, xyz, etemp=20000.0).singlepoint()
+        assert abs(r.energy[i] - p.energy) <= TIGHT_E
+        assert np.max(np.abs(r.charges[i] - p.charges)) <= TIGHT_QG
+        assert np.max(np.abs(r.gradients[i] - p.gradient)) <= TIGHT_QG
+
+
+@pytest.mark.gpu
 def test_large_molecule_runs_on_plain_engine():
     big = W.water_cluster(90, seed=3)                 # 540 AOs, above the batched limit
     small = W.alkane(4, 0.02, seed=4)

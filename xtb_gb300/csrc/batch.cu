@@ -313,19 +313,33 @@ __device__ void scc_iteration(BatchMol* b, const DevThresh& th, double etemp, in
     __syncthreads();
     stage_tridiag(nao, b->tri_d, b->tri_e2, sm);
     __syncthreads();
-    {
+    // levels ja .. jb - 1 by multisection
+    auto bisect_levels = [&](int ja, int jb) {
         const float* fsm = reinterpret_cast<const float*>(sm + 2 * nao);
         const int per_pass = (int)(blockDim.x / BIS_G);
-        for (int j0 = 0; j0 < nao; j0 += per_pass) {   // uniform trip count: whole warps stay together
+        for (int j0 = ja; j0 < jb; j0 += per_pass) {   // uniform trip count: whole warps stay together
             const int j = j0 + (int)(threadIdx.x / BIS_G);
-            const bool valid = j < nao;
+            const bool valid = j < jb;
             const double v = d_bisect_group<true>(nao, sm, sm + nao, fsm, fsm + nao, b->bounds, valid ? j : 0, valid);
             if (valid && threadIdx.x % BIS_G == 0) b->emo[j] = v;
         }
-    }
+    };
+    // inside the SCC only the levels that can carry occupation: the lowest nocc + max(8, n / 8),
+    // the rest (with a second smearing) only when the last of them lies less than 60 kT above a
+    // Fermi level (the smearing is exactly zero from 50 kT); the last diagonalisation takes all
+    const int klev = (b->lastdiag || it >= maxiter) ? nao : min(nao, max(b->nel_a, b->nel_b) + max(8, nao / 8));
+    bisect_levels(0, klev);
+    for (int j = klev + (int)threadIdx.x; j < nao; j += (int)blockDim.x) b->emo[j] = 1.0e300;
     __syncthreads();
     d_fermi(nao, b->emo, b->nel_a, b->nel_b, etemp, b->focc, b->focca, b->foccb, b->fscal, b->kocc);
     __syncthreads();
+    if (klev < nao &&
+        b->emo[klev - 1] - fmax(b->fscal[1], b->fscal[2]) < 60.0 * KB_AU * AUTOEV * etemp) {   // block-uniform
+        bisect_levels(klev, nao);
+        __syncthreads();
+        d_fermi(nao, b->emo, b->nel_a, b->nel_b, etemp, b->focc, b->focca, b->foccb, b->fscal, b->kocc);
+        __syncthreads();
+    }
     const int kocc = *b->kocc;
     double* U1 = b->iscr;
     CTA_FOR(j, kocc) d_inviter<2>(nao, b->tri_d, b->tri_e, b->emo, b->bounds, b->Y, U1, U1 + nn, U1 + 2 * nn,
