@@ -358,7 +358,7 @@ __device__ void scc_iteration(BatchMol* b, const DevThresh& th, double etemp, in
     cta_dgemm<false, true>(nao, nao, nao, 1.0, b->T1, nao, b->C, nao, 0.0, b->P, nao, GF_SYM, b->kocc, nullptr, sm);
     cta_mirror_lower(nao, b->P, nao);
     // populations, energies, mixing
-    WARP_FOR(mu, nao) d_rowsums(m, b->P, b->S, b->D, b->Q, b->H0, b->rows, mu, lane);
+    CTA_FOR(mu, nao) d_rowsums_thread(m, b->P, b->S, b->D, b->Q, b->H0, b->rows, mu);
     __syncthreads();
     CTA_FOR(a, nat) d_atom_pop(m, b->rows, b->qsh, b->q, b->dipm, b->qp, b->eh0, a);
     __syncthreads();

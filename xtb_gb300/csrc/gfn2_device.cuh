@@ -630,6 +630,30 @@ __device__ inline void d_rowsums(DevMol m, const double* __restrict__ P, const d
 }
 
 
+// The same row sums by one thread per row, for the small matrices of the batched engine: a warp
+// FP64 instruction costs the same with any number of lanes active, and at n ~ 100 the eleven
+// five-level shuffle sums of the warp form outweigh the products.
+__device__ inline void d_rowsums_thread(DevMol m, const double* __restrict__ P, const double* __restrict__ S,
+                                       const double* __restrict__ D, const double* __restrict__ Q,
+                                       const double* __restrict__ H0, double* __restrict__ rows, int mu) {
+    const size_t nao = m.nao, nn = nao * nao, off = (size_t)mu * nao;
+    double acc[11];
+#pragma unroll
+    for (int k = 0; k < 11; ++k) acc[k] = 0.0;
+    for (int nu = 0; nu < m.nao; ++nu) {
+        const double p = P[off + nu];
+        acc[0] = fma(p, S[off + nu], acc[0]);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) acc[1 + k] = fma(p, D[k * nn + off + nu], acc[1 + k]);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) acc[4 + k] = fma(p, Q[k * nn + off + nu], acc[4 + k]);
+        acc[10] = fma(p, H0[off + nu], acc[10]);
+    }
+#pragma unroll
+    for (int k = 0; k < 11; ++k) rows[(size_t)mu * 12 + k] = acc[k];
+}
+
+
 // Pass 2: one thread per atom.
 __device__ inline void d_atom_pop(DevMol m, const double* __restrict__ rows, double* __restrict__ qsh, double* __restrict__ q,
                            double* __restrict__ dipm, double* __restrict__ qp, double* __restrict__ eh0, int a) {
