@@ -46,7 +46,7 @@ def test_results_do_not_depend_on_the_forms(precision):
 
 
 def test_wide_tiles_match_the_row_form():
-    """From 4096 AOs the upper-triangle tridiagonalisation runs tiles of 16 x 64 (two columns per
+    """From 2560 AOs the upper-triangle tridiagonalisation runs tiles of 16 x 64 (two columns per
     lane): (H2O)683, 4098 AOs, in split mode, against the row form."""
     Z, xyz = W.water_cluster(683, seed=5)
     saved = X.get_tuning()

@@ -753,7 +753,9 @@ static void sytrd_sym_launch(cudaStream_t st, int n, double* A, int lda, double*
     XG_CUDA(cudaGetDevice(&dev));
     XG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     const size_t smem = sytrd_sym_smem(n);
-    const bool wide = n >= 4096;
+    // tiles of 16 x 64 (two columns per lane) from 2560 on: half the row-sum shuffles per element
+    // (measured: 70.9 against 73.3 ms at 2930, level at 1536-2048)
+    const bool wide = n >= 2560;
     const void* fn = wide ? (const void*)k_sytrd_sym<2> : (const void*)k_sytrd_sym<1>;
     allow_max_dynamic_smem(fn);
     XG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxblk, fn, SYM_NT, smem));
