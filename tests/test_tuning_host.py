@@ -51,3 +51,39 @@ def test_span_then_tail_latency(monkeypatch, spans, lats, want):
     assert (s["plain_workers"], s["iters_per_step"], s["pool_max_nao"], s["coop_blocks"]) == cands[want]
     assert len(s["span_s"]) == len(s["p99_s"]) == 3
     assert tuning.schedule(reqs, candidates=cands) is s                 # kept per stream
+
+
+def test_finalists_decide_by_median(monkeypatch):
+    """A candidate that looks best in its first pass but not in its repeats loses to one that is
+    steadily short: the choice goes by the finalists' median span."""
+    cands = ((8, 1, 192, 76), (6, 1, 256, -20), (4, 1, 512, 0), (6, 1, 512, 0))
+    seq = {cands[0]: [3.60, 4.20, 4.30], cands[1]: [3.80, 3.78, 3.82], cands[2]: [3.90, 4.00, 4.10],
+           cands[3]: [5.00]}
+    calls = {}
+
+    class Srv:
+        def __init__(self, plain_workers, iters_per_step, pool_max_nao, coop_blocks, **kw):
+            c = (plain_workers, iters_per_step, pool_max_nao, coop_blocks)
+            k = calls.get(c, 0)
+            calls[c] = k + 1
+            self.span = seq[c][k]
+            self.k = 0
+
+        def submit(self, *a, **kw):
+            self.k += 1
+            return self.k
+
+        def wait(self, i, check=True):
+            return _Res(self.span * i / 100.0, 1.0)
+
+        def close(self):
+            pass
+
+    monkeypatch.setattr(X, "Server", Srv)
+    monkeypatch.setattr(tuning, "_schedules", {})
+    reqs = [{"numbers": [1, 1], "positions": [[0.0, 0.0, float(k)], [0.0, 0.0, k + 1.4]], "gradient": False}
+            for k in range(100)]
+    s = tuning.schedule(reqs, candidates=cands)
+    assert (s["plain_workers"], s["iters_per_step"], s["pool_max_nao"], s["coop_blocks"]) == cands[1]
+    assert calls == {cands[0]: 3, cands[1]: 3, cands[2]: 3, cands[3]: 1}     # three finalists, two repeats
+    assert len(s["span_s"][tuning._label(cands[1])]) == 3
