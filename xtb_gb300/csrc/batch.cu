@@ -522,7 +522,10 @@ __global__ void __launch_bounds__(BT) k_batch_setup_b(BatchMol* __restrict__ mol
 }
 
 // up to max_iter SCC iterations of every molecule in the SCC stage
-__global__ void __launch_bounds__(BT) k_batch_scc(BatchMol* __restrict__ mols, int nmol, DevThresh th, double etemp,
+// four molecules per SM (at most 64 registers): the SCC's dependent FP64 chains and shared-
+// memory round trips need the other blocks' warps to hide them (3502 single points/s at two per
+// SM, 3608 at three, 3735 at four with a few hundred bytes of spills, no more at five)
+__global__ void __launch_bounds__(BT, 4) k_batch_scc(BatchMol* __restrict__ mols, int nmol, DevThresh th, double etemp,
                                                   int maxiter, int max_iter) {
     extern __shared__ double sm[];
     BatchMol* b = mol_in_stage(mols, nmol, BS_SCC);
