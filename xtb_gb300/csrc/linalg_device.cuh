@@ -900,10 +900,19 @@ __device__ inline void d_ormtr_apply(int n, const double* __restrict__ V, const 
         const double t = tau[k];
         if (t == 0.0) continue;
         const double* vk = V + (size_t)k * n;
-        double s = 0.0;
-        for (int i = k + 1 + lane; i < n; i += 32) s = fma(vk[i], y[i], s);
-        s = warp_sum(s) * t;
-        for (int i = k + 1 + lane; i < n; i += 32) y[i] -= s * vk[i];
+        // four partial sums: with about one warp per scheduler nothing hides a single
+        // 64-cycle dependent FMA chain
+        double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+        int i = k + 1 + lane;
+        for (; i + 96 < n; i += 128) {
+            s0 = fma(vk[i], y[i], s0);
+            s1 = fma(vk[i + 32], y[i + 32], s1);
+            s2 = fma(vk[i + 64], y[i + 64], s2);
+            s3 = fma(vk[i + 96], y[i + 96], s3);
+        }
+        for (; i < n; i += 32) s0 = fma(vk[i], y[i], s0);
+        const double s = warp_sum((s0 + s1) + (s2 + s3)) * t;
+        for (i = k + 1 + lane; i < n; i += 32) y[i] -= s * vk[i];
         __syncwarp();
     }
 }
