@@ -45,6 +45,39 @@ def test_results_do_not_depend_on_the_forms(precision):
     assert np.max(np.abs(a.gradient - b.gradient)) <= 1e-8
 
 
+@pytest.mark.parametrize("name", ["h3+", "water", "ammonia", "methane", "ethane", "water6", "decane"])
+def test_small_matrices_in_both_forms(name):
+    """The upper-triangle tridiagonalisation on matrices of 3 to 62 AOs (one tile, a partial
+    first row block, more blocks than tiles) against the row form."""
+    mols = {
+        "h3+": ([1, 1, 1], [[0.0, 0.0, 0.0], [0.0, 0.0, 1.65], [0.0, 1.43, 0.83]], 1),
+        "water": ([8, 1, 1], [[0.0, 0.0, 0.0], [0.0, 1.43, 1.1], [0.0, -1.43, 1.1]], 0),
+        "ammonia": ([7, 1, 1, 1], [[0.0, 0.0, 0.0], [0.0, 1.77, 0.72], [1.53, -0.89, 0.72], [-1.53, -0.89, 0.72]], 0),
+        "methane": ([6, 1, 1, 1, 1], [[0, 0, 0], [1.19, 1.19, 1.19], [-1.19, -1.19, 1.19], [-1.19, 1.19, -1.19],
+                                      [1.19, -1.19, -1.19]], 0),
+    }
+    if name in mols:
+        Z, xyz, charge = mols[name]
+        Z, xyz = np.array(Z), np.array(xyz, dtype=float)
+    else:
+        Z, xyz = {"ethane": W.alkane(2, 0.02, seed=1), "water6": W.water_cluster(6, seed=1),
+                  "decane": W.alkane(10, 0.02, seed=1)}[name]
+        charge = 0
+    saved = X.get_tuning()
+    try:
+        X.set_tuning(3, saved["blocked_min_fp64"], saved["blocked_min_split"])
+        a = X.Calculator(Z, xyz, charge=charge).singlepoint()
+        X.set_tuning(1 << 30, saved["blocked_min_fp64"], saved["blocked_min_split"])
+        b = X.Calculator(Z, xyz, charge=charge).singlepoint()
+    finally:
+        X.set_tuning(saved["sytrd_sym_min"], saved["blocked_min_fp64"], saved["blocked_min_split"])
+    assert a.converged and b.converged and a.iterations == b.iterations
+    assert abs(a.energy - b.energy) <= 1e-10
+    assert np.max(np.abs(a.charges - b.charges)) <= 1e-9
+    assert np.max(np.abs(a.gradient - b.gradient)) <= 1e-9
+    assert np.max(np.abs(a.emo - b.emo)) <= 1e-10
+
+
 def test_wide_tiles_match_the_row_form():
     """From 2560 AOs the upper-triangle tridiagonalisation runs tiles of 16 x 64 (two columns per
     lane): (H2O)683, 4098 AOs, in split mode, against the row form."""
