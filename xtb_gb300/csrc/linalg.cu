@@ -968,10 +968,60 @@ __global__ void __launch_bounds__(8 * ORM_NB) k_larft_all(int nref, const double
     }
 }
 
+// The Gram matrices S_b = V_b V_b^T of every block of reflectors in one launch, split over the
+// rows of V (slice z of block b in blockIdx.z = b * nsplit + z; partial products in P, summed by
+// k_gram_reduce in a fixed order).  They depend on V alone, so they stay off the chain of the
+// products with Y.
+__global__ void __launch_bounds__(256) k_gram_all(int n, int nref, const double* __restrict__ V, int nsplit, int kc,
+                                                  double* __restrict__ P) {
+    __shared__ double smem[GEMM_SMEM];
+    const int b = blockIdx.z / nsplit, z = blockIdx.z % nsplit;
+    const int k0 = b * ORM_NB, kn = min(ORM_NB, nref - k0);
+    const int r0 = k0 + 1, m = n - r0;
+    const double* Vb = V + (size_t)k0 * n + r0;
+    double* Pz = P + ((size_t)b * nsplit + z) * ORM_NB * ORM_NB;
+    const int c0 = z * kc, cn = min(kc, m - c0);
+    const int i0 = blockIdx.y * GBM, j0 = blockIdx.x * GBN;
+    if (cn <= 0) {
+        for (int t = threadIdx.x; t < GBM * GBN; t += blockDim.x) {
+            const int i = i0 + t / GBN, j = j0 + t % GBN;
+            if (i < kn && j < kn) Pz[(size_t)i * ORM_NB + j] = 0.0;
+        }
+        return;
+    }
+    dgemm_tile<false, true>(kn, kn, cn, 1.0, Vb + c0, n, Vb + c0, n, 0.0, Pz, ORM_NB, 0, nullptr, nullptr, i0, j0,
+                            smem);
+}
+
+__global__ void k_gram_reduce(int nblk, int nsplit, const double* __restrict__ P, double* __restrict__ Sall) {
+    const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long per = (long)ORM_NB * ORM_NB;
+    if (t >= (long)nblk * per) return;
+    const long b = t / per, e = t % per;
+    double s = 0.0;
+    for (int z = 0; z < nsplit; ++z) s += P[(b * nsplit + z) * per + e];
+    Sall[t] = s;
+}
+
+// W_b = V_b^T T_b (m_b x kn) of every block in one launch, so that the chain of products with Y
+// is G = V_b Y, Y -= W_b G: two products per block, with the triangular factor folded in ahead.
+__global__ void __launch_bounds__(256) k_wy_all(int n, int nref, const double* __restrict__ V,
+                                                const double* __restrict__ Tall, double* __restrict__ Wall) {
+    __shared__ double smem[GEMM_SMEM];
+    const int b = blockIdx.z;
+    const int k0 = b * ORM_NB, kn = min(ORM_NB, nref - k0);
+    const int r0 = k0 + 1, m = n - r0;
+    const int i0 = blockIdx.y * GBM, j0 = blockIdx.x * GBN;
+    if (i0 >= m || j0 >= kn) return;
+    const double* Vb = V + (size_t)k0 * n + r0;
+    dgemm_tile<true, false>(m, kn, kn, 1.0, Vb, n, Tall + (size_t)b * ORM_NB * ORM_NB, ORM_NB, 0.0,
+                            Wall + (size_t)b * n * ORM_NB, ORM_NB, GF_B_UPPER, nullptr, nullptr, i0, j0, smem);
+}
+
 size_t ormtr_workspace(int n) {
     const size_t nblk = (size_t)std::max(1, ceil_div(std::max(n - 2, 1), ORM_NB));
-    return (size_t)ORM_SPLIT * ORM_NB * std::max(n, ORM_NB) + 2 * (size_t)ORM_NB * n +
-           2 * nblk * ORM_NB * ORM_NB;
+    return (size_t)ORM_SPLIT * ORM_NB * ((size_t)std::max(n, ORM_NB) + ORM_NB) + (size_t)ORM_NB * n +
+           2 * nblk * ORM_NB * ORM_NB + nblk * (size_t)n * ORM_NB;
 }
 
 void ormtr_blocked(cudaStream_t st, int n, const double* V, const double* tau, double* Y, const int* d_ncol,
@@ -980,41 +1030,43 @@ void ormtr_blocked(cudaStream_t st, int n, const double* V, const double* tau, d
     const int nref = n - 2;
     const int nblk = ceil_div(nref, ORM_NB);
     double* partial = work;
-    double* G = partial + (size_t)ORM_SPLIT * ORM_NB * std::max(n, ORM_NB);
-    double* G2 = G + (size_t)ORM_NB * n;
-    double* Sall = G2 + (size_t)ORM_NB * n;
+    double* G = partial + (size_t)ORM_SPLIT * ORM_NB * ((size_t)std::max(n, ORM_NB) + ORM_NB);
+    double* Sall = G + (size_t)ORM_NB * n;
     double* Tall = Sall + (size_t)nblk * ORM_NB * ORM_NB;
-    // Gram matrices S_b = V_b V_b^T of every block, then all T factors in one launch
-    for (int b = 0; b < nblk; ++b) {
-        const int k0 = b * ORM_NB, kn = std::min(ORM_NB, nref - k0);
-        const int r0 = k0 + 1, m = n - r0;
-        const double* Vb = V + (size_t)k0 * n + r0;   // kn rows of length m (zeros above each vector's start)
-        dgemm_splitk(st, false, true, kn, kn, m, 1.0, Vb, n, Vb, n, 0.0, Sall + (size_t)b * ORM_NB * ORM_NB, ORM_NB,
-                     ORM_SPLIT, partial, nullptr);
+    double* Wall = Tall + (size_t)nblk * ORM_NB * ORM_NB;
+    // Gram matrices of every block (one launch), all T factors (one launch), W_b = V_b^T T_b
+    // (one launch)
+    {
+        const int kc = ((ceil_div(n, ORM_SPLIT) + GBK - 1) / GBK) * GBK;
+        const int nsplit = ceil_div(n, kc);
+        const dim3 grid(ORM_NB / GBN, ORM_NB / GBM, nblk * nsplit);
+        k_gram_all<<<grid, 256, 0, st>>>(n, nref, V, nsplit, kc, partial);
+        XG_LAUNCH_CHECK();
+        k_gram_reduce<<<ceil_div((long)nblk * ORM_NB * ORM_NB, 256), 256, 0, st>>>(nblk, nsplit, partial, Sall);
+        XG_LAUNCH_CHECK();
     }
     const size_t smem = (size_t)ORM_NB * LARFT_LD * sizeof(double);
     allow_max_dynamic_smem((const void*)k_larft_all);
     k_larft_all<<<nblk, 8 * ORM_NB, smem, st>>>(nref, tau, Sall, Tall);
     XG_LAUNCH_CHECK();
+    k_wy_all<<<dim3(ORM_NB / GBN, ceil_div(n, GBM), nblk), 256, 0, st>>>(n, nref, V, Tall, Wall);
+    XG_LAUNCH_CHECK();
     for (int b = nblk - 1; b >= 0; --b) {
         const int k0 = b * ORM_NB, kn = std::min(ORM_NB, nref - k0);
         const int r0 = k0 + 1, m = n - r0;
         const double* Vb = V + (size_t)k0 * n + r0;
-        const double* T = Tall + (size_t)b * ORM_NB * ORM_NB;
-        // G = Vb Y[r0:, :ncol];  G2 = T G;  Y[r0:, :ncol] -= Vb^T G2
+        const double* Wb = Wall + (size_t)b * n * ORM_NB;
+        // G = Vb Y[r0:, :ncol];  Y[r0:, :ncol] -= W_b G
         if (slices) {
             split_gemm(st, false, false, kn, n, m, 1.0, Vb, n, Y + (size_t)r0 * n, n, 0.0, G, n, slices, split_work,
                        nullptr, d_ncol);
+            split_gemm(st, false, false, m, n, kn, -1.0, Wb, ORM_NB, G, n, 1.0, Y + (size_t)r0 * n, n, slices,
+                       split_work, nullptr, d_ncol);
         } else {
             dgemm_splitk(st, false, false, kn, n, m, 1.0, Vb, n, Y + (size_t)r0 * n, n, 0.0, G, n, ORM_SPLIT,
                          partial, d_ncol);
+            dgemm(st, false, false, m, n, kn, -1.0, Wb, ORM_NB, G, n, 1.0, Y + (size_t)r0 * n, n, 0, nullptr, d_ncol);
         }
-        dgemm(st, false, false, kn, n, kn, 1.0, T, ORM_NB, G, n, 0.0, G2, n, GF_A_UPPER, nullptr, d_ncol);
-        if (slices)
-            split_gemm(st, true, false, m, n, kn, -1.0, Vb, n, G2, n, 1.0, Y + (size_t)r0 * n, n, slices, split_work,
-                       nullptr, d_ncol);
-        else
-            dgemm(st, true, false, m, n, kn, -1.0, Vb, n, G2, n, 1.0, Y + (size_t)r0 * n, n, 0, nullptr, d_ncol);
     }
 }
 
