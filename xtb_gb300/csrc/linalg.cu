@@ -344,11 +344,11 @@ static void sytrd_launch(cudaStream_t st, int n, double* A, int lda, double* V, 
 //
 // One cooperative launch of P x Q blocks and ONE grid barrier per column s (pivot row s, trailing
 // rows and columns g = s+1 .. n-1, all indices global):
-//   tile pass  the trailing upper triangle in tiles of 16 rows x 32 RT columns, tile (I, c) owned
-//      by block (I mod P, c mod Q) -- on the rows of odd cycles I / P by block (I mod P,
-//      2 rL + 1 - c mod Q), rL the class of the last chunk -- for the whole reduction (a block
-//      with fewer tiles than warps
-//      splits them into row parts): each tile applies the pending update of column s-1
+//   tile pass  the trailing upper triangle in tiles of 16 rows x 32 RT columns (RT = 2 from
+//      2560 on), tile (I, c) owned by block (I mod P, c mod Q) -- on the rows of odd cycles
+//      I / P by block (I mod P, 2 rL + 1 - c mod Q), rL the class of the last chunk -- for the
+//      whole reduction (a block with fewer tiles than warps splits them into row parts): each
+//      tile applies the pending update of column s-1
 //      (A -= v w^T + w v^T), writes the elements back, and adds its row sums and column sums of
 //      A x into ax (FP64 atomics; x is the column's pivot row, not yet normalised) and its share
 //      of x^T A x into the column's scalar (3 FMAs per tile from the reduced sums).  Three ax
