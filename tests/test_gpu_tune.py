@@ -135,3 +135,13 @@ def test_capped_cooperative_tridiagonalisation():
                     assert abs(a.energy - b.energy) <= 1e-9, (sym, cap)
     finally:
         X.set_tuning(saved["sytrd_sym_min"], saved["blocked_min_fp64"], saved["blocked_min_split"])
+
+
+def test_sytrd_timing_entry_point():
+    """xtbgb_sytrdMs times one tridiagonalisation with a chosen form and grid cap and refuses
+    sizes and forms outside its range."""
+    for form, cap in ((0, 0), (1, 0), (1, 38), (-1, 0)):
+        assert X.sytrd_ms(300, form, cap, 1) > 0.0
+    for n, form in ((2, 1), (9000, 1), (300, 2)):
+        with pytest.raises(X.XTBException):
+            X.sytrd_ms(n, form, 0, 1)
