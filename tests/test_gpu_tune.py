@@ -79,8 +79,8 @@ def test_small_matrices_in_both_forms(name):
 
 
 def test_wide_tiles_match_the_row_form():
-    """From 2560 AOs the upper-triangle tridiagonalisation runs tiles of 16 x 64 (two columns per
-    lane): (H2O)683, 4098 AOs, in split mode, against the row form."""
+    """From 1800 AOs the upper-triangle tridiagonalisation runs tiles of 16 x 64 (two columns per
+    lane) with 16 warps per block: (H2O)683, 4098 AOs, in split mode, against the row form."""
     Z, xyz = W.water_cluster(683, seed=5)
     saved = X.get_tuning()
     try:

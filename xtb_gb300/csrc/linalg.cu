@@ -345,7 +345,7 @@ static void sytrd_launch(cudaStream_t st, int n, double* A, int lda, double* V, 
 // One cooperative launch of P x Q blocks and ONE grid barrier per column s (pivot row s, trailing
 // rows and columns g = s+1 .. n-1, all indices global):
 //   tile pass  the trailing upper triangle in tiles of 16 rows x 32 RT columns (RT = 2 from
-//      2560 on), tile (I, c) owned by block (I mod P, c mod Q) -- on the rows of odd cycles
+//      1800 on), tile (I, c) owned by block (I mod P, c mod Q) -- on the rows of odd cycles
 //      I / P by block (I mod P, 2 rL + 1 - c mod Q), rL the class of the last chunk -- for the
 //      whole reduction (a block with fewer tiles than warps splits them into row parts): each
 //      tile applies the pending update of column s-1
@@ -362,9 +362,7 @@ static void sytrd_launch(cudaStream_t st, int n, double* A, int lda, double* V, 
 //      of the m entries, which is all its next tile pass reads.  Each entry has one owner block
 //      that writes V and adds x'^2 into the next column's |x[1:]|^2.
 constexpr int SYM_RB = 16;            // rows of a tile
-constexpr int SYM_NT = 256;
 constexpr int SYM_PF = 2;             // vector-phase entries per thread loaded with the column's scalars
-static_assert(SYM_NT == 256, "the block reduction of the tile pass sums 8 x 32 shares");
 
 // One task of the tile pass: rows r0 .. r0 + RPT - 1 of a tile, columns jt (-1 past the end).
 // A block with fewer tiles than warps splits its tiles into row parts (RPT = 16 / parts), so
@@ -450,8 +448,8 @@ __device__ __forceinline__ void sym_compute(const double (&at)[SYM_RB][RT], doub
         }
 }
 
-template <int RT>
-__global__ void __launch_bounds__(SYM_NT) k_sytrd_sym(int n, int P, int Q, double* __restrict__ A, int lda,
+template <int RT, int NT>
+__global__ void __launch_bounds__(NT) k_sytrd_sym(int n, int P, int Q, double* __restrict__ A, int lda,
                                                       double* __restrict__ V, double* __restrict__ tau,
                                                       double* __restrict__ d, double* __restrict__ e,
                                                       double* __restrict__ ws) {
@@ -460,9 +458,10 @@ __global__ void __launch_bounds__(SYM_NT) k_sytrd_sym(int n, int P, int Q, doubl
     double* X = sm;                   // pivot row x of the current column (this block's entries)
     double* Vp = X + n;               // v and w of the previous column (the pending update)
     double* Wp = Vp + n;
-    double* r1 = Wp + n;              // [SYM_NT] per-thread shares of x^T A x
-    double* r2 = r1 + SYM_NT;         // [SYM_NT] per-thread shares of |x[1:]|^2
-    double* scal = r2 + SYM_NT;       // [8] the column's scalars
+    static_assert(NT % 128 == 0, "the block reduction sums groups of four warps");
+    double* r1 = Wp + n;              // [NT] per-thread shares of x^T A x
+    double* r2 = r1 + NT;         // [NT] per-thread shares of |x[1:]|^2
+    double* scal = r2 + NT;       // [8] the column's scalars
     int* pre = reinterpret_cast<int*>(scal + 8);   // [R + 1] tiles before each of this block's row blocks
     cg::grid_group grid = cg::this_grid();
     const int G = gridDim.x;
@@ -551,7 +550,7 @@ __global__ void __launch_bounds__(SYM_NT) k_sytrd_sym(int n, int P, int Q, doubl
     };
 
     // prologue 1: the tile table, the scalar arrays and the first two ax buffers cleared
-    for (int a = threadIdx.x; a < R; a += SYM_NT) {
+    for (int a = threadIdx.x; a < R; a += NT) {
         const int cf = cfirst(p + P * a);
         pre[a + 1] = cf < nch ? (nch - 1 - cf) / Q + 1 : 0;
     }
@@ -560,14 +559,14 @@ __global__ void __launch_bounds__(SYM_NT) k_sytrd_sym(int n, int P, int Q, doubl
         pre[0] = 0;
         for (int a = 0; a < R; ++a) pre[a + 1] += pre[a];
     }
-    for (size_t i = (size_t)blockIdx.x * SYM_NT + threadIdx.x; i < 6 * (size_t)n; i += (size_t)G * SYM_NT)
+    for (size_t i = (size_t)blockIdx.x * NT + threadIdx.x; i < 6 * (size_t)n; i += (size_t)G * NT)
         if (i < 2 * (size_t)n || i >= 3 * (size_t)n) ws[i] = 0.0;
     grid.sync();
     // prologue 2: pivot row of column 0 on this block's entries, its norm
     double nx2p = 0.0;
     {
         const int ne = entries(1);
-        for (int t = threadIdx.x; t < ne; t += SYM_NT) {
+        for (int t = threadIdx.x; t < ne; t += NT) {
             const int g = entry_at(1, t);
             if (g < 0) continue;
             const double v = A[g];
@@ -588,7 +587,7 @@ __global__ void __launch_bounds__(SYM_NT) k_sytrd_sym(int n, int P, int Q, doubl
         // ---- tile pass
         column_tasks(s);
         double txa = 0.0;
-        for (int t = wid; t < ntask; t += SYM_NT / 32) {
+        for (int t = wid; t < ntask; t += NT / 32) {
             int r0, jt[RT];
             decode(t, r0, jt);
             switch (parts) {
@@ -617,8 +616,15 @@ __global__ void __launch_bounds__(SYM_NT) k_sytrd_sym(int n, int P, int Q, doubl
         __syncthreads();
         if (wid < 2) {
             const double* r = wid ? r2 : r1;
-            double v = ((r[lane] + r[lane + 32]) + (r[lane + 64] + r[lane + 96])) +
-                       ((r[lane + 128] + r[lane + 160]) + (r[lane + 192] + r[lane + 224]));
+            double v0 = 0.0, v1 = 0.0, v2 = 0.0, v3 = 0.0;
+#pragma unroll
+            for (int w = 0; w < NT / 32; w += 4) {
+                v0 += r[lane + 32 * w];
+                v1 += r[lane + 32 * (w + 1)];
+                v2 += r[lane + 32 * (w + 2)];
+                v3 += r[lane + 32 * (w + 3)];
+            }
+            double v = (v0 + v1) + (v2 + v3);
             v = warp_sum(v);
             if (lane == 0) atomicAdd(wid ? &s_nx2[s] : &s_txa[s], v);
         }
@@ -630,7 +636,7 @@ __global__ void __launch_bounds__(SYM_NT) k_sytrd_sym(int n, int P, int Q, doubl
         double pa[SYM_PF], pa0[SYM_PF];
 #pragma unroll
         for (int k = 0; k < SYM_PF; ++k) {
-            const int t = threadIdx.x + k * SYM_NT;
+            const int t = threadIdx.x + k * NT;
             gp[k] = t < ne ? entry_at(g0, t) : -1;
             pa[k] = gp[k] >= 0 ? ax[gp[k]] : 0.0;
             pa0[k] = gp[k] >= 0 ? a0row[gp[k]] : 0.0;
@@ -669,7 +675,7 @@ __global__ void __launch_bounds__(SYM_NT) k_sytrd_sym(int n, int P, int Q, doubl
             }
         } else {
             // this block's slices: zeros of row s of V left of column s + 1, the ax buffer of column s + 2
-            const int tid = threadIdx.x - 32, nt = SYM_NT - 32;
+            const int tid = threadIdx.x - 32, nt = NT - 32;
             const int pv = (g0 + G - 1) / G;
             for (int c = blockIdx.x * pv + tid; c < min(g0, (blockIdx.x + 1) * pv); c += nt)
                 V[(size_t)s * n + c] = 0.0;
@@ -709,7 +715,7 @@ __global__ void __launch_bounds__(SYM_NT) k_sytrd_sym(int n, int P, int Q, doubl
 #pragma unroll
         for (int k = 0; k < SYM_PF; ++k)
             if (gp[k] >= 0) entry(gp[k], pa[k], pa0[k]);
-        for (int t = threadIdx.x + SYM_PF * SYM_NT; t < ne; t += SYM_NT) {
+        for (int t = threadIdx.x + SYM_PF * NT; t < ne; t += NT) {
             const int g = entry_at(g0, t);
             if (g >= 0) entry(g, ax[g], a0row[g]);
         }
@@ -722,11 +728,11 @@ __global__ void __launch_bounds__(SYM_NT) k_sytrd_sym(int n, int P, int Q, doubl
         e[n - 1] = 0.0;
     }
     if (lead)
-        for (int i = threadIdx.x; i < 2 * n; i += SYM_NT) V[(size_t)(n - 2) * n + i] = 0.0;
+        for (int i = threadIdx.x; i < 2 * n; i += NT) V[(size_t)(n - 2) * n + i] = 0.0;
 }
 
-static size_t sytrd_sym_smem(int n) {
-    return (3 * (size_t)n + 2 * SYM_NT + 8) * sizeof(double) + ((size_t)n / SYM_RB + 2) * sizeof(int);
+static size_t sytrd_sym_smem(int n, int nt) {
+    return (3 * (size_t)n + 2 * (size_t)nt + 8) * sizeof(double) + ((size_t)n / SYM_RB + 2) * sizeof(int);
 }
 
 // P x Q blocks for at most G: a near-square factorisation keeps each block's share of the
@@ -752,13 +758,17 @@ static void sytrd_sym_launch(cudaStream_t st, int n, double* A, int lda, double*
     int dev = 0, nsm = 0, maxblk = 0;
     XG_CUDA(cudaGetDevice(&dev));
     XG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    const size_t smem = sytrd_sym_smem(n);
-    // tiles of 16 x 64 (two columns per lane) from 2560 on: half the row-sum shuffles per element
-    // (measured: 70.9 against 73.3 ms at 2930, level at 1536-2048)
-    const bool wide = n >= 2560;
-    const void* fn = wide ? (const void*)k_sytrd_sym<2> : (const void*)k_sytrd_sym<1>;
+    // 16 warps per block from 1024 on (more warps hide the tile pass's dependent chains) and
+    // tiles of 16 x 64 (two columns per lane: half the row-sum shuffles per element) from 1800
+    // on.  Measured (ms, 16 x 32 / 256 threads against this choice): 1024 10.45 / 10.37, 1800
+    // 27.1 / 25.8, 2048 33.8 / 31.8, 2930 73.6 / 67.8; at 768 eight warps stay faster (6.92 / 7.07)
+    const int nt = n >= 1024 ? 512 : 256;
+    const bool wide = n >= 1800;
+    const size_t smem = sytrd_sym_smem(n, nt);
+    const void* fn = wide ? (nt == 512 ? (const void*)k_sytrd_sym<2, 512> : (const void*)k_sytrd_sym<2, 256>)
+                          : (nt == 512 ? (const void*)k_sytrd_sym<1, 512> : (const void*)k_sytrd_sym<1, 256>);
     allow_max_dynamic_smem(fn);
-    XG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxblk, fn, SYM_NT, smem));
+    XG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxblk, fn, nt, smem));
     if (maxblk < 1) throw CudaError("sytrd: kernel does not fit on an SM");
     int G = std::min(nsm, SYTRD_SLOTS);
     if (max_blocks > 0) G = std::min(G, max_blocks);
@@ -766,7 +776,7 @@ static void sytrd_sym_launch(cudaStream_t st, int n, double* A, int lda, double*
     sym_grid(G, P, Q);
     const int blocks = P * Q;
     void* args[] = {&n, &P, &Q, &A, &lda, &V, &tau, &d, &e, &ws};
-    XG_CUDA(cudaLaunchCooperativeKernel(fn, blocks, SYM_NT, args, smem, st));
+    XG_CUDA(cudaLaunchCooperativeKernel(fn, blocks, nt, args, smem, st));
     ++launch_counter();
 }
 
@@ -785,7 +795,7 @@ void sytrd_form(cudaStream_t st, int n, double* A, int lda, double* V, double* t
     }
     // the upper-triangle form (its three A x buffers and three per-column scalar arrays live after
     // the row form's 2n + 2 SYTRD_SLOTS doubles of p)
-    const bool sym_fits = n >= 3 && sytrd_sym_smem(n) <= 220 * 1024;
+    const bool sym_fits = n >= 3 && sytrd_sym_smem(n, 512) <= 220 * 1024;
     if (form < 0) form = n >= tuned_sytrd_sym_min() ? 1 : 0;
     if (form == 1 && sym_fits) {
         sytrd_sym_launch(st, n, A, lda, V, tau, d, e, p + 2 * (size_t)n + 2 * SYTRD_SLOTS, max_blocks);
