@@ -51,9 +51,9 @@ PHASES = ("setup", "integrals", "cholesky", "hbuild", "stdform", "sytrd", "triei
 # DRAM bytes per matrix element of one tridiagonalisation launch; traffic grows as n^2.
 # Row form k_sytrd: ncu capture of the (H2O)300 single point (26.43 MB read + 4.47 MB written,
 # n = 1800).  Upper-triangle form k_sytrd_sym: ncu capture at n = 3072 with the 16 x 64 tiles
-# it runs from 2560 AOs (38.95 MB read + 98.62 MB written).
+# and 512 threads per block it runs from 1800 AOs (39.33 MB read + 242.39 MB written).
 SYTRD_BYTES_PER_ELEM = (26.430976e6 + 4.467968e6) / 1800.0 ** 2
-SYTRD_SYM_BYTES_PER_ELEM = (38.952192e6 + 98.618112e6) / 3072.0 ** 2
+SYTRD_SYM_BYTES_PER_ELEM = (39.325952e6 + 242.387968e6) / 3072.0 ** 2
 
 
 def sytrd_form(n):
