@@ -855,13 +855,21 @@ __global__ void k_levels_gate(int k, const double* __restrict__ w, const double*
 }
 
 // ------------------------------------------------------------------ inverse iteration
-__global__ void __launch_bounds__(64) k_inviter(int n, const double* __restrict__ d, const double* __restrict__ e,
+// One thread per eigenvector, its chain of O(n) dependent FP64 steps.  A warp's FP64
+// instructions cost the SM's narrow FP64 pipe the same whatever the number of active lanes, so
+// the columns spread over every SM (one block each, consecutive columns per block so that the
+// scratch rows stay coalesced) instead of filling few SMs with full warps: with two full warps
+// per SM the pipe, not the chain's latency, set the time.
+__global__ void __launch_bounds__(256) k_inviter(int n, const double* __restrict__ d, const double* __restrict__ e,
                           const double* __restrict__ w, const double* __restrict__ bounds, double* __restrict__ Y,
                           double* __restrict__ U1, double* __restrict__ U2, double* __restrict__ U3,
                           double* __restrict__ ML, unsigned char* __restrict__ piv, const int* __restrict__ ncol) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= n || (ncol && j >= *ncol)) return;
-    d_inviter<8>(n, d, e, w, bounds, Y, U1, U2, U3, ML, piv, j);
+    const int nc = ncol ? min(n, *ncol) : n;
+    const int per = (nc + (int)gridDim.x - 1) / (int)gridDim.x;   // columns of this block
+    for (int c = threadIdx.x; c < per; c += blockDim.x) {
+        const int j = blockIdx.x * per + c;
+        if (j < nc) d_inviter<8>(n, d, e, w, bounds, Y, U1, U2, U3, ML, piv, j);
+    }
 }
 
 __global__ void k_reorth(int n, const double* __restrict__ w, const double* __restrict__ bounds, double ctol,
@@ -919,8 +927,14 @@ void tridiag_eigvals_rest(cudaStream_t st, int n, const double* d, const double*
 void tridiag_eigvecs(cudaStream_t st, int n, const double* d, const double* e, const double* bounds, const double* w,
                      double* Y, double* scratch, unsigned char* pivbuf, const int* ncol) {
     const size_t nn = (size_t)n * n;
-    k_inviter<<<ceil_div(n, 64), 64, 0, st>>>(n, d, e, w, bounds, Y, scratch, scratch + nn, scratch + 2 * nn,
-                                              scratch + 3 * nn, pivbuf, ncol);
+    int dev = 0, nsm = 0;
+    XG_CUDA(cudaGetDevice(&dev));
+    XG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    // one block per SM; whole warps for up to n / nsm columns each (the device count may be lower)
+    const int nb = std::max(1, std::min(nsm, n));
+    const int nt = std::min(256, 32 * ceil_div(ceil_div(n, nb), 32));
+    k_inviter<<<nb, nt, 0, st>>>(n, d, e, w, bounds, Y, scratch, scratch + nn, scratch + 2 * nn, scratch + 3 * nn,
+                                 pivbuf, ncol);
     XG_LAUNCH_CHECK();
     k_reorth<<<ceil_div((long)n * 32, 128), 128, 0, st>>>(n, w, bounds, 1.0e-7, Y, scratch, scratch + nn,
                                                         scratch + 2 * nn, scratch + 3 * nn, pivbuf, ncol);
