@@ -32,6 +32,7 @@ module xtb_gb300_api
    public :: xtbgb_setBlockedBacktransform, xtbgb_fp64PeakTflops, xtbgb_writeRestart
    public :: xtbgb_readRestart, xtbgb_setExternalChargesHardness, xtbgb_getSolvationEnergyParts
    public :: xtbgb_setSolventSalt, xtbgb_setSolventKernel, xtbgb_autotune, xtbgb_sytrdMs
+   public :: xtbgb_backtransformCheck
    public :: xtbgb_getTuning, xtbgb_setTuning, xtbgb_fp64PeakDetail, xtbgb_fp64LatencyCycles
    public :: xtbgb_reciprocalCheck, xtbgb_splitGemmCheck, xtbgb_batchGetDipoles
    public :: xtbgb_batchGetEnergyParts, xtbgb_batchGetStatus, xtbgb_batchGetStats, xtbgb_batchNao
@@ -506,6 +507,16 @@ module xtb_gb300_api
          integer(c_int), value :: form
          integer(c_int), value :: max_blocks
          integer(c_int), value :: reps
+      end function
+
+      integer(c_int) function xtbgb_backtransformCheck(env, n, ncol, slices, out) &
+            bind(C, name="xtbgb_backtransformCheck")
+         import :: c_int, c_ptr, c_double
+         type(c_ptr), value :: env
+         integer(c_int), value :: n
+         integer(c_int), value :: ncol
+         integer(c_int), value :: slices
+         real(c_double), intent(out) :: out(*)
       end function
 
       subroutine xtbgb_getTuning(env, out) bind(C, name="xtbgb_getTuning")

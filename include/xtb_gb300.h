@@ -117,6 +117,12 @@ extern int xtbgb_autotune(xtb_TEnvironment env, double* out, int nout);
  * form 0 the row form, 1 the upper-triangle form, -1 the tuned choice; max_blocks > 0 caps the
  * cooperative grid.  Returns -1 on error (reported on env). */
 extern double xtbgb_sytrdMs(xtb_TEnvironment env, int n, int form, int max_blocks, int reps);
+/* The eigenvector back-transformation Z = Q Y of the first ncol (1..n) columns of a random
+ * n x n matrix (3 <= n <= 8192; Q from tridiagonalising a random symmetric matrix) by the
+ * compact-WY form (slices 0: FP64 column strips, 1..8: split-precision products with that many
+ * bf16 digits) against the one-warp-per-vector form: out[0] max |difference| / max |Z|, out[1]
+ * and out[2] the two forms' CUDA-event ms.  Returns 0, or 1 on error (reported on env). */
+extern int xtbgb_backtransformCheck(xtb_TEnvironment env, int n, int ncol, int slices, double* out);
 /* The current device's choices: out[0..2] as above, out[3] 1 when measured, 0 for defaults. */
 extern void xtbgb_getTuning(xtb_TEnvironment env, double* out);
 /* Pin the current device's choices (sizes in AOs; for tests and for callers with their own

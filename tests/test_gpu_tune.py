@@ -145,3 +145,21 @@ def test_sytrd_timing_entry_point():
     for n, form in ((2, 1), (9000, 1), (300, 2)):
         with pytest.raises(X.XTBException):
             X.sytrd_ms(n, form, 0, 1)
+
+
+@pytest.mark.parametrize("n,ncol", [(5, 3), (300, 300), (700, 7), (1000, 1000), (1800, 1200), (2600, 2600)])
+def test_fp64_strip_backtransformation(n, ncol):
+    """The FP64 compact-WY back-transformation (one launch, a strip of columns per block) against
+    one warp per vector: strips of 1 to 16 columns, idle blocks (7 columns over all SMs), and
+    strips wider than one pass (2600 columns)."""
+    err, ms_warp, ms_strips = X.backtransform_check(n, ncol, 0)
+    assert err <= 1e-12, (n, ncol, err)
+    assert ms_warp > 0.0 and ms_strips > 0.0
+
+
+def test_split_backtransformation_check():
+    err, _, _ = X.backtransform_check(1200, 600, 5)
+    assert err <= 1e-9
+    for n, ncol, slices in ((2, 1, 0), (300, 0, 0), (300, 301, 0), (300, 10, 9)):
+        with pytest.raises(X.XTBException):
+            X.backtransform_check(n, ncol, slices)

@@ -894,6 +894,26 @@ double xtbgb_sytrdMs(xtb_TEnvironment env, int n, int form, int max_blocks, int 
     }
 }
 
+int xtbgb_backtransformCheck(xtb_TEnvironment env, int n, int ncol, int slices, double* out) {
+    static const char* src = "xtbgb_backtransformCheck";
+    if (!check_env(env)) return 1;
+    if (xg::device_count() == 0) {
+        env->error("no CUDA device available for the GFN2 engine", src);
+        return 1;
+    }
+    if (!out || n < 3 || n > 8192 || ncol < 1 || ncol > n || slices < 0 || slices > 8) {
+        env->error("n must lie in 3..8192, ncol in 1..n and slices in 0..8 (out not null)", src);
+        return 1;
+    }
+    try {
+        xg::check_backtransform(n, ncol, slices, out);
+        return 0;
+    } catch (const std::exception& e) {
+        env->error(e.what(), src);
+        return 1;
+    }
+}
+
 int xtbgb_autotune(xtb_TEnvironment env, double* out, int nout) {
     static const char* src = "xtbgb_autotune";
     if (!check_env(env)) return 0;

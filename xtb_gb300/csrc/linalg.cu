@@ -1042,6 +1042,129 @@ __global__ void __launch_bounds__(256) k_wy_all(int n, int nref, const double* _
                             Wall + (size_t)b * n * ORM_NB, ORM_NB, GF_B_UPPER, nullptr, nullptr, i0, j0, smem);
 }
 
+// FP64 back-transformation from the compact-WY factors in one launch.  Block c owns a strip of
+// consecutive columns of Y and applies H_b = I - V_b^T T_b V_b to it for b = last .. 0:
+// G = V_b Y (kn x w), G' = T_b G, Y -= V_b^T G' on rows r0 .. n-1 (V_b: reflectors k0 .. k0+kn-1,
+// stored from column r0 on).  The strips are independent, so no block waits for another and
+// every SM gets the same share of the n^2 w FMAs (the GEMM chain of the split form needs a
+// launch per block product, with its waves and split-K partials); every FP64 instruction is an
+// FMA on operands in shared memory, registers or coalesced rows of V.
+constexpr int STRIP_W = 16;                 // columns of one pass of a strip
+constexpr int STRIP_RK = 32;                // rows of V_b and Y staged per step of G = V_b Y
+constexpr int STRIP_LD = STRIP_RK + 1;
+constexpr int STRIP_NT = 2 * ORM_NB;        // thread (c, jt): reflector c, columns jt, jt + 2, ...
+constexpr size_t STRIP_SMEM = (size_t)(ORM_NB * STRIP_LD + STRIP_RK * STRIP_W + 2 * ORM_NB * STRIP_W) * sizeof(double);
+
+// one pass over W columns (jb .. jb+W-1) of the strip; W is compile-time so that no FMA slot of
+// the narrow FP64 pipe goes to a column outside the strip
+template <int W>
+__device__ void strip_pass(int n, int nref, const double* __restrict__ V, const double* __restrict__ Tall,
+                           double* __restrict__ Y, int jb, double* sm) {
+    constexpr int NP = (W + 1) / 2;           // column slots of a thread
+    double* Vs = sm;                          // [ORM_NB][STRIP_LD]: V_b rows (then T_b rows) by 32 columns
+    double* Ys = Vs + ORM_NB * STRIP_LD;      // [STRIP_RK][STRIP_W]
+    double* Gs = Ys + STRIP_RK * STRIP_W;     // [ORM_NB][STRIP_W]: G = V_b Y
+    double* Gp = Gs + ORM_NB * STRIP_W;       // [ORM_NB][STRIP_W]: T_b G
+    const int t = threadIdx.x, c = t % ORM_NB, jt = t / ORM_NB;
+    const int nblk = (nref + ORM_NB - 1) / ORM_NB;
+    for (int b = nblk - 1; b >= 0; --b) {
+        const int k0 = b * ORM_NB, kn = min(ORM_NB, nref - k0);
+        const int r0 = k0 + 1, m = n - r0;
+        const double* Vb = V + (size_t)k0 * n + r0;
+        double acc[NP];
+#pragma unroll
+        for (int i = 0; i < NP; ++i) acc[i] = 0.0;
+        // G = V_b Y[r0:, strip], 32 rows at a time (rows of V_b past kn and past m are zero)
+        for (int rc = 0; rc < m; rc += STRIP_RK) {
+            const int rl = min(STRIP_RK, m - rc);
+            for (int e = t; e < ORM_NB * STRIP_RK; e += STRIP_NT) {
+                const int cc = e / STRIP_RK, r = e % STRIP_RK;
+                Vs[cc * STRIP_LD + r] = (cc < kn && r < rl) ? Vb[(size_t)cc * n + rc + r] : 0.0;
+            }
+            for (int e = t; e < STRIP_RK * STRIP_W; e += STRIP_NT) {
+                const int r = e / STRIP_W, j = e % STRIP_W;
+                Ys[e] = (r < rl && j < W) ? Y[(size_t)(r0 + rc + r) * n + jb + j] : 0.0;
+            }
+            __syncthreads();
+#pragma unroll 8
+            for (int r = 0; r < STRIP_RK; ++r) {
+                const double v = Vs[c * STRIP_LD + r];
+#pragma unroll
+                for (int i = 0; i < NP; ++i)
+                    if (jt + 2 * i < W) acc[i] = fma(v, Ys[r * STRIP_W + jt + 2 * i], acc[i]);
+            }
+            __syncthreads();
+        }
+#pragma unroll
+        for (int i = 0; i < NP; ++i)
+            if (jt + 2 * i < W) Gs[c * STRIP_W + jt + 2 * i] = acc[i];
+        __syncthreads();
+        // G' = T_b G (T_b upper triangular, zero past kn), T_b staged by 32 columns
+        const double* Tb = Tall + (size_t)b * ORM_NB * ORM_NB;
+#pragma unroll
+        for (int i = 0; i < NP; ++i) acc[i] = 0.0;
+        for (int cc = 0; cc < kn; cc += STRIP_RK) {
+            for (int e = t; e < ORM_NB * STRIP_RK; e += STRIP_NT) {
+                const int rr = e / STRIP_RK, l = e % STRIP_RK;
+                Vs[rr * STRIP_LD + l] = Tb[(size_t)rr * ORM_NB + cc + l];
+            }
+            __syncthreads();
+#pragma unroll 8
+            for (int l = 0; l < STRIP_RK; ++l) {
+                const double tv = Vs[c * STRIP_LD + l];
+#pragma unroll
+                for (int i = 0; i < NP; ++i)
+                    if (jt + 2 * i < W) acc[i] = fma(tv, Gs[(cc + l) * STRIP_W + jt + 2 * i], acc[i]);
+            }
+            __syncthreads();
+        }
+#pragma unroll
+        for (int i = 0; i < NP; ++i)
+            if (jt + 2 * i < W) Gp[c * STRIP_W + jt + 2 * i] = acc[i];
+        __syncthreads();
+        // Y[r0 + r, strip] -= sum_c V_b[c][r] G'[c][:], one row per thread (V_b rows coalesced)
+        for (int r = t; r < m; r += STRIP_NT) {
+            double y[W];
+#pragma unroll
+            for (int j = 0; j < W; ++j) y[j] = 0.0;
+            const double* vr = Vb + r;
+#pragma unroll 4
+            for (int cc = 0; cc < kn; ++cc) {
+                const double v = vr[(size_t)cc * n];
+#pragma unroll
+                for (int j = 0; j < W; ++j) y[j] = fma(v, Gp[cc * STRIP_W + j], y[j]);
+            }
+            double* yr = Y + (size_t)(r0 + r) * n + jb;
+#pragma unroll
+            for (int j = 0; j < W; ++j) yr[j] -= y[j];
+        }
+        __syncthreads();   // the next block reads these rows of the strip through other threads
+    }
+}
+
+template <int W>
+__device__ __forceinline__ void strip_dispatch(int w, int n, int nref, const double* V, const double* Tall, double* Y,
+                                               int jb, double* sm) {
+    if constexpr (W > 1) {
+        if (w < W) {
+            strip_dispatch<W - 1>(w, n, nref, V, Tall, Y, jb, sm);
+            return;
+        }
+    }
+    strip_pass<W>(n, nref, V, Tall, Y, jb, sm);
+}
+
+__global__ void __launch_bounds__(STRIP_NT) k_ormtr_strips(int n, int nref, const double* __restrict__ V,
+                                                           const double* __restrict__ Tall, double* __restrict__ Y,
+                                                           const int* __restrict__ ncol) {
+    extern __shared__ double strip_sm[];
+    const int nc = ncol ? min(n, *ncol) : n;
+    const int per = (nc + (int)gridDim.x - 1) / (int)gridDim.x;   // columns of this block's strip
+    const int ja = blockIdx.x * per, jz = min(nc, ja + per);
+    for (int jb = ja; jb < jz; jb += STRIP_W)
+        strip_dispatch<STRIP_W>(min(STRIP_W, jz - jb), n, nref, V, Tall, Y, jb, strip_sm);
+}
+
 size_t ormtr_workspace(int n) {
     const size_t nblk = (size_t)std::max(1, ceil_div(std::max(n - 2, 1), ORM_NB));
     return (size_t)ORM_SPLIT * ORM_NB * ((size_t)std::max(n, ORM_NB) + ORM_NB) + (size_t)ORM_NB * n +
@@ -1073,6 +1196,16 @@ void ormtr_blocked(cudaStream_t st, int n, const double* V, const double* tau, d
     allow_max_dynamic_smem((const void*)k_larft_all);
     k_larft_all<<<nblk, 8 * ORM_NB, smem, st>>>(nref, tau, Sall, Tall);
     XG_LAUNCH_CHECK();
+    if (!slices) {
+        // FP64: every block of reflectors on column strips, one launch, one block per SM
+        int dev = 0, nsm = 0;
+        XG_CUDA(cudaGetDevice(&dev));
+        XG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+        allow_max_dynamic_smem((const void*)k_ormtr_strips);
+        k_ormtr_strips<<<std::max(1, std::min(nsm, n)), STRIP_NT, STRIP_SMEM, st>>>(n, nref, V, Tall, Y, d_ncol);
+        XG_LAUNCH_CHECK();
+        return;
+    }
     k_wy_all<<<dim3(ORM_NB / GBN, ceil_div(n, GBM), nblk), 256, 0, st>>>(n, nref, V, Tall, Wall);
     XG_LAUNCH_CHECK();
     for (int b = nblk - 1; b >= 0; --b) {
@@ -1081,16 +1214,10 @@ void ormtr_blocked(cudaStream_t st, int n, const double* V, const double* tau, d
         const double* Vb = V + (size_t)k0 * n + r0;
         const double* Wb = Wall + (size_t)b * n * ORM_NB;
         // G = Vb Y[r0:, :ncol];  Y[r0:, :ncol] -= W_b G
-        if (slices) {
-            split_gemm(st, false, false, kn, n, m, 1.0, Vb, n, Y + (size_t)r0 * n, n, 0.0, G, n, slices, split_work,
-                       nullptr, d_ncol);
-            split_gemm(st, false, false, m, n, kn, -1.0, Wb, ORM_NB, G, n, 1.0, Y + (size_t)r0 * n, n, slices,
-                       split_work, nullptr, d_ncol);
-        } else {
-            dgemm_splitk(st, false, false, kn, n, m, 1.0, Vb, n, Y + (size_t)r0 * n, n, 0.0, G, n, ORM_SPLIT,
-                         partial, d_ncol);
-            dgemm(st, false, false, m, n, kn, -1.0, Wb, ORM_NB, G, n, 1.0, Y + (size_t)r0 * n, n, 0, nullptr, d_ncol);
-        }
+        split_gemm(st, false, false, kn, n, m, 1.0, Vb, n, Y + (size_t)r0 * n, n, 0.0, G, n, slices, split_work,
+                   nullptr, d_ncol);
+        split_gemm(st, false, false, m, n, kn, -1.0, Wb, ORM_NB, G, n, 1.0, Y + (size_t)r0 * n, n, slices,
+                   split_work, nullptr, d_ncol);
     }
 }
 

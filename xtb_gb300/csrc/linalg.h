@@ -51,7 +51,8 @@ void tridiag_eigvecs(cudaStream_t st, int n, const double* d, const double* e, c
 void ormtr(cudaStream_t st, int n, const double* V, const double* tau, const double* Y, double* Zt,
            const int* ncol = nullptr);
 // Y[:, j] = Q Y[:, j] in place for j < *ncol (all if null), Q = H(0) ... H(n-3): compact-WY blocks
-// of 128 reflectors applied as GEMMs; work: ormtr_workspace(n) doubles
+// of 128 reflectors (FP64: every block on column strips in one launch; split precision: two
+// tensor-core GEMMs per block); work: ormtr_workspace(n) doubles
 size_t ormtr_workspace(int n);
 // the same product, one warp per vector, in place (better below a few thousand AOs)
 void ormtr_inplace(cudaStream_t st, int n, const double* V, const double* tau, double* Y, const int* ncol);

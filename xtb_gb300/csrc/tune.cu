@@ -4,6 +4,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cstring>
 #include <mutex>
 
 #include "linalg.h"
@@ -51,6 +52,20 @@ double best_ms(cudaStream_t st, cudaEvent_t e0, cudaEvent_t e1, int reps, F&& f)
         best = std::min(best, (double)ms);
     }
     return best;
+}
+
+// out[0] = max |A - B|, out[1] = max |A| over rows < n, columns < nc (row stride n); non-negative
+// doubles order like their bit patterns
+__global__ void k_tune_maxdiff(int n, int nc, const double* __restrict__ A, const double* __restrict__ B,
+                               unsigned long long* __restrict__ out) {
+    double md = 0.0, ma = 0.0;
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < (long)n * nc; t += (long)gridDim.x * blockDim.x) {
+        const size_t o = (size_t)(t / nc) * n + (size_t)(t % nc);
+        md = fmax(md, fabs(A[o] - B[o]));
+        ma = fmax(ma, fabs(A[o]));
+    }
+    atomicMax(&out[0], (unsigned long long)__double_as_longlong(md));
+    atomicMax(&out[1], (unsigned long long)__double_as_longlong(ma));
 }
 
 // smallest tested size from which `fast` wins at every larger tested size (INT_MAX: never)
@@ -128,6 +143,79 @@ double time_sytrd(int n, int form, int max_blocks, int reps) {
     return ms;
 }
 
+void check_backtransform(int n, int ncol, int slices, double* out) {
+    if (n < 3 || n > 8192 || ncol < 1 || ncol > n || slices < 0 || slices > 8)
+        throw std::runtime_error("check_backtransform: n must lie in 3..8192, ncol in 1..n, slices in 0..8");
+    cudaStream_t st = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    XG_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    XG_CUDA(cudaEventCreate(&e0));
+    XG_CUDA(cudaEventCreate(&e1));
+    const size_t nn = (size_t)n * n;
+    const size_t split_ws = slices ? (split_gemm_workspace(n, n, n, slices) + 255) / 256 * 256 : 0;
+    const size_t doubles = 5 * nn + 3 * (size_t)n + sytrd_workspace(n) + ormtr_workspace(n) + 64;
+    char* buf = nullptr;
+    XG_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&buf), doubles * sizeof(double) + split_ws + 512, st));
+    try {
+        char* sgw = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(buf) + 255) / 256 * 256);
+        double* A = reinterpret_cast<double*>(sgw + split_ws);
+        double* V = A + nn;
+        double* Y0 = V + nn;
+        double* Y1 = Y0 + nn;
+        double* Y2 = Y1 + nn;
+        double* tau = Y2 + nn;
+        double* d = tau + n;
+        double* e = d + n;
+        double* p = e + n;
+        double* ormw = p + sytrd_workspace(n);
+        int* dcol = reinterpret_cast<int*>(ormw + ormtr_workspace(n));
+        unsigned long long* mx = reinterpret_cast<unsigned long long*>(dcol + 16);
+        k_tune_sym<<<ceil_div((long)nn, 256), 256, 0, st>>>(n, 91u + n, A);
+        k_tune_sym<<<ceil_div((long)nn, 256), 256, 0, st>>>(n, 7u + n, Y0);
+        XG_LAUNCH_CHECK();
+        sytrd_form(st, n, A, n, V, tau, d, e, p, -1);
+        XG_CUDA(cudaMemcpyAsync(dcol, &ncol, sizeof(int), cudaMemcpyHostToDevice, st));
+        XG_CUDA(cudaMemsetAsync(mx, 0, 2 * sizeof(unsigned long long), st));
+        auto warp = [&](double* Y) { ormtr_inplace(st, n, V, tau, Y, dcol); };
+        auto blocked = [&](double* Y) { ormtr_blocked(st, n, V, tau, Y, dcol, ormw, slices, slices ? sgw : nullptr); };
+        float ms[2] = {0.0f, 0.0f};
+        double* dst[2] = {Y1, Y2};
+        for (int f = 0; f < 2; ++f) {
+            XG_CUDA(cudaMemcpyAsync(dst[f], Y0, nn * sizeof(double), cudaMemcpyDeviceToDevice, st));
+            f ? blocked(dst[f]) : warp(dst[f]);   // warm-up
+            XG_CUDA(cudaMemcpyAsync(dst[f], Y0, nn * sizeof(double), cudaMemcpyDeviceToDevice, st));
+            XG_CUDA(cudaEventRecord(e0, st));
+            f ? blocked(dst[f]) : warp(dst[f]);
+            XG_CUDA(cudaEventRecord(e1, st));
+            XG_CUDA(cudaEventSynchronize(e1));
+            XG_CUDA(cudaEventElapsedTime(&ms[f], e0, e1));
+        }
+        k_tune_maxdiff<<<304, 256, 0, st>>>(n, ncol, Y1, Y2, mx);
+        XG_LAUNCH_CHECK();
+        unsigned long long h[2];
+        XG_CUDA(cudaMemcpyAsync(h, mx, sizeof(h), cudaMemcpyDeviceToHost, st));
+        XG_CUDA(cudaStreamSynchronize(st));
+        double md, ma;
+        std::memcpy(&md, &h[0], sizeof(double));
+        std::memcpy(&ma, &h[1], sizeof(double));
+        out[0] = ma > 0.0 ? md / ma : md;
+        out[1] = ms[0];
+        out[2] = ms[1];
+    } catch (...) {
+        cudaFreeAsync(buf, st);
+        cudaStreamSynchronize(st);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        cudaStreamDestroy(st);
+        throw;
+    }
+    XG_CUDA(cudaFreeAsync(buf, st));
+    XG_CUDA(cudaStreamSynchronize(st));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaStreamDestroy(st);
+}
+
 Tuned autotune() {
     const int dev = current_device();
     {
@@ -176,8 +264,9 @@ Tuned autotune() {
             sym_wins.push_back(ms[1] < ms[0]);
         }
         t.sytrd_sym_min = crossover(tsz, sym_wins);
-        // 2. back-transformation of n / 2 vectors: one warp per vector against compact-WY GEMMs
-        const std::vector<int> bsz = {600, 900, 1200, 1500, 1800, 2400};
+        // 2. back-transformation of n / 2 vectors: one warp per vector against the compact-WY form
+        //    (FP64: column strips in one launch; split: the GEMM chain on the tensor cores)
+        const std::vector<int> bsz = {300, 450, 600, 900, 1200, 1500, 1800, 2400};
         std::vector<bool> fp64_wins, split_wins;
         for (int n : bsz) {
             k_tune_sym<<<ceil_div((long)n * n, 256), 256, 0, st>>>(n, 91u + n, A);

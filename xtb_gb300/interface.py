@@ -91,6 +91,7 @@ def load_library(path=LIBPATH):
         "xtbgb_fp64PeakDetail": (None, [C.POINTER(C.c_double)]),
         "xtbgb_autotune": (C.c_int, [vp, dp, C.c_int]),
         "xtbgb_sytrdMs": (C.c_double, [vp, C.c_int, C.c_int, C.c_int, C.c_int]),
+        "xtbgb_backtransformCheck": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, dp]),
         "xtbgb_setExternalChargesHardness": (None, [vp, vp, C.c_int, dp, dp, dp]),
         "xtbgb_writeRestart": (C.c_int, [vp, vp, vp, C.c_char_p]),
         "xtbgb_readRestart": (C.c_int, [vp, vp, vp, C.c_char_p]),
@@ -532,6 +533,20 @@ def sytrd_ms(n, form=-1, max_blocks=0, reps=3):
     ms = lib.xtbgb_sytrdMs(env.h, int(n), int(form), int(max_blocks), int(reps))
     env.check()
     return float(ms)
+
+
+def backtransform_check(n, ncol, slices=0):
+    """Compact-WY eigenvector back-transformation (slices 0: FP64 column strips, > 0: split
+    products) against the one-warp-per-vector form on ncol columns of a random n x n matrix
+    (xtbgb_backtransformCheck): (max |difference| / max |Z|, warp-form ms, compact-WY ms)."""
+    lib = load_library()
+    env = Environment(0)
+    out = np.zeros(3)
+    rc = lib.xtbgb_backtransformCheck(env.h, int(n), int(ncol), int(slices), _dptr(out))
+    env.check()
+    if rc != 0:
+        raise XTBException("xtbgb_backtransformCheck failed")
+    return float(out[0]), float(out[1]), float(out[2])
 
 
 def get_tuning():
