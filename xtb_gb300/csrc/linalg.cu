@@ -1074,18 +1074,34 @@ __device__ void strip_pass(int n, int nref, const double* __restrict__ V, const 
         double acc[NP];
 #pragma unroll
         for (int i = 0; i < NP; ++i) acc[i] = 0.0;
-        // G = V_b Y[r0:, strip], 32 rows at a time (rows of V_b past kn and past m are zero)
-        for (int rc = 0; rc < m; rc += STRIP_RK) {
+        // G = V_b Y[r0:, strip], 32 rows at a time (rows of V_b past kn and past m are zero); the
+        // next chunk's operands are loaded into registers while the current one is multiplied
+        constexpr int PV = ORM_NB * STRIP_RK / STRIP_NT, PY = STRIP_RK * STRIP_W / STRIP_NT;
+        double pv[PV], py[PY];
+        auto fetch = [&](int rc) {
             const int rl = min(STRIP_RK, m - rc);
-            for (int e = t; e < ORM_NB * STRIP_RK; e += STRIP_NT) {
-                const int cc = e / STRIP_RK, r = e % STRIP_RK;
-                Vs[cc * STRIP_LD + r] = (cc < kn && r < rl) ? Vb[(size_t)cc * n + rc + r] : 0.0;
+#pragma unroll
+            for (int u = 0; u < PV; ++u) {
+                const int e = t + u * STRIP_NT, cc = e / STRIP_RK, r = e % STRIP_RK;
+                pv[u] = (cc < kn && r < rl) ? Vb[(size_t)cc * n + rc + r] : 0.0;
             }
-            for (int e = t; e < STRIP_RK * STRIP_W; e += STRIP_NT) {
-                const int r = e / STRIP_W, j = e % STRIP_W;
-                Ys[e] = (r < rl && j < W) ? Y[(size_t)(r0 + rc + r) * n + jb + j] : 0.0;
+#pragma unroll
+            for (int u = 0; u < PY; ++u) {
+                const int e = t + u * STRIP_NT, r = e / STRIP_W, j = e % STRIP_W;
+                py[u] = (r < rl && j < W) ? Y[(size_t)(r0 + rc + r) * n + jb + j] : 0.0;
             }
+        };
+        fetch(0);
+        for (int rc = 0; rc < m; rc += STRIP_RK) {
+#pragma unroll
+            for (int u = 0; u < PV; ++u) {
+                const int e = t + u * STRIP_NT;
+                Vs[(e / STRIP_RK) * STRIP_LD + e % STRIP_RK] = pv[u];
+            }
+#pragma unroll
+            for (int u = 0; u < PY; ++u) Ys[t + u * STRIP_NT] = py[u];
             __syncthreads();
+            if (rc + STRIP_RK < m) fetch(rc + STRIP_RK);
 #pragma unroll 8
             for (int r = 0; r < STRIP_RK; ++r) {
                 const double v = Vs[c * STRIP_LD + r];
@@ -1122,21 +1138,29 @@ __device__ void strip_pass(int n, int nref, const double* __restrict__ V, const 
         for (int i = 0; i < NP; ++i)
             if (jt + 2 * i < W) Gp[c * STRIP_W + jt + 2 * i] = acc[i];
         __syncthreads();
-        // Y[r0 + r, strip] -= sum_c V_b[c][r] G'[c][:], one row per thread (V_b rows coalesced)
-        for (int r = t; r < m; r += STRIP_NT) {
-            double y[W];
+        // Y[r0 + r, strip] -= sum_c V_b[c][r] G'[c][:]: thread (r, half) takes one row and half of
+        // the columns (128 rows per round keep the last round of short blocks fuller; V_b rows
+        // are coalesced over the threads)
+        {
+            constexpr int H = (W + 1) / 2;
+            const int half = t / ORM_NB, j0 = half * H;
+            for (int r = t % ORM_NB; r < m; r += ORM_NB) {
+                double y[H];
 #pragma unroll
-            for (int j = 0; j < W; ++j) y[j] = 0.0;
-            const double* vr = Vb + r;
+                for (int j = 0; j < H; ++j) y[j] = 0.0;
+                const double* vr = Vb + r;
 #pragma unroll 4
-            for (int cc = 0; cc < kn; ++cc) {
-                const double v = vr[(size_t)cc * n];
+                for (int cc = 0; cc < kn; ++cc) {
+                    const double v = vr[(size_t)cc * n];
 #pragma unroll
-                for (int j = 0; j < W; ++j) y[j] = fma(v, Gp[cc * STRIP_W + j], y[j]);
+                    for (int j = 0; j < H; ++j)
+                        if (j0 + j < W) y[j] = fma(v, Gp[cc * STRIP_W + j0 + j], y[j]);
+                }
+                double* yr = Y + (size_t)(r0 + r) * n + jb + j0;
+#pragma unroll
+                for (int j = 0; j < H; ++j)
+                    if (j0 + j < W) yr[j] -= y[j];
             }
-            double* yr = Y + (size_t)(r0 + r) * n + jb;
-#pragma unroll
-            for (int j = 0; j < W; ++j) yr[j] -= y[j];
         }
         __syncthreads();   // the next block reads these rows of the strip through other threads
     }
