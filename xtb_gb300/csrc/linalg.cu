@@ -82,13 +82,15 @@ static void dgemm_launch(cudaStream_t st, bool ta, bool tb, int M, int N, int K,
 void dgemm(cudaStream_t st, bool ta, bool tb, int M, int N, int K, double alpha, const double* A, int lda,
            const double* B, int ldb, double beta, double* C, int ldc, int flags, const int* dK, const int* dN) {
     if (M <= 0 || N <= 0) return;
-    // Products of two triangular matrices (the standard form's Hu X and X^T (Hu X)) have tiles
-    // whose K ranges run from one tile to all of K: at a few thousand AOs their largest 64 x 64
-    // tiles alone are about the average work per SM and ran at half speed beside other tiles on
-    // their SM (n = 1800: Hu X 3.3 ms, 0.59 TFLOP/s).  32 x 32 tiles cut the largest tile's share
-    // by 8: the standard form at n = 1800 went from 7.6 to 5.6 ms per SCC iteration.
-    const bool tri2 = (flags & GF_B_UPPER) && (flags & (GF_A_UPPER | GF_A_LOWER));
-    if (tri2 && std::max(M, N) <= 4096) dgemm_launch<32>(st, ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, flags, dK, dN);
+    // Structured products (triangular operands: the standard form's Hu X and X^T (Hu X), C = X Z;
+    // the symmetric density) have tiles whose K ranges or counts vary from tile to tile: at a few
+    // thousand AOs their largest 64 x 64 tiles alone are about the average work per SM and ran at
+    // half speed beside other tiles on their SM (n = 1800: Hu X 3.3 ms, 0.59 TFLOP/s).  32 x 32
+    // tiles cut the largest tile's share by 8; measured at n = 1800 per SCC iteration: standard
+    // form 7.6 -> 5.6 ms, C = X Z 4.6 -> 3.0 ms, density 3.7 -> 3.3 ms.  Dense products keep 64.
+    const bool small_tiles = (flags & (GF_A_UPPER | GF_SYM)) || ((flags & GF_B_UPPER) && (flags & GF_A_LOWER));
+    if (small_tiles && std::max(M, N) <= 4096)
+        dgemm_launch<32>(st, ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, flags, dK, dN);
     else dgemm_launch<GBM>(st, ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, flags, dK, dN);
 }
 
