@@ -594,8 +594,9 @@ def run_split(args, ws, rank):
         "roofline": {"bound": "fp64", "kernel": sytrd_form(n)[0], "achieved": ach, "peak": peak, "unit": "TFLOP/s",
                      "frac": ach / peak if peak else None, "launch_ms": sy,
                      "traffic": sytrd_form(n)[1], "traffic_unit": "bytes per launch",
-                     "note": "the tridiagonalisation stays FP64 and dominates; split products are in "
-                             "backtransform/density/gradient",
+                     "note": "the tridiagonalisation stays FP64 and dominates; split products are C = X Z, "
+                             "the density and the energy-weighted density (the back-transformation takes "
+                             "the tuned form: FP64 column strips below the split chain's crossover)",
                      "peak_detail": peak_detail},
         "clocks": clk,
     }

@@ -47,17 +47,25 @@ def test_split_rejects_bad_slice_count():
         X.Calculator(Z, xyz, precision="split", slices=3)
 
 
-def test_split_at_the_tensor_core_sizes_matches_the_oracle_fixture():
-    """C200H402 (602 atoms, 1202 AOs): from 1000 AOs the split mode also takes the blocked
-    back-transformation on the tensor cores.  Against the committed oracle fixture at the
-    spec tolerances, and against the FP64 mode of the engine (reported bound 1e-8 Eh)."""
+@pytest.mark.parametrize("chain", [True, False])
+def test_split_at_the_tensor_core_sizes_matches_the_oracle_fixture(chain):
+    """C200H402 (602 atoms, 1202 AOs) in split mode, with the back-transformation as the
+    tensor-core GEMM chain (pinned from 1000 AOs) and as the tuned device chooses (on GB300 the
+    FP64 column strips up to 1500 AOs).  Against the committed oracle fixture at the north-star
+    tolerances, and against the FP64 mode of the engine (reported bound 1e-8 Eh)."""
     import os
     path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "c200h402_seed1.npz")
     if not os.path.exists(path):
         pytest.skip("fixture c200h402_seed1 not generated")
     fx = np.load(path)
     Z, xyz = fx["numbers"], fx["positions"]
-    f, s = both(Z, xyz)
+    saved = X.get_tuning()
+    try:
+        if chain:
+            X.set_tuning(saved["sytrd_sym_min"], saved["blocked_min_fp64"], 1000)
+        f, s = both(Z, xyz)
+    finally:
+        X.set_tuning(saved["sytrd_sym_min"], saved["blocked_min_fp64"], saved["blocked_min_split"])
     assert abs(s.energy - fx["energy"]) <= TOL_E
     assert np.max(np.abs(s.charges - fx["charges"])) <= TOL_Q
     assert np.max(np.abs(s.gradient - fx["gradient"])) <= TOL_G

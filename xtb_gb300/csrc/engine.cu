@@ -671,9 +671,11 @@ void run_singlepoint(const HostMol& hm, const SPSettings& set, Wavefunction& wfn
         }
         tridiag_eigvecs(st, nao, tri_d, tri_e, bounds, emo, Y, iscr, piv, info + 1);
         tm.mark(PH_BACKTR);
-        // Y[:, :kocc] = Q Y: compact-WY GEMMs pay off for large n, one warp per vector below
-        if (nao >= set.blocked_threshold())
-            ormtr_blocked(st, nao, V, tri_tau, Y, info + 1, ormw, split ? set.slices : 0, sgw);
+        // Y[:, :kocc] = Q Y: compact-WY form (FP64 strips or split GEMMs) for large n, one warp per
+        // vector below
+        const int bform = set.backtransform_form(nao, split);
+        if (bform > 0)
+            ormtr_blocked(st, nao, V, tri_tau, Y, info + 1, ormw, bform == 2 ? set.slices : 0, sgw);
         else
             ormtr_inplace(st, nao, V, tri_tau, Y, info + 1);
         if (split)
@@ -722,7 +724,7 @@ void run_singlepoint(const HostMol& hm, const SPSettings& set, Wavefunction& wfn
     if (keep_orbitals) {
         // all MO coefficients of the last iteration (only occupied ones were needed inside the SCC)
         tridiag_eigvecs(st, nao, tri_d, tri_e, bounds, emo, Y, iscr, piv, nullptr);
-        if (nao >= set.blocked_threshold()) ormtr_blocked(st, nao, V, tri_tau, Y, nullptr, ormw);
+        if (set.backtransform_form(nao, false) > 0) ormtr_blocked(st, nao, V, tri_tau, Y, nullptr, ormw);
         else ormtr_inplace(st, nao, V, tri_tau, Y, nullptr);
         dgemm(st, false, false, nao, nao, nao, 1.0, X, nao, Y, nao, 0.0, C, nao, GF_A_UPPER);
     }

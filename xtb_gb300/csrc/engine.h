@@ -18,11 +18,18 @@ struct SPSettings {
     // the reduction to standard form and the eigensolver stay FP64
     int precision = 0;
     int slices = 5;
-    // AO count from which the back-transformation of the eigenvectors runs as compact-WY
-    // GEMMs instead of one warp per vector; -1 takes the device's threshold for the precision
-    // (tune.h: measured by the autotuner, else the defaults measured once on GB300)
+    // AO count from which the back-transformation of the eigenvectors runs in the compact-WY form
+    // (FP64 column strips; with split products the tensor-core GEMM chain) instead of one warp
+    // per vector; -1 takes the device's thresholds (tune.h: measured by the autotuner, else the
+    // defaults measured once on GB300)
     int blocked_min = -1;
-    int blocked_threshold() const { return blocked_min >= 0 ? blocked_min : tuned_blocked_min(precision); }
+    // back-transformation of n AOs: 0 one warp per vector, 1 FP64 column strips, 2 the
+    // split-precision GEMM chain (split mode only, where it beats both FP64 forms)
+    int backtransform_form(int n, bool split) const {
+        if (blocked_min >= 0) return n >= blocked_min ? (split ? 2 : 1) : 0;
+        if (split && n >= tuned_blocked_min(1)) return 2;
+        return n >= tuned_blocked_min(0) ? 1 : 0;
+    }
     // CUDA stream priority of the single point's stream (lower is more urgent; clamped to the
     // device's range; 0 is the default priority)
     int stream_priority = 0;

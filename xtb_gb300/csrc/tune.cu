@@ -280,7 +280,7 @@ Tuned autotune() {
             const double s = best_ms(st, e0, e1, 2, [&] { ormtr_blocked(st, n, V, tau, Y, ncol, ormw, 5, sgw); });
             t.backtr_rows.insert(t.backtr_rows.end(), {(double)n, w, b, s});
             fp64_wins.push_back(b < w);
-            split_wins.push_back(s < w);
+            split_wins.push_back(s < std::min(w, b));   // split mode runs the faster FP64 form below
         }
         t.blocked_min_fp64 = crossover(bsz, fp64_wins);
         t.blocked_min_split = crossover(bsz, split_wins);

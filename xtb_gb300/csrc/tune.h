@@ -16,8 +16,10 @@ struct Tuned {
     int sytrd_sym_min = 1 << 30;    // AOs from which the upper-triangle tridiagonalisation runs
                                     // (never by default: on GB300 the row form measured faster up
                                     // to 1024 AOs, its per-column latency being lower)
-    int blocked_min_fp64 = 600;     // AOs from which the compact-WY back-transformation runs
-    int blocked_min_split = 1000;   // the same with split-precision products
+    int blocked_min_fp64 = 300;     // AOs from which the compact-WY back-transformation runs
+                                    // (FP64 column strips)
+    int blocked_min_split = 1500;   // AOs from which split mode runs it as tensor-core GEMMs
+                                    // (below, split mode takes the faster FP64 form)
     int level = 0;                  // 0: defaults, 1: measured on this device
     double seconds = 0.0;           // time the measurement took
     // measurements: (n, row form ms, upper-triangle form ms) and
