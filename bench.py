@@ -266,7 +266,7 @@ def autotune_served(args, reqs):
     """The engine's autotuner, before any timing: the kernel-form crossovers of this device, then
     the request loop's schedule on this stream (unless given on the command line)."""
     from xtb_gb300 import tuning
-    forms = tuning.kernel_forms()
+    forms = device_forms(args)
     out = {"kernel_forms": forms}
     if args.workers is None or args.iters_per_step is None or args.pool_max_nao is None or args.coop_blocks is None:
         sched = tuning.schedule(reqs, pool_gib=args.pool_gib, precision=args.served_precision, slices=args.slices)
@@ -280,6 +280,17 @@ def autotune_served(args, reqs):
         if args.coop_blocks is None:
             args.coop_blocks = sched["coop_blocks"]
     return out
+
+
+def device_forms(args):
+    """The device's kernel-form choices: measured by the autotuner, or pinned with --forms
+    (sytrd_sym_min,blocked_min_fp64,blocked_min_split), e.g. to repeat a measured run's choices
+    under a profiler, whose per-launch overhead would skew the tuner's timings."""
+    if args.forms:
+        sym, fp64, split = (int(v) for v in args.forms.split(","))
+        X.set_tuning(sym, fp64, split)
+        return X.get_tuning()
+    return X.autotune()
 
 
 def run_served(args, ws, rank):
@@ -464,7 +475,7 @@ def run_plain(args, ws, rank):
     metric, desc = workload_spec(args)
     Z, xyz = PLAIN_WORKLOADS[args.workload][1](W)
     lib = X.load_library()
-    X.autotune()          # the device's kernel forms, as the served run and the engine use them
+    device_forms(args)    # the device's kernel forms, as the served run and the engine use them
     calc = X.Calculator(Z, xyz, keep_orbitals=False)
     for _ in range(args.warmup):
         r = calc.singlepoint()
@@ -530,7 +541,7 @@ def run_split(args, ws, rank):
     metric, desc = workload_spec(args)
     Z, xyz = SPLIT_WORKLOADS[args.workload][1](W)
     lib = X.load_library()
-    X.autotune()          # the device's kernel forms, as the served run and the engine use them
+    device_forms(args)    # the device's kernel forms, as the served run and the engine use them
     cs = X.Calculator(Z, xyz, keep_orbitals=False, precision="split", slices=args.slices)
     for _ in range(args.warmup):
         r = cs.singlepoint()
@@ -769,6 +780,8 @@ def main():
     ap.add_argument("--cpu-batch-sample", type=int, default=512,
                     help="batch4096: molecules of the set the CPU restatement runs")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--forms", default=None,
+                    help="pin the kernel forms instead of autotuning: sytrd_sym_min,blocked_min_fp64,blocked_min_split")
     ap.add_argument("--no-configs", action="store_true", help="served: skip the three other configurations")
     args = ap.parse_args()
     ws, rank, _ = dist_setup()
