@@ -286,6 +286,7 @@ def device_forms(args):
     """The device's kernel-form choices: measured by the autotuner, or pinned with --forms
     (sytrd_sym_min,blocked_min_fp64,blocked_min_split), e.g. to repeat a measured run's choices
     under a profiler, whose per-launch overhead would skew the tuner's timings."""
+    from xtb_gb300 import interface as X
     if args.forms:
         sym, fp64, split = (int(v) for v in args.forms.split(","))
         X.set_tuning(sym, fp64, split)
