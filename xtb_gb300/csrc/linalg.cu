@@ -1076,12 +1076,18 @@ constexpr size_t STRIP_SMEM = (size_t)(ORM_NB * STRIP_LD + STRIP_RK * STRIP_W + 
 template <int W>
 __device__ void strip_pass(int n, int nref, const double* __restrict__ V, const double* __restrict__ Tall,
                            double* __restrict__ Y, int jb, double* sm) {
-    constexpr int NP = (W + 1) / 2;           // column slots of a thread
+    // even widths: thread (c, jt) takes columns jt, jt + 2, ...; odd widths: the threads of the
+    // first 128 take every column and the others only stage operands (a split would leave one
+    // empty FMA slot per step in half of the threads)
+    constexpr bool ONE = (W & 1) != 0;
+    constexpr int NP = ONE ? W : W / 2;       // column slots of a thread
     double* Vs = sm;                          // [ORM_NB][STRIP_LD]: V_b rows (then T_b rows) by 32 columns
     double* Ys = Vs + ORM_NB * STRIP_LD;      // [STRIP_RK][STRIP_W]
     double* Gs = Ys + STRIP_RK * STRIP_W;     // [ORM_NB][STRIP_W]: G = V_b Y
     double* Gp = Gs + ORM_NB * STRIP_W;       // [ORM_NB][STRIP_W]: T_b G
     const int t = threadIdx.x, c = t % ORM_NB, jt = t / ORM_NB;
+    const bool act = !ONE || jt == 0;         // warp-uniform
+    auto col = [&](int i) { return ONE ? i : jt + 2 * i; };
     const int nblk = (nref + ORM_NB - 1) / ORM_NB;
     for (int b = nblk - 1; b >= 0; --b) {
         const int k0 = b * ORM_NB, kn = min(ORM_NB, nref - k0);
@@ -1118,18 +1124,19 @@ __device__ void strip_pass(int n, int nref, const double* __restrict__ V, const 
             for (int u = 0; u < PY; ++u) Ys[t + u * STRIP_NT] = py[u];
             __syncthreads();
             if (rc + STRIP_RK < m) fetch(rc + STRIP_RK);
+            if (act) {
 #pragma unroll 8
-            for (int r = 0; r < STRIP_RK; ++r) {
-                const double v = Vs[c * STRIP_LD + r];
+                for (int r = 0; r < STRIP_RK; ++r) {
+                    const double v = Vs[c * STRIP_LD + r];
 #pragma unroll
-                for (int i = 0; i < NP; ++i)
-                    if (jt + 2 * i < W) acc[i] = fma(v, Ys[r * STRIP_W + jt + 2 * i], acc[i]);
+                    for (int i = 0; i < NP; ++i) acc[i] = fma(v, Ys[r * STRIP_W + col(i)], acc[i]);
+                }
             }
             __syncthreads();
         }
+        if (act)
 #pragma unroll
-        for (int i = 0; i < NP; ++i)
-            if (jt + 2 * i < W) Gs[c * STRIP_W + jt + 2 * i] = acc[i];
+            for (int i = 0; i < NP; ++i) Gs[c * STRIP_W + col(i)] = acc[i];
         __syncthreads();
         // G' = T_b G (T_b upper triangular, zero past kn), T_b staged by 32 columns
         const double* Tb = Tall + (size_t)b * ORM_NB * ORM_NB;
@@ -1141,18 +1148,19 @@ __device__ void strip_pass(int n, int nref, const double* __restrict__ V, const 
                 Vs[rr * STRIP_LD + l] = Tb[(size_t)rr * ORM_NB + cc + l];
             }
             __syncthreads();
+            if (act) {
 #pragma unroll 8
-            for (int l = 0; l < STRIP_RK; ++l) {
-                const double tv = Vs[c * STRIP_LD + l];
+                for (int l = 0; l < STRIP_RK; ++l) {
+                    const double tv = Vs[c * STRIP_LD + l];
 #pragma unroll
-                for (int i = 0; i < NP; ++i)
-                    if (jt + 2 * i < W) acc[i] = fma(tv, Gs[(cc + l) * STRIP_W + jt + 2 * i], acc[i]);
+                    for (int i = 0; i < NP; ++i) acc[i] = fma(tv, Gs[(cc + l) * STRIP_W + col(i)], acc[i]);
+                }
             }
             __syncthreads();
         }
+        if (act)
 #pragma unroll
-        for (int i = 0; i < NP; ++i)
-            if (jt + 2 * i < W) Gp[c * STRIP_W + jt + 2 * i] = acc[i];
+            for (int i = 0; i < NP; ++i) Gp[c * STRIP_W + col(i)] = acc[i];
         __syncthreads();
         // Y[r0 + r, strip] -= sum_c V_b[c][r] G'[c][:]: thread (r, half) takes one row and half of
         // the columns (128 rows per round keep the last round of short blocks fuller; V_b rows
@@ -1194,7 +1202,7 @@ __device__ __forceinline__ void strip_dispatch(int w, int n, int nref, const dou
     strip_pass<W>(n, nref, V, Tall, Y, jb, sm);
 }
 
-__global__ void __launch_bounds__(STRIP_NT) k_ormtr_strips(int n, int nref, const double* __restrict__ V,
+__global__ void __launch_bounds__(STRIP_NT, 1) k_ormtr_strips(int n, int nref, const double* __restrict__ V,
                                                            const double* __restrict__ Tall, double* __restrict__ Y,
                                                            const int* __restrict__ ncol) {
     extern __shared__ double strip_sm[];
