@@ -1202,7 +1202,10 @@ __device__ __forceinline__ void strip_dispatch(int w, int n, int nref, const dou
     strip_pass<W>(n, nref, V, Tall, Y, jb, sm);
 }
 
-__global__ void __launch_bounds__(STRIP_NT, 1) k_ormtr_strips(int n, int nref, const double* __restrict__ V,
+// At most 128 registers: one block per SM by the grid, but a block that held most of the SM's
+// register file (226 registers unbounded) kept other requests' kernels off its SM in the served
+// stream (17.6 against 18.5-18.9 single points/s), for no gain of its own.
+__global__ void __launch_bounds__(STRIP_NT, 2) k_ormtr_strips(int n, int nref, const double* __restrict__ V,
                                                            const double* __restrict__ Tall, double* __restrict__ Y,
                                                            const int* __restrict__ ncol) {
     extern __shared__ double strip_sm[];
