@@ -525,7 +525,18 @@ __global__ void k_atm_pairs(DevMol m, const double* __restrict__ c6, const doubl
     gt[tt] = g;
 }
 
-// One thread per pair (i > j), loop over k < j; gradient and dE/dCN of k by atomics.
+// The derivative polynomial of the ATM angular factor for the pair whose squared distance is x
+// (y, z: the other two): x^3 + x^2 (y + z) + x (3 y^2 + 2 y z + 3 z^2) - 5 (y - z)^2 (y + z), with
+// u = y + z, v = y - z and 3 y^2 + 2 y z + 3 z^2 = 2 u^2 + v^2 (ten FP64 operations).
+__device__ __forceinline__ double atm_dpoly(double x, double y, double z) {
+    const double u = y + z, v = y - z, v2 = v * v;
+    const double w = fma(2.0 * u, u, v2);
+    return fma(x, fma(x, x + u, w), -5.0 * u * v2);
+}
+
+// One thread per pair (i > j), loop over k < j; gradient and dE/dCN of k by atomics.  The terms
+// of i and j that share a factor across k (the i-j distance vector, the C6 derivative ratios of
+// the pair) are summed over k first and applied once after the loop.
 __global__ void k_d4_atm(DevMol m, const double* __restrict__ ir, const double* __restrict__ tp,
                          const double* __restrict__ s6, const double* __restrict__ ga, const double* __restrict__ gt,
                          long npair, double* __restrict__ e_pair, double* __restrict__ dEdcn,
@@ -542,10 +553,13 @@ __global__ void k_d4_atm(DevMol m, const double* __restrict__ ir, const double* 
     const double r2ij = rij[0] * rij[0] + rij[1] * rij[1] + rij[2] * rij[2];
     double esum = 0.0;
     if (r2ij <= cut2) {
-        double gi[3] = {0, 0, 0}, gj[3] = {0, 0, 0}, dci = 0.0, dcj = 0.0;
+        // gi = -(S1 rij + sum_k dGr2 rik), gj = S1 rij - sum_k dGr3 rjk with S1 = sum_k dGr1;
+        // dci = gi_j H + sum_k h gt_ik, dcj = gj_i H + sum_k h gt_jk with H = sum_k h
+        double gik[3] = {0, 0, 0}, gjk[3] = {0, 0, 0}, s1 = 0.0, hs = 0.0, dci = 0.0, dcj = 0.0;
         const size_t pij = (size_t)ja * n + ia;
         const double irij = ir[pij], tij = tp[pij], sij = s6[pij];
         const double gi_j = ga[(size_t)ia * n + ja], gj_i = ga[pij];
+        const double w1 = s9 * irij * irij;
         for (int ka = 0; ka < ja; ++ka) {
             const double rik[3] = {x[3 * ka] - x[3 * ia], x[3 * ka + 1] - x[3 * ia + 1], x[3 * ka + 2] - x[3 * ia + 2]};
             const double r2ik = rik[0] * rik[0] + rik[1] * rik[1] + rik[2] * rik[2];
@@ -564,36 +578,32 @@ __global__ void k_d4_atm(DevMol m, const double* __restrict__ ir, const double* 
             const double fdmp = rcp_fast(1.0 + 6.0 * cralp);
             const double dfdmp = -(2.0 * 16.0 * cralp) * fdmp * fdmp;
             const double c9f = c9 * fdmp, c9d = dfdmp * c9 * ang;
-            const double dE = -ang * c9f;
-            const double dang1 = -ang_fact * (r2ij * r2ij * r2ij + r2ij * r2ij * (r2jk + r2ik) +
-                                              r2ij * (3.0 * r2jk * r2jk + 2.0 * r2jk * r2ik + 3.0 * r2ik * r2ik) -
-                                              5.0 * sq(r2jk - r2ik) * (r2jk + r2ik));
-            const double dang2 = -ang_fact * (r2ik * r2ik * r2ik + r2ik * r2ik * (r2jk + r2ij) +
-                                              r2ik * (3.0 * r2jk * r2jk + 2.0 * r2jk * r2ij + 3.0 * r2ij * r2ij) -
-                                              5.0 * sq(r2jk - r2ij) * (r2jk + r2ij));
-            const double dang3 = -ang_fact * (r2jk * r2jk * r2jk + r2jk * r2jk * (r2ik + r2ij) +
-                                              r2jk * (3.0 * r2ik * r2ik + 2.0 * r2ik * r2ij + 3.0 * r2ij * r2ij) -
-                                              5.0 * sq(r2ik - r2ij) * (r2ik + r2ij));
-            const double dGr1 = s9 * (c9d - dang1 * c9f) * (irij * irij);
-            const double dGr2 = s9 * (c9d - dang2 * c9f) * (irik * irik);
-            const double dGr3 = s9 * (c9d - dang3 * c9f) * (irjk * irjk);
-            esum += dE * s9;
+            // dGr_x = s9 (c9d - dang_x c9f) / r_x^2 with dang_x = -ang_fact P_x
+            const double qf = ang_fact * c9f;
+            const double dGr1 = fma(qf, atm_dpoly(r2ij, r2jk, r2ik), c9d) * w1;
+            const double dGr2 = fma(qf, atm_dpoly(r2ik, r2jk, r2ij), c9d) * (s9 * irik * irik);
+            const double dGr3 = fma(qf, atm_dpoly(r2jk, r2ik, r2ij), c9d) * (s9 * irjk * irjk);
+            esum = fma(-ang, c9f, esum);
+            s1 += dGr1;
             for (int q = 0; q < 3; ++q) {
-                gi[q] -= dGr1 * rij[q] + dGr2 * rik[q];
-                gj[q] += dGr1 * rij[q] - dGr3 * rjk[q];
-                atomicAdd(&grad[3 * ka + q], dGr2 * rik[q] + dGr3 * rjk[q]);
+                const double a2 = dGr2 * rik[q], a3 = dGr3 * rjk[q];
+                gik[q] += a2;
+                gjk[q] += a3;
+                atomicAdd(&grad[3 * ka + q], a2 + a3);
             }
-            const double h = -0.5 * s9 * ang * fdmp * c9;
-            dci += h * (gi_j + gt[pik]);
-            dcj += h * (gj_i + gt[pjk]);
+            const double h = (-0.5 * s9) * ang * c9f;
+            hs += h;
+            dci = fma(h, gt[pik], dci);
+            dcj = fma(h, gt[pjk], dcj);
             atomicAdd(&dEdcn[ka], h * (ga[pik] + ga[pjk]));
         }
         for (int q = 0; q < 3; ++q) {
-            atomicAdd(&grad[3 * ia + q], gi[q]);
-            atomicAdd(&grad[3 * ja + q], gj[q]);
+            atomicAdd(&grad[3 * ia + q], -fma(s1, rij[q], gik[q]));
+            atomicAdd(&grad[3 * ja + q], fma(s1, rij[q], -gjk[q]));
         }
-        atomicAdd(&dEdcn[ia], dci);
-        atomicAdd(&dEdcn[ja], dcj);
+        atomicAdd(&dEdcn[ia], fma(gi_j, hs, dci));
+        atomicAdd(&dEdcn[ja], fma(gj_i, hs, dcj));
+        esum *= s9;
     }
     e_pair[t] = esum;
 }
