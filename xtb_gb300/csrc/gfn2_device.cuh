@@ -1160,6 +1160,15 @@ __device__ inline void d_broyden_unpack(DevMol m, const double* __restrict__ v, 
 }
 
 // three-body (ATM) dispersion, atm_gradient_latp / deriv_atm_triple (src/disp/dftd4.F90:2023-2177, 2354-2433)
+// The derivative polynomial of the ATM angular factor for the pair whose squared distance is x
+// (y, z: the other two): x^3 + x^2 (y + z) + x (3 y^2 + 2 y z + 3 z^2) - 5 (y - z)^2 (y + z), with
+// u = y + z, v = y - z and 3 y^2 + 2 y z + 3 z^2 = 2 u^2 + v^2 (ten FP64 operations).
+__device__ __forceinline__ double atm_dpoly(double x, double y, double z) {
+    const double u = y + z, v = y - z, v2 = v * v;
+    const double w = fma(2.0 * u, u, v2);
+    return fma(x, fma(x, x + u, w), -5.0 * u * v2);
+}
+
 __device__ inline void d_d4_atm(DevMol m, const double* __restrict__ c6, const double* __restrict__ dc6, long npair,
                          double* __restrict__ e_pair, double* __restrict__ dEdcn, double* __restrict__ grad, long t) {
     int ia, ja;
@@ -1194,21 +1203,17 @@ __device__ inline void d_d4_atm(DevMol m, const double* __restrict__ c6, const d
             const double rrr3 = rrr1 * rrr2;
             const double ang_fact = 0.375 / (rrr2 * rrr3);
             const double ang = ang_fact * (r2ij + r2jk - r2ik) * (r2ij - r2jk + r2ik) * (-r2ij + r2jk + r2ik) + 1.0 / rrr3;
-            const double cralp = pow(ccc1 / rrr1, 16.0 / 3.0);
+            // (C_ijk / R_ijk)^(16/3) = x^5 cbrt(x): one cube root instead of a general power
+            const double xr = ccc1 / rrr1, xr2 = xr * xr;
+            const double cralp = xr2 * xr2 * xr * cbrt(xr);
             const double fdmp = 1.0 / (1.0 + 6.0 * cralp);
             const double dfdmp = -(2.0 * 16.0 * cralp) * fdmp * fdmp;
             const double dE = -fdmp * ang * c9;
-            const double dang1 = -ang_fact * (r2ij * r2ij * r2ij + r2ij * r2ij * (r2jk + r2ik) +
-                                              r2ij * (3.0 * r2jk * r2jk + 2.0 * r2jk * r2ik + 3.0 * r2ik * r2ik) -
-                                              5.0 * sq(r2jk - r2ik) * (r2jk + r2ik));
+            const double dang1 = -ang_fact * atm_dpoly(r2ij, r2jk, r2ik);
             const double dGr1 = (-dang1 * c9 * fdmp + dfdmp * c9 * ang) / r2ij;
-            const double dang2 = -ang_fact * (r2ik * r2ik * r2ik + r2ik * r2ik * (r2jk + r2ij) +
-                                              r2ik * (3.0 * r2jk * r2jk + 2.0 * r2jk * r2ij + 3.0 * r2ij * r2ij) -
-                                              5.0 * sq(r2jk - r2ij) * (r2jk + r2ij));
+            const double dang2 = -ang_fact * atm_dpoly(r2ik, r2jk, r2ij);
             const double dGr2 = (-dang2 * c9 * fdmp + dfdmp * c9 * ang) / r2ik;
-            const double dang3 = -ang_fact * (r2jk * r2jk * r2jk + r2jk * r2jk * (r2ik + r2ij) +
-                                              r2jk * (3.0 * r2ik * r2ik + 2.0 * r2ik * r2ij + 3.0 * r2ij * r2ij) -
-                                              5.0 * sq(r2ik - r2ij) * (r2ik + r2ij));
+            const double dang3 = -ang_fact * atm_dpoly(r2jk, r2ik, r2ij);
             const double dGr3 = (-dang3 * c9 * fdmp + dfdmp * c9 * ang) / r2jk;
             const double s9 = 5.0;
             esum += dE * s9;

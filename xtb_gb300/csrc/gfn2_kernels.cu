@@ -525,15 +525,6 @@ __global__ void k_atm_pairs(DevMol m, const double* __restrict__ c6, const doubl
     gt[tt] = g;
 }
 
-// The derivative polynomial of the ATM angular factor for the pair whose squared distance is x
-// (y, z: the other two): x^3 + x^2 (y + z) + x (3 y^2 + 2 y z + 3 z^2) - 5 (y - z)^2 (y + z), with
-// u = y + z, v = y - z and 3 y^2 + 2 y z + 3 z^2 = 2 u^2 + v^2 (ten FP64 operations).
-__device__ __forceinline__ double atm_dpoly(double x, double y, double z) {
-    const double u = y + z, v = y - z, v2 = v * v;
-    const double w = fma(2.0 * u, u, v2);
-    return fma(x, fma(x, x + u, w), -5.0 * u * v2);
-}
-
 // One thread per pair (i > j), loop over k < j; gradient and dE/dCN of k by atomics.  The terms
 // of i and j that share a factor across k (the i-j distance vector, the C6 derivative ratios of
 // the pair) are summed over k first and applied once after the loop.
