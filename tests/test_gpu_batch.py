@@ -1,6 +1,6 @@
 """Batched engine (one thread block per molecule) against the plain engine and the oracle.
 
-Tolerances: the spec bar against the oracle (|dE| <= 1e-6 Eh, charges <= 1e-5 e,
+Tolerances: the parity bar against the oracle (|dE| <= 1e-6 Eh, charges <= 1e-5 e,
 gradient <= 1e-5 Eh/bohr, SCC iterations +-1).  Against the plain GPU engine, which runs
 the same device arithmetic in a different launch shape (only summation orders differ),
 the bar is tighter: |dE| <= 1e-9 Eh, charges and gradient <= 1e-7.

@@ -1,7 +1,7 @@
 """Split-precision mode of the engine (back-transformation, density and energy-weighted
 density as BF16 tensor-core digit products) against the FP64 mode and the oracle.
 
-Bar: the benchmark spec's tolerances against the oracle (|dE| <= 1e-6 Eh, charges <= 1e-5 e,
+Bar: the parity tolerances against the oracle (|dE| <= 1e-6 Eh, charges <= 1e-5 e,
 gradient <= 1e-5 Eh/bohr, iterations +-1); against the FP64 mode of the same engine the
 differences are reported and bounded tighter (1e-8 Eh, 1e-7).
 """
@@ -51,7 +51,7 @@ def test_split_rejects_bad_slice_count():
 def test_split_at_the_tensor_core_sizes_matches_the_oracle_fixture(chain):
     """C200H402 (602 atoms, 1202 AOs) in split mode, with the back-transformation as the
     tensor-core GEMM chain (pinned from 1000 AOs) and as the tuned device chooses (on GB300 the
-    FP64 column strips up to 1500 AOs).  Against the committed oracle fixture at the north-star
+    FP64 column strips up to 1500 AOs).  Against the committed oracle fixture at the parity
     tolerances, and against the FP64 mode of the engine (reported bound 1e-8 Eh)."""
     import os
     path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "c200h402_seed1.npz")
