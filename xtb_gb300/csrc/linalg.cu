@@ -26,7 +26,18 @@ namespace xg {
 // GF_B_UPPER tiles need K up to j0 + 64 (descending columns first), GF_A_LOWER up to
 // i0 + 64 (descending rows first); GF_SYM enumerates only the tiles on or below the diagonal.
 __device__ __forceinline__ void dgemm_tile_order(int b, int tm, int tn, int flags, int& it, int& jt) {
-    if (flags & GF_SYM) {
+    if (flags & GF_SYM_UP) {
+        // rows 0, 1, ...; row r holds tiles jt = r .. tn-1 (equal K: any order balances)
+        int r = 0;
+        for (;;) {
+            const int cnt = tn - r;
+            if (b < cnt || r + 1 >= tm || r + 1 >= tn) break;
+            b -= cnt;
+            ++r;
+        }
+        it = r;
+        jt = r + b;
+    } else if (flags & GF_SYM) {
         // rows tm-1, tm-2, ...; row r holds tiles jt = 0..min(r, tn-1)
         int r = tm - 1;
         for (;;) {
@@ -50,6 +61,11 @@ __device__ __forceinline__ void dgemm_tile_order(int b, int tm, int tn, int flag
 }
 
 inline int dgemm_tile_count(int tm, int tn, int flags) {
+    if (flags & GF_SYM_UP) {
+        int c = 0;
+        for (int r = 0; r < std::min(tm, tn); ++r) c += tn - r;
+        return c;
+    }
     if (!(flags & GF_SYM)) return tm * tn;
     int c = 0;
     for (int r = 0; r < tm; ++r) c += std::min(r, tn - 1) + 1;
@@ -270,9 +286,10 @@ void potrf_upper(cudaStream_t st, int n, double* A, int lda, int* d_info) {
         if (m > 0) {
             k_potrf_trsm<<<ceil_div(m, 128), 128, 0, st>>>(n, A, lda, k0);
             XG_LAUNCH_CHECK();
-            // A22 -= U12^T U12
+            // A22 -= U12^T U12, upper triangle only (the only part the next panels read)
             double* U12 = A + (size_t)k0 * lda + k0 + b;
-            dgemm(st, true, false, m, m, b, -1.0, U12, lda, U12, lda, 1.0, A + (size_t)(k0 + b) * lda + k0 + b, lda);
+            dgemm(st, true, false, m, m, b, -1.0, U12, lda, U12, lda, 1.0, A + (size_t)(k0 + b) * lda + k0 + b, lda,
+                  GF_SYM_UP);
         }
     }
     k_zero_lower<<<ceil_div((long)n * n, 256), 256, 0, st>>>(n, A, lda);

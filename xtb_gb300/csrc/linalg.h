@@ -7,7 +7,7 @@
 namespace xg {
 
 // structure flags of dgemm
-constexpr int GF_B_UPPER = 1, GF_A_LOWER = 2, GF_A_UPPER = 4, GF_SYM = 8;
+constexpr int GF_B_UPPER = 1, GF_A_LOWER = 2, GF_A_UPPER = 4, GF_SYM = 8, GF_SYM_UP = 16;
 // C = alpha op(A) op(B) + beta C (see linalg.cu for the flags; dK / dN optional device bounds)
 void dgemm(cudaStream_t st, bool ta, bool tb, int M, int N, int K, double alpha, const double* A, int lda,
            const double* B, int ldb, double beta, double* C, int ldc, int flags = 0, const int* dK = nullptr,

@@ -18,6 +18,7 @@ constexpr int GBM = 64, GBN = 64, GBK = 16;
 //   GF_A_LOWER  op(A)[i,k] = 0 for k > i      (k < i0 + 64 per tile)
 //   GF_A_UPPER  op(A)[i,k] = 0 for k < i      (k >= i0 per tile)
 //   GF_SYM      C symmetric: only tiles touching the lower triangle are computed (mirror afterwards)
+//   GF_SYM_UP   C symmetric and only its upper triangle wanted: tiles touching the upper triangle
 // dK / dN (optional, device): K and N limited to *dK / *dN at run time.
 // One TB x TB tile (i0, j0) of the product (TB = 64 or 32), computed by a 256-thread block: thread
 // (tx, ty) owns rows ty + 16 r and columns tx + 16 c, r, c < TB / 16.
@@ -33,6 +34,7 @@ __device__ inline void dgemm_tile(int M, int N, int K, double alpha, const doubl
     if (dN) N = min(N, *dN);
     if (j0 >= N) return;
     if ((flags & GF_SYM) && j0 >= i0 + TM) return;
+    if ((flags & GF_SYM_UP) && i0 >= j0 + TN) return;
     if (dK) K = min(K, *dK);
     int kbeg = 0, kend = K;
     if (flags & GF_B_UPPER) kend = min(kend, j0 + TN);
