@@ -110,64 +110,6 @@ void dgemm(cudaStream_t st, bool ta, bool tb, int M, int N, int K, double alpha,
     else dgemm_launch<GBM>(st, ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, flags, dK, dN);
 }
 
-// ------------------------------------------------------------------ split-K GEMM
-// Skinny products with a long K (the Gram matrix and the projections of the blocked
-// back-transformation) have few output tiles; grid.z splits K so that every SM gets work.
-// Slice z writes its partial product to P + z * M * N (row-major, ld N); k_reduce_slices sums
-// the slices in a fixed order (deterministic, no atomics).
-template <bool TA, bool TB>
-__global__ void __launch_bounds__(256) k_dgemm_slices(int M, int N, int K, int kc, const double* __restrict__ A,
-                                                      int lda, const double* __restrict__ B, int ldb,
-                                                      double* __restrict__ P, const int* __restrict__ dN) {
-    __shared__ double smem[GEMM_SMEM];
-    const int z = blockIdx.z, k0 = z * kc;
-    const int kn = min(kc, K - k0);
-    const double* Az = TA ? A + (size_t)k0 * lda : A + k0;
-    const double* Bz = TB ? B + k0 : B + (size_t)k0 * ldb;
-    double* Pz = P + (size_t)z * M * N;
-    if (kn <= 0) {
-        // empty slice: zero its tile so that the reduction can sum every slice
-        const int i0 = blockIdx.y * GBM, j0 = blockIdx.x * GBN;
-        for (int t = threadIdx.x; t < GBM * GBN; t += blockDim.x) {
-            const int i = i0 + t / GBN, j = j0 + t % GBN;
-            if (i < M && j < N) Pz[(size_t)i * N + j] = 0.0;
-        }
-        return;
-    }
-    dgemm_tile<TA, TB>(M, N, kn, 1.0, Az, lda, Bz, ldb, 0.0, Pz, N, 0, nullptr, dN, blockIdx.y * GBM,
-                       blockIdx.x * GBN, smem);
-}
-
-__global__ void k_reduce_slices(int M, int N, int nsplit, double alpha, const double* __restrict__ P, double beta,
-                                double* __restrict__ C, int ldc, const int* __restrict__ dN) {
-    const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= (long)M * N) return;
-    const int i = (int)(t / N), j = (int)(t % N);
-    if (dN && j >= *dN) return;
-    double s = 0.0;
-    for (int z = 0; z < nsplit; ++z) s += P[(size_t)z * M * N + t];
-    double v = alpha * s;
-    if (beta != 0.0) v += beta * C[(size_t)i * ldc + j];
-    C[(size_t)i * ldc + j] = v;
-}
-
-void dgemm_splitk(cudaStream_t st, bool ta, bool tb, int M, int N, int K, double alpha, const double* A, int lda,
-                  const double* B, int ldb, double beta, double* C, int ldc, int nsplit, double* partial,
-                  const int* dN) {
-    if (M <= 0 || N <= 0) return;
-    nsplit = std::max(1, std::min(nsplit, std::max(1, K / 64)));
-    const int kc = ((ceil_div(K, nsplit) + GBK - 1) / GBK) * GBK;
-    nsplit = ceil_div(K, kc);
-    dim3 grid(ceil_div(N, GBN), ceil_div(M, GBM), nsplit);
-    if (!ta && !tb) k_dgemm_slices<false, false><<<grid, 256, 0, st>>>(M, N, K, kc, A, lda, B, ldb, partial, dN);
-    else if (ta && !tb) k_dgemm_slices<true, false><<<grid, 256, 0, st>>>(M, N, K, kc, A, lda, B, ldb, partial, dN);
-    else if (!ta && tb) k_dgemm_slices<false, true><<<grid, 256, 0, st>>>(M, N, K, kc, A, lda, B, ldb, partial, dN);
-    else k_dgemm_slices<true, true><<<grid, 256, 0, st>>>(M, N, K, kc, A, lda, B, ldb, partial, dN);
-    XG_LAUNCH_CHECK();
-    k_reduce_slices<<<ceil_div((long)M * N, 256), 256, 0, st>>>(M, N, nsplit, alpha, partial, beta, C, ldc, dN);
-    XG_LAUNCH_CHECK();
-}
-
 // copy the lower triangle onto the upper one (after a GF_SYM product)
 __global__ void k_mirror_lower(int n, double* __restrict__ C, int ldc) {
     const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;

@@ -60,10 +60,6 @@ void ormtr_inplace(cudaStream_t st, int n, const double* V, const double* tau, d
 // split_gemm_workspace(n, n, n, slices) bytes)
 void ormtr_blocked(cudaStream_t st, int n, const double* V, const double* tau, double* Y, const int* ncol,
                    double* work, int slices = 0, void* split_work = nullptr);
-// C = alpha op(A) op(B) + beta C with K split into nsplit slices (partial: nsplit * M * N doubles)
-void dgemm_splitk(cudaStream_t st, bool ta, bool tb, int M, int N, int K, double alpha, const double* A, int lda,
-                  const double* B, int ldb, double beta, double* C, int ldc, int nsplit, double* partial,
-                  const int* dN = nullptr);
 // measured FP64 throughput of the current device (TFLOP/s): the largest of two FMA probes and
 // the FP64 GEMM at 4096^3; fp64_peak_detail gives the three figures of the last measurement
 double fp64_peak_tflops();
