@@ -103,9 +103,11 @@ void dgemm(cudaStream_t st, bool ta, bool tb, int M, int N, int K, double alpha,
     // thousand AOs their largest 64 x 64 tiles alone are about the average work per SM and ran at
     // half speed beside other tiles on their SM (n = 1800: Hu X 3.3 ms, 0.59 TFLOP/s).  32 x 32
     // tiles cut the largest tile's share by 8; measured at n = 1800 per SCC iteration: standard
-    // form 7.6 -> 5.6 ms, C = X Z 4.6 -> 3.0 ms, density 3.7 -> 3.3 ms.  Dense products keep 64.
+    // form 7.6 -> 5.6 ms, C = X Z 4.6 -> 3.0 ms, density 3.7 -> 3.3 ms.  Up to 2048 the dense
+    // products (the Cholesky's trailing updates, P S for the bond orders) gain a little as well
+    // (the (H2O)300 single point 581.5 -> 579.4 ms); larger dense products keep 64 x 64 tiles.
     const bool small_tiles = (flags & (GF_A_UPPER | GF_SYM)) || ((flags & GF_B_UPPER) && (flags & GF_A_LOWER));
-    if (small_tiles && std::max(M, N) <= 4096)
+    if ((small_tiles && std::max(M, N) <= 4096) || std::max(M, N) <= 2048)
         dgemm_launch<32>(st, ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, flags, dK, dN);
     else dgemm_launch<GBM>(st, ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, flags, dK, dN);
 }
